@@ -1,0 +1,254 @@
+"""Pin the oracle (the CPU restatement) to the reference's own tests for this
+path, re-expressed here, and to the committed golden fixtures.
+
+Reference tests restated:
+* source/tit/sph/kernel.test.cpp:33-91   kernel normalisation over the sphere
+  and over the box, 1D/2D/3D, h in {1, 0.1, 0.01}
+* source/tit/sph/kernel.test.cpp:95-122  gradient against an exact
+  derivative at x = h^2 (0.1, 0.1, 0.1), single and summed components
+* source/tit/geom/search.test.cpp:130-163 grid search against the naive
+  O(N^2) search on 200 std::mt19937{123} points, radii {0.01, 0.1, 0.5, 1},
+  grid size hints 0.5 r and 5 r, and the empty case
+The comparisons use the reference's CHECK_APPROX_EQ tolerance, an absolute
+tiny_v = cbrt(DBL_EPSILON) ~ 6.06e-6 (core/math.hpp:141-163).
+"""
+
+from __future__ import annotations
+
+import math
+import pathlib
+
+import numpy as np
+import pytest
+import sympy as sp
+
+import oracle
+from titsolver_gb300 import physics, scenarios
+
+TINY = 6.0554544523933395e-06
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+KERNELS = range(6)
+RADII = (0.01, 0.1, 0.5, 1.0)
+
+# Exact unit kernels of kernel.gen.cpp:520-553 (pieces: (cutoff, poly)).
+_q = sp.symbols("q", nonnegative=True)
+_R = sp.Rational
+UNIT = {
+    0: [(2, _R(1, 4) * (2 - _q) ** 3), (1, -(1 - _q) ** 3)],
+    1: [(_R(5, 2), (_R(5, 2) - _q) ** 4), (_R(3, 2), -5 * (_R(3, 2) - _q) ** 4),
+        (_R(1, 2), 10 * (_R(1, 2) - _q) ** 4)],
+    2: [(3, (3 - _q) ** 5), (2, -6 * (2 - _q) ** 5), (1, 15 * (1 - _q) ** 5)],
+    3: [(2, (1 + 2 * _q) * (1 - _q / 2) ** 4)],
+    4: [(2, (1 + 3 * _q + _R(35, 12) * _q ** 2) * (1 - _q / 2) ** 6)],
+    5: [(2, (1 + 4 * _q + _R(25, 4) * _q ** 2 + 4 * _q ** 3) * (1 - _q / 2) ** 8)],
+}
+
+
+def _gauss_radial(kernel, dim, h):
+    """int W dV over the support sphere by Gauss-Legendre on each piece."""
+    radius, _ = oracle.kernel_info(kernel, dim)
+    cuts = sorted({0.0} | {float(c) for c, _ in UNIT[kernel]})
+    xg, wg = np.polynomial.legendre.leggauss(24)
+    area = 2.0 * math.pi ** (dim / 2) / math.gamma(dim / 2)
+    total = 0.0
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        qs = 0.5 * (b - a) * xg + 0.5 * (a + b)
+        for qi, wi in zip(qs, wg):
+            x = np.zeros(dim)
+            x[0] = qi * h
+            total += 0.5 * (b - a) * wi * oracle.kernel_value(kernel, x, h) * area * (qi * h) ** (dim - 1) * h
+    return total
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("dim", (1, 2, 3))
+@pytest.mark.parametrize("h", (1.0, 0.1, 0.01))
+def test_kernel_normalised_over_sphere(kernel, dim, h):
+    assert abs(_gauss_radial(kernel, dim, h) - 1.0) <= TINY
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("dim", (1, 2))
+def test_kernel_normalised_over_box(kernel, dim):
+    # Midpoint rule over [-R, R]^dim: checks symmetry and that W vanishes
+    # outside the support (the box integral stays 1).
+    h = 0.1
+    radius, _ = oracle.kernel_info(kernel, dim)
+    R = radius * h
+    n = 4000 if dim == 1 else 240
+    g = (np.arange(n) + 0.5) / n * 2 * R - R
+    cell = (2 * R / n) ** dim
+    if dim == 1:
+        total = sum(oracle.kernel_value(kernel, np.array([x]), h) for x in g) * cell
+    else:
+        total = sum(oracle.kernel_value(kernel, np.array([x, y]), h)
+                    for x in g for y in g) * cell
+    assert abs(total - 1.0) <= 2e-3
+
+
+def _exact_grad(kernel, x, h):
+    """Exact gradient from the sympy derivative of the unit kernel."""
+    dim = len(x)
+    _, w = oracle.kernel_info(kernel, dim)
+    r = math.sqrt(sum(xi * xi for xi in x))
+    q = r / h
+    d = sum(sp.diff(poly, _q).subs(_q, sp.Float(q, 40)) for c, poly in UNIT[kernel] if q < c)
+    s = float(w * h ** -dim * d / h)
+    return np.array([s * xi / r for xi in x])
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("h", (1.0, 0.1, 0.01))
+def test_kernel_grad_matches_exact_derivative(kernel, h):
+    x = h * h * np.array([0.1, 0.1, 0.1])
+    g = oracle.kernel_grad(kernel, x, h)
+    e = _exact_grad(kernel, x, h)
+    assert abs(g[0] - e[0]) <= TINY
+    assert abs(g.sum() - e.sum()) <= TINY
+
+
+def test_kernel_values_golden():
+    z = np.load(GOLDEN / "kernels.npz")
+    for dim in (2, 3):
+        x = z[f"x_{dim}d"]
+        for k in KERNELS:
+            W = np.array([oracle.kernel_value(k, xi, 0.1) for xi in x])
+            gW = np.array([oracle.kernel_grad(k, xi, 0.1) for xi in x])
+            np.testing.assert_allclose(W, z[f"W_{k}_{dim}d"], rtol=1e-14, atol=0)
+            np.testing.assert_allclose(gW, z[f"gW_{k}_{dim}d"], rtol=1e-13, atol=1e-300)
+
+
+def test_tait_round_trip():
+    rho0, cs0 = 1000.0, 31.32
+    for rho in (990.0, 1000.0, 1003.7, 1020.0):
+        p, c, H = oracle.tait(rho, rho0, cs0, 7.0)
+        assert p == pytest.approx(rho0 * cs0 ** 2 / 7 * ((rho / rho0) ** 7 - 1), rel=1e-13)
+        assert c == pytest.approx(cs0 * (rho / rho0) ** 3, rel=1e-14)
+        assert oracle.density_from_potential(H, rho0, cs0, 7.0) == pytest.approx(rho, rel=1e-13)
+
+
+def _rows(off, idx):
+    return [list(idx[off[i]:off[i + 1]]) for i in range(len(off) - 1)]
+
+
+@pytest.mark.parametrize("dim", (2, 3))
+def test_search_matches_naive_mt19937(dim):
+    pts = oracle.mt19937_uniform_points(123, 200, dim)
+    z = np.load(GOLDEN / "search_mt19937.npz")
+    np.testing.assert_array_equal(pts, z[f"points_{dim}d"])
+    for r in RADII:
+        naive = _rows(*oracle.naive_search(pts, r, inclusive=False))
+        assert not all(len(row) == 0 for row in naive)
+        assert naive == _rows(z[f"naive_{dim}d_{r}_off"], z[f"naive_{dim}d_{r}_idx"])
+        for scale in (0.5, 5.0):
+            grid = _rows(*oracle.grid_search(pts, r, scale * r, nthreads=4))
+            assert grid == naive, (dim, r, scale)
+
+
+def test_search_empty():
+    off, idx = oracle.grid_search(np.zeros((0, 2)), 0.1, 0.1)
+    assert off.tolist() == [0] and idx.size == 0
+
+
+def test_search_inclusive_ties_on_lattice():
+    # A lattice of spacing dx with radius 4 dx has neighbours at exactly the
+    # radius; the reference predicate is inclusive (bsphere.hpp:52-54).
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    r = scn["r"][: scn["tanks"][0]["n_fluid"]]
+    dx = scn["dx"]
+    grid = _rows(*oracle.grid_search(r, 4 * dx, 2 * dx))
+    incl = _rows(*oracle.naive_search(r, 4 * dx, inclusive=True))
+    excl = _rows(*oracle.naive_search(r, 4 * dx, inclusive=False))
+    assert grid == incl
+    assert grid != excl
+    # Interior lattice points have 49 neighbours (self included).
+    assert max(len(row) for row in grid) == 49
+
+
+def test_search_f32_matches_naive_f32():
+    pts = oracle.mt19937_uniform_points(123, 200, 3).astype(np.float32)
+    off, idx = oracle.grid_search_f32(pts, 0.1, 0.05)
+    rows = _rows(off, idx)
+    p = pts.astype(np.float32)
+    for i in range(0, 200, 17):
+        d = p - p[i]
+        s = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        assert rows[i] == list(np.nonzero(s <= np.float32(0.1) * np.float32(0.1))[0])
+
+
+def test_summation_density_golden():
+    z = np.load(GOLDEN / "cloud_small.npz")
+    for prec in (0, 1):
+        rho, cnt, hs = oracle.summation_density(z["r"], float(z["h"]), float(z["m"]), 3, prec)
+        np.testing.assert_array_equal(cnt, z[f"count_{prec}"])
+        np.testing.assert_array_equal(hs, z[f"hash_{prec}"])
+        np.testing.assert_allclose(rho, z[f"rho_{prec}"], rtol=1e-12 if prec == 0 else 1e-6)
+
+
+def test_summation_density_interior_lattice_is_rho0():
+    # On a regular lattice with m = rho0 dx^2, the interior summation density
+    # is rho0 within the kernel's discretisation error.
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    nf = scn["tanks"][0]["n_fluid"]
+    r = scn["r"][:nf]
+    t = scn["tanks"][0]
+    rho, cnt, _ = oracle.summation_density(r, t["h"], t["m"], 3)
+    dx = scn["dx"]
+    lo, hi = r.min(axis=0) + 4 * dx, r.max(axis=0) - 4 * dx
+    inner = np.all((r >= lo - 1e-12) & (r <= hi + 1e-12), axis=1)
+    assert inner.sum() > 300
+    # Exact-distance ties (4 dx) round either way: 45..49 neighbours.
+    assert cnt[inner].min() >= 45 and cnt[inner].max() == 49
+    np.testing.assert_allclose(rho[inner], 1000.0, rtol=1e-2)
+
+
+def _golden_states(path, prefix, steps, scn, params):
+    z = np.load(GOLDEN / path)
+    st = oracle.State(scn)
+    done = 0
+    for s in steps:
+        if s > done:
+            oracle.step(params, st, s - done)
+            done = s
+        for name, arr in (("r", st.r), ("v", st.v), ("rho", st.rho),
+                          ("dv_dt", st.dv_dt), ("drho_dt", st.drho_dt)):
+            ref = z[f"{prefix}_{s}_{name}"]
+            np.testing.assert_allclose(arr, ref, rtol=1e-11, atol=1e-9 * (np.abs(ref).max() + 1e-300))
+
+
+def test_dam_break_golden_both_term_sets():
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    _golden_states("dam_break_small.npz", "baseline", (0, 1, 10), scn, physics.baseline_params(2))
+    _golden_states("dam_break_small.npz", "reference", (0, 1, 10), scn, physics.reference_params(2))
+
+
+def test_dam3d_and_batched_golden():
+    _golden_states("dam3d_small.npz", "baseline", (0, 2), scenarios.dam_break_3d(nx_per_H=8),
+                   physics.baseline_params(3))
+    _golden_states("batched_small.npz", "baseline", (0, 3),
+                   scenarios.batched_tanks(n_tanks=4, n_range=(6, 12), seed=11),
+                   physics.baseline_params(2))
+
+
+def test_oracle_thread_count_independent():
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    a, b = oracle.State(scn), oracle.State(scn)
+    oracle.step(physics.baseline_params(2), a, 3, nthreads=1)
+    oracle.step(physics.baseline_params(2), b, 3, nthreads=7)
+    np.testing.assert_array_equal(a.r, b.r)
+    np.testing.assert_array_equal(a.rho, b.rho)
+
+
+def test_oracle_step_physics_sanity():
+    # Mass is constant by construction; the column starts to collapse: the
+    # fluid gains kinetic energy and stays inside the tank.
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    st = oracle.State(scn)
+    nf = scn["tanks"][0]["n_fluid"]
+    oracle.step(physics.baseline_params(2), st, 20)
+    assert np.all(np.isfinite(st.r)) and np.all(np.isfinite(st.rho))
+    assert np.abs(st.v[:nf]).max() > 0.01
+    assert st.r[:nf, 1].min() > -1e-3
+    # Fixed particles never move.
+    np.testing.assert_array_equal(st.r[nf:], scn["r"][nf:])
+    assert np.all(st.v[nf:] == 0.0)

@@ -1,0 +1,104 @@
+"""Build the in-tree CUDA library ``titsolver_gb300/_lib/libtitgpu.so``.
+
+Every ``csrc/*.cu`` translation unit is compiled for sm_103a in parallel and
+linked into one shared library with the C ABI of ``include/titgpu.h``.
+Nothing is installed outside the package directory.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures
+import os
+import pathlib
+import shutil
+import subprocess
+import sys
+
+PKG = pathlib.Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+OUT_DIR = PKG / "_lib"
+OBJ_DIR = PKG / "_build"
+LIB = OUT_DIR / "libtitgpu.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = [
+    "-O3",
+    "-lineinfo",
+    "-std=c++20",
+    "--expt-relaxed-constexpr",
+    "-Xcompiler",
+    "-fPIC",
+    "-Xcompiler",
+    "-Wall",
+    "-Xptxas",
+    "-warn-spills",
+]
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc")
+    if exe is None:
+        cand = pathlib.Path("/usr/local/cuda/bin/nvcc")
+        if cand.exists():
+            return str(cand)
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required")
+    return exe
+
+
+def _sources() -> list[pathlib.Path]:
+    return sorted(CSRC.glob("*.cu"))
+
+
+def _deps() -> list[pathlib.Path]:
+    return sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "titgpu.h"]
+
+
+def _compile(src: pathlib.Path, verbose: bool) -> pathlib.Path:
+    obj = OBJ_DIR / (src.stem + ".o")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-I", str(ROOT / "include"), "-c",
+           str(src), "-o", str(obj)]
+    if verbose:
+        cmd.insert(-4, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {src.name}:\n{res.stdout}\n{res.stderr}")
+    if verbose and res.stderr:
+        sys.stderr.write(res.stderr)
+    return obj
+
+
+def up_to_date() -> bool:
+    if not LIB.exists():
+        return False
+    t = LIB.stat().st_mtime
+    return all(p.stat().st_mtime <= t for p in _sources() + _deps() + [pathlib.Path(__file__)])
+
+
+def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> pathlib.Path:
+    """Compile and link the library; returns its path."""
+    if not force and up_to_date():
+        return LIB
+    OUT_DIR.mkdir(exist_ok=True)
+    OBJ_DIR.mkdir(exist_ok=True)
+    srcs = _sources()
+    jobs = jobs or min(len(srcs), max(1, os.cpu_count() or 1))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=jobs) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--verbose", action="store_true", help="print ptxas register/spill report")
+    a = ap.parse_args()
+    print(build(force=a.force, verbose=a.verbose))

@@ -1,0 +1,798 @@
+// abi.cu - the C ABI of include/titgpu.h over the typed engines.
+//
+// Host responsibilities: argument validation (the reference asserts in Debug
+// builds and throws tit::Exception from TIT_ENSURE; here every failure is a
+// status code with a message in tg_last_error), the per-tank cell grids,
+// device allocation, CUDA-graph capture of one step, and profiling.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "sort.cuh"
+
+struct tg_context {
+  tg::Context c;
+};
+
+namespace tg {
+
+cudaError_t Context::alloc(void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) allocations.push_back(*p);
+  return e;
+}
+
+void Context::release_all() {
+  invalidate_graph();
+  for (void* p : allocations) cudaFree(p);
+  allocations.clear();
+  d_tanks = nullptr;
+  d_id_base = d_wall_from = d_tank_of = nullptr;
+  d_dt = d_dt_last = d_time = nullptr;
+  d_err = d_wall_count = nullptr;
+  keys_a = keys_b = vals_a = vals_b = nullptr;
+  sort_scratch = nullptr;
+  cell_start = wall_list = nullptr;
+  d_stage = d_stage2 = d_stage3 = d_stage4 = nullptr;
+  d_sd_rho = nullptr;
+  d_sd_count = nullptr;
+  d_sd_hash = nullptr;
+  d_cloud_rec = nullptr;
+  uploaded = false;
+}
+
+void Context::invalidate_graph() {
+  if (graph_exec != nullptr) {
+    cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+  }
+}
+
+int Context::group_begin(int group) {
+  if (!profile) return -1;
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(stream, &st);
+  if (st != cudaStreamCaptureStatusNone) return -1;
+  PendingEvent pe{group, nullptr, nullptr};
+  for (cudaEvent_t* ev : {&pe.start, &pe.stop}) {
+    if (!event_pool.empty()) {
+      *ev = event_pool.back();
+      event_pool.pop_back();
+    } else {
+      cudaEventCreate(ev);
+    }
+  }
+  cudaEventRecord(pe.start, stream);
+  pending.push_back(pe);
+  return static_cast<int>(pending.size()) - 1;
+}
+
+void Context::group_end(int token) {
+  if (token < 0) return;
+  cudaEventRecord(pending[static_cast<size_t>(token)].stop, stream);
+}
+
+void Context::drain_profile() {
+  if (pending.empty()) return;
+  cudaStreamSynchronize(stream);
+  for (const PendingEvent& pe : pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, pe.start, pe.stop);
+    switch (pe.group) {
+      case kGroupSort: prof.sort_ms += ms; break;
+      case kGroupReorder: prof.reorder_ms += ms; break;
+      case kGroupWalls: prof.walls_ms += ms; break;
+      case kGroupForces: prof.forces_ms += ms; break;
+      default: prof.post_ms += ms; break;
+    }
+    event_pool.push_back(pe.start);
+    event_pool.push_back(pe.stop);
+  }
+  pending.clear();
+}
+
+}  // namespace tg
+
+namespace {
+
+using tg::Context;
+
+int fail(Context* C, int status, const std::string& msg) {
+  if (C != nullptr) C->last_error = msg;
+  return status;
+}
+
+int cuda_fail(Context* C, cudaError_t e, const char* where) {
+  std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) {
+    return fail(C, TG_ERR_OUT_OF_MEMORY, msg);
+  }
+  return fail(C, TG_ERR_CUDA, msg);
+}
+
+#define TG_CUDA(C, call)                                   \
+  do {                                                     \
+    const cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail((C), e_, #call); \
+  } while (0)
+
+bool valid_params(const tg_params* P, std::string* why) {
+  if (P->dim != 2 && P->dim != 3) {
+    *why = "dim must be 2 or 3";
+    return false;
+  }
+  if (P->precision != TG_FP64 && P->precision != TG_FP32C) {
+    *why = "precision must be TG_FP64 or TG_FP32C";
+    return false;
+  }
+  if (P->kernel < 0 || P->kernel > 5) {
+    *why = "unknown kernel";
+    return false;
+  }
+  if (P->integrator != TG_SSPRK3 && P->integrator != TG_SSPRK2) {
+    *why = "this build runs the SSPRK integrators (TG_SSPRK3, TG_SSPRK2)";
+    return false;
+  }
+  if (P->viscosity != TG_VISC_MORRIS && P->viscosity != TG_VISC_MONAGHAN) {
+    *why = "unknown viscosity model";
+    return false;
+  }
+  if (P->diffusion < 0 || P->diffusion > 2) {
+    *why = "unknown diffusion model";
+    return false;
+  }
+  if (P->post_integrate != TG_POST_PREPARE) {
+    *why = "this build runs post_integrate = TG_POST_PREPARE";
+    return false;
+  }
+  if (P->cells_per_radius < 1 || P->cells_per_radius > 3) {
+    *why = "cells_per_radius must be 1, 2 or 3";
+    return false;
+  }
+  if (!(P->xi > 1.0) || !(P->g >= 0.0) || !(P->mu >= 0.0) ||
+      !(P->alpha >= 0.0) || !(P->delta >= 0.0) || !(P->cfl > 0.0) ||
+      !(P->c_force > 0.0) || !(P->c_visc > 0.0)) {
+    *why = "physical constants out of range";
+    return false;
+  }
+  return true;
+}
+
+double kernel_weight(int k, int dim) {
+  const double pi = 3.14159265358979323846;
+  const double area = 2.0 * std::sqrt(std::pow(pi, dim)) / std::tgamma(dim / 2.0);
+  return 1.0 / (tg::kernel_zero_moment(k, dim) * area);
+}
+
+int key_bits_for(uint32_t total_cells) {
+  int bits = 1;
+  while (bits < 32 && (static_cast<uint64_t>(1) << bits) < total_cells) ++bits;
+  return bits;
+}
+
+}  // namespace
+
+extern "C" {
+
+void tg_params_default(tg_params* p) {
+  if (p == nullptr) return;
+  std::memset(p, 0, sizeof(*p));
+  p->dim = 2;
+  p->precision = TG_FP64;
+  p->kernel = TG_KERNEL_WENDLAND_C4;
+  p->integrator = TG_SSPRK3;
+  p->viscosity = TG_VISC_MORRIS;
+  p->diffusion = TG_DIFF_FERRARI;
+  p->post_integrate = TG_POST_PREPARE;
+  p->cells_per_radius = 1;
+  p->kahan = 1;
+  p->xi = 7.0;
+  p->g = 9.81;
+  p->mu = 0.001;
+  p->alpha = 0.02;
+  p->delta = 0.1;
+  p->cfl = 0.4;
+  p->c_force = 0.25;
+  p->c_visc = 0.125;
+}
+
+const char* tg_status_string(int status) {
+  switch (status) {
+    case TG_OK: return "ok";
+    case TG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case TG_ERR_CUDA: return "CUDA error";
+    case TG_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case TG_ERR_NOT_READY: return "no particles uploaded";
+    case TG_ERR_DEVICE_STATE: return "device error word raised";
+    case TG_ERR_CAPACITY: return "output capacity too small";
+    case TG_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* tg_last_error(tg_context* ctx) {
+  return ctx == nullptr ? "null context" : ctx->c.last_error.c_str();
+}
+
+int tg_context_create(const tg_params* params, tg_context** out) {
+  if (out == nullptr || params == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::string why;
+  if (!valid_params(params, &why)) return TG_ERR_INVALID_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return TG_ERR_NO_DEVICE;
+  }
+  tg_context* ctx = new (std::nothrow) tg_context();
+  if (ctx == nullptr) return TG_ERR_OUT_OF_MEMORY;
+  Context& C = ctx->c;
+  C.P = *params;
+  cudaGetDevice(&C.device);
+  if (cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return TG_ERR_CUDA;
+  }
+  C.phys.xi = params->xi;
+  C.phys.g = params->g;
+  C.phys.mu = params->mu;
+  C.phys.alpha = params->alpha;
+  C.phys.cfl = params->cfl;
+  C.phys.c_force = params->c_force;
+  C.phys.c_visc = params->c_visc;
+  C.phys.xi_is_7 = params->xi == 7.0 ? 1 : 0;
+  C.phys.viscosity = params->viscosity;
+  C.phys.diffusion = params->diffusion;
+  C.phys.kernel = params->kernel;
+  C.k = params->cells_per_radius;
+  const bool f64 = params->precision == TG_FP64;
+  if (params->dim == 2) {
+    C.engine = f64 ? tg::make_engine_2d_f64(params->kernel)
+                   : tg::make_engine_2d_f32(params->kernel);
+  } else {
+    C.engine = f64 ? tg::make_engine_3d_f64(params->kernel)
+                   : tg::make_engine_3d_f32(params->kernel);
+  }
+  if (!C.engine) {
+    cudaStreamDestroy(C.stream);
+    delete ctx;
+    return TG_ERR_INVALID_ARGUMENT;
+  }
+  *out = ctx;
+  return TG_OK;
+}
+
+int tg_context_destroy(tg_context* ctx) {
+  if (ctx == nullptr) return TG_OK;
+  Context& C = ctx->c;
+  cudaStreamSynchronize(C.stream);
+  C.pending.clear();
+  for (cudaEvent_t e : C.event_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : C.timer_ev) {
+    if (e != nullptr) cudaEventDestroy(e);
+  }
+  C.release_all();
+  C.engine.reset();
+  cudaStreamDestroy(C.stream);
+  delete ctx;
+  return TG_OK;
+}
+
+int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
+                        const double* r, const double* v, const double* rho) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  const int dim = C.P.dim;
+  if (n_tanks < 1 || tanks == nullptr) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "need at least one tank");
+  }
+  int64_t n = 0, nf = 0, nw = 0;
+  for (int32_t t = 0; t < n_tanks; ++t) {
+    const tg_tank& T = tanks[t];
+    if (T.n_fluid < 0 || T.n_wall < 0 || !(T.h > 0.0) || !(T.m > 0.0) ||
+        !(T.rho0 > 0.0) || !(T.cs0 > 0.0) || !std::isfinite(T.h) ||
+        !std::isfinite(T.m) || !std::isfinite(T.rho0) || !std::isfinite(T.cs0)) {
+      return fail(&C, TG_ERR_INVALID_ARGUMENT,
+                  "tank " + std::to_string(t) + ": invalid counts or constants");
+    }
+    n += T.n_fluid + T.n_wall;
+    nf += T.n_fluid;
+    nw += T.n_wall;
+  }
+  if (n >= (int64_t{1} << 31) - 1) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "more than 2^31 - 2 particles");
+  }
+  if (n > 0 && (r == nullptr || v == nullptr || rho == nullptr)) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "null particle array");
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    bool ok = std::isfinite(rho[i]) && rho[i] > 0.0;
+    for (int k = 0; k < dim; ++k) {
+      ok = ok && std::isfinite(r[i * dim + k]) && std::isfinite(v[i * dim + k]);
+    }
+    if (!ok) {
+      return fail(&C, TG_ERR_INVALID_ARGUMENT,
+                  "particle " + std::to_string(i) +
+                      ": non-finite state or non-positive density");
+    }
+  }
+
+  // Per-tank grids.
+  std::vector<tg::TankDev> td(static_cast<size_t>(n_tanks));
+  std::vector<uint32_t> id_base(static_cast<size_t>(n_tanks));
+  std::vector<uint32_t> wall_from(static_cast<size_t>(n_tanks));
+  uint64_t total_cells = 0;
+  int64_t base = 0;
+  for (int32_t t = 0; t < n_tanks; ++t) {
+    const tg_tank& T = tanks[t];
+    const int64_t nt = T.n_fluid + T.n_wall;
+    tg::TankDev& D = td[t];
+    std::memset(&D, 0, sizeof(D));
+    const double R = tg::kernel_unit_radius(C.P.kernel) * T.h;
+    const double cs = R / C.k * (1.0 + 1.0 / 65536.0);
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (nt > 0) {
+      for (int k = 0; k < dim; ++k) lo[k] = hi[k] = r[base * dim + k];
+      for (int64_t i = base; i < base + nt; ++i) {
+        for (int k = 0; k < dim; ++k) {
+          lo[k] = std::min(lo[k], r[i * dim + k]);
+          hi[k] = std::max(hi[k], r[i * dim + k]);
+        }
+      }
+    }
+    const double headroom = 0.5 * (hi[1] - lo[1]);
+    uint64_t cells = 1;
+    for (int k = 0; k < 3; ++k) {
+      if (k < dim) {
+        D.lo[k] = lo[k] - (R + cs);
+        double top = hi[k] + (R + cs) + (k == 1 ? headroom : 0.0);
+        const double ncf = std::max(1.0, std::ceil((top - D.lo[k]) / cs));
+        if (ncf > 2.0e9) {
+          return fail(&C, TG_ERR_INVALID_ARGUMENT, "tank grid too large");
+        }
+        D.nc[k] = static_cast<int32_t>(ncf);
+      } else {
+        D.lo[k] = 0.0;
+        D.nc[k] = 1;
+      }
+      cells *= static_cast<uint64_t>(D.nc[k]);
+    }
+    D.cs = cs;
+    D.inv_cs = 1.0 / cs;
+    D.cell_off = static_cast<uint32_t>(total_cells);
+    total_cells += cells;
+    if (total_cells >= (uint64_t{1} << 31)) {
+      return fail(&C, TG_ERR_INVALID_ARGUMENT,
+                  "more than 2^31 grid cells; lower cells_per_radius");
+    }
+    D.h = T.h;
+    D.hinv = 1.0 / T.h;
+    D.radius2 = R * R;
+    const float hf = static_cast<float>(T.h);
+    const float Rf = static_cast<float>(tg::kernel_unit_radius(C.P.kernel)) * hf;
+    D.radius2_f = Rf * Rf;
+    D.cs_f = static_cast<float>(cs);
+    double hinv_d = 1.0;
+    for (int k = 0; k < dim; ++k) hinv_d *= D.hinv;
+    D.w = kernel_weight(C.P.kernel, dim) * hinv_d;
+    D.wg = D.w * D.hinv;
+    D.m = T.m;
+    D.rho0 = T.rho0;
+    D.cs0 = T.cs0;
+    D.B = T.rho0 * T.cs0 * T.cs0 / C.P.xi;
+    D.diff_k = 2.0 * C.P.delta * T.h * T.cs0;
+    D.visc_eps2 = 0.01 * T.h * T.h;
+    D.n_fluid = static_cast<uint32_t>(T.n_fluid);
+    id_base[t] = static_cast<uint32_t>(base);
+    wall_from[t] = static_cast<uint32_t>(base + T.n_fluid);
+    base += nt;
+  }
+
+  // (Re)allocate.
+  cudaStreamSynchronize(C.stream);
+  C.release_all();
+  C.n = n;
+  C.n_fluid = nf;
+  C.n_wall = nw;
+  C.ntanks = n_tanks;
+  C.tanks.assign(tanks, tanks + n_tanks);
+  C.tankdev = td;
+  C.id_base = id_base;
+  C.wall_from = wall_from;
+  C.total_cells = static_cast<uint32_t>(total_cells);
+  C.key_bits = key_bits_for(C.total_cells);
+  const int64_t nn = n > 0 ? n : 1;
+  auto A = [&](auto*& p, size_t bytes) -> cudaError_t {
+    return C.alloc(reinterpret_cast<void**>(&p), bytes);
+  };
+  TG_CUDA(&C, A(C.d_tanks, sizeof(tg::TankDev) * n_tanks));
+  TG_CUDA(&C, A(C.d_id_base, sizeof(uint32_t) * n_tanks));
+  TG_CUDA(&C, A(C.d_wall_from, sizeof(uint32_t) * n_tanks));
+  TG_CUDA(&C, A(C.d_tank_of, sizeof(uint32_t) * nn));
+  TG_CUDA(&C, A(C.d_dt, sizeof(double) * n_tanks));
+  TG_CUDA(&C, A(C.d_dt_last, sizeof(double) * n_tanks));
+  TG_CUDA(&C, A(C.d_time, sizeof(double) * n_tanks));
+  TG_CUDA(&C, A(C.d_err, sizeof(uint32_t)));
+  TG_CUDA(&C, A(C.d_wall_count, sizeof(uint32_t)));
+  TG_CUDA(&C, A(C.keys_a, sizeof(uint32_t) * nn));
+  TG_CUDA(&C, A(C.keys_b, sizeof(uint32_t) * nn));
+  TG_CUDA(&C, A(C.vals_a, sizeof(uint32_t) * nn));
+  TG_CUDA(&C, A(C.vals_b, sizeof(uint32_t) * nn));
+  TG_CUDA(&C, C.alloc(&C.sort_scratch, tg::radix_sort_scratch_bytes(nn)));
+  TG_CUDA(&C, A(C.cell_start, sizeof(uint32_t) * (total_cells + 1)));
+  TG_CUDA(&C, A(C.wall_list, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
+  TG_CUDA(&C, A(C.d_stage, sizeof(double) * nn * dim));
+  TG_CUDA(&C, A(C.d_stage2, sizeof(double) * nn * dim));
+  TG_CUDA(&C, A(C.d_stage3, sizeof(double) * nn * dim));
+  TG_CUDA(&C, A(C.d_stage4, sizeof(double) * nn * dim));
+  TG_CUDA(&C, A(C.d_sd_rho, sizeof(double) * nn));
+  TG_CUDA(&C, A(C.d_sd_count, sizeof(int32_t) * nn));
+  TG_CUDA(&C, A(C.d_sd_hash, sizeof(uint64_t) * nn));
+  TG_CUDA(&C, C.alloc(&C.d_cloud_rec, 32 * static_cast<size_t>(nn)));
+  TG_CUDA(&C, C.engine->allocate(C));
+
+  std::vector<uint32_t> tank_of(static_cast<size_t>(nn), 0);
+  base = 0;
+  for (int32_t t = 0; t < n_tanks; ++t) {
+    const int64_t nt = tanks[t].n_fluid + tanks[t].n_wall;
+    for (int64_t i = 0; i < nt; ++i) tank_of[base + i] = static_cast<uint32_t>(t);
+    base += nt;
+  }
+  std::vector<double> inf(static_cast<size_t>(n_tanks),
+                          std::numeric_limits<double>::infinity());
+  std::vector<double> zeros(static_cast<size_t>(n_tanks), 0.0);
+  cudaStream_t s = C.stream;
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_tanks, td.data(), sizeof(tg::TankDev) * n_tanks,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_id_base, id_base.data(), sizeof(uint32_t) * n_tanks,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_wall_from, wall_from.data(),
+                              sizeof(uint32_t) * n_tanks, cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_tank_of, tank_of.data(), sizeof(uint32_t) * nn,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_dt, inf.data(), sizeof(double) * n_tanks,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_dt_last, zeros.data(), sizeof(double) * n_tanks,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_time, zeros.data(), sizeof(double) * n_tanks,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemsetAsync(C.d_err, 0, sizeof(uint32_t), s));
+  if (n > 0) {
+    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage, r, sizeof(double) * n * dim,
+                                cudaMemcpyHostToDevice, s));
+    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage2, v, sizeof(double) * n * dim,
+                                cudaMemcpyHostToDevice, s));
+    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage3, rho, sizeof(double) * n,
+                                cudaMemcpyHostToDevice, s));
+    TG_CUDA(&C, C.engine->upload_state(C, false));
+  }
+  TG_CUDA(&C, cudaStreamSynchronize(s));
+  C.uploaded = true;
+  C.walls_fresh = false;
+  return TG_OK;
+}
+
+int tg_particles_update(tg_context* ctx, const double* r, const double* v,
+                        const double* rho, const double* dv_dt) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (C.n == 0) return TG_OK;
+  if (r == nullptr || v == nullptr || rho == nullptr) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "null particle array");
+  }
+  const int dim = C.P.dim;
+  cudaStream_t s = C.stream;
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_stage, r, sizeof(double) * C.n * dim,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_stage2, v, sizeof(double) * C.n * dim,
+                              cudaMemcpyHostToDevice, s));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_stage3, rho, sizeof(double) * C.n,
+                              cudaMemcpyHostToDevice, s));
+  if (dv_dt != nullptr) {
+    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage4, dv_dt, sizeof(double) * C.n * dim,
+                                cudaMemcpyHostToDevice, s));
+  }
+  TG_CUDA(&C, C.engine->upload_state(C, dv_dt != nullptr));
+  C.walls_fresh = false;
+  return TG_OK;
+}
+
+int tg_prepare(tg_context* ctx) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  TG_CUDA(&C, C.engine->enqueue_prepare(C));
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  C.walls_fresh = true;
+  return TG_OK;
+}
+
+int tg_step(tg_context* ctx, int32_t n_steps, double* dt_out) {
+  if (ctx == nullptr || n_steps < 0) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (n_steps > 0 && C.n > 0) {
+    if (C.use_graph && !C.profile) {
+      if (C.graph_exec == nullptr) {
+        cudaGraph_t graph = nullptr;
+        const int64_t before = C.launches;
+        TG_CUDA(&C, cudaStreamBeginCapture(C.stream,
+                                           cudaStreamCaptureModeThreadLocal));
+        const cudaError_t e = C.engine->enqueue_step(C);
+        const cudaError_t e2 = cudaStreamEndCapture(C.stream, &graph);
+        if (e != cudaSuccess) return cuda_fail(&C, e, "enqueue_step");
+        if (e2 != cudaSuccess) return cuda_fail(&C, e2, "cudaStreamEndCapture");
+        C.graph_kernels = C.launches - before;
+        C.launches = before;
+        const cudaError_t e3 = cudaGraphInstantiate(&C.graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e3 != cudaSuccess) {
+          C.graph_exec = nullptr;
+          return cuda_fail(&C, e3, "cudaGraphInstantiate");
+        }
+      }
+      for (int32_t i = 0; i < n_steps; ++i) {
+        TG_CUDA(&C, cudaGraphLaunch(C.graph_exec, C.stream));
+        C.launches += C.graph_kernels;
+      }
+    } else {
+      for (int32_t i = 0; i < n_steps; ++i) {
+        TG_CUDA(&C, C.engine->enqueue_step(C));
+        C.prof.stages += C.P.integrator == TG_SSPRK2 ? 2 : 3;
+        C.prof.forces_launches += C.P.integrator == TG_SSPRK2 ? 2 : 3;
+      }
+    }
+    C.prof.steps += n_steps;
+    C.walls_fresh = false;
+  }
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  C.drain_profile();
+  uint32_t err = 0;
+  TG_CUDA(&C, cudaMemcpy(&err, C.d_err, sizeof(err), cudaMemcpyDeviceToHost));
+  if (dt_out != nullptr) {
+    TG_CUDA(&C, cudaMemcpy(dt_out, C.d_dt_last, sizeof(double) * C.ntanks,
+                           cudaMemcpyDeviceToHost));
+  }
+  if (err & (TG_DEV_NONFINITE_STATE | TG_DEV_BAD_DT)) {
+    return fail(&C, TG_ERR_DEVICE_STATE,
+                "device error word " + std::to_string(err) +
+                    " (non-finite state or bad time step)");
+  }
+  return TG_OK;
+}
+
+int tg_time(tg_context* ctx, double* time_out) {
+  if (ctx == nullptr || time_out == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  TG_CUDA(&C, cudaMemcpy(time_out, C.d_time, sizeof(double) * C.ntanks,
+                         cudaMemcpyDeviceToHost));
+  return TG_OK;
+}
+
+int tg_particles_download(tg_context* ctx, int32_t field, double* out) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (field < TG_FIELD_R || field > TG_FIELD_CS) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "unknown field");
+  }
+  if (C.n == 0) return TG_OK;
+  if (out == nullptr) return fail(&C, TG_ERR_INVALID_ARGUMENT, "null output");
+  if ((field == TG_FIELD_RHO || field == TG_FIELD_P || field == TG_FIELD_CS) &&
+      !C.walls_fresh && C.n_wall > 0) {
+    TG_CUDA(&C, C.engine->enqueue_prepare(C));
+    C.walls_fresh = true;
+  }
+  TG_CUDA(&C, C.engine->enqueue_pack(C, field));
+  const int comps = (field == TG_FIELD_R || field == TG_FIELD_V ||
+                     field == TG_FIELD_DV_DT)
+                        ? C.P.dim
+                        : 1;
+  TG_CUDA(&C, cudaMemcpyAsync(out, C.d_stage, sizeof(double) * C.n * comps,
+                              cudaMemcpyDeviceToHost, C.stream));
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  return TG_OK;
+}
+
+int tg_neighbour_counts(tg_context* ctx, int32_t* counts, uint64_t* hashes) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (C.n == 0) return TG_OK;
+  TG_CUDA(&C, C.engine->enqueue_neighbours(C, C.d_sd_count, C.d_sd_hash,
+                                           nullptr, nullptr));
+  if (counts != nullptr) {
+    TG_CUDA(&C, cudaMemcpyAsync(counts, C.d_sd_count, sizeof(int32_t) * C.n,
+                                cudaMemcpyDeviceToHost, C.stream));
+  }
+  if (hashes != nullptr) {
+    TG_CUDA(&C, cudaMemcpyAsync(hashes, C.d_sd_hash, sizeof(uint64_t) * C.n,
+                                cudaMemcpyDeviceToHost, C.stream));
+  }
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  return TG_OK;
+}
+
+int tg_neighbour_lists(tg_context* ctx, int64_t* offsets, int32_t* indices,
+                       int64_t capacity) {
+  if (ctx == nullptr || offsets == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  const int64_t n = C.n;
+  offsets[0] = 0;
+  if (n == 0) return TG_OK;
+  std::vector<int32_t> counts(static_cast<size_t>(n));
+  const int st = tg_neighbour_counts(ctx, counts.data(), nullptr);
+  if (st != TG_OK) return st;
+  for (int64_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + counts[i];
+  const int64_t total = offsets[n];
+  if (indices == nullptr || capacity < total) {
+    return fail(&C, TG_ERR_CAPACITY,
+                "neighbour lists need " + std::to_string(total) + " entries");
+  }
+  int64_t* d_off = nullptr;
+  int32_t* d_idx = nullptr;
+  TG_CUDA(&C, cudaMalloc(&d_off, sizeof(int64_t) * (n + 1)));
+  cudaError_t e = cudaMalloc(&d_idx, sizeof(int32_t) * (total > 0 ? total : 1));
+  if (e != cudaSuccess) {
+    cudaFree(d_off);
+    return cuda_fail(&C, e, "cudaMalloc");
+  }
+  e = cudaMemcpyAsync(d_off, offsets, sizeof(int64_t) * (n + 1),
+                      cudaMemcpyHostToDevice, C.stream);
+  if (e == cudaSuccess) {
+    e = C.engine->enqueue_neighbours(C, nullptr, nullptr, d_off, d_idx);
+  }
+  if (e == cudaSuccess) {
+    e = cudaMemcpyAsync(indices, d_idx, sizeof(int32_t) * total,
+                        cudaMemcpyDeviceToHost, C.stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(C.stream);
+  cudaFree(d_off);
+  cudaFree(d_idx);
+  if (e != cudaSuccess) return cuda_fail(&C, e, "tg_neighbour_lists");
+  for (int64_t i = 0; i < n; ++i) {
+    std::sort(indices + offsets[i], indices + offsets[i + 1]);
+  }
+  return TG_OK;
+}
+
+int tg_summation_density(tg_context* ctx, int32_t pos_precision,
+                         double* rho_out, int32_t* counts, uint64_t* hashes) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (pos_precision != TG_POS_FP64 && pos_precision != TG_POS_FP32) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "unknown position precision");
+  }
+  if (C.n == 0) return TG_OK;
+  TG_CUDA(&C, C.engine->enqueue_sumdens(C, pos_precision, C.d_sd_rho,
+                                        C.d_sd_count, C.d_sd_hash));
+  if (rho_out != nullptr) {
+    TG_CUDA(&C, cudaMemcpyAsync(rho_out, C.d_sd_rho, sizeof(double) * C.n,
+                                cudaMemcpyDeviceToHost, C.stream));
+  }
+  if (counts != nullptr) {
+    TG_CUDA(&C, cudaMemcpyAsync(counts, C.d_sd_count, sizeof(int32_t) * C.n,
+                                cudaMemcpyDeviceToHost, C.stream));
+  }
+  if (hashes != nullptr) {
+    TG_CUDA(&C, cudaMemcpyAsync(hashes, C.d_sd_hash, sizeof(uint64_t) * C.n,
+                                cudaMemcpyDeviceToHost, C.stream));
+  }
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  C.drain_profile();
+  return TG_OK;
+}
+
+int tg_summation_density_resident(tg_context* ctx, int32_t pos_precision) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (pos_precision != TG_POS_FP64 && pos_precision != TG_POS_FP32) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "unknown position precision");
+  }
+  if (C.n == 0) return TG_OK;
+  TG_CUDA(&C, C.engine->enqueue_sumdens(C, pos_precision, C.d_sd_rho,
+                                        C.d_sd_count, C.d_sd_hash));
+  return TG_OK;
+}
+
+int tg_device_status(tg_context* ctx, uint32_t* flags) {
+  if (ctx == nullptr || flags == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  *flags = 0;
+  if (!C.uploaded) return TG_OK;
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  TG_CUDA(&C, cudaMemcpy(flags, C.d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  TG_CUDA(&C, cudaMemset(C.d_err, 0, sizeof(uint32_t)));
+  return TG_OK;
+}
+
+int tg_profile_enable(tg_context* ctx, int32_t enable) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  C.drain_profile();
+  C.profile = enable != 0;
+  std::memset(&C.prof, 0, sizeof(C.prof));
+  return TG_OK;
+}
+
+int tg_profile_read(tg_context* ctx, tg_profile* out) {
+  if (ctx == nullptr || out == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  C.drain_profile();
+  *out = C.prof;
+  return TG_OK;
+}
+
+int tg_set_graph(tg_context* ctx, int32_t enable) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  ctx->c.use_graph = enable != 0;
+  return TG_OK;
+}
+
+int tg_launch_count(tg_context* ctx, int64_t* count) {
+  if (ctx == nullptr || count == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  *count = ctx->c.launches;
+  return TG_OK;
+}
+
+int tg_synchronize(tg_context* ctx) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  TG_CUDA(&ctx->c, cudaStreamSynchronize(ctx->c.stream));
+  return TG_OK;
+}
+
+int tg_timer_start(tg_context* ctx) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  for (cudaEvent_t& ev : C.timer_ev) {
+    if (ev == nullptr) TG_CUDA(&C, cudaEventCreate(&ev));
+  }
+  TG_CUDA(&C, cudaEventRecord(C.timer_ev[0], C.stream));
+  return TG_OK;
+}
+
+int tg_timer_stop(tg_context* ctx, double* ms) {
+  if (ctx == nullptr || ms == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (C.timer_ev[0] == nullptr) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "timer not started");
+  }
+  TG_CUDA(&C, cudaEventRecord(C.timer_ev[1], C.stream));
+  TG_CUDA(&C, cudaEventSynchronize(C.timer_ev[1]));
+  float f = 0.f;
+  TG_CUDA(&C, cudaEventElapsedTime(&f, C.timer_ev[0], C.timer_ev[1]));
+  *ms = f;
+  return TG_OK;
+}
+
+int tg_host_alloc(size_t bytes, void** out) {
+  if (out == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const cudaError_t e = cudaMallocHost(out, bytes > 0 ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? TG_ERR_OUT_OF_MEMORY : TG_ERR_CUDA;
+  }
+  return TG_OK;
+}
+
+int tg_host_free(void* ptr) {
+  if (ptr != nullptr) cudaFreeHost(ptr);
+  return TG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,140 @@
+// engine.cuh - host-side context of the C ABI and the engine interface that
+// the per-(dimension, form, kernel) templates implement.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace tg {
+
+struct Context;
+
+// Kernel groups timed by the profiler.
+enum Group { kGroupSort = 0, kGroupReorder, kGroupWalls, kGroupForces,
+             kGroupPost, kGroupCount };
+
+struct EngineBase {
+  virtual ~EngineBase() = default;
+  // Allocate the typed state for C.n particles.
+  virtual cudaError_t allocate(Context& C) = 0;
+  // Copy host AoS arrays (upload order) into the home state.
+  // Unpack the staged host arrays (upload order: r, v, rho in d_stage,
+  // d_stage2, d_stage3; dv/dt in d_stage4 when with_dv) into the home state.
+  virtual cudaError_t upload_state(Context& C, bool with_dv) = 0;
+  // Enqueue one full integrator step on C.stream.
+  virtual cudaError_t enqueue_step(Context& C) = 0;
+  // Enqueue FluidEquations::prepare: search + wall extrapolation, leaving
+  // the home state in the new cell order.
+  virtual cudaError_t enqueue_prepare(Context& C) = 0;
+  // Enqueue a pack of one field into the device staging buffer (upload
+  // order).
+  virtual cudaError_t enqueue_pack(Context& C, int field) = 0;
+  // Enqueue the neighbour export (counts/hashes by id; indices at offsets).
+  virtual cudaError_t enqueue_neighbours(Context& C, int32_t* counts,
+                                         uint64_t* hashes,
+                                         const int64_t* offsets,
+                                         int32_t* indices) = 0;
+  // Enqueue search + summation density; outputs by id on the device.
+  virtual cudaError_t enqueue_sumdens(Context& C, int pos_precision,
+                                      double* rho, int32_t* counts,
+                                      uint64_t* hashes) = 0;
+  // Kernel launches of one step.
+  virtual int64_t launches_per_step(Context& C) = 0;
+};
+
+std::unique_ptr<EngineBase> make_engine_2d_f64(int kernel);
+std::unique_ptr<EngineBase> make_engine_2d_f32(int kernel);
+std::unique_ptr<EngineBase> make_engine_3d_f64(int kernel);
+std::unique_ptr<EngineBase> make_engine_3d_f32(int kernel);
+
+struct PendingEvent {
+  int group;
+  cudaEvent_t start, stop;
+};
+
+struct Context {
+  tg_params P{};
+  PhysDev phys{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+
+  // Particles and tanks.
+  int64_t n = 0, n_fluid = 0, n_wall = 0;
+  int32_t ntanks = 0;
+  std::vector<tg_tank> tanks;
+  std::vector<TankDev> tankdev;
+  std::vector<uint32_t> id_base;    // first upload index of each tank
+  std::vector<uint32_t> wall_from;  // first wall upload index of each tank
+  uint32_t total_cells = 0;
+  int key_bits = 0;
+  int k = 1;
+  bool uploaded = false;
+
+  // Common device buffers.
+  TankDev* d_tanks = nullptr;
+  uint32_t* d_id_base = nullptr;
+  uint32_t* d_wall_from = nullptr;
+  uint32_t* d_tank_of = nullptr;  // tank of each upload index
+  double* d_dt = nullptr;
+  double* d_dt_last = nullptr;
+  double* d_time = nullptr;
+  uint32_t* d_err = nullptr;
+  uint32_t* d_wall_count = nullptr;
+  uint32_t* keys_a = nullptr;
+  uint32_t* keys_b = nullptr;
+  uint32_t* vals_a = nullptr;
+  uint32_t* vals_b = nullptr;
+  void* sort_scratch = nullptr;
+  uint32_t* cell_start = nullptr;
+  uint32_t* wall_list = nullptr;
+  double* d_stage = nullptr;  // n * dim doubles: upload / download staging
+  double* d_stage2 = nullptr;
+  double* d_stage3 = nullptr;
+  double* d_stage4 = nullptr;
+  cudaEvent_t timer_ev[2] = {nullptr, nullptr};
+  // Summation-density outputs (by id) and records.
+  double* d_sd_rho = nullptr;
+  int32_t* d_sd_count = nullptr;
+  uint64_t* d_sd_hash = nullptr;
+  void* d_cloud_rec = nullptr;
+
+  std::vector<void*> allocations;  // everything above and the engine's
+  std::unique_ptr<EngineBase> engine;
+
+  // Results of the last sort (set by the engine while enqueueing).
+  const uint32_t* sorted_keys = nullptr;
+  const uint32_t* perm = nullptr;
+
+  // CUDA graph of one step.
+  bool use_graph = true;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_kernels = 0;
+
+  bool walls_fresh = false;
+
+  // Profiling.
+  bool profile = false;
+  tg_profile prof{};
+  std::vector<PendingEvent> pending;
+  std::vector<cudaEvent_t> event_pool;
+
+  int64_t launches = 0;
+  std::string last_error;
+
+  cudaError_t alloc(void** p, size_t bytes);
+  void release_all();
+  void invalidate_graph();
+
+  // Profiling helpers (no-ops unless profile is on and not capturing).
+  int group_begin(int group);
+  void group_end(int token);
+  void drain_profile();
+};
+
+}  // namespace tg

@@ -1,0 +1,12 @@
+// engine_2d_f64.cu - instantiation of the 2D FP64 engines for every
+// smoothing kernel (one translation unit per dimension and form, so the
+// build compiles them in parallel).
+#include "engine_impl.cuh"
+
+namespace tg {
+
+std::unique_ptr<EngineBase> make_engine_2d_f64(int kernel) {
+  return make_engine<2, TG_FP64>(kernel);
+}
+
+}  // namespace tg

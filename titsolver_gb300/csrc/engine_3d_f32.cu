@@ -1,0 +1,12 @@
+// engine_3d_f32.cu - instantiation of the 3D FP32-compensated engines for every
+// smoothing kernel (one translation unit per dimension and form, so the
+// build compiles them in parallel).
+#include "engine_impl.cuh"
+
+namespace tg {
+
+std::unique_ptr<EngineBase> make_engine_3d_f32(int kernel) {
+  return make_engine<3, TG_FP32C>(kernel);
+}
+
+}  // namespace tg

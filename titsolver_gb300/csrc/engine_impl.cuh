@@ -1,0 +1,274 @@
+// engine_impl.cuh - the typed engine: buffer layout and kernel sequencing of
+// one step for a (dimension, arithmetic form, smoothing kernel) triple.
+#pragma once
+
+#include <memory>
+
+#include "engine.cuh"
+#include "fluid.cuh"
+#include "sort.cuh"
+
+namespace tg {
+
+inline unsigned grid_for(int64_t n, int block) {
+  return static_cast<unsigned>((n + block - 1) / block);
+}
+
+template<int D, int F, int K>
+class Engine final : public EngineBase {
+ public:
+  using L = Layout<D, F>;
+  using R = typename L::R;
+  using PosRec = typename L::PosRec;
+  using DatRec = typename L::DatRec;
+
+  cudaError_t allocate(Context& C) override {
+    const int64_t n = C.n > 0 ? C.n : 1;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](auto*& p, int64_t count) {
+      if (e == cudaSuccess) {
+        e = C.alloc(reinterpret_cast<void**>(&p),
+                    static_cast<size_t>(count) * sizeof(*p));
+      }
+    };
+    for (StateBuf<R>* S : {&X_, &Y_}) {
+      for (int k = 0; k < 3; ++k) {
+        S->pos[k] = nullptr;
+        S->vel[k] = nullptr;
+        S->dv[k] = nullptr;
+      }
+      for (int k = 0; k < D; ++k) {
+        A(S->pos[k], n);
+        A(S->vel[k], n);
+        A(S->dv[k], n);
+      }
+      A(S->rho, n);
+      A(S->drho, n);
+      A(S->id, n);
+      A(S->tank, n);
+    }
+    for (StartBuf<R>& U : U_) {
+      for (int k = 0; k < 3; ++k) {
+        U.pos[k] = nullptr;
+        U.vel[k] = nullptr;
+      }
+      for (int k = 0; k < D; ++k) {
+        A(U.pos[k], n);
+        A(U.vel[k], n);
+      }
+      A(U.rho, n);
+    }
+    A(posrec_, n);
+    A(datrec_, n);
+    return e;
+  }
+
+  cudaError_t upload_state(Context& C, bool with_dv) override {
+    if (C.n == 0) return cudaSuccess;
+    k_unpack<D, R><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
+        X_, C.d_stage, C.d_stage2, C.d_stage3, with_dv ? C.d_stage4 : nullptr,
+        C.d_tank_of, C.d_tanks, C.d_wall_from, C.n);
+    C.launches += 1;
+    return cudaGetLastError();
+  }
+
+  cudaError_t enqueue_step(Context& C) override {
+    if (C.n == 0) return cudaSuccess;
+    static const double w3[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
+    static const double w2[2] = {1.0, 1.0 / 2.0};
+    const bool rk2 = C.P.integrator == TG_SSPRK2;
+    const int stages = rk2 ? 2 : 3;
+    const double* w = rk2 ? w2 : w3;
+    for (int s = 0; s < stages; ++s) {
+      cudaError_t e = enqueue_stage(C, s, w[s]);
+      if (e != cudaSuccess) return e;
+    }
+    const int tok = C.group_begin(kGroupForces);
+    k_step_end<<<grid_for(C.ntanks, 128), 128, 0, C.stream>>>(
+        C.d_dt, C.d_dt_last, C.d_time, C.d_err, C.ntanks);
+    C.launches += 1;
+    C.group_end(tok);
+    return cudaGetLastError();
+  }
+
+  cudaError_t enqueue_prepare(Context& C) override {
+    if (C.n == 0) return cudaSuccess;
+    cudaError_t e = enqueue_sort(C);
+    if (e != cudaSuccess) return e;
+    StageArgs<D, F> a = args(C, 0);
+    a.compute_dt = 0;
+    a.carry_derivs = 1;
+    int tok = C.group_begin(kGroupReorder);
+    k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
+    C.launches += 1;
+    C.group_end(tok);
+    tok = C.group_begin(kGroupWalls);
+    if (C.n_wall > 0) {
+      k_walls<D, F, K><<<grid_for(C.n_wall, 128), 128, 0, C.stream>>>(
+          a, C.n_wall);
+      C.launches += 1;
+    }
+    k_commit<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
+    C.launches += 1;
+    C.group_end(tok);
+    return cudaGetLastError();
+  }
+
+  cudaError_t enqueue_pack(Context& C, int field) override {
+    if (C.n == 0) return cudaSuccess;
+    k_pack<D, R><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
+        X_, C.d_tanks, C.phys, field, C.d_stage, C.n);
+    C.launches += 1;
+    return cudaGetLastError();
+  }
+
+  cudaError_t enqueue_neighbours(Context& C, int32_t* counts,
+                                 uint64_t* hashes, const int64_t* offsets,
+                                 int32_t* indices) override {
+    if (C.n == 0) return cudaSuccess;
+    cudaError_t e = enqueue_sort(C);
+    if (e != cudaSuccess) return e;
+    StageArgs<D, F> a = args(C, 0);
+    a.compute_dt = 0;
+    k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
+    k_neigh_count<D, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(
+        a, C.d_id_base, counts, hashes, offsets, indices);
+    C.launches += 2;
+    return cudaGetLastError();
+  }
+
+  cudaError_t enqueue_sumdens(Context& C, int pos_precision, double* rho,
+                              int32_t* counts, uint64_t* hashes) override {
+    if (C.n == 0) return cudaSuccess;
+    cudaError_t e = enqueue_sort(C);
+    if (e != cudaSuccess) return e;
+    const bool f32 = pos_precision == TG_POS_FP32;
+    int tok = C.group_begin(kGroupReorder);
+    if (f32) {
+      k_cloud_records<D, true><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
+          X_.pos[0], X_.pos[1], X_.pos[2], X_.id, X_.tank, C.perm,
+          C.d_cloud_rec, Y_.id, Y_.tank, C.n);
+    } else {
+      k_cloud_records<D, false><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
+          X_.pos[0], X_.pos[1], X_.pos[2], X_.id, X_.tank, C.perm,
+          C.d_cloud_rec, Y_.id, Y_.tank, C.n);
+    }
+    C.launches += 1;
+    C.group_end(tok);
+    CloudArgs<D> ca{C.d_cloud_rec, Y_.id,  Y_.tank, C.cell_start, C.d_tanks,
+                    C.n,           C.k,    rho,     counts,       hashes,
+                    C.d_id_base};
+    tok = C.group_begin(kGroupForces);
+    if (f32) {
+      k_sumdens<D, K, true><<<grid_for(C.n, 128), 128, 0, C.stream>>>(ca);
+    } else {
+      k_sumdens<D, K, false><<<grid_for(C.n, 128), 128, 0, C.stream>>>(ca);
+    }
+    C.launches += 1;
+    C.group_end(tok);
+    return cudaGetLastError();
+  }
+
+  int64_t launches_per_step(Context& C) override {
+    const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
+    const int stages = C.P.integrator == TG_SSPRK2 ? 2 : 3;
+    const int per_stage = 1 + 3 * passes + 1 + 2 + (C.n_wall > 0 ? 1 : 0);
+    return static_cast<int64_t>(stages) * per_stage + 1;
+  }
+
+ private:
+  StageArgs<D, F> args(Context& C, int stage) {
+    StageArgs<D, F> a{};
+    a.X = X_;
+    a.Y = Y_;
+    a.Usrc = U_[(stage + 1) % 2];
+    a.Udst = U_[stage % 2];
+    a.perm = C.perm;
+    a.posrec = posrec_;
+    a.datrec = datrec_;
+    a.cell_start = C.cell_start;
+    a.tanks = C.d_tanks;
+    a.phys = C.phys;
+    a.dt = C.d_dt;
+    a.wall_list = C.wall_list;
+    a.wall_count = C.d_wall_count;
+    a.err = C.d_err;
+    a.n = C.n;
+    a.k = C.k;
+    a.copy_start = stage == 0 ? 1 : 0;
+    a.compute_dt = stage == 0 ? 1 : 0;
+    a.lincomb = stage == 0 ? 0 : 1;
+    a.w_new = 1.0;
+    a.kahan = C.P.kahan;
+    a.carry_derivs = 0;
+    return a;
+  }
+
+  cudaError_t enqueue_sort(Context& C) {
+    const int tok = C.group_begin(kGroupSort);
+    k_keys<D><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
+        X_.pos[0], X_.pos[1], X_.pos[2], X_.tank, C.d_tanks, C.n, C.keys_a,
+        C.d_err, C.d_wall_count);
+    C.launches += 1;
+    bool in_b = false;
+    cudaError_t e = radix_sort(C.keys_a, C.vals_a, C.keys_b, C.vals_b, C.n,
+                               C.key_bits, true, C.sort_scratch, &in_b,
+                               C.stream, &C.launches);
+    if (e != cudaSuccess) return e;
+    C.sorted_keys = in_b ? C.keys_b : C.keys_a;
+    C.perm = in_b ? C.vals_b : C.vals_a;
+    e = build_cell_table(C.sorted_keys, C.n, C.total_cells, C.cell_start,
+                         C.stream, &C.launches);
+    C.group_end(tok);
+    return e;
+  }
+
+  cudaError_t enqueue_stage(Context& C, int s, double w) {
+    cudaError_t e = enqueue_sort(C);
+    if (e != cudaSuccess) return e;
+    StageArgs<D, F> a = args(C, s);
+    a.w_new = w;
+    int tok = C.group_begin(kGroupReorder);
+    k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
+    C.launches += 1;
+    C.group_end(tok);
+    if (C.n_wall > 0) {
+      tok = C.group_begin(kGroupWalls);
+      k_walls<D, F, K><<<grid_for(C.n_wall, 128), 128, 0, C.stream>>>(
+          a, C.n_wall);
+      C.launches += 1;
+      C.group_end(tok);
+    }
+    tok = C.group_begin(kGroupForces);
+    k_forces<D, F, K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+    C.launches += 1;
+    C.group_end(tok);
+    return cudaGetLastError();
+  }
+
+  StateBuf<R> X_{}, Y_{};
+  StartBuf<R> U_[2]{};
+  PosRec* posrec_ = nullptr;
+  DatRec* datrec_ = nullptr;
+};
+
+template<int D, int F>
+std::unique_ptr<EngineBase> make_engine(int kernel) {
+  switch (kernel) {
+    case TG_KERNEL_CUBIC_SPLINE:
+      return std::make_unique<Engine<D, F, TG_KERNEL_CUBIC_SPLINE>>();
+    case TG_KERNEL_QUARTIC_SPLINE:
+      return std::make_unique<Engine<D, F, TG_KERNEL_QUARTIC_SPLINE>>();
+    case TG_KERNEL_QUINTIC_SPLINE:
+      return std::make_unique<Engine<D, F, TG_KERNEL_QUINTIC_SPLINE>>();
+    case TG_KERNEL_WENDLAND_C2:
+      return std::make_unique<Engine<D, F, TG_KERNEL_WENDLAND_C2>>();
+    case TG_KERNEL_WENDLAND_C4:
+      return std::make_unique<Engine<D, F, TG_KERNEL_WENDLAND_C4>>();
+    case TG_KERNEL_WENDLAND_C6:
+      return std::make_unique<Engine<D, F, TG_KERNEL_WENDLAND_C6>>();
+    default: return nullptr;
+  }
+}
+
+}  // namespace tg

@@ -1,0 +1,951 @@
+// fluid.cuh - stage kernels of the GB300 WCSPH step, templated on dimension
+// (D = 2, 3), arithmetic form (TG_FP64, TG_FP32C) and smoothing kernel K.
+//
+// One stage of the reference's SSPRK substep (time_integrator.hpp:190-210:
+// prepare, [dt], continuity, momentum, Euler update; then lincomb) runs as:
+//   k_keys      cell key of every particle (FP64 positions)
+//   radix sort  stable, 32-bit keys (sort.cu)
+//   k_cell_table
+//   k_reorder   gather the state into cell order, pack neighbour records,
+//               Tait p, cs (+ the dt min-reduction in the first stage)
+//   k_walls     Shepard extrapolation of the wall density
+//               (FluidEquations::setup_boundary, fluid_equations.hpp:122-164)
+//   k_forces    fused continuity + momentum sums in gather form, Euler
+//               update and SSPRK linear combination
+//               (fluid_equations.hpp:232-305, time_integrator.hpp:203-223)
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+
+#include "common.cuh"
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Records.
+struct alignas(16) Pos64_2 { double x, y; };
+struct alignas(32) Pos64_3 { double x, y, z, w; };
+struct alignas(32) Dat64 { double vx, vy, vz, rho, P, c, invrho, pad; };
+struct alignas(8) Pos32_2 { float x, y; };
+struct alignas(16) Pos32_3 { float x, y, z, w; };
+struct alignas(32) Dat32 { float vx, vy, vz, drho, P, c, invrho, pad; };
+
+template<int D, int F>
+struct Layout;
+template<int D>
+struct Layout<D, TG_FP64> {
+  using R = double;
+  using PosRec = std::conditional_t<D == 2, Pos64_2, Pos64_3>;
+  using DatRec = Dat64;
+};
+template<int D>
+struct Layout<D, TG_FP32C> {
+  using R = float;
+  using PosRec = std::conditional_t<D == 2, Pos32_2, Pos32_3>;
+  using DatRec = Dat32;
+};
+
+__device__ __forceinline__ void load_pos(const Pos64_2* p, uint32_t j,
+                                         double* x) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p + j));
+  x[0] = a.x;
+  x[1] = a.y;
+}
+__device__ __forceinline__ void load_pos(const Pos64_3* p, uint32_t j,
+                                         double* x) {
+  const double2* q = reinterpret_cast<const double2*>(p + j);
+  const double2 a = __ldg(q), b = __ldg(q + 1);
+  x[0] = a.x;
+  x[1] = a.y;
+  x[2] = b.x;
+}
+__device__ __forceinline__ void load_pos(const Pos32_2* p, uint32_t j,
+                                         float* x) {
+  const float2 a = __ldg(reinterpret_cast<const float2*>(p + j));
+  x[0] = a.x;
+  x[1] = a.y;
+}
+__device__ __forceinline__ void load_pos(const Pos32_3* p, uint32_t j,
+                                         float* x) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p + j));
+  x[0] = a.x;
+  x[1] = a.y;
+  x[2] = a.z;
+}
+__device__ __forceinline__ Dat64 load_dat(const Dat64* p, uint32_t j) {
+  const double2* q = reinterpret_cast<const double2*>(p + j);
+  const double2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2),
+                d = __ldg(q + 3);
+  return Dat64{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y};
+}
+__device__ __forceinline__ Dat32 load_dat(const Dat32* p, uint32_t j) {
+  const float4* q = reinterpret_cast<const float4*>(p + j);
+  const float4 a = __ldg(q), b = __ldg(q + 1);
+  return Dat32{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+}
+// Coherent (non-__ldg) loads for kernels that also write the record array.
+__device__ __forceinline__ Dat64 load_dat_coherent(const Dat64* p,
+                                                   uint32_t j) {
+  return p[j];
+}
+__device__ __forceinline__ Dat32 load_dat_coherent(const Dat32* p,
+                                                   uint32_t j) {
+  return p[j];
+}
+
+// ---------------------------------------------------------------------------
+// Buffers.
+template<class R>
+struct StateBuf {
+  double* pos[3];
+  R* vel[3];
+  R* rho;  // FP64: rho; FP32C: rho - rho0
+  R* dv[3];
+  R* drho;
+  uint32_t* id;  // upload index | kWallBit for walls
+  uint32_t* tank;
+};
+
+template<class R>
+struct StartBuf {
+  double* pos[3];
+  R* vel[3];
+  R* rho;
+};
+
+template<int D, int F>
+struct StageArgs {
+  using L = Layout<D, F>;
+  using R = typename L::R;
+  StateBuf<R> X, Y;
+  StartBuf<R> Usrc, Udst;
+  const uint32_t* perm;
+  typename L::PosRec* posrec;
+  typename L::DatRec* datrec;
+  const uint32_t* cell_start;
+  const TankDev* tanks;
+  PhysDev phys;
+  double* dt;
+  uint32_t* wall_list;
+  uint32_t* wall_count;
+  uint32_t* err;
+  int64_t n;
+  int k;             // cells per radius
+  int copy_start;    // stage 0: Udst = current state
+  int compute_dt;    // stage 0: min-reduce dt
+  int lincomb;       // apply (1 - w) Udst + w new
+  double w_new;
+  int kahan;
+  int carry_derivs;  // also gather dv/dt and drho/dt into Y
+};
+
+// ---------------------------------------------------------------------------
+// Neighbour-cell traversal over the (2k+1)^D block of cells around c,
+// clipped to the tank grid.  Merged: one [begin, end) range per row of
+// cells (rows are contiguous in cell order).  Per cell: one range per cell
+// with its cell offset (dx, dy, dz) relative to c.
+template<int D, bool PerCell, class Fn>
+__device__ __forceinline__ void for_cells(const TankDev& T, const int* c,
+                                          int k,
+                                          const uint32_t* __restrict__ cstart,
+                                          Fn&& fn) {
+  const int nx = T.nc[0], ny = T.nc[1];
+  const int zlo = D == 3 ? max(c[2] - k, 0) : 0;
+  const int zhi = D == 3 ? min(c[2] + k, T.nc[2] - 1) : 0;
+  const int ylo = max(c[1] - k, 0), yhi = min(c[1] + k, ny - 1);
+  const int xlo = max(c[0] - k, 0), xhi = min(c[0] + k, nx - 1);
+  for (int z = zlo; z <= zhi; ++z) {
+    for (int y = ylo; y <= yhi; ++y) {
+      const uint32_t row =
+          T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx;
+      if constexpr (!PerCell) {
+        fn(__ldg(cstart + row + xlo), __ldg(cstart + row + xhi + 1), 0, 0, 0);
+      } else {
+        uint32_t s = __ldg(cstart + row + xlo);
+        for (int x = xlo; x <= xhi; ++x) {
+          const uint32_t e = __ldg(cstart + row + x + 1);
+          fn(s, e, x - c[0], y - c[1], D == 3 ? z - c[2] : 0);
+          s = e;
+        }
+      }
+    }
+  }
+}
+
+// Bit-exact squared distance: d = a - b per axis, then
+// (d0*d0 + d1*d1) + d2*d2, every operation rounded (no FMA contraction),
+// as the oracle's BSphere::contains restatement.
+template<int D>
+__device__ __forceinline__ double dist2_exact(const double* a,
+                                              const double* b, double* d) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) d[k] = __dsub_rn(a[k], b[k]);
+  double s = __dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1]));
+  if constexpr (D == 3) s = __dadd_rn(s, __dmul_rn(d[2], d[2]));
+  return s;
+}
+template<int D>
+__device__ __forceinline__ float dist2_exact(const float* a, const float* b,
+                                             float* d) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) d[k] = __fsub_rn(a[k], b[k]);
+  float s = __fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1]));
+  if constexpr (D == 3) s = __fadd_rn(s, __fmul_rn(d[2], d[2]));
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+template<int D>
+__global__ void __launch_bounds__(256)
+    k_keys(const double* __restrict__ px,
+           const double* __restrict__ py, const double* __restrict__ pz,
+           const uint32_t* __restrict__ tank, const TankDev* __restrict__ tanks,
+           int64_t n, uint32_t* __restrict__ keys, uint32_t* err,
+           uint32_t* wall_count) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i == 0 && wall_count != nullptr) *wall_count = 0;
+  if (i >= n) return;
+  const TankDev& T = tanks[tank[i]];
+  double p[3] = {px[i], py[i], D == 3 ? pz[i] : 0.0};
+  int c[3] = {0, 0, 0};
+  bool outside = false;
+  cell_of<D>(T, p, c, outside);
+  keys[i] = flat_cell<D>(T, c);
+  if (outside) {
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) finite = finite && isfinite(p[k]);
+    atomicOr(err, finite ? static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID)
+                         : static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
+  }
+}
+
+// ---------------------------------------------------------------------------
+template<int D, int F>
+__global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
+  using R = typename StageArgs<D, F>::R;
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool valid = j < A.n;
+  double dt_a = __longlong_as_double(0x7ff0000000000000ll);
+  uint32_t tk = 0xffffffffu;
+  if (valid) {
+    const uint32_t src = A.perm[j];
+    double p[3];
+    R v[3];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      p[k] = A.X.pos[k][src];
+      v[k] = A.X.vel[k][src];
+    }
+    const R rho = A.X.rho[src];
+    const uint32_t id = A.X.id[src];
+    tk = A.X.tank[src];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      A.Y.pos[k][j] = p[k];
+      A.Y.vel[k][j] = v[k];
+    }
+    A.Y.rho[j] = rho;
+    A.Y.id[j] = id;
+    A.Y.tank[j] = tk;
+    if (A.carry_derivs) {
+#pragma unroll
+      for (int k = 0; k < D; ++k) A.Y.dv[k][j] = A.X.dv[k][src];
+      A.Y.drho[j] = A.X.drho[src];
+    }
+    if (A.copy_start) {
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        A.Udst.pos[k][j] = p[k];
+        A.Udst.vel[k][j] = v[k];
+      }
+      A.Udst.rho[j] = rho;
+    } else {
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        A.Udst.pos[k][j] = A.Usrc.pos[k][src];
+        A.Udst.vel[k][j] = A.Usrc.vel[k][src];
+      }
+      A.Udst.rho[j] = A.Usrc.rho[src];
+    }
+    const TankDev& T = A.tanks[tk];
+    // Neighbour position record.
+    if constexpr (F == TG_FP64) {
+      if constexpr (D == 2) {
+        A.posrec[j] = Pos64_2{p[0], p[1]};
+      } else {
+        A.posrec[j] = Pos64_3{p[0], p[1], p[2], 0.0};
+      }
+    } else {
+      int c[3] = {0, 0, 0};
+      bool outside = false;
+      cell_of<D>(T, p, c, outside);
+      float o[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        o[k] = static_cast<float>(p[k] - (T.lo[k] + c[k] * T.cs));
+      }
+      if constexpr (D == 2) {
+        A.posrec[j] = Pos32_2{o[0], o[1]};
+      } else {
+        A.posrec[j] = Pos32_3{o[0], o[1], o[2], 0.f};
+      }
+    }
+    if (id & kWallBit) {
+      const uint32_t slot = atomicAdd(A.wall_count, 1u);
+      A.wall_list[slot] = static_cast<uint32_t>(j);
+    } else {
+      // Tait state of the fluid particle.
+      if constexpr (F == TG_FP64) {
+        double pr, c;
+        tait_f64(A.phys, T, rho, pr, c);
+        const double inv = 1.0 / rho;
+        A.datrec[j] = Dat64{v[0], v[1], D == 3 ? v[2] : 0.0, rho,
+                            pr * inv * inv, c, inv, 0.0};
+        if (A.compute_dt) {
+          double dvv[3];
+#pragma unroll
+          for (int k = 0; k < D; ++k) dvv[k] = A.X.dv[k][src];
+          double v2 = v[0] * v[0] + v[1] * v[1];
+          double a2 = dvv[0] * dvv[0] + dvv[1] * dvv[1];
+          if constexpr (D == 3) {
+            v2 += v[2] * v[2];
+            a2 += dvv[2] * dvv[2];
+          }
+          const double h = T.h;
+          const double dt_ac = A.phys.cfl * h / (c + sqrt(v2));
+          const double dt_vi = A.phys.c_visc * h * h * rho / A.phys.mu;
+          const double dt_fo =
+              A.phys.c_force * sqrt(h / fmax(sqrt(a2), A.phys.g));
+          dt_a = fmin(dt_ac, fmin(dt_vi, dt_fo));
+        }
+      } else {
+        float pr, c;
+        tait_f32(A.phys, T, rho, pr, c);
+        const float inv = 1.f / (static_cast<float>(T.rho0) + rho);
+        A.datrec[j] = Dat32{v[0], v[1], D == 3 ? v[2] : 0.f, rho,
+                            pr * inv * inv, c, inv, 0.f};
+        if (A.compute_dt) {
+          float dvv[3];
+#pragma unroll
+          for (int k = 0; k < D; ++k) dvv[k] = A.X.dv[k][src];
+          float v2 = v[0] * v[0] + v[1] * v[1];
+          float a2 = dvv[0] * dvv[0] + dvv[1] * dvv[1];
+          if constexpr (D == 3) {
+            v2 += v[2] * v[2];
+            a2 += dvv[2] * dvv[2];
+          }
+          const float h = static_cast<float>(T.h);
+          const float rhof = static_cast<float>(T.rho0) + rho;
+          const float dt_ac = static_cast<float>(A.phys.cfl) * h / (c + sqrtf(v2));
+          const float dt_vi =
+              static_cast<float>(A.phys.c_visc) * h * h * rhof /
+              static_cast<float>(A.phys.mu);
+          const float dt_fo =
+              static_cast<float>(A.phys.c_force) *
+              sqrtf(h / fmaxf(sqrtf(a2), static_cast<float>(A.phys.g)));
+          dt_a = static_cast<double>(fminf(dt_ac, fminf(dt_vi, dt_fo)));
+        }
+      }
+    }
+  }
+  if (A.compute_dt) {
+    // Warp-level min when the whole warp is in one tank, else per lane.
+    const uint32_t t0 = __shfl_sync(0xffffffffu, tk, 0);
+    if (__all_sync(0xffffffffu, tk == t0 || tk == 0xffffffffu)) {
+      double m = dt_a;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+      }
+      if ((threadIdx.x & 31) == 0 && t0 != 0xffffffffu &&
+          m < __longlong_as_double(0x7ff0000000000000ll)) {
+        atomic_min_pos(A.dt + t0, m);
+      }
+    } else if (valid && dt_a < __longlong_as_double(0x7ff0000000000000ll)) {
+      atomic_min_pos(A.dt + tk, dt_a);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Wall extrapolation (fluid_equations.hpp:122-164) with a zero wall normal:
+//   rho_e = rho(H),  H = sum_b V_b H(rho_b) W_be / sum_b V_b W_be over fluid
+//   neighbours b (H = 0 when the Shepard sum is tiny); v_e = 0.
+template<int D, int F, int K>
+__global__ void __launch_bounds__(128)
+    k_walls(StageArgs<D, F> A, int64_t n_walls) {
+  using R = typename StageArgs<D, F>::R;
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n_walls) return;
+  const uint32_t e = A.wall_list[t];
+  const uint32_t tk = A.Y.tank[e];
+  const TankDev& T = A.tanks[tk];
+  double pe[3] = {A.Y.pos[0][e], A.Y.pos[1][e], D == 3 ? A.Y.pos[2][e] : 0.0};
+  int c[3] = {0, 0, 0};
+  bool outside = false;
+  cell_of<D>(T, pe, c, outside);
+  R rho_e;
+  if constexpr (F == TG_FP64) {
+    const double R2 = T.radius2, hinv = T.hinv, w = T.w, m = T.m;
+    double S = 0.0, H = 0.0;
+    for_cells<D, false>(T, c, A.k, A.cell_start,
+                        [&](uint32_t s, uint32_t en, int, int, int) {
+      for (uint32_t j = s; j < en; ++j) {
+        if (A.Y.id[j] & kWallBit) continue;
+        double pb[3], d[3];
+        load_pos(A.posrec, j, pb);
+        const double s2 = dist2_exact<D>(pb, pe, d);
+        if (s2 > R2) continue;
+        const Dat64 b = load_dat_coherent(A.datrec, j);
+        const double q = sqrt(s2) * hinv;
+        const double W = w * KernelPoly<K>::value(q);
+        const double Vb = m * b.invrho;
+        const double Hb = potential_f64(A.phys, T, b.rho);
+        S += Vb * W;
+        H += Vb * Hb * W;
+      }
+    });
+    const double Hs = fabs(S) <= 6.0554544523933395e-06 ? 0.0 : H / S;
+    rho_e = density_from_potential_f64(A.phys, T, Hs);
+    double pr, cc;
+    tait_f64(A.phys, T, rho_e, pr, cc);
+    const double inv = 1.0 / rho_e;
+    A.datrec[e] = Dat64{0.0, 0.0, 0.0, rho_e, pr * inv * inv, cc, inv, 0.0};
+  } else {
+    const float R2 = T.radius2_f, hinv = static_cast<float>(T.hinv);
+    const float w = static_cast<float>(T.w), m = static_cast<float>(T.m);
+    const float csz = T.cs_f;
+    float oe[3] = {0.f, 0.f, 0.f};
+    load_pos(A.posrec, e, oe);
+    Kahan S, H;
+    for_cells<D, true>(T, c, A.k, A.cell_start,
+                       [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      float oes[3];
+      oes[0] = oe[0] - dx * csz;
+      oes[1] = oe[1] - dy * csz;
+      oes[2] = D == 3 ? oe[2] - dz * csz : 0.f;
+      for (uint32_t j = s; j < en; ++j) {
+        if (A.Y.id[j] & kWallBit) continue;
+        float ob[3], d[3];
+        load_pos(A.posrec, j, ob);
+        const float s2 = dist2_exact<D>(oes, ob, d);
+        if (s2 > R2) continue;
+        const Dat32 b = load_dat_coherent(A.datrec, j);
+        const float q = sqrtf(s2) * hinv;
+        const float W = w * KernelPoly<K>::value(q);
+        const float Vb = m * b.invrho;
+        const float Hb = potential_f32(A.phys, T, b.drho);
+        S.add(Vb * W);
+        H.add(Vb * Hb * W);
+      }
+    });
+    const float Ss = S.value();
+    const float Hs = fabsf(Ss) <= 6.0554544523933395e-06f ? 0.f : H.value() / Ss;
+    rho_e = deviation_from_potential_f32(A.phys, T, Hs);
+    float pr, cc;
+    tait_f32(A.phys, T, rho_e, pr, cc);
+    const float inv = 1.f / (static_cast<float>(T.rho0) + rho_e);
+    A.datrec[e] = Dat32{0.f, 0.f, 0.f, rho_e, pr * inv * inv, cc, inv, 0.f};
+  }
+  // The wall's home state.
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    A.X.pos[k][e] = pe[k];
+    A.X.vel[k][e] = R(0);
+    A.X.dv[k][e] = R(0);
+  }
+  A.X.rho[e] = rho_e;
+  A.X.drho[e] = R(0);
+  A.X.id[e] = A.Y.id[e];
+  A.X.tank[e] = tk;
+}
+
+// ---------------------------------------------------------------------------
+// Fused continuity + momentum + update, gather form.  For a fluid target a
+// and every neighbour b != a (walls included):
+//   drho_a += m F [ v_ab . r_ab + D_ab ],            grad W_ab = F r_ab
+//   dv_a   += m (Pi_ab - P_ab) F r_ab,               dv_a starts at -g e_1
+// with P_ab = p_a/rho_a^2 + p_b/rho_b^2 and
+//   Ferrari  D_ab = max(c_a, c_b)(rho_a - rho_b) |r_ab| / rho_b
+//   Molteni  D_ab = 2 delta h c0 (rho_a - rho_b) / rho_b
+//   Morris   Pi_ab = 2 mu (v_ab . r_ab) / (rho_a rho_b |r_ab|^2)
+//   Monaghan Pi_ab = alpha h (c_a+c_b) (v_ab.r_ab) / ((|r|^2 + 0.01h^2)
+//                    (rho_a+rho_b)) for v_ab . r_ab < 0, else 0
+// then r' = r + dt v, v' = v + dt dv, rho' = rho + dt drho and, in the later
+// SSPRK stages, u = (1 - w) u_n + w u'.
+template<int D, int F, int K>
+__global__ void __launch_bounds__(128, 4) k_forces(StageArgs<D, F> A) {
+  using R = typename StageArgs<D, F>::R;
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const uint32_t id = A.Y.id[i];
+  if (id & kWallBit) return;
+  const uint32_t tk = A.Y.tank[i];
+  const TankDev& T = A.tanks[tk];
+  double pa[3] = {A.Y.pos[0][i], A.Y.pos[1][i], D == 3 ? A.Y.pos[2][i] : 0.0};
+  int c[3] = {0, 0, 0};
+  bool outside = false;
+  cell_of<D>(T, pa, c, outside);
+  const int visc = A.phys.viscosity, diff = A.phys.diffusion;
+  R dv_out[3];
+  R drho_out;
+  R va[3];
+  R rho_self;
+  if constexpr (F == TG_FP64) {
+    const Dat64 a = load_dat(A.datrec, static_cast<uint32_t>(i));
+    va[0] = a.vx;
+    va[1] = a.vy;
+    va[2] = a.vz;
+    rho_self = a.rho;
+    const double R2 = T.radius2, hinv = T.hinv, wg = T.wg, m = T.m;
+    const double mu2 = 2.0 * A.phys.mu, ah = A.phys.alpha * T.h;
+    const double eps2 = T.visc_eps2, dk = T.diff_k;
+    double drho = 0.0;
+    double dv[3] = {0.0, -A.phys.g, 0.0};
+    for_cells<D, false>(T, c, A.k, A.cell_start,
+                        [&](uint32_t s, uint32_t en, int, int, int) {
+      for (uint32_t j = s; j < en; ++j) {
+        if (j == static_cast<uint32_t>(i)) continue;
+        double pb[3], d[3];
+        load_pos(A.posrec, j, pb);
+        const double s2 = dist2_exact<D>(pa, pb, d);
+        if (s2 > R2) continue;
+        const Dat64 b = load_dat(A.datrec, j);
+        const double rinv = rsqrt(s2);
+        const double r = s2 * rinv;
+        const double q = r * hinv;
+        const double Fk = grad_factor<K>(q, rinv, wg, hinv);
+        const double vb[3] = {b.vx, b.vy, b.vz};
+        double vd = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) vd += (va[k] - vb[k]) * d[k];
+        const double drab = a.rho - b.rho;
+        double cont = vd;
+        if (diff == TG_DIFF_FERRARI) {
+          cont += fmax(a.c, b.c) * drab * r * b.invrho;
+        } else if (diff == TG_DIFF_MOLTENI) {
+          cont += dk * drab * b.invrho;
+        }
+        drho += m * Fk * cont;
+        double Pi;
+        if (visc == TG_VISC_MORRIS) {
+          Pi = mu2 * vd * a.invrho * b.invrho * (rinv * rinv);
+        } else {
+          Pi = vd < 0.0 ? ah * vd * (a.c + b.c) /
+                              ((s2 + eps2) * (a.rho + b.rho))
+                        : 0.0;
+        }
+        const double coef = m * (Pi - (a.P + b.P)) * Fk;
+#pragma unroll
+        for (int k = 0; k < D; ++k) dv[k] += coef * d[k];
+      }
+    });
+#pragma unroll
+    for (int k = 0; k < D; ++k) dv_out[k] = dv[k];
+    drho_out = drho;
+  } else {
+    const Dat32 a = load_dat(A.datrec, static_cast<uint32_t>(i));
+    va[0] = a.vx;
+    va[1] = a.vy;
+    va[2] = a.vz;
+    rho_self = a.drho;
+    float oa[3] = {0.f, 0.f, 0.f};
+    load_pos(A.posrec, static_cast<uint32_t>(i), oa);
+    const float R2 = T.radius2_f, hinv = static_cast<float>(T.hinv);
+    const float wg = static_cast<float>(T.wg), m = static_cast<float>(T.m);
+    const float mu2 = static_cast<float>(2.0 * A.phys.mu);
+    const float ah = static_cast<float>(A.phys.alpha * T.h);
+    const float eps2 = static_cast<float>(T.visc_eps2);
+    const float dk = static_cast<float>(T.diff_k);
+    const float rho0x2 = static_cast<float>(2.0 * T.rho0);
+    const float csz = T.cs_f;
+    const bool kahan = A.kahan != 0;
+    Kahan drho;
+    Kahan dv[3];
+    dv[1].s = static_cast<float>(-A.phys.g);
+    for_cells<D, true>(T, c, A.k, A.cell_start,
+                       [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      float oas[3];
+      oas[0] = oa[0] - dx * csz;
+      oas[1] = oa[1] - dy * csz;
+      oas[2] = D == 3 ? oa[2] - dz * csz : 0.f;
+      for (uint32_t j = s; j < en; ++j) {
+        if (j == static_cast<uint32_t>(i)) continue;
+        float ob[3], d[3];
+        load_pos(A.posrec, j, ob);
+#pragma unroll
+        for (int k = 0; k < D; ++k) d[k] = oas[k] - ob[k];
+        float s2 = d[0] * d[0] + d[1] * d[1];
+        if constexpr (D == 3) s2 += d[2] * d[2];
+        if (s2 > R2) continue;
+        const Dat32 b = load_dat(A.datrec, j);
+        const float rinv = rsqrtf(s2);
+        const float r = s2 * rinv;
+        const float q = r * hinv;
+        const float Fk = grad_factor<K>(q, rinv, wg, hinv);
+        const float vb[3] = {b.vx, b.vy, b.vz};
+        float vd = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) vd += (va[k] - vb[k]) * d[k];
+        const float drab = a.drho - b.drho;
+        float cont = vd;
+        if (diff == TG_DIFF_FERRARI) {
+          cont += fmaxf(a.c, b.c) * drab * r * b.invrho;
+        } else if (diff == TG_DIFF_MOLTENI) {
+          cont += dk * drab * b.invrho;
+        }
+        const float dr = m * Fk * cont;
+        float Pi;
+        if (visc == TG_VISC_MORRIS) {
+          Pi = mu2 * vd * a.invrho * b.invrho * (rinv * rinv);
+        } else {
+          Pi = vd < 0.f ? __fdividef(ah * vd * (a.c + b.c),
+                                     (s2 + eps2) * (rho0x2 + a.drho + b.drho))
+                        : 0.f;
+        }
+        const float coef = m * (Pi - (a.P + b.P)) * Fk;
+        if (kahan) {
+          drho.add(dr);
+#pragma unroll
+          for (int k = 0; k < D; ++k) dv[k].add(coef * d[k]);
+        } else {
+          drho.s += dr;
+#pragma unroll
+          for (int k = 0; k < D; ++k) dv[k].s += coef * d[k];
+        }
+      }
+    });
+#pragma unroll
+    for (int k = 0; k < D; ++k) dv_out[k] = dv[k].value();
+    drho_out = drho.value();
+  }
+
+  // Euler update (time_integrator.hpp:203-207) and SSPRK lincomb (:212-223).
+  const double dt = A.dt[tk];
+  const R dtr = static_cast<R>(dt);
+  double pn[3];
+  R vn[3];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    pn[k] = pa[k] + dt * static_cast<double>(va[k]);
+    vn[k] = va[k] + dtr * dv_out[k];
+  }
+  R rn = rho_self + dtr * drho_out;
+  if (A.lincomb) {
+    const double w = A.w_new, w0 = 1.0 - A.w_new;
+    const R wr = static_cast<R>(w), w0r = static_cast<R>(w0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      pn[k] = w0 * A.Udst.pos[k][i] + w * pn[k];
+      vn[k] = w0r * A.Udst.vel[k][i] + wr * vn[k];
+    }
+    rn = w0r * A.Udst.rho[i] + wr * rn;
+  }
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    A.X.pos[k][i] = pn[k];
+    A.X.vel[k][i] = vn[k];
+    A.X.dv[k][i] = dv_out[k];
+  }
+  A.X.rho[i] = rn;
+  A.X.drho[i] = drho_out;
+  A.X.id[i] = id;
+  A.X.tank[i] = tk;
+  bool finite = isfinite(static_cast<double>(rn));
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    finite = finite && isfinite(pn[k]) && isfinite(static_cast<double>(vn[k]));
+  }
+  if (!finite) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour export: counts and order-independent hashes of the neighbour
+// set (tank-local upload ids), with the same predicate as k_forces.
+template<int D, int F>
+__global__ void __launch_bounds__(128)
+    k_neigh_count(StageArgs<D, F> A, const uint32_t* __restrict__ id_base,
+                  int32_t* __restrict__ counts, uint64_t* __restrict__ hashes,
+                  const int64_t* __restrict__ offsets,
+                  int32_t* __restrict__ indices) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const uint32_t id = A.Y.id[i] & kIdMask;
+  const uint32_t tk = A.Y.tank[i];
+  const TankDev& T = A.tanks[tk];
+  const uint32_t base = id_base[tk];
+  double pa[3] = {A.Y.pos[0][i], A.Y.pos[1][i], D == 3 ? A.Y.pos[2][i] : 0.0};
+  int c[3] = {0, 0, 0};
+  bool outside = false;
+  cell_of<D>(T, pa, c, outside);
+  int32_t cnt = 0;
+  uint64_t hs = 0;
+  int64_t out = offsets != nullptr ? offsets[id] : 0;
+  if constexpr (F == TG_FP64) {
+    for_cells<D, false>(T, c, A.k, A.cell_start,
+                        [&](uint32_t s, uint32_t en, int, int, int) {
+      for (uint32_t j = s; j < en; ++j) {
+        double pb[3], d[3];
+        load_pos(A.posrec, j, pb);
+        if (dist2_exact<D>(pb, pa, d) > T.radius2) continue;
+        const uint32_t lid = (A.Y.id[j] & kIdMask) - base;
+        ++cnt;
+        hs += splitmix64(static_cast<uint64_t>(lid) + 1u);
+        if (indices != nullptr) indices[out++] = static_cast<int32_t>(lid);
+      }
+    });
+  } else {
+    float oa[3] = {0.f, 0.f, 0.f};
+    load_pos(A.posrec, static_cast<uint32_t>(i), oa);
+    const float csz = T.cs_f;
+    for_cells<D, true>(T, c, A.k, A.cell_start,
+                       [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      float oas[3];
+      oas[0] = oa[0] - dx * csz;
+      oas[1] = oa[1] - dy * csz;
+      oas[2] = D == 3 ? oa[2] - dz * csz : 0.f;
+      for (uint32_t j = s; j < en; ++j) {
+        float ob[3], d[3];
+        load_pos(A.posrec, j, ob);
+#pragma unroll
+        for (int k = 0; k < D; ++k) d[k] = oas[k] - ob[k];
+        float s2 = d[0] * d[0] + d[1] * d[1];
+        if constexpr (D == 3) s2 += d[2] * d[2];
+        if (s2 > T.radius2_f) continue;
+        const uint32_t lid = (A.Y.id[j] & kIdMask) - base;
+        ++cnt;
+        hs += splitmix64(static_cast<uint64_t>(lid) + 1u);
+        if (indices != nullptr) indices[out++] = static_cast<int32_t>(lid);
+      }
+    });
+  }
+  if (counts != nullptr) counts[id] = cnt;
+  if (hashes != nullptr) hashes[id] = hs;
+}
+
+// ---------------------------------------------------------------------------
+// Summation density over a point cloud (fluid_equations.hpp:498-502 form,
+// self included): rho_a = sum_b m W_ab, with neighbour counts and hashes.
+// FP64 positions: FP64 predicate and sum.  FP32 positions: the positions are
+// rounded to float once; predicate and kernel in FP32, compensated sum.
+template<int D>
+struct CloudArgs {
+  const void* pos;  // Pos64_* or Pos32_* absolute positions, cell order
+  const uint32_t* id;
+  const uint32_t* tank;
+  const uint32_t* cell_start;
+  const TankDev* tanks;
+  int64_t n;
+  int k;
+  double* rho;       // by upload id
+  int32_t* counts;   // by upload id
+  uint64_t* hashes;  // by upload id
+  const uint32_t* id_base;
+};
+
+template<int D, int K, bool F32>
+__global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const uint32_t id = A.id[i] & kIdMask;
+  const uint32_t tk = A.tank[i];
+  const TankDev& T = A.tanks[tk];
+  const uint32_t base = A.id_base[tk];
+  int32_t cnt = 0;
+  uint64_t hs = 0;
+  double rho;
+  if constexpr (!F32) {
+    using P = std::conditional_t<D == 2, Pos64_2, Pos64_3>;
+    const P* pr = static_cast<const P*>(A.pos);
+    double pa[3] = {0.0, 0.0, 0.0};
+    load_pos(pr, static_cast<uint32_t>(i), pa);
+    int c[3] = {0, 0, 0};
+    bool outside = false;
+    cell_of<D>(T, pa, c, outside);
+    const double R2 = T.radius2, hinv = T.hinv, wm = T.w * T.m;
+    double acc = 0.0;
+    for_cells<D, false>(T, c, A.k, A.cell_start,
+                        [&](uint32_t s, uint32_t en, int, int, int) {
+      for (uint32_t j = s; j < en; ++j) {
+        double pb[3], d[3];
+        load_pos(pr, j, pb);
+        const double s2 = dist2_exact<D>(pa, pb, d);
+        if (s2 > R2) continue;
+        acc += wm * KernelPoly<K>::value(sqrt(s2) * hinv);
+        ++cnt;
+        hs += splitmix64(static_cast<uint64_t>((A.id[j] & kIdMask) - base) + 1u);
+      }
+    });
+    rho = acc;
+  } else {
+    using P = std::conditional_t<D == 2, Pos32_2, Pos32_3>;
+    const P* pr = static_cast<const P*>(A.pos);
+    float pa[3] = {0.f, 0.f, 0.f};
+    load_pos(pr, static_cast<uint32_t>(i), pa);
+    double pad[3] = {pa[0], pa[1], pa[2]};
+    int c[3] = {0, 0, 0};
+    bool outside = false;
+    cell_of<D>(T, pad, c, outside);
+    const float R2 = T.radius2_f, hinv = static_cast<float>(T.hinv);
+    const float wm = static_cast<float>(T.w) * static_cast<float>(T.m);
+    Kahan acc;
+    for_cells<D, false>(T, c, A.k, A.cell_start,
+                        [&](uint32_t s, uint32_t en, int, int, int) {
+      for (uint32_t j = s; j < en; ++j) {
+        float pb[3], d[3];
+        load_pos(pr, j, pb);
+        const float s2 = dist2_exact<D>(pa, pb, d);
+        if (s2 > R2) continue;
+        acc.add(wm * KernelPoly<K>::value(sqrtf(s2) * hinv));
+        ++cnt;
+        hs += splitmix64(static_cast<uint64_t>((A.id[j] & kIdMask) - base) + 1u);
+      }
+    });
+    rho = static_cast<double>(acc.value());
+  }
+  if (A.rho != nullptr) A.rho[id] = rho;
+  if (A.counts != nullptr) A.counts[id] = cnt;
+  if (A.hashes != nullptr) A.hashes[id] = hs;
+}
+
+// ---------------------------------------------------------------------------
+// Prepare-only commit: the fluid home state takes the gathered cell-order
+// copy (walls were written by k_walls).
+template<int D, int F>
+__global__ void __launch_bounds__(256) k_commit(StageArgs<D, F> A) {
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= A.n) return;
+  const uint32_t id = A.Y.id[j];
+  if (id & kWallBit) return;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    A.X.pos[k][j] = A.Y.pos[k][j];
+    A.X.vel[k][j] = A.Y.vel[k][j];
+    A.X.dv[k][j] = A.Y.dv[k][j];
+  }
+  A.X.rho[j] = A.Y.rho[j];
+  A.X.drho[j] = A.Y.drho[j];
+  A.X.id[j] = id;
+  A.X.tank[j] = A.Y.tank[j];
+}
+
+// Upload: AoS doubles in upload order into the SoA home state.
+template<int D, class R>
+__global__ void __launch_bounds__(256)
+    k_unpack(StateBuf<R> X, const double* __restrict__ r,
+             const double* __restrict__ v, const double* __restrict__ rho,
+             const double* __restrict__ dv, const uint32_t* __restrict__ tank_of,
+             const TankDev* tanks, const uint32_t* __restrict__ wall_from,
+             int64_t n) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t tk = tank_of[i];
+  const bool wall = static_cast<uint32_t>(i) >= wall_from[tk];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    X.pos[k][i] = r[i * D + k];
+    X.vel[k][i] = static_cast<R>(v[i * D + k]);
+    X.dv[k][i] = dv != nullptr ? static_cast<R>(dv[i * D + k]) : R(0);
+  }
+  if constexpr (sizeof(R) == 8) {
+    X.rho[i] = static_cast<R>(rho[i]);
+  } else {
+    X.rho[i] = static_cast<R>(rho[i] - tanks[tk].rho0);
+  }
+  X.drho[i] = R(0);
+  X.id[i] = static_cast<uint32_t>(i) | (wall ? kWallBit : 0u);
+  X.tank[i] = tk;
+}
+
+// Download: one field of the home state into upload order (AoS for vectors).
+template<int D, class R>
+__global__ void __launch_bounds__(256)
+    k_pack(StateBuf<R> X, const TankDev* tanks, PhysDev phys, int field,
+           double* __restrict__ out, int64_t n) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t id = X.id[i] & kIdMask;
+  const uint32_t tk = X.tank[i];
+  const TankDev& T = tanks[tk];
+  switch (field) {
+    case TG_FIELD_R:
+#pragma unroll
+      for (int k = 0; k < D; ++k) out[int64_t(id) * D + k] = X.pos[k][i];
+      break;
+    case TG_FIELD_V:
+#pragma unroll
+      for (int k = 0; k < D; ++k) out[int64_t(id) * D + k] = X.vel[k][i];
+      break;
+    case TG_FIELD_DV_DT:
+#pragma unroll
+      for (int k = 0; k < D; ++k) out[int64_t(id) * D + k] = X.dv[k][i];
+      break;
+    case TG_FIELD_DRHO_DT: out[id] = X.drho[i]; break;
+    default: {
+      double rho;
+      if constexpr (sizeof(R) == 8) {
+        rho = X.rho[i];
+      } else {
+        rho = T.rho0 + static_cast<double>(X.rho[i]);
+      }
+      if (field == TG_FIELD_RHO) {
+        out[id] = rho;
+      } else {
+        double p, c;
+        tait_f64(phys, T, rho, p, c);
+        out[id] = field == TG_FIELD_P ? p : c;
+      }
+    }
+  }
+}
+
+// End of step: advance per-tank time, keep dt, reset the dt reduction.
+static __global__ void k_step_end(double* dt, double* dt_last, double* time,
+                           uint32_t* err, int ntanks) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntanks) return;
+  const double d = dt[t];
+  if (isfinite(d)) {
+    if (!(d > 0.0)) atomicOr(err, static_cast<uint32_t>(TG_DEV_BAD_DT));
+    time[t] += d;
+    dt_last[t] = d;
+  }
+  dt[t] = __longlong_as_double(0x7ff0000000000000ll);
+}
+
+// Cloud records for the summation density: absolute positions in cell order
+// (FP64, or rounded once to FP32), ids and tanks.
+template<int D, bool F32>
+__global__ void __launch_bounds__(256)
+    k_cloud_records(const double* __restrict__ px,
+                    const double* __restrict__ py,
+                    const double* __restrict__ pz,
+                    const uint32_t* __restrict__ id_in,
+                    const uint32_t* __restrict__ tank_in,
+                    const uint32_t* __restrict__ perm, void* rec,
+                    uint32_t* __restrict__ id_out,
+                    uint32_t* __restrict__ tank_out, int64_t n) {
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const uint32_t s = perm[j];
+  const double x = px[s], y = py[s], z = D == 3 ? pz[s] : 0.0;
+  if constexpr (F32) {
+    if constexpr (D == 2) {
+      static_cast<Pos32_2*>(rec)[j] = Pos32_2{float(x), float(y)};
+    } else {
+      static_cast<Pos32_3*>(rec)[j] = Pos32_3{float(x), float(y), float(z), 0.f};
+    }
+  } else {
+    if constexpr (D == 2) {
+      static_cast<Pos64_2*>(rec)[j] = Pos64_2{x, y};
+    } else {
+      static_cast<Pos64_3*>(rec)[j] = Pos64_3{x, y, z, 0.0};
+    }
+  }
+  id_out[j] = id_in[s];
+  tank_out[j] = tank_in[s];
+}
+
+}  // namespace tg

@@ -1,0 +1,231 @@
+// sort.cu - stable LSD radix sort of cell keys and the cell-start table.
+//
+// One pass per 8-bit digit, three kernels per pass:
+//   upsweep   per-tile digit histograms (tile = 256 threads x 8 keys),
+//             stored digit-major: hist[digit * ntiles + tile]
+//   rowscan   one block per digit: exclusive scan of its row over tiles,
+//             and the row total
+//   downsweep each tile ranks its keys stably (warp __match_any_sync per
+//             item, items in tile order) and scatters them to
+//             digit_base + row_scan + warp offset + rank
+// Keys of one warp are loaded warp-striped (item i of lane l sits at
+// warp_base + 32 i + l), so processing items in order, lanes in order, keeps
+// the input order within equal digits.  No kernel waits on another block.
+#include "sort.cuh"
+
+namespace tg {
+namespace {
+
+constexpr int kWarps = kSortThreads / 32;
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+    k_radix_upsweep(const uint32_t* __restrict__ keys, int64_t n, int shift,
+                    uint32_t* __restrict__ hist, int ntiles) {
+  __shared__ uint32_t s_hist[kRadixBins];
+  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) s_hist[i] = 0;
+  __syncthreads();
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kSortTile;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+    const int64_t idx = base + warp * (32 * kSortItems) + it * 32 + lane;
+    if (idx < n) {
+      const uint32_t d = (keys[idx] >> shift) & (kRadixBins - 1);
+      atomicAdd(&s_hist[d], 1u);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) {
+    hist[static_cast<int64_t>(i) * ntiles + blockIdx.x] = s_hist[i];
+  }
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v,
+                                                         uint32_t* s_warp,
+                                                         uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < nwarps ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nwarps) s_warp[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  const uint32_t warp_excl = warp > 0 ? s_warp[warp - 1] : 0u;
+  *total = s_warp[nwarps - 1];
+  __syncthreads();
+  return warp_excl + x - v;
+}
+
+__global__ void __launch_bounds__(256)
+    k_radix_rowscan(uint32_t* __restrict__ hist, int ntiles,
+                    uint32_t* __restrict__ row_total) {
+  __shared__ uint32_t s_warp[32];
+  uint32_t* row = hist + static_cast<int64_t>(blockIdx.x) * ntiles;
+  uint32_t carry = 0;
+  for (int base = 0; base < ntiles; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const uint32_t v = i < ntiles ? row[i] : 0u;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
+    if (i < ntiles) row[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) row_total[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+    k_radix_downsweep(const uint32_t* __restrict__ keys_in,
+                      const uint32_t* __restrict__ vals_in,
+                      uint32_t* __restrict__ keys_out,
+                      uint32_t* __restrict__ vals_out, int64_t n, int shift,
+                      const uint32_t* __restrict__ row_scan,
+                      const uint32_t* __restrict__ row_total, int ntiles) {
+  __shared__ uint32_t s_base[kRadixBins];
+  __shared__ uint32_t s_cnt[kWarps][kRadixBins];
+  __shared__ uint32_t s_warp[32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // Digit bases: exclusive scan of the row totals (256 digits, 256 threads).
+  {
+    const uint32_t v = row_total[threadIdx.x];
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
+    s_base[threadIdx.x] =
+        ex + row_scan[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x];
+  }
+  for (int w = 0; w < kWarps; ++w) s_cnt[w][threadIdx.x] = 0;
+  __syncthreads();
+
+  const int64_t base =
+      static_cast<int64_t>(blockIdx.x) * kSortTile + warp * (32 * kSortItems);
+  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  int digit[kSortItems];
+  const uint32_t lt = lanemask_lt();
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+    const int64_t idx = base + it * 32 + lane;
+    const bool valid = idx < n;
+    key[it] = valid ? keys_in[idx] : 0u;
+    val[it] = valid ? (vals_in ? vals_in[idx] : static_cast<uint32_t>(idx)) : 0u;
+    digit[it] = valid ? static_cast<int>((key[it] >> shift) & (kRadixBins - 1))
+                      : kRadixBins;
+    const uint32_t peers = __match_any_sync(0xffffffffu, digit[it]);
+    uint32_t before = 0;
+    if (valid) before = s_cnt[warp][digit[it]];
+    __syncwarp();
+    rank[it] = before + __popc(peers & lt);
+    const int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) s_cnt[warp][digit[it]] = before + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // Exclusive prefix of the per-warp counts, per digit.
+  {
+    uint32_t run = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      const uint32_t c = s_cnt[w][threadIdx.x];
+      s_cnt[w][threadIdx.x] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+    if (digit[it] < kRadixBins) {
+      const uint32_t pos =
+          s_base[digit[it]] + s_cnt[warp][digit[it]] + rank[it];
+      keys_out[pos] = key[it];
+      vals_out[pos] = val[it];
+    }
+  }
+}
+
+__global__ void k_cell_table(const uint32_t* __restrict__ keys, int64_t n,
+                             uint32_t total_cells,
+                             uint32_t* __restrict__ cell_start) {
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j > n) return;
+  const int64_t prev = j == 0 ? -1 : static_cast<int64_t>(keys[j - 1]);
+  const int64_t cur = j == n ? static_cast<int64_t>(total_cells)
+                             : static_cast<int64_t>(keys[j]);
+  for (int64_t c = prev + 1; c <= cur; ++c) {
+    cell_start[c] = static_cast<uint32_t>(j);
+  }
+}
+
+}  // namespace
+
+size_t radix_sort_scratch_bytes(int64_t n) {
+  const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
+  return static_cast<size_t>(kRadixBins) * (ntiles + 1) * sizeof(uint32_t) +
+         256;
+}
+
+cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
+                       uint32_t* vals_b, int64_t n, int key_bits,
+                       bool identity_vals, void* scratch, bool* result_in_b,
+                       cudaStream_t stream, int64_t* launches) {
+  *result_in_b = false;
+  if (n <= 0) return cudaSuccess;
+  const int ntiles = static_cast<int>((n + kSortTile - 1) / kSortTile);
+  uint32_t* hist = static_cast<uint32_t*>(scratch);
+  uint32_t* row_total = hist + static_cast<int64_t>(kRadixBins) * ntiles;
+  const int passes = key_bits <= 0 ? 1 : (key_bits + kRadixBits - 1) / kRadixBits;
+  uint32_t* ki = keys_a;
+  uint32_t* vi = vals_a;
+  uint32_t* ko = keys_b;
+  uint32_t* vo = vals_b;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = p * kRadixBits;
+    k_radix_upsweep<<<ntiles, kSortThreads, 0, stream>>>(ki, n, shift, hist,
+                                                         ntiles);
+    k_radix_rowscan<<<kRadixBins, 256, 0, stream>>>(hist, ntiles, row_total);
+    k_radix_downsweep<<<ntiles, kSortThreads, 0, stream>>>(
+        ki, (p == 0 && identity_vals) ? nullptr : vi, ko, vo, n, shift, hist,
+        row_total, ntiles);
+    *launches += 3;
+    uint32_t* tk = ki;
+    ki = ko;
+    ko = tk;
+    uint32_t* tv = vi;
+    vi = vo;
+    vo = tv;
+  }
+  *result_in_b = (passes % 2) == 1;
+  return cudaGetLastError();
+}
+
+cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
+                             uint32_t total_cells, uint32_t* cell_start,
+                             cudaStream_t stream, int64_t* launches) {
+  const int64_t threads = n + 1;
+  const int block = 256;
+  const int64_t grid = (threads + block - 1) / block;
+  k_cell_table<<<static_cast<unsigned>(grid), block, 0, stream>>>(
+      sorted_keys, n, total_cells, cell_start);
+  *launches += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace tg

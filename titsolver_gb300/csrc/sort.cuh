@@ -1,0 +1,40 @@
+// sort.cuh - cell-key sort of the neighbour search: a stable LSD radix sort
+// of 32-bit cell keys with 32-bit payloads, and the cell-start table.
+//
+// Replaces the reference's GridIndex construction (atomic count, prefix sum,
+// atomic fill; source/tit/geom/search/grid_search.hpp:58-84) with a stable
+// sort, so the order of particles inside a cell is a pure function of the
+// previous order and the results are run-to-run deterministic.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tg {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadixBins = 1 << kRadixBits;
+constexpr int kSortThreads = 256;             // 8 warps
+constexpr int kSortItems = 8;                 // per thread
+constexpr int kSortTile = kSortThreads * kSortItems;
+
+// Scratch needed by radix_sort for n keys (bytes): per-tile histograms.
+size_t radix_sort_scratch_bytes(int64_t n);
+
+// Sort (keys, vals) by the low key_bits of keys, stable.  keys_a/vals_a hold
+// the input (identity_vals: the payload is 0..n-1 and vals_a is not read);
+// the result lands in (keys_a, vals_a) or (keys_b, vals_b), as returned
+// through *result_in_b.  Each pass issues three kernels; *launches counts
+// them.
+cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
+                       uint32_t* vals_b, int64_t n, int key_bits,
+                       bool identity_vals, void* scratch, bool* result_in_b,
+                       cudaStream_t stream, int64_t* launches);
+
+// cell_start[c] = first sorted index whose key >= c, for c in
+// [0, total_cells]; cell_start[total_cells] = n.
+cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
+                             uint32_t total_cells, uint32_t* cell_start,
+                             cudaStream_t stream, int64_t* launches);
+
+}  // namespace tg
