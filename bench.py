@@ -1,0 +1,438 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 WCSPH hot path (one JSON line on rank 0).
+
+Workload (default, ``--config c1``): 2D dam break at scale, H = 1,
+dx = H/800 (1,280,000 fluid particles at dx (i+1, j+1)) in a 5.366H x 3H
+tank with three layers of fixed wall particles, Wendland C2 kernel (h = 2dx),
+Tait EOS (rho0 = 1000, xi = 7, cs0 = 10 sqrt(gH)), hydrostatic start,
+Monaghan alpha = 0.02, delta-SPH delta = 0.1, SSPRK3 at CFL 0.25.  A step is
+one full SSPRK3 step (three neighbour rebuilds, three fused force passes).
+
+* ``value``: FP32-compensated form, particle-updates/s = fluid particles x
+  steps / device time, state resident in HBM (working set > L2), CUDA-graph
+  replay, timed with CUDA events on the library's stream.
+* ``forms.fp64``: the plain FP64 form on the same workload.
+* ``l2_error_vs_fp64``: relative L2 error of rho and r, FP32C vs FP64, after
+  the same number of steps from the same start.
+* ``e2e``: the same metric through the C ABI with host buffers: every step
+  uploads r, v, rho, dv/dt from pinned host memory, steps, and downloads
+  them again (tg_particles_update / tg_step / tg_particles_download).
+* ``roofline``: the fused force kernel (k_forces): algorithmic bytes per
+  launch = fluid particles x 3S (S = state bytes per particle) over its mean
+  launch time from a profiled pass with CUDA events on the same stream.
+* ``cpu_baseline``: the oracle (the C++ restatement of the reference's CPU
+  path) on the host cores, on a bounded sample of the same workload.
+
+``--impl reference`` times that CPU path alone (the reference itself needs
+C++26 / GCC 16 and cannot be built here).  ``--gpus N`` under
+torch.distributed.run runs N independent replicas (the path does not shard
+across GPUs) and reports their summed throughput over the slowest rank.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-updates/s: FP32-comp vs plain FP64 WCSPH, 1 GB300, at stated L2 error"
+UNIT = "particle-updates/s"
+
+
+def _peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def state_bytes(dim: int, form: str) -> int:
+    """S: algorithmic state bytes per particle (positions, velocity, density)."""
+    if form == "fp64":
+        return 8 * (2 * dim + 1)
+    return 8 * dim + 4 * dim + 4
+
+
+def bytes_per_update(dim: int, form: str) -> int:
+    """Algorithmic bytes per particle-update: 3 (3S + 8d + 16)."""
+    return 3 * (3 * state_bytes(dim, form) + 8 * dim + 16)
+
+
+def make_config(name: str):
+    from titsolver_gb300 import scenarios
+
+    if name == "c1":
+        return ("2D dam break H=1, dx=H/800 (1,280,000 fluid + 3-layer walls), "
+                "Wendland C2 h=2dx, Tait rho0=1000 xi=7 cs0=10sqrt(gH), alpha=0.02, "
+                "delta-SPH 0.1, SSPRK3 CFL 0.25"), lambda: scenarios.dam_break_2d(nx_per_H=800)
+    if name == "c0":
+        return ("2D dam break H=1, dx=H/80 (12,800 fluid + 3-layer walls), same physics"), \
+            lambda: scenarios.dam_break_2d(nx_per_H=80)
+    if name == "c3":
+        return ("512 independent 2D dam breaks, column N~U{20..120} particles, aspect "
+                "U[0.5,2], dx=1/80, same physics"), lambda: scenarios.batched_tanks(512)
+    if name == "c4":
+        return ("3D dam break 2Hx1Hx1H, dx=H/200 (16,000,000 fluid + 3-layer walls), "
+                "Wendland C2 h=1.3dx, same physics"), lambda: scenarios.dam_break_3d(nx_per_H=200)
+    if name == "c4half":
+        return ("3D dam break 2Hx1HxH/2, dx=H/200 (8,000,000 fluid + 3-layer walls), "
+                "Wendland C2 h=1.3dx, same physics"), \
+            lambda: scenarios.dam_break_3d(nx_per_H=200, column=(2.0, 1.0, 0.5))
+    raise SystemExit(f"unknown config {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[4:]))
+                except ValueError:
+                    continue
+        os.unlink(self.tmp.name)
+        if not rows:
+            return None
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[3][1:]) if v == "Active"})
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in loaded),
+                "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+def forces_traffic(dim: int, form: str, n_fluid: int):
+    p = ROOT / "profiles" / "forces_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    key = f"{form}_{dim}d"
+    if key not in d:
+        return None
+    return float(d[key]["dram_bytes_per_fluid_particle"]) * n_fluid
+
+
+def cpu_sample(budget_s: float, steps: int, threads: int) -> dict:
+    """Time the oracle (CPU restatement of the reference path) on a dam break
+    sized so that `steps` steps take about budget_s seconds."""
+    import oracle
+    from titsolver_gb300 import physics, scenarios
+
+    P = physics.baseline_params(2)
+    cal = scenarios.dam_break_2d(nx_per_H=40)
+    st = oracle.State(cal)
+    t0 = time.perf_counter()
+    oracle.step(P, st, 1, nthreads=threads)
+    rate = cal["tanks"][0]["n_fluid"] / max(time.perf_counter() - t0, 1e-6)
+    want = rate * budget_s / max(steps, 1)
+    nx = int(max(40, min(800, math.sqrt(want / 2.0))))
+    scn = scenarios.dam_break_2d(nx_per_H=nx)
+    st = oracle.State(scn)
+    nf = scn["tanks"][0]["n_fluid"]
+    t0 = time.perf_counter()
+    oracle.step(P, st, steps, nthreads=threads)
+    sec = time.perf_counter() - t0
+    return {"value": nf * steps / sec, "seconds": sec, "fluid": nf, "nx_per_H": nx,
+            "steps": steps, "threads": threads}
+
+
+def run_reference(args, ranks) -> dict:
+    import oracle
+
+    threads = oracle.default_threads()
+    # Each timed step is one SSPRK3 step of a dam break sized so the whole
+    # run takes about two minutes of host time.
+    res = cpu_sample(120.0, args.steps, threads)
+    workload, _ = make_config(args.config)
+    sample = (f"2D dam break dx=H/{res['nx_per_H']} ({res['fluid']} fluid), same physics, "
+              f"{res['steps']} SSPRK3 steps per timed run ({res['seconds']:.1f} s)")
+    return {
+        "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * res["seconds"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded dam-break lattice, hydrostatic start)",
+        "config": {"workload": workload, "sample": sample},
+        "impl": "reference",
+        "cpu_baseline": {"value": res["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks):
+    from titsolver_gb300 import _abi
+
+    ctx = _abi.Context(params)
+    ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+    if warmup:
+        ctx.step(warmup)
+    ranks.barrier()
+    l0 = ctx.launch_count()
+    ctx.timer_start()
+    ctx.step(steps)
+    ms = ctx.timer_stop()
+    launches = ctx.launch_count() - l0
+    ranks.barrier()
+    prof = None
+    if profile_steps:
+        ctx.profile_enable(True)
+        ctx.step(profile_steps)
+        prof = ctx.profile_read()
+        ctx.profile_enable(False)
+    return ctx, ms, launches, prof
+
+
+def run_gpu(args, ranks) -> dict | None:
+    from titsolver_gb300 import _abi, physics, scenarios
+
+    workload, make = make_config(args.config)
+    scn = make()
+    dim = scn["dim"]
+    nf = scenarios.n_fluid(scn)
+    nw = int(sum(t["n_wall"] for t in scn["tanks"]))
+    dev = ranks.local_rank
+    peaks = _peaks()
+
+    # FP32-compensated form: the headline.
+    P32 = physics.baseline_params(dim, precision=_abi.TG_FP32C)
+    P32.device = dev
+    clocks = ClockSampler(dev)
+    clocks.start()
+    ctx32, ms32, launches, prof32 = gpu_leg(scn, P32, args.warmup, args.steps,
+                                            min(args.steps, 20), ranks)
+    clk = clocks.stop()
+    sec32 = ms32 / 1e3
+    value, t_max = (nf * args.steps / sec32, sec32)
+    if ranks.world_size > 1:
+        from titsolver_gb300.replicas import aggregate
+        value, t_max = aggregate(nf * args.steps, sec32, ranks)
+
+    # Plain FP64 form on the same workload and the same number of steps.
+    P64 = physics.baseline_params(dim, precision=_abi.TG_FP64)
+    P64.device = dev
+    k64 = args.steps if args.fp64_steps is None else args.fp64_steps
+    ctx64, ms64, _, prof64 = gpu_leg(scn, P64, args.warmup, k64, min(k64, 20), ranks)
+    value64 = nf * k64 / (ms64 / 1e3)
+
+    # Error of the compensated form against FP64 after the same steps.
+    err = None
+    total32 = args.warmup + args.steps + min(args.steps, 20)
+    total64 = args.warmup + k64 + min(k64, 20)
+    if total32 == total64:
+        f = np.concatenate([np.r_[np.ones(t["n_fluid"], bool), np.zeros(t["n_wall"], bool)]
+                            for t in scn["tanks"]])
+        r32, r64 = ctx32.download(_abi.TG_FIELD_R)[f], ctx64.download(_abi.TG_FIELD_R)[f]
+        d32, d64 = ctx32.download(_abi.TG_FIELD_RHO)[f], ctx64.download(_abi.TG_FIELD_RHO)[f]
+        r0 = scn["r"][f]
+        err = {"steps": total32,
+               "rho": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
+               "r": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
+               "r_vs_displacement": float(np.linalg.norm(r32 - r64) /
+                                          max(np.linalg.norm(r64 - r0), 1e-300)),
+               "rho_vs_deviation": float(np.linalg.norm(d32 - d64) /
+                                         max(np.linalg.norm(d64 - 1000.0), 1e-300))}
+    ctx64.close()
+
+    # End to end through the C ABI with pinned host buffers.
+    n = scn["r"].shape[0]
+    pin = {k: _abi.PinnedArray(shape) for k, shape in
+           (("r", (n, dim)), ("v", (n, dim)), ("rho", (n,)), ("dv", (n, dim)))}
+    ctx32.download(_abi.TG_FIELD_R, pin["r"].array)
+    ctx32.download(_abi.TG_FIELD_V, pin["v"].array)
+    ctx32.download(_abi.TG_FIELD_RHO, pin["rho"].array)
+    ctx32.download(_abi.TG_FIELD_DV_DT, pin["dv"].array)
+    ke = max(1, min(args.steps, args.e2e_steps))
+
+    def e2e_step():
+        ctx32.update(pin["r"].array, pin["v"].array, pin["rho"].array, pin["dv"].array)
+        ctx32.step(1)
+        ctx32.download(_abi.TG_FIELD_R, pin["r"].array)
+        ctx32.download(_abi.TG_FIELD_V, pin["v"].array)
+        ctx32.download(_abi.TG_FIELD_RHO, pin["rho"].array)
+        ctx32.download(_abi.TG_FIELD_DV_DT, pin["dv"].array)
+
+    for _ in range(2):
+        e2e_step()
+    ranks.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        e2e_step()
+    te = time.perf_counter() - t0
+    e2e_value = nf * ke / te
+    if ranks.world_size > 1:
+        from titsolver_gb300.replicas import aggregate
+        e2e_value, _ = aggregate(nf * ke, te, ranks)
+    hd_bytes = n * 8 * (3 * dim + 1)
+    ctx32.close()
+
+    # Roofline of the fused force kernel.
+    forces_avg_ms = prof32["forces_ms"] / max(prof32["forces_launches"], 1)
+    alg = nf * 3 * state_bytes(dim, "fp32c")
+    achieved = alg / (forces_avg_ms / 1e3) / 1e9
+    traffic = forces_traffic(dim, "fp32c", nf)
+    roofline = {"bound": "hbm", "kernel": "k_forces (fused continuity+momentum+RK update)",
+                "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "peak_source": f"{peaks['source']} hbm_gbs",
+                "alg_bytes_per_launch": alg, "avg_launch_ms": forces_avg_ms}
+
+    def shares(p):
+        tot = p["sort_ms"] + p["reorder_ms"] + p["walls_ms"] + p["forces_ms"]
+        return {k: round(p[k] / tot, 4) for k in ("sort_ms", "reorder_ms", "walls_ms", "forces_ms")}
+
+    out = None
+    if ranks.rank == 0:
+        cpu = None
+        if ranks.world_size == 1 and not args.no_cpu:
+            import oracle
+            threads = oracle.default_threads()
+            c = cpu_sample(args.cpu_budget, 2, threads)
+            cpu = {"value": c["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": (f"2D dam break dx=H/{c['nx_per_H']} ({c['fluid']} fluid), "
+                              f"same physics, {c['steps']} SSPRK3 steps, {c['seconds']:.1f} s, "
+                              "oracle built g++ -O3 -ffp-contract=off")}
+        ws = scn["r"].shape[0] * 260
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (compensated sums; f64 positions and time)",
+            "data": "synthetic (seeded dam-break lattice, hydrostatic start)",
+            "config": {"workload": workload, "fluid_particles": nf, "wall_particles": nw,
+                       "form": "fp32c", "kahan": True, "parallelism": "replicas",
+                       "l2": f"inputs larger than L2 (working set ~{ws / 1e6:.0f} MB > 129 MB)"},
+            "forms": {
+                "fp32c": {"value": value, "ms_per_step": ms32 / args.steps,
+                          "kernel_shares": shares(prof32)},
+                "fp64": {"value": value64, "ms_per_step": ms64 / k64, "steps": k64,
+                         "kernel_shares": shares(prof64)},
+                "speedup_fp32c_over_fp64": value / value64 if value64 > 0 else None,
+            },
+            "l2_error_vs_fp64": err,
+            "bytes_per_update": {"fp32c": bytes_per_update(dim, "fp32c"),
+                                 "fp64": bytes_per_update(dim, "fp64")},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": hd_bytes,
+                    "d2h_bytes_per_step": hd_bytes, "steps": ke},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+    return out
+
+
+def run_single_form(args, ranks) -> dict | None:
+    """One form on the configured workload (used under ncu)."""
+    from titsolver_gb300 import _abi, physics, scenarios
+
+    workload, make = make_config(args.config)
+    scn = make()
+    nf = scenarios.n_fluid(scn)
+    form = _abi.TG_FP32C if args.only == "fp32c" else _abi.TG_FP64
+    P = physics.baseline_params(scn["dim"], precision=form)
+    P.device = ranks.local_rank
+    ctx, ms, launches, prof = gpu_leg(scn, P, args.warmup, args.steps, 0, ranks)
+    ctx.close()
+    if ranks.rank != 0:
+        return None
+    return {"metric": METRIC, "value": nf * args.steps / (ms / 1e3), "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "form": args.only,
+            "config": {"workload": workload}, "gpu_launches": launches}
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gpu", "reference"), default="gpu")
+    ap.add_argument("--config", default="c1")
+    ap.add_argument("--fp64-steps", type=int, default=None,
+                    help="FP64 timed steps (default: --steps)")
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", choices=("fp32c", "fp64"), default=None,
+                    help="time one form only (profiling runs); prints its value")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    from titsolver_gb300.replicas import init_from_env
+
+    ranks = init_from_env()
+    try:
+        if args.impl == "reference":
+            if ranks.rank != 0:
+                return 0
+            print(json.dumps(run_reference(args, ranks)), flush=True)
+            return 0
+        from titsolver_gb300 import build as gpu_build
+        if ranks.rank == 0:
+            gpu_build.build()
+        ranks.barrier()
+        if args.only is not None:
+            out = run_single_form(args, ranks)
+        else:
+            out = run_gpu(args, ranks)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return 0
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -128,7 +128,7 @@ typedef struct tg_params {
   int32_t post_integrate;   /* TG_POST_* */
   int32_t cells_per_radius; /* grid cells per support radius, 1..3 */
   int32_t kahan;            /* FP32C: 1 = compensated sums, 0 = plain */
-  int32_t reserved0;
+  int32_t device;           /* CUDA device ordinal; -1 = the current one */
   double xi;      /* Tait polytropic index */
   double g;       /* gravity, acting along -axis 1 */
   double mu;      /* Morris dynamic viscosity */

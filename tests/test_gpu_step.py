@@ -1,0 +1,200 @@
+"""GPU integrator steps against the oracle, through the C ABI.
+
+Tolerances (relative L2 over the fluid particles):
+* plain FP64 after 1 step: r, v, rho <= 1e-12; dv/dt, drho/dt <= 1e-9
+  (summation order, FMA and algebraic rearrangement only)
+* plain FP64 after 100 steps of the 12,800-particle dam break: r <= 1e-9,
+  v and rho <= 1e-7
+* FP32-compensated after 100 steps vs the FP64 oracle: rho <= 1e-4,
+  r <= 1e-5
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import fluid_mask, gpu_context, gpu_state, oracle_run, rel_l2
+from titsolver_gb300 import _abi, physics, scenarios
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(scn, P, steps, tol_state, tol_deriv=None, walls=True):
+    with gpu_context(scn, P) as ctx:
+        dt = ctx.step(steps)
+        g = gpu_state(ctx)
+    o = oracle_run(scn, P, steps)
+    f = fluid_mask(scn)
+    np.testing.assert_allclose(dt, o.dt, rtol=1e-12)
+    np.testing.assert_allclose(g["time"], o.time, rtol=1e-12)
+    assert rel_l2(g["r"][f], o.r[f]) <= tol_state
+    assert rel_l2(g["v"][f], o.v[f]) <= tol_state * 1e3 + 1e-300
+    assert rel_l2(g["rho"][f], o.rho[f]) <= tol_state
+    if walls and (~f).any():
+        assert rel_l2(g["rho"][~f], o.rho[~f]) <= tol_state
+        np.testing.assert_array_equal(g["r"][~f], o.r[~f])
+        assert np.all(g["v"][~f] == 0.0)
+    if tol_deriv is not None:
+        assert rel_l2(g["dv_dt"][f], o.dv_dt[f]) <= tol_deriv
+        assert rel_l2(g["drho_dt"][f], o.drho_dt[f]) <= tol_deriv
+    return g, o
+
+
+@pytest.mark.parametrize("term_set", ("baseline", "reference"))
+def test_one_step_fp64_2d(gpu_lib, term_set):
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    P = getattr(physics, f"{term_set}_params")(2)
+    _compare(scn, P, 1, 1e-12, 1e-9)
+
+
+@pytest.mark.parametrize("kernel", range(6))
+def test_one_step_fp64_every_kernel(gpu_lib, kernel):
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    _compare(scn, physics.reference_params(2, kernel=kernel), 1, 1e-12, 1e-9)
+
+
+def test_one_step_fp64_3d(gpu_lib):
+    scn = scenarios.dam_break_3d(nx_per_H=8)
+    _compare(scn, physics.baseline_params(3), 1, 1e-12, 1e-9)
+    _compare(scn, physics.reference_params(3), 1, 1e-12, 1e-9)
+
+
+def test_ssprk2_fp64(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    P = physics.baseline_params(2)
+    P.integrator = _abi.TG_SSPRK2
+    _compare(scn, P, 3, 1e-12, 1e-9)
+
+
+def test_batched_tanks_fp64(gpu_lib):
+    scn = scenarios.batched_tanks(n_tanks=8, n_range=(6, 14), seed=2)
+    _compare(scn, physics.baseline_params(2), 3, 1e-12, 1e-9)
+
+
+def test_golden_dam_break_fp64(gpu_lib):
+    import pathlib
+    z = np.load(pathlib.Path(__file__).resolve().parent / "golden" / "dam_break_small.npz")
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    f = fluid_mask(scn)
+    for term_set in ("baseline", "reference"):
+        P = getattr(physics, f"{term_set}_params")(2)
+        with gpu_context(scn, P) as ctx:
+            ctx.step(10)
+            g = gpu_state(ctx)
+        for name in ("r", "v", "rho"):
+            ref = z[f"{term_set}_10_{name}"]
+            assert rel_l2(g[name][f], ref[f]) <= (1e-10 if name != "v" else 1e-8), (term_set, name)
+
+
+def test_hundred_steps_fp64_c0(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=80)
+    P = physics.baseline_params(2)
+    with gpu_context(scn, P) as ctx:
+        ctx.step(100)
+        g = gpu_state(ctx)
+    o = oracle_run(scn, P, 100)
+    f = fluid_mask(scn)
+    assert rel_l2(g["r"][f], o.r[f]) <= 1e-9
+    assert rel_l2(g["v"][f], o.v[f]) <= 1e-7
+    assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-7
+
+
+def test_fp32_compensated_vs_fp64_oracle(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=80)
+    P64 = physics.baseline_params(2)
+    P32 = physics.baseline_params(2, precision=_abi.TG_FP32C)
+    with gpu_context(scn, P32) as ctx:
+        ctx.step(100)
+        g = gpu_state(ctx)
+    o = oracle_run(scn, P64, 100)
+    f = fluid_mask(scn)
+    assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-4
+    assert rel_l2(g["r"][f], o.r[f]) <= 1e-5
+    # Mass is exact by construction (constant per-particle mass).
+    assert np.all(np.isfinite(g["rho"]))
+
+
+def test_graph_and_direct_launches_bit_identical(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    P = physics.baseline_params(2)
+    out = []
+    for graph in (True, False, True):
+        with gpu_context(scn, P) as ctx:
+            ctx.set_graph(graph)
+            ctx.step(5)
+            out.append(gpu_state(ctx))
+    for k in ("r", "v", "rho", "dv_dt"):
+        np.testing.assert_array_equal(out[0][k], out[1][k])
+        np.testing.assert_array_equal(out[0][k], out[2][k])
+
+
+def test_update_round_trip_continues_the_run(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    P = physics.baseline_params(2)
+    with gpu_context(scn, P) as a, gpu_context(scn, P) as b:
+        a.step(4)
+        b.step(2)
+        s = gpu_state(b)
+        b.update(s["r"], s["v"], s["rho"], s["dv_dt"])
+        b.step(2)
+        ga, gb = gpu_state(a), gpu_state(b)
+    f = fluid_mask(scn)
+    assert rel_l2(gb["r"][f], ga["r"][f]) <= 1e-13
+    assert rel_l2(gb["rho"][f], ga["rho"][f]) <= 1e-13
+
+
+def test_profile_and_launch_counts(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    with gpu_context(scn, physics.baseline_params(2)) as ctx:
+        ctx.profile_enable(True)
+        before = ctx.launch_count()
+        ctx.step(2)
+        prof = ctx.profile_read()
+        assert prof["forces_ms"] > 0 and prof["sort_ms"] > 0
+        assert prof["steps"] == 2 and prof["forces_launches"] == 6
+        assert ctx.launch_count() - before > 20
+
+
+def test_planted_coincident_particles_raise_device_state(gpu_lib):
+    # Two distinct particles at one point make the Ferrari term 0/0; the
+    # kernel flags a non-finite state and tg_step reports it (no GPU fault).
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    scn = dict(scn)
+    r = scn["r"].copy()
+    r[1] = r[0]
+    scn["r"] = r
+    with gpu_context(scn, physics.reference_params(2)) as ctx:
+        with pytest.raises(_abi.TgError) as ei:
+            ctx.step(1)
+        assert ei.value.status == _abi.TG_ERR_DEVICE_STATE
+        assert ctx.device_status() & _abi.TG_DEV_NONFINITE_STATE
+
+
+def test_invalid_upload_rejected_on_host(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=10)
+    r = scn["r"].copy()
+    r[3, 0] = np.nan
+    with _abi.Context(physics.baseline_params(2)) as ctx:
+        with pytest.raises(_abi.TgError) as ei:
+            ctx.upload(scn["tanks"], r, scn["v"], scn["rho"])
+        assert ei.value.status == _abi.TG_ERR_INVALID_ARGUMENT
+        bad = [dict(scn["tanks"][0], h=-1.0)]
+        with pytest.raises(_abi.TgError):
+            ctx.upload(bad, scn["r"], scn["v"], scn["rho"])
+        with pytest.raises(_abi.TgError) as ei:
+            ctx.step(1)
+        assert ei.value.status == _abi.TG_ERR_NOT_READY
+
+
+def test_deterministic_runs(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=40)
+    P = physics.baseline_params(2, precision=_abi.TG_FP32C)
+    res = []
+    for _ in range(2):
+        with gpu_context(scn, P) as ctx:
+            ctx.step(10)
+            res.append(gpu_state(ctx))
+    np.testing.assert_array_equal(res[0]["r"], res[1]["r"])
+    np.testing.assert_array_equal(res[0]["rho"], res[1]["rho"])

@@ -54,7 +54,7 @@ class TgParams(ctypes.Structure):
         ("post_integrate", ctypes.c_int32),
         ("cells_per_radius", ctypes.c_int32),
         ("kahan", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32),
+        ("device", ctypes.c_int32),
         ("xi", ctypes.c_double),
         ("g", ctypes.c_double),
         ("mu", ctypes.c_double),

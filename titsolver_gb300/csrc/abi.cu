@@ -194,6 +194,7 @@ void tg_params_default(tg_params* p) {
   p->post_integrate = TG_POST_PREPARE;
   p->cells_per_radius = 1;
   p->kahan = 1;
+  p->device = -1;
   p->xi = 7.0;
   p->g = 9.81;
   p->mu = 0.001;
@@ -231,6 +232,11 @@ int tg_context_create(const tg_params* params, tg_context** out) {
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
     return TG_ERR_NO_DEVICE;
+  }
+  if (params->device >= ndev) return TG_ERR_INVALID_ARGUMENT;
+  if (params->device >= 0 && cudaSetDevice(params->device) != cudaSuccess) {
+    cudaGetLastError();
+    return TG_ERR_CUDA;
   }
   tg_context* ctx = new (std::nothrow) tg_context();
   if (ctx == nullptr) return TG_ERR_OUT_OF_MEMORY;

@@ -161,17 +161,24 @@ __global__ void __launch_bounds__(kSortThreads)
   }
 }
 
-__global__ void k_cell_table(const uint32_t* __restrict__ keys, int64_t n,
-                             uint32_t total_cells,
-                             uint32_t* __restrict__ cell_start) {
-  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (j > n) return;
-  const int64_t prev = j == 0 ? -1 : static_cast<int64_t>(keys[j - 1]);
-  const int64_t cur = j == n ? static_cast<int64_t>(total_cells)
-                             : static_cast<int64_t>(keys[j]);
-  for (int64_t c = prev + 1; c <= cur; ++c) {
-    cell_start[c] = static_cast<uint32_t>(j);
+// One thread per cell: cell_start[c] = lower_bound(keys, c).  Every cell
+// costs the same (log2 n probes), so long runs of empty cells (air above
+// the water, the grid margins) do not serialise on one thread.
+__global__ void __launch_bounds__(256)
+    k_cell_table(const uint32_t* __restrict__ keys, int64_t n,
+                 uint32_t total_cells, uint32_t* __restrict__ cell_start) {
+  const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (c > static_cast<int64_t>(total_cells)) return;
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (static_cast<int64_t>(__ldg(keys + mid)) < c) {
+      lo = mid + 1;
+    } else {
+      hi = mid;
+    }
   }
+  cell_start[c] = static_cast<uint32_t>(lo);
 }
 
 }  // namespace
@@ -219,7 +226,7 @@ cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
 cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
                              uint32_t total_cells, uint32_t* cell_start,
                              cudaStream_t stream, int64_t* launches) {
-  const int64_t threads = n + 1;
+  const int64_t threads = static_cast<int64_t>(total_cells) + 1;
   const int block = 256;
   const int64_t grid = (threads + block - 1) / block;
   k_cell_table<<<static_cast<unsigned>(grid), block, 0, stream>>>(

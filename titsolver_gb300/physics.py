@@ -26,6 +26,7 @@ def reference_params(dim: int = 2, precision: int = _abi.TG_FP64,
     p.post_integrate = _abi.TG_POST_PREPARE
     p.cells_per_radius = 1
     p.kahan = 1
+    p.device = -1
     p.xi = 7.0
     p.g = 9.81
     p.mu = 0.001
