@@ -249,6 +249,32 @@ int tg_timer_stop(tg_context* ctx, double* ms);
 int tg_host_alloc(size_t bytes, void** out);
 int tg_host_free(void* ptr);
 
+/* Summation density of a point cloud that allocates nothing.  No
+ * counterpart in the reference: it serves callers that may not allocate
+ * device memory (a host framework that owns all device memory and forbids
+ * allocation inside its callbacks, or a real-time loop that must not block
+ * in the allocator).  Inputs and outputs are caller-owned DEVICE pointers:
+ * r (n x dim doubles, AoS), rho (n doubles), counts (n int32), hashes
+ * (n uint64); any output may be NULL but not all.  The result equals
+ * tg_summation_density with TG_POS_FP64 on the same points (all particles
+ * alike, self included, inclusive 2h predicate).
+ *
+ * Scratch is a fixed file-scope device array of about 4.6 MB that every GPU
+ * loading this library holds until exit; n above TG_NOALLOC_MAX_POINTS
+ * returns TG_ERR_CAPACITY.  Work is enqueued on `stream` (NULL = legacy
+ * default stream) without synchronising; results are ready when the stream
+ * reaches that point.  The first call on a device looks up the scratch
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  Every call shares the one
+ * array, which keeps the last call's contents (each call rewrites all it
+ * reads), so calls that overlap on the GPU (different streams or threads
+ * without ordering) race and corrupt each other. */
+#define TG_NOALLOC_MAX_POINTS 65536
+int tg_summation_density_noalloc(int32_t dim, int32_t kernel, int64_t n,
+                                 const double* r, double h, double m,
+                                 double* rho, int32_t* counts, uint64_t* hashes,
+                                 void* stream);
+
 /* Human-readable text of a status code, and of the context's last error. */
 const char* tg_status_string(int status);
 const char* tg_last_error(tg_context* ctx);

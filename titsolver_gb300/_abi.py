@@ -25,6 +25,8 @@ TG_ERR_DEVICE_STATE = 5
 TG_ERR_CAPACITY = 6
 TG_ERR_NO_DEVICE = 7
 
+TG_NOALLOC_MAX_POINTS = 65536
+
 TG_DEV_NONFINITE_STATE = 1
 TG_DEV_OUTSIDE_GRID = 2
 TG_DEV_BAD_DT = 4
@@ -121,6 +123,9 @@ SIGNATURES = [
     ("tg_timer_stop", ctypes.c_int, [_P, _D]),
     ("tg_host_alloc", ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     ("tg_host_free", ctypes.c_int, [_P]),
+    ("tg_summation_density_noalloc", ctypes.c_int,
+     [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _P, ctypes.c_double, ctypes.c_double,
+      _P, _P, _P, _P]),
     ("tg_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("tg_last_error", ctypes.c_char_p, [_P]),
 ]
