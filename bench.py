@@ -209,6 +209,12 @@ def run_reference(args, ranks) -> dict:
     }
 
 
+def tune(P, args) -> None:
+    if args.cells_per_radius is not None:
+        P.cells_per_radius = args.cells_per_radius
+    P.kahan = args.kahan
+
+
 def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks):
     from titsolver_gb300 import _abi
 
@@ -246,6 +252,7 @@ def run_gpu(args, ranks) -> dict | None:
     # FP32-compensated form: the headline.
     P32 = physics.baseline_params(dim, precision=_abi.TG_FP32C)
     P32.device = dev
+    tune(P32, args)
     clocks = ClockSampler(dev)
     clocks.start()
     ctx32, ms32, launches, prof32 = gpu_leg(scn, P32, args.warmup, args.steps,
@@ -260,6 +267,7 @@ def run_gpu(args, ranks) -> dict | None:
     # Plain FP64 form on the same workload and the same number of steps.
     P64 = physics.baseline_params(dim, precision=_abi.TG_FP64)
     P64.device = dev
+    tune(P64, args)
     k64 = args.steps if args.fp64_steps is None else args.fp64_steps
     ctx64, ms64, _, prof64 = gpu_leg(scn, P64, args.warmup, k64, min(k64, 20), ranks)
     value64 = nf * k64 / (ms64 / 1e3)
@@ -382,6 +390,7 @@ def run_single_form(args, ranks) -> dict | None:
     form = _abi.TG_FP32C if args.only == "fp32c" else _abi.TG_FP64
     P = physics.baseline_params(scn["dim"], precision=form)
     P.device = ranks.local_rank
+    tune(P, args)
     ctx, ms, launches, prof = gpu_leg(scn, P, args.warmup, args.steps, 0, ranks)
     ctx.close()
     if ranks.rank != 0:
@@ -389,6 +398,7 @@ def run_single_form(args, ranks) -> dict | None:
     return {"metric": METRIC, "value": nf * args.steps / (ms / 1e3), "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "form": args.only,
+            "cells_per_radius": P.cells_per_radius, "kahan": P.kahan,
             "config": {"workload": workload}, "gpu_launches": launches}
 
 
@@ -404,6 +414,9 @@ def main() -> int:
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cells-per-radius", type=int, default=None,
+                    help="grid cells per support radius (default: library default)")
+    ap.add_argument("--kahan", type=int, choices=(0, 1), default=1)
     ap.add_argument("--only", choices=("fp32c", "fp64"), default=None,
                     help="time one form only (profiling runs); prints its value")
     args = ap.parse_args()

@@ -259,9 +259,10 @@ int tg_host_free(void* ptr);
  * tg_summation_density with TG_POS_FP64 on the same points (all particles
  * alike, self included, inclusive 2h predicate).
  *
- * Scratch is a fixed file-scope device array of about 4.6 MB that every GPU
- * loading this library holds until exit; n above TG_NOALLOC_MAX_POINTS
- * returns TG_ERR_CAPACITY.  Work is enqueued on `stream` (NULL = legacy
+ * Scratch is a fixed file-scope device array of 4,495,616 bytes (about
+ * 4.5 MB) that every GPU loading this library holds until exit; n above
+ * TG_NOALLOC_MAX_POINTS returns TG_ERR_CAPACITY.  Work is enqueued on
+ * `stream` (NULL = legacy
  * default stream) without synchronising; results are ready when the stream
  * reaches that point.  The first call on a device looks up the scratch
  * array's device address (cudaGetSymbolAddress) with that device current;

@@ -35,18 +35,21 @@ void Context::release_all() {
   for (void* p : allocations) cudaFree(p);
   allocations.clear();
   d_tanks = nullptr;
+  d_tank_off = nullptr;
   d_id_base = d_wall_from = d_tank_of = nullptr;
   d_dt = d_dt_last = d_time = nullptr;
   d_err = d_wall_count = nullptr;
   keys_a = keys_b = vals_a = vals_b = nullptr;
   sort_scratch = nullptr;
   cell_start = wall_list = nullptr;
+  cell_scratch = nullptr;
   d_stage = d_stage2 = d_stage3 = d_stage4 = nullptr;
   d_sd_rho = nullptr;
   d_sd_count = nullptr;
   d_sd_hash = nullptr;
   d_cloud_rec = nullptr;
   uploaded = false;
+  keys_valid = false;
 }
 
 void Context::invalidate_graph() {
@@ -192,7 +195,7 @@ void tg_params_default(tg_params* p) {
   p->viscosity = TG_VISC_MORRIS;
   p->diffusion = TG_DIFF_FERRARI;
   p->post_integrate = TG_POST_PREPARE;
-  p->cells_per_radius = 1;
+  p->cells_per_radius = 2;
   p->kahan = 1;
   p->device = -1;
   p->xi = 7.0;
@@ -258,6 +261,13 @@ int tg_context_create(const tg_params* params, tg_context** out) {
   C.phys.viscosity = params->viscosity;
   C.phys.diffusion = params->diffusion;
   C.phys.kernel = params->kernel;
+  C.phys.xi_f = static_cast<float>(params->xi);
+  C.phys.g_f = static_cast<float>(params->g);
+  C.phys.mu_f = static_cast<float>(params->mu);
+  C.phys.alpha_f = static_cast<float>(params->alpha);
+  C.phys.cfl_f = static_cast<float>(params->cfl);
+  C.phys.c_force_f = static_cast<float>(params->c_force);
+  C.phys.c_visc_f = static_cast<float>(params->c_visc);
   C.k = params->cells_per_radius;
   const bool f64 = params->precision == TG_FP64;
   if (params->dim == 2) {
@@ -354,7 +364,9 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
         }
       }
     }
-    const double headroom = 0.5 * (hi[1] - lo[1]);
+    // Headroom above the tank for splashes (particles beyond the grid are
+    // clamped into its border cells, which stays exact but slows them).
+    const double headroom = 0.25 * (hi[1] - lo[1]);
     uint64_t cells = 1;
     for (int k = 0; k < 3; ++k) {
       if (k < dim) {
@@ -397,6 +409,17 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     D.diff_k = 2.0 * C.P.delta * T.h * T.cs0;
     D.visc_eps2 = 0.01 * T.h * T.h;
     D.n_fluid = static_cast<uint32_t>(T.n_fluid);
+    D.h_f = static_cast<float>(D.h);
+    D.hinv_f = static_cast<float>(D.hinv);
+    D.w_f = static_cast<float>(D.w);
+    D.wg_f = static_cast<float>(D.wg);
+    D.m_f = static_cast<float>(D.m);
+    D.rho0_f = static_cast<float>(D.rho0);
+    D.cs0_f = static_cast<float>(D.cs0);
+    D.B_f = static_cast<float>(D.B);
+    D.diff_k_f = static_cast<float>(D.diff_k);
+    D.visc_eps2_f = static_cast<float>(D.visc_eps2);
+    D.c02_f = static_cast<float>(D.cs0 * D.cs0);
     id_base[t] = static_cast<uint32_t>(base);
     wall_from[t] = static_cast<uint32_t>(base + T.n_fluid);
     base += nt;
@@ -420,6 +443,7 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     return C.alloc(reinterpret_cast<void**>(&p), bytes);
   };
   TG_CUDA(&C, A(C.d_tanks, sizeof(tg::TankDev) * n_tanks));
+  TG_CUDA(&C, A(C.d_tank_off, sizeof(uint32_t) * n_tanks));
   TG_CUDA(&C, A(C.d_id_base, sizeof(uint32_t) * n_tanks));
   TG_CUDA(&C, A(C.d_wall_from, sizeof(uint32_t) * n_tanks));
   TG_CUDA(&C, A(C.d_tank_of, sizeof(uint32_t) * nn));
@@ -434,6 +458,8 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, A(C.vals_b, sizeof(uint32_t) * nn));
   TG_CUDA(&C, C.alloc(&C.sort_scratch, tg::radix_sort_scratch_bytes(nn)));
   TG_CUDA(&C, A(C.cell_start, sizeof(uint32_t) * (total_cells + 1)));
+  TG_CUDA(&C, C.alloc(&C.cell_scratch,
+                      tg::cell_table_scratch_bytes(static_cast<uint32_t>(total_cells))));
   TG_CUDA(&C, A(C.wall_list, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
   TG_CUDA(&C, A(C.d_stage, sizeof(double) * nn * dim));
   TG_CUDA(&C, A(C.d_stage2, sizeof(double) * nn * dim));
@@ -459,6 +485,10 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, cudaMemcpyAsync(C.d_tanks, td.data(), sizeof(tg::TankDev) * n_tanks,
                               cudaMemcpyHostToDevice, s));
   TG_CUDA(&C, cudaMemcpyAsync(C.d_id_base, id_base.data(), sizeof(uint32_t) * n_tanks,
+                              cudaMemcpyHostToDevice, s));
+  std::vector<uint32_t> tank_off(static_cast<size_t>(n_tanks));
+  for (int32_t t = 0; t < n_tanks; ++t) tank_off[t] = td[t].cell_off;
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_tank_off, tank_off.data(), sizeof(uint32_t) * n_tanks,
                               cudaMemcpyHostToDevice, s));
   TG_CUDA(&C, cudaMemcpyAsync(C.d_wall_from, wall_from.data(),
                               sizeof(uint32_t) * n_tanks, cudaMemcpyHostToDevice, s));
@@ -527,6 +557,7 @@ int tg_step(tg_context* ctx, int32_t n_steps, double* dt_out) {
   Context& C = ctx->c;
   if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
   if (n_steps > 0 && C.n > 0) {
+    TG_CUDA(&C, C.engine->ensure_keys(C));
     if (C.use_graph && !C.profile) {
       if (C.graph_exec == nullptr) {
         cudaGraph_t graph = nullptr;

@@ -2,18 +2,22 @@
 // kernels, Tait EOS, cell grid addressing and per-tank constants.
 //
 // Layout in HBM (per context, all arrays in "cell order", i.e. particles
-// sorted by (tank, cell key), ties kept in the order of the previous sort):
+// sorted by global cell key, ties kept in the order of the previous sort):
 //   state X      positions (FP64, SoA per axis), velocity, density
 //                (FP64, or FP32 deviation rho - rho0 in the compensated
 //                form), dv/dt, drho/dt, id (upload index, bit 31 = wall),
-//                tank
-//   state Y      the same, gathered into the new cell order of a stage
+//                cell key, and in the compensated form the FP32 offset of
+//                the position from its cell corner
+//   state Y      positions and ids gathered into the new cell order of a
+//                stage (all fields when a prepare pass commits them back)
 //   pos records  neighbour positions packed per particle (FP64 absolute, or
-//                FP32 offsets from the particle's own cell corner)
+//                the FP32 cell offsets)
 //   data records v, rho, P = p / rho^2, cs, 1 / rho packed per particle
 //   step start   positions, velocity, density at the step start (two
 //                buffers, permuted along with every re-sort)
 //   cell table   first sorted index of every cell of every tank (+1 end)
+// The tank of a particle is implied by its cell key (tanks own disjoint,
+// consecutive key ranges).
 #pragma once
 
 #include <cstdint>
@@ -47,6 +51,9 @@ struct TankDev {
   double visc_eps2;    // 0.01 h^2 (Monaghan)
   uint32_t n_fluid;    // for bookkeeping
   uint32_t pad;
+  // FP32 copies for the compensated form (no FP64 conversions in kernels).
+  float h_f, hinv_f, w_f, wg_f, m_f, rho0_f, cs0_f, B_f, diff_k_f;
+  float visc_eps2_f, c02_f, pad_f;
 };
 
 struct PhysDev {
@@ -59,6 +66,7 @@ struct PhysDev {
   int32_t viscosity;
   int32_t diffusion;
   int32_t kernel;
+  float xi_f, g_f, mu_f, alpha_f, cfl_f, c_force_f, c_visc_f, pad_f;
 };
 
 // ---------------------------------------------------------------------------
@@ -248,6 +256,40 @@ __device__ __forceinline__ void cell_of(const TankDev& T, const double* x,
   }
 }
 
+// Tank of a global cell key: the last tank whose first cell is <= key.
+__device__ __forceinline__ uint32_t tank_of_key(uint32_t key,
+                                                const uint32_t* __restrict__ off,
+                                                int ntanks) {
+  int lo = 0, hi = ntanks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(off + mid) <= key) {
+      lo = mid;
+    } else {
+      hi = mid - 1;
+    }
+  }
+  return static_cast<uint32_t>(lo);
+}
+
+// Cell coordinates of a key of tank T (inverse of flat_cell).
+template<int D>
+__device__ __forceinline__ void cell_from_key(const TankDev& T, uint32_t key,
+                                              int* c) {
+  const uint32_t f = key - T.cell_off;
+  const uint32_t nx = static_cast<uint32_t>(T.nc[0]);
+  c[0] = static_cast<int>(f % nx);
+  const uint32_t rest = f / nx;
+  if constexpr (D == 2) {
+    c[1] = static_cast<int>(rest);
+    c[2] = 0;
+  } else {
+    const uint32_t ny = static_cast<uint32_t>(T.nc[1]);
+    c[1] = static_cast<int>(rest % ny);
+    c[2] = static_cast<int>(rest / ny);
+  }
+}
+
 template<int D>
 __device__ __forceinline__ uint32_t flat_cell(const TankDev& T, const int* c) {
   uint32_t f = static_cast<uint32_t>(c[0]);
@@ -304,9 +346,9 @@ __device__ __forceinline__ double density_from_potential_f64(
 // Compensated form: d = drho / rho0 in FP32.
 __device__ __forceinline__ void tait_f32(const PhysDev& P, const TankDev& T,
                                          float drho, float& p, float& c) {
-  const float d = drho / static_cast<float>(T.rho0);
-  const float B = static_cast<float>(T.B);
-  const float c0 = static_cast<float>(T.cs0);
+  const float d = __fdividef(drho, T.rho0_f);
+  const float B = T.B_f;
+  const float c0 = T.cs0_f;
   if (P.xi_is_7) {
     const float poly =
         7.f + d * (21.f + d * (35.f + d * (35.f + d * (21.f + d * (7.f + d)))));
@@ -315,30 +357,30 @@ __device__ __forceinline__ void tait_f32(const PhysDev& P, const TankDev& T,
     c = c0 * (x * x * x);
   } else {
     const float l = log1pf(d);
-    p = B * expm1f(static_cast<float>(P.xi) * l);
-    c = c0 * expf(0.5f * static_cast<float>(P.xi - 1.0) * l);
+    p = B * expm1f(P.xi_f * l);
+    c = c0 * expf(0.5f * (P.xi_f - 1.f) * l);
   }
 }
 
 __device__ __forceinline__ float potential_f32(const PhysDev& P,
                                                const TankDev& T, float drho) {
-  const float d = drho / static_cast<float>(T.rho0);
-  const float c02 = static_cast<float>(T.cs0 * T.cs0);
+  const float d = __fdividef(drho, T.rho0_f);
+  const float c02 = T.c02_f;
   if (P.xi_is_7) {
     const float poly =
         6.f + d * (15.f + d * (20.f + d * (15.f + d * (6.f + d))));
-    return c02 * d * poly / 6.f;
+    return c02 * d * poly * (1.f / 6.f);
   }
-  const float xi_1 = static_cast<float>(P.xi - 1.0);
+  const float xi_1 = P.xi_f - 1.f;
   return c02 * expm1f(xi_1 * log1pf(d)) / xi_1;
 }
 
 // Returns the density deviation rho - rho0.
 __device__ __forceinline__ float deviation_from_potential_f32(
     const PhysDev& P, const TankDev& T, float H) {
-  const float xi_1 = static_cast<float>(P.xi - 1.0);
-  const float u = xi_1 * H / static_cast<float>(T.cs0 * T.cs0);
-  return static_cast<float>(T.rho0) * expm1f(log1pf(u) / xi_1);
+  const float xi_1 = P.xi_f - 1.f;
+  const float u = xi_1 * H / T.c02_f;
+  return T.rho0_f * expm1f(log1pf(u) / xi_1);
 }
 
 // ---------------------------------------------------------------------------

@@ -25,8 +25,11 @@ struct EngineBase {
   virtual cudaError_t allocate(Context& C) = 0;
   // Copy host AoS arrays (upload order) into the home state.
   // Unpack the staged host arrays (upload order: r, v, rho in d_stage,
-  // d_stage2, d_stage3; dv/dt in d_stage4 when with_dv) into the home state.
+  // d_stage2, d_stage3; dv/dt in d_stage4 when with_dv) into the home state,
+  // then compute the cell keys.
   virtual cudaError_t upload_state(Context& C, bool with_dv) = 0;
+  // Recompute the home cell keys from the positions if they are stale.
+  virtual cudaError_t ensure_keys(Context& C) = 0;
   // Enqueue one full integrator step on C.stream.
   virtual cudaError_t enqueue_step(Context& C) = 0;
   // Enqueue FluidEquations::prepare: search + wall extrapolation, leaving
@@ -78,6 +81,7 @@ struct Context {
 
   // Common device buffers.
   TankDev* d_tanks = nullptr;
+  uint32_t* d_tank_off = nullptr;  // first global cell of each tank
   uint32_t* d_id_base = nullptr;
   uint32_t* d_wall_from = nullptr;
   uint32_t* d_tank_of = nullptr;  // tank of each upload index
@@ -92,6 +96,7 @@ struct Context {
   uint32_t* vals_b = nullptr;
   void* sort_scratch = nullptr;
   uint32_t* cell_start = nullptr;
+  void* cell_scratch = nullptr;
   uint32_t* wall_list = nullptr;
   double* d_stage = nullptr;  // n * dim doubles: upload / download staging
   double* d_stage2 = nullptr;
@@ -117,6 +122,7 @@ struct Context {
   int64_t graph_kernels = 0;
 
   bool walls_fresh = false;
+  bool keys_valid = false;  // home keys match the home positions
 
   // Profiling.
   bool profile = false;

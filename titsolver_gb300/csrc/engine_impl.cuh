@@ -32,11 +32,7 @@ class Engine final : public EngineBase {
       }
     };
     for (StateBuf<R>* S : {&X_, &Y_}) {
-      for (int k = 0; k < 3; ++k) {
-        S->pos[k] = nullptr;
-        S->vel[k] = nullptr;
-        S->dv[k] = nullptr;
-      }
+      *S = StateBuf<R>{};
       for (int k = 0; k < D; ++k) {
         A(S->pos[k], n);
         A(S->vel[k], n);
@@ -45,13 +41,14 @@ class Engine final : public EngineBase {
       A(S->rho, n);
       A(S->drho, n);
       A(S->id, n);
-      A(S->tank, n);
+    }
+    // The home keys live in the sort's first key buffer.
+    X_.key = C.keys_a;
+    if constexpr (F == TG_FP32C) {
+      for (int k = 0; k < D; ++k) A(X_.off[k], n);
     }
     for (StartBuf<R>& U : U_) {
-      for (int k = 0; k < 3; ++k) {
-        U.pos[k] = nullptr;
-        U.vel[k] = nullptr;
-      }
+      U = StartBuf<R>{};
       for (int k = 0; k < D; ++k) {
         A(U.pos[k], n);
         A(U.vel[k], n);
@@ -69,6 +66,16 @@ class Engine final : public EngineBase {
         X_, C.d_stage, C.d_stage2, C.d_stage3, with_dv ? C.d_stage4 : nullptr,
         C.d_tank_of, C.d_tanks, C.d_wall_from, C.n);
     C.launches += 1;
+    C.keys_valid = false;
+    return ensure_keys(C);
+  }
+
+  cudaError_t ensure_keys(Context& C) override {
+    if (C.keys_valid || C.n == 0) return cudaSuccess;
+    k_keys<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
+        X_, C.d_tank_of, C.d_tanks, C.n, C.d_err);
+    C.launches += 1;
+    C.keys_valid = true;
     return cudaGetLastError();
   }
 
@@ -97,27 +104,28 @@ class Engine final : public EngineBase {
     if (e != cudaSuccess) return e;
     StageArgs<D, F> a = args(C, 0);
     a.compute_dt = 0;
-    a.carry_derivs = 1;
+    a.carry = 1;
     int tok = C.group_begin(kGroupReorder);
-    k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
-    C.launches += 1;
+    e = reorder(C, a);
     C.group_end(tok);
+    if (e != cudaSuccess) return e;
     tok = C.group_begin(kGroupWalls);
     if (C.n_wall > 0) {
-      k_walls<D, F, K><<<grid_for(C.n_wall, 128), 128, 0, C.stream>>>(
+      k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
           a, C.n_wall);
       C.launches += 1;
     }
     k_commit<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
     C.launches += 1;
     C.group_end(tok);
+    C.keys_valid = true;
     return cudaGetLastError();
   }
 
   cudaError_t enqueue_pack(Context& C, int field) override {
     if (C.n == 0) return cudaSuccess;
     k_pack<D, R><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
-        X_, C.d_tanks, C.phys, field, C.d_stage, C.n);
+        X_, C.d_tank_of, C.d_tanks, C.phys, field, C.d_stage, C.n);
     C.launches += 1;
     return cudaGetLastError();
   }
@@ -130,10 +138,13 @@ class Engine final : public EngineBase {
     if (e != cudaSuccess) return e;
     StageArgs<D, F> a = args(C, 0);
     a.compute_dt = 0;
-    k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
+    e = reorder(C, a);
+    if (e != cudaSuccess) return e;
     k_neigh_count<D, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(
         a, C.d_id_base, counts, hashes, offsets, indices);
-    C.launches += 2;
+    C.launches += 1;
+    // The sort used the home keys as scratch and nothing rewrote them.
+    C.keys_valid = false;
     return cudaGetLastError();
   }
 
@@ -146,18 +157,18 @@ class Engine final : public EngineBase {
     int tok = C.group_begin(kGroupReorder);
     if (f32) {
       k_cloud_records<D, true><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
-          X_.pos[0], X_.pos[1], X_.pos[2], X_.id, X_.tank, C.perm,
-          C.d_cloud_rec, Y_.id, Y_.tank, C.n);
+          X_.pos[0], X_.pos[1], X_.pos[2], X_.id, C.perm, C.d_cloud_rec,
+          Y_.id, C.n);
     } else {
       k_cloud_records<D, false><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
-          X_.pos[0], X_.pos[1], X_.pos[2], X_.id, X_.tank, C.perm,
-          C.d_cloud_rec, Y_.id, Y_.tank, C.n);
+          X_.pos[0], X_.pos[1], X_.pos[2], X_.id, C.perm, C.d_cloud_rec,
+          Y_.id, C.n);
     }
     C.launches += 1;
     C.group_end(tok);
-    CloudArgs<D> ca{C.d_cloud_rec, Y_.id,  Y_.tank, C.cell_start, C.d_tanks,
-                    C.n,           C.k,    rho,     counts,       hashes,
-                    C.d_id_base};
+    CloudArgs<D> ca{C.d_cloud_rec, Y_.id, C.sorted_keys, C.cell_start,
+                    C.d_tanks,     C.d_tank_off, C.ntanks, C.n,
+                    C.k,           rho,   counts, hashes,  C.d_id_base};
     tok = C.group_begin(kGroupForces);
     if (f32) {
       k_sumdens<D, K, true><<<grid_for(C.n, 128), 128, 0, C.stream>>>(ca);
@@ -166,13 +177,14 @@ class Engine final : public EngineBase {
     }
     C.launches += 1;
     C.group_end(tok);
+    C.keys_valid = false;
     return cudaGetLastError();
   }
 
   int64_t launches_per_step(Context& C) override {
     const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
     const int stages = C.P.integrator == TG_SSPRK2 ? 2 : 3;
-    const int per_stage = 1 + 3 * passes + 1 + 2 + (C.n_wall > 0 ? 1 : 0);
+    const int per_stage = 3 * passes + 2 + 2 + (C.n_wall > 0 ? 1 : 0);
     return static_cast<int64_t>(stages) * per_stage + 1;
   }
 
@@ -184,10 +196,13 @@ class Engine final : public EngineBase {
     a.Usrc = U_[(stage + 1) % 2];
     a.Udst = U_[stage % 2];
     a.perm = C.perm;
+    a.skey = C.sorted_keys;
     a.posrec = posrec_;
     a.datrec = datrec_;
     a.cell_start = C.cell_start;
     a.tanks = C.d_tanks;
+    a.tank_off = C.d_tank_off;
+    a.ntanks = C.ntanks;
     a.phys = C.phys;
     a.dt = C.d_dt;
     a.wall_list = C.wall_list;
@@ -200,25 +215,32 @@ class Engine final : public EngineBase {
     a.lincomb = stage == 0 ? 0 : 1;
     a.w_new = 1.0;
     a.kahan = C.P.kahan;
-    a.carry_derivs = 0;
+    a.carry = 0;
     return a;
   }
 
-  cudaError_t enqueue_sort(Context& C) {
-    const int tok = C.group_begin(kGroupSort);
-    k_keys<D><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
-        X_.pos[0], X_.pos[1], X_.pos[2], X_.tank, C.d_tanks, C.n, C.keys_a,
-        C.d_err, C.d_wall_count);
+  cudaError_t reorder(Context& C, const StageArgs<D, F>& a) {
+    cudaError_t e = cudaMemsetAsync(C.d_wall_count, 0, sizeof(uint32_t), C.stream);
+    if (e != cudaSuccess) return e;
+    k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
     C.launches += 1;
+    return cudaGetLastError();
+  }
+
+  // Sort the home keys (valid on entry) into cell order and build the cell
+  // table.  The sort uses the home key buffer as scratch.
+  cudaError_t enqueue_sort(Context& C) {
+    cudaError_t e = ensure_keys(C);
+    if (e != cudaSuccess) return e;
+    const int tok = C.group_begin(kGroupSort);
     bool in_b = false;
-    cudaError_t e = radix_sort(C.keys_a, C.vals_a, C.keys_b, C.vals_b, C.n,
-                               C.key_bits, true, C.sort_scratch, &in_b,
-                               C.stream, &C.launches);
+    e = radix_sort(C.keys_a, C.vals_a, C.keys_b, C.vals_b, C.n, C.key_bits,
+                   true, C.sort_scratch, &in_b, C.stream, &C.launches);
     if (e != cudaSuccess) return e;
     C.sorted_keys = in_b ? C.keys_b : C.keys_a;
     C.perm = in_b ? C.vals_b : C.vals_a;
     e = build_cell_table(C.sorted_keys, C.n, C.total_cells, C.cell_start,
-                         C.stream, &C.launches);
+                         C.cell_scratch, C.stream, &C.launches);
     C.group_end(tok);
     return e;
   }
@@ -229,12 +251,12 @@ class Engine final : public EngineBase {
     StageArgs<D, F> a = args(C, s);
     a.w_new = w;
     int tok = C.group_begin(kGroupReorder);
-    k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
-    C.launches += 1;
+    e = reorder(C, a);
     C.group_end(tok);
+    if (e != cudaSuccess) return e;
     if (C.n_wall > 0) {
       tok = C.group_begin(kGroupWalls);
-      k_walls<D, F, K><<<grid_for(C.n_wall, 128), 128, 0, C.stream>>>(
+      k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
           a, C.n_wall);
       C.launches += 1;
       C.group_end(tok);
@@ -243,6 +265,8 @@ class Engine final : public EngineBase {
     k_forces<D, F, K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
     C.launches += 1;
     C.group_end(tok);
+    // k_forces and k_walls wrote the keys of the new positions.
+    C.keys_valid = true;
     return cudaGetLastError();
   }
 

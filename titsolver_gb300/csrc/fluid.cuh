@@ -3,16 +3,19 @@
 //
 // One stage of the reference's SSPRK substep (time_integrator.hpp:190-210:
 // prepare, [dt], continuity, momentum, Euler update; then lincomb) runs as:
-//   k_keys      cell key of every particle (FP64 positions)
-//   radix sort  stable, 32-bit keys (sort.cu)
+//   radix sort  stable sort of the cell keys (sort.cu)
 //   k_cell_table
 //   k_reorder   gather the state into cell order, pack neighbour records,
 //               Tait p, cs (+ the dt min-reduction in the first stage)
 //   k_walls     Shepard extrapolation of the wall density
 //               (FluidEquations::setup_boundary, fluid_equations.hpp:122-164)
 //   k_forces    fused continuity + momentum sums in gather form, Euler
-//               update and SSPRK linear combination
+//               update, SSPRK linear combination, and the cell key (and
+//               FP32 cell offset) of the new position for the next sort
 //               (fluid_equations.hpp:232-305, time_integrator.hpp:203-223)
+// Keys come from FP64 positions in k_keys only after an upload; afterwards
+// k_forces and k_walls write them, so no kernel recomputes cells from FP64
+// positions (FP64 issue is scarce on GB300).
 #pragma once
 
 #include <cstdint>
@@ -103,8 +106,9 @@ struct StateBuf {
   R* rho;  // FP64: rho; FP32C: rho - rho0
   R* dv[3];
   R* drho;
-  uint32_t* id;  // upload index | kWallBit for walls
-  uint32_t* tank;
+  uint32_t* id;   // upload index | kWallBit for walls
+  uint32_t* key;  // global cell key (home state only)
+  float* off[3];  // FP32C: offset from the cell corner (home state only)
 };
 
 template<class R>
@@ -121,10 +125,13 @@ struct StageArgs {
   StateBuf<R> X, Y;
   StartBuf<R> Usrc, Udst;
   const uint32_t* perm;
+  const uint32_t* skey;  // sorted keys (cell order)
   typename L::PosRec* posrec;
   typename L::DatRec* datrec;
   const uint32_t* cell_start;
   const TankDev* tanks;
+  const uint32_t* tank_off;  // first global cell of each tank
+  int ntanks;
   PhysDev phys;
   double* dt;
   uint32_t* wall_list;
@@ -137,7 +144,7 @@ struct StageArgs {
   int lincomb;       // apply (1 - w) Udst + w new
   double w_new;
   int kahan;
-  int carry_derivs;  // also gather dv/dt and drho/dt into Y
+  int carry;         // prepare pass: gather every field into Y
 };
 
 // ---------------------------------------------------------------------------
@@ -195,23 +202,33 @@ __device__ __forceinline__ float dist2_exact(const float* a, const float* b,
   return s;
 }
 
+__device__ __forceinline__ bool finite_bits(double x) {
+  return (static_cast<unsigned long long>(__double_as_longlong(x)) &
+          0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+
 // ---------------------------------------------------------------------------
-template<int D>
+// Cell key (and FP32 offset) of every home particle from its FP64 position;
+// runs after an upload.  The tank comes from the upload index.
+template<int D, int F>
 __global__ void __launch_bounds__(256)
-    k_keys(const double* __restrict__ px,
-           const double* __restrict__ py, const double* __restrict__ pz,
-           const uint32_t* __restrict__ tank, const TankDev* __restrict__ tanks,
-           int64_t n, uint32_t* __restrict__ keys, uint32_t* err,
-           uint32_t* wall_count) {
+    k_keys(StateBuf<typename Layout<D, F>::R> X,
+           const uint32_t* __restrict__ tank_of,
+           const TankDev* __restrict__ tanks, int64_t n, uint32_t* err) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i == 0 && wall_count != nullptr) *wall_count = 0;
   if (i >= n) return;
-  const TankDev& T = tanks[tank[i]];
-  double p[3] = {px[i], py[i], D == 3 ? pz[i] : 0.0};
+  const TankDev& T = tanks[tank_of[X.id[i] & kIdMask]];
+  double p[3] = {X.pos[0][i], X.pos[1][i], D == 3 ? X.pos[2][i] : 0.0};
   int c[3] = {0, 0, 0};
   bool outside = false;
   cell_of<D>(T, p, c, outside);
-  keys[i] = flat_cell<D>(T, c);
+  X.key[i] = flat_cell<D>(T, c);
+  if constexpr (F == TG_FP32C) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      X.off[k][i] = static_cast<float>(p[k] - (T.lo[k] + c[k] * T.cs));
+    }
+  }
   if (outside) {
     bool finite = true;
 #pragma unroll
@@ -231,6 +248,9 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
   uint32_t tk = 0xffffffffu;
   if (valid) {
     const uint32_t src = A.perm[j];
+    const uint32_t key = A.skey[j];
+    tk = tank_of_key(key, A.tank_off, A.ntanks);
+    const TankDev& T = A.tanks[tk];
     double p[3];
     R v[3];
 #pragma unroll
@@ -240,18 +260,16 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
     }
     const R rho = A.X.rho[src];
     const uint32_t id = A.X.id[src];
-    tk = A.X.tank[src];
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-      A.Y.pos[k][j] = p[k];
-      A.Y.vel[k][j] = v[k];
-    }
-    A.Y.rho[j] = rho;
+    for (int k = 0; k < D; ++k) A.Y.pos[k][j] = p[k];
     A.Y.id[j] = id;
-    A.Y.tank[j] = tk;
-    if (A.carry_derivs) {
+    if (A.carry) {
 #pragma unroll
-      for (int k = 0; k < D; ++k) A.Y.dv[k][j] = A.X.dv[k][src];
+      for (int k = 0; k < D; ++k) {
+        A.Y.vel[k][j] = v[k];
+        A.Y.dv[k][j] = A.X.dv[k][src];
+      }
+      A.Y.rho[j] = rho;
       A.Y.drho[j] = A.X.drho[src];
     }
     if (A.copy_start) {
@@ -269,7 +287,6 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
       }
       A.Udst.rho[j] = A.Usrc.rho[src];
     }
-    const TankDev& T = A.tanks[tk];
     // Neighbour position record.
     if constexpr (F == TG_FP64) {
       if constexpr (D == 2) {
@@ -278,14 +295,9 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
         A.posrec[j] = Pos64_3{p[0], p[1], p[2], 0.0};
       }
     } else {
-      int c[3] = {0, 0, 0};
-      bool outside = false;
-      cell_of<D>(T, p, c, outside);
       float o[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-      for (int k = 0; k < D; ++k) {
-        o[k] = static_cast<float>(p[k] - (T.lo[k] + c[k] * T.cs));
-      }
+      for (int k = 0; k < D; ++k) o[k] = A.X.off[k][src];
       if constexpr (D == 2) {
         A.posrec[j] = Pos32_2{o[0], o[1]};
       } else {
@@ -323,7 +335,7 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
       } else {
         float pr, c;
         tait_f32(A.phys, T, rho, pr, c);
-        const float inv = 1.f / (static_cast<float>(T.rho0) + rho);
+        const float inv = __frcp_rn(T.rho0_f + rho);
         A.datrec[j] = Dat32{v[0], v[1], D == 3 ? v[2] : 0.f, rho,
                             pr * inv * inv, c, inv, 0.f};
         if (A.compute_dt) {
@@ -336,15 +348,12 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
             v2 += v[2] * v[2];
             a2 += dvv[2] * dvv[2];
           }
-          const float h = static_cast<float>(T.h);
-          const float rhof = static_cast<float>(T.rho0) + rho;
-          const float dt_ac = static_cast<float>(A.phys.cfl) * h / (c + sqrtf(v2));
-          const float dt_vi =
-              static_cast<float>(A.phys.c_visc) * h * h * rhof /
-              static_cast<float>(A.phys.mu);
+          const float h = T.h_f;
+          const float rhof = T.rho0_f + rho;
+          const float dt_ac = A.phys.cfl_f * h / (c + sqrtf(v2));
+          const float dt_vi = A.phys.c_visc_f * h * h * rhof / A.phys.mu_f;
           const float dt_fo =
-              static_cast<float>(A.phys.c_force) *
-              sqrtf(h / fmaxf(sqrtf(a2), static_cast<float>(A.phys.g)));
+              A.phys.c_force_f * sqrtf(h / fmaxf(sqrtf(a2), A.phys.g_f));
           dt_a = static_cast<double>(fminf(dt_ac, fminf(dt_vi, dt_fo)));
         }
       }
@@ -373,40 +382,54 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
 // Wall extrapolation (fluid_equations.hpp:122-164) with a zero wall normal:
 //   rho_e = rho(H),  H = sum_b V_b H(rho_b) W_be / sum_b V_b W_be over fluid
 //   neighbours b (H = 0 when the Shepard sum is tiny); v_e = 0.
+// A team of kWallTeam lanes shares one wall: each lane takes every
+// kWallTeam-th candidate, then the team reduces by shuffles.
+constexpr int kWallTeam = 8;
+
 template<int D, int F, int K>
 __global__ void __launch_bounds__(128)
     k_walls(StageArgs<D, F> A, int64_t n_walls) {
   using R = typename StageArgs<D, F>::R;
-  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= n_walls) return;
-  const uint32_t e = A.wall_list[t];
-  const uint32_t tk = A.Y.tank[e];
+  const int64_t t =
+      (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / kWallTeam;
+  const int lane = threadIdx.x % kWallTeam;
+  const bool valid = t < n_walls;
+  const uint32_t e = valid ? A.wall_list[t] : 0u;
+  const uint32_t key = valid ? A.skey[e] : 0u;
+  const uint32_t tk = valid ? tank_of_key(key, A.tank_off, A.ntanks) : 0u;
   const TankDev& T = A.tanks[tk];
-  double pe[3] = {A.Y.pos[0][e], A.Y.pos[1][e], D == 3 ? A.Y.pos[2][e] : 0.0};
   int c[3] = {0, 0, 0};
-  bool outside = false;
-  cell_of<D>(T, pe, c, outside);
-  R rho_e;
+  cell_from_key<D>(T, key, c);
+  R rho_e = R(0);
   if constexpr (F == TG_FP64) {
+    double pe[3] = {0.0, 0.0, 0.0};
+    if (valid) load_pos(A.posrec, e, pe);
     const double R2 = T.radius2, hinv = T.hinv, w = T.w, m = T.m;
     double S = 0.0, H = 0.0;
-    for_cells<D, false>(T, c, A.k, A.cell_start,
-                        [&](uint32_t s, uint32_t en, int, int, int) {
-      for (uint32_t j = s; j < en; ++j) {
-        if (A.Y.id[j] & kWallBit) continue;
-        double pb[3], d[3];
-        load_pos(A.posrec, j, pb);
-        const double s2 = dist2_exact<D>(pb, pe, d);
-        if (s2 > R2) continue;
-        const Dat64 b = load_dat_coherent(A.datrec, j);
-        const double q = sqrt(s2) * hinv;
-        const double W = w * KernelPoly<K>::value(q);
-        const double Vb = m * b.invrho;
-        const double Hb = potential_f64(A.phys, T, b.rho);
-        S += Vb * W;
-        H += Vb * Hb * W;
-      }
-    });
+    if (valid) {
+      for_cells<D, false>(T, c, A.k, A.cell_start,
+                          [&](uint32_t s, uint32_t en, int, int, int) {
+        for (uint32_t j = s + lane; j < en; j += kWallTeam) {
+          if (A.Y.id[j] & kWallBit) continue;
+          double pb[3], d[3];
+          load_pos(A.posrec, j, pb);
+          const double s2 = dist2_exact<D>(pb, pe, d);
+          if (s2 > R2) continue;
+          const Dat64 b = load_dat_coherent(A.datrec, j);
+          const double W = w * KernelPoly<K>::value(sqrt(s2) * hinv);
+          const double Vb = m * b.invrho;
+          const double Hb = potential_f64(A.phys, T, b.rho);
+          S += Vb * W;
+          H += Vb * Hb * W;
+        }
+      });
+    }
+#pragma unroll
+    for (int o = kWallTeam / 2; o > 0; o >>= 1) {
+      S += __shfl_xor_sync(0xffffffffu, S, o, kWallTeam);
+      H += __shfl_xor_sync(0xffffffffu, H, o, kWallTeam);
+    }
+    if (!valid || lane != 0) return;
     const double Hs = fabs(S) <= 6.0554544523933395e-06 ? 0.0 : H / S;
     rho_e = density_from_potential_f64(A.phys, T, Hs);
     double pr, cc;
@@ -414,52 +437,61 @@ __global__ void __launch_bounds__(128)
     const double inv = 1.0 / rho_e;
     A.datrec[e] = Dat64{0.0, 0.0, 0.0, rho_e, pr * inv * inv, cc, inv, 0.0};
   } else {
-    const float R2 = T.radius2_f, hinv = static_cast<float>(T.hinv);
-    const float w = static_cast<float>(T.w), m = static_cast<float>(T.m);
+    const float R2 = T.radius2_f, hinv = T.hinv_f;
+    const float w = T.w_f, m = T.m_f;
     const float csz = T.cs_f;
     float oe[3] = {0.f, 0.f, 0.f};
-    load_pos(A.posrec, e, oe);
+    if (valid) load_pos(A.posrec, e, oe);
     Kahan S, H;
-    for_cells<D, true>(T, c, A.k, A.cell_start,
-                       [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
-      float oes[3];
-      oes[0] = oe[0] - dx * csz;
-      oes[1] = oe[1] - dy * csz;
-      oes[2] = D == 3 ? oe[2] - dz * csz : 0.f;
-      for (uint32_t j = s; j < en; ++j) {
-        if (A.Y.id[j] & kWallBit) continue;
-        float ob[3], d[3];
-        load_pos(A.posrec, j, ob);
-        const float s2 = dist2_exact<D>(oes, ob, d);
-        if (s2 > R2) continue;
-        const Dat32 b = load_dat_coherent(A.datrec, j);
-        const float q = sqrtf(s2) * hinv;
-        const float W = w * KernelPoly<K>::value(q);
-        const float Vb = m * b.invrho;
-        const float Hb = potential_f32(A.phys, T, b.drho);
-        S.add(Vb * W);
-        H.add(Vb * Hb * W);
-      }
-    });
-    const float Ss = S.value();
-    const float Hs = fabsf(Ss) <= 6.0554544523933395e-06f ? 0.f : H.value() / Ss;
+    if (valid) {
+      for_cells<D, true>(T, c, A.k, A.cell_start,
+                         [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+        float oes[3];
+        oes[0] = oe[0] - dx * csz;
+        oes[1] = oe[1] - dy * csz;
+        oes[2] = D == 3 ? oe[2] - dz * csz : 0.f;
+        for (uint32_t j = s + lane; j < en; j += kWallTeam) {
+          if (A.Y.id[j] & kWallBit) continue;
+          float ob[3], d[3];
+          load_pos(A.posrec, j, ob);
+          const float s2 = dist2_exact<D>(oes, ob, d);
+          if (s2 > R2) continue;
+          const Dat32 b = load_dat_coherent(A.datrec, j);
+          const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
+          const float Vb = m * b.invrho;
+          const float Hb = potential_f32(A.phys, T, b.drho);
+          S.add(Vb * W);
+          H.add(Vb * Hb * W);
+        }
+      });
+    }
+    float Ss = S.value(), Hv = H.value();
+#pragma unroll
+    for (int o = kWallTeam / 2; o > 0; o >>= 1) {
+      Ss += __shfl_xor_sync(0xffffffffu, Ss, o, kWallTeam);
+      Hv += __shfl_xor_sync(0xffffffffu, Hv, o, kWallTeam);
+    }
+    if (!valid || lane != 0) return;
+    const float Hs = fabsf(Ss) <= 6.0554544523933395e-06f ? 0.f : Hv / Ss;
     rho_e = deviation_from_potential_f32(A.phys, T, Hs);
     float pr, cc;
     tait_f32(A.phys, T, rho_e, pr, cc);
-    const float inv = 1.f / (static_cast<float>(T.rho0) + rho_e);
+    const float inv = 1.f / (T.rho0_f + rho_e);
     A.datrec[e] = Dat32{0.f, 0.f, 0.f, rho_e, pr * inv * inv, cc, inv, 0.f};
+#pragma unroll
+    for (int k = 0; k < D; ++k) A.X.off[k][e] = oe[k];
   }
   // The wall's home state.
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    A.X.pos[k][e] = pe[k];
+    A.X.pos[k][e] = A.Y.pos[k][e];
     A.X.vel[k][e] = R(0);
     A.X.dv[k][e] = R(0);
   }
   A.X.rho[e] = rho_e;
   A.X.drho[e] = R(0);
   A.X.id[e] = A.Y.id[e];
-  A.X.tank[e] = tk;
+  A.X.key[e] = key;
 }
 
 // ---------------------------------------------------------------------------
@@ -474,26 +506,37 @@ __global__ void __launch_bounds__(128)
 //   Monaghan Pi_ab = alpha h (c_a+c_b) (v_ab.r_ab) / ((|r|^2 + 0.01h^2)
 //                    (rho_a+rho_b)) for v_ab . r_ab < 0, else 0
 // then r' = r + dt v, v' = v + dt dv, rho' = rho + dt drho and, in the later
-// SSPRK stages, u = (1 - w) u_n + w u'.
+// SSPRK stages, u = (1 - w) u_n + w u'.  Last, the key (and FP32 offset)
+// of the new position for the next sort.
+// Resident 128-thread blocks per SM requested for k_forces: 8 for the 2D
+// compensated form (64 registers, latency hiding for its L1-bound loop), 6
+// in 3D (its wider state needs more registers), 4 for FP64 (its FP64 pipe
+// is the limit).
+template<int D, int F>
+constexpr int forces_min_blocks() {
+  return F == TG_FP32C ? (D == 2 ? 8 : 6) : 4;
+}
+
 template<int D, int F, int K>
-__global__ void __launch_bounds__(128, 4) k_forces(StageArgs<D, F> A) {
+__global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(StageArgs<D, F> A) {
   using R = typename StageArgs<D, F>::R;
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   const uint32_t id = A.Y.id[i];
   if (id & kWallBit) return;
-  const uint32_t tk = A.Y.tank[i];
+  const uint32_t key = A.skey[i];
+  const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
   const TankDev& T = A.tanks[tk];
-  double pa[3] = {A.Y.pos[0][i], A.Y.pos[1][i], D == 3 ? A.Y.pos[2][i] : 0.0};
   int c[3] = {0, 0, 0};
-  bool outside = false;
-  cell_of<D>(T, pa, c, outside);
+  cell_from_key<D>(T, key, c);
   const int visc = A.phys.viscosity, diff = A.phys.diffusion;
-  R dv_out[3];
+  R dv_out[3] = {R(0), R(0), R(0)};
   R drho_out;
   R va[3];
   R rho_self;
   if constexpr (F == TG_FP64) {
+    double pa[3] = {0.0, 0.0, 0.0};
+    load_pos(A.posrec, static_cast<uint32_t>(i), pa);
     const Dat64 a = load_dat(A.datrec, static_cast<uint32_t>(i));
     va[0] = a.vx;
     va[1] = a.vy;
@@ -553,18 +596,18 @@ __global__ void __launch_bounds__(128, 4) k_forces(StageArgs<D, F> A) {
     rho_self = a.drho;
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
-    const float R2 = T.radius2_f, hinv = static_cast<float>(T.hinv);
-    const float wg = static_cast<float>(T.wg), m = static_cast<float>(T.m);
-    const float mu2 = static_cast<float>(2.0 * A.phys.mu);
-    const float ah = static_cast<float>(A.phys.alpha * T.h);
-    const float eps2 = static_cast<float>(T.visc_eps2);
-    const float dk = static_cast<float>(T.diff_k);
-    const float rho0x2 = static_cast<float>(2.0 * T.rho0);
+    const float R2 = T.radius2_f, hinv = T.hinv_f;
+    const float wg = T.wg_f, m = T.m_f;
+    const float mu2 = 2.f * A.phys.mu_f;
+    const float ah = A.phys.alpha_f * T.h_f;
+    const float eps2 = T.visc_eps2_f;
+    const float dk = T.diff_k_f;
+    const float rho0x2 = 2.f * T.rho0_f;
     const float csz = T.cs_f;
     const bool kahan = A.kahan != 0;
     Kahan drho;
     Kahan dv[3];
-    dv[1].s = static_cast<float>(-A.phys.g);
+    dv[1].s = -A.phys.g_f;
     for_cells<D, true>(T, c, A.k, A.cell_start,
                        [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
       float oas[3];
@@ -622,43 +665,80 @@ __global__ void __launch_bounds__(128, 4) k_forces(StageArgs<D, F> A) {
     drho_out = drho.value();
   }
 
-  // Euler update (time_integrator.hpp:203-207) and SSPRK lincomb (:212-223).
+  // Euler update (time_integrator.hpp:203-207) and SSPRK lincomb (:212-223):
+  // positions in FP64, the rest in the form's type.
   const double dt = A.dt[tk];
-  const R dtr = static_cast<R>(dt);
-  double pn[3];
+  R dtr;
+  if constexpr (F == TG_FP64) {
+    dtr = dt;
+  } else {
+    dtr = __double2float_rn(dt);
+  }
+  double pn[3] = {0.0, 0.0, 0.0};
   R vn[3];
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    pn[k] = pa[k] + dt * static_cast<double>(va[k]);
+    pn[k] = fma(dt, static_cast<double>(va[k]), A.Y.pos[k][i]);
     vn[k] = va[k] + dtr * dv_out[k];
   }
   R rn = rho_self + dtr * drho_out;
   if (A.lincomb) {
     const double w = A.w_new, w0 = 1.0 - A.w_new;
-    const R wr = static_cast<R>(w), w0r = static_cast<R>(w0);
+    R wr, w0r;
+    if constexpr (F == TG_FP64) {
+      wr = w;
+      w0r = w0;
+    } else {
+      wr = __double2float_rn(w);
+      w0r = __double2float_rn(w0);
+    }
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-      pn[k] = w0 * A.Udst.pos[k][i] + w * pn[k];
+      pn[k] = fma(w0, A.Udst.pos[k][i], w * pn[k]);
       vn[k] = w0r * A.Udst.vel[k][i] + wr * vn[k];
     }
     rn = w0r * A.Udst.rho[i] + wr * rn;
   }
+  // Cell key (and offset) of the new position.
+  int cn[3] = {0, 0, 0};
+  if constexpr (F == TG_FP64) {
+    bool outside = false;
+    cell_of<D>(T, pn, cn, outside);
+    if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
+  } else {
+    // Offset from the old cell corner (exact FP64 difference, rounded once),
+    // then a shift by whole cells in FP32, clamped at the grid border.
+    bool outside = false;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const float o = __double2float_rn(
+          pn[k] - fma(static_cast<double>(c[k]), T.cs, T.lo[k]));
+      const float f = floorf(__fdividef(o, T.cs_f));
+      int ck = c[k] + (isfinite(f) ? static_cast<int>(f) : 0);
+      if (ck < 0 || ck >= T.nc[k]) {
+        outside = true;
+        ck = min(max(ck, 0), T.nc[k] - 1);
+      }
+      cn[k] = ck;
+      A.X.off[k][i] = o - static_cast<float>(ck - c[k]) * T.cs_f;
+    }
+    if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
+  }
+  A.X.key[i] = flat_cell<D>(T, cn);
+  bool finite = true;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     A.X.pos[k][i] = pn[k];
     A.X.vel[k][i] = vn[k];
     A.X.dv[k][i] = dv_out[k];
+    finite = finite && finite_bits(pn[k]) && isfinite(vn[k]);
   }
   A.X.rho[i] = rn;
   A.X.drho[i] = drho_out;
   A.X.id[i] = id;
-  A.X.tank[i] = tk;
-  bool finite = isfinite(static_cast<double>(rn));
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    finite = finite && isfinite(pn[k]) && isfinite(static_cast<double>(vn[k]));
+  if (!(finite && isfinite(rn))) {
+    atomicOr(A.err, static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
   }
-  if (!finite) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
 }
 
 // ---------------------------------------------------------------------------
@@ -673,17 +753,18 @@ __global__ void __launch_bounds__(128)
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   const uint32_t id = A.Y.id[i] & kIdMask;
-  const uint32_t tk = A.Y.tank[i];
+  const uint32_t key = A.skey[i];
+  const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
   const TankDev& T = A.tanks[tk];
   const uint32_t base = id_base[tk];
-  double pa[3] = {A.Y.pos[0][i], A.Y.pos[1][i], D == 3 ? A.Y.pos[2][i] : 0.0};
   int c[3] = {0, 0, 0};
-  bool outside = false;
-  cell_of<D>(T, pa, c, outside);
+  cell_from_key<D>(T, key, c);
   int32_t cnt = 0;
   uint64_t hs = 0;
   int64_t out = offsets != nullptr ? offsets[id] : 0;
   if constexpr (F == TG_FP64) {
+    double pa[3] = {0.0, 0.0, 0.0};
+    load_pos(A.posrec, static_cast<uint32_t>(i), pa);
     for_cells<D, false>(T, c, A.k, A.cell_start,
                         [&](uint32_t s, uint32_t en, int, int, int) {
       for (uint32_t j = s; j < en; ++j) {
@@ -734,9 +815,11 @@ template<int D>
 struct CloudArgs {
   const void* pos;  // Pos64_* or Pos32_* absolute positions, cell order
   const uint32_t* id;
-  const uint32_t* tank;
+  const uint32_t* skey;  // sorted keys
   const uint32_t* cell_start;
   const TankDev* tanks;
+  const uint32_t* tank_off;
+  int ntanks;
   int64_t n;
   int k;
   double* rho;       // by upload id
@@ -750,9 +833,12 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   const uint32_t id = A.id[i] & kIdMask;
-  const uint32_t tk = A.tank[i];
+  const uint32_t key = A.skey[i];
+  const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
   const TankDev& T = A.tanks[tk];
   const uint32_t base = A.id_base[tk];
+  int c[3] = {0, 0, 0};
+  cell_from_key<D>(T, key, c);
   int32_t cnt = 0;
   uint64_t hs = 0;
   double rho;
@@ -761,9 +847,6 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
     const P* pr = static_cast<const P*>(A.pos);
     double pa[3] = {0.0, 0.0, 0.0};
     load_pos(pr, static_cast<uint32_t>(i), pa);
-    int c[3] = {0, 0, 0};
-    bool outside = false;
-    cell_of<D>(T, pa, c, outside);
     const double R2 = T.radius2, hinv = T.hinv, wm = T.w * T.m;
     double acc = 0.0;
     for_cells<D, false>(T, c, A.k, A.cell_start,
@@ -784,12 +867,8 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
     const P* pr = static_cast<const P*>(A.pos);
     float pa[3] = {0.f, 0.f, 0.f};
     load_pos(pr, static_cast<uint32_t>(i), pa);
-    double pad[3] = {pa[0], pa[1], pa[2]};
-    int c[3] = {0, 0, 0};
-    bool outside = false;
-    cell_of<D>(T, pad, c, outside);
-    const float R2 = T.radius2_f, hinv = static_cast<float>(T.hinv);
-    const float wm = static_cast<float>(T.w) * static_cast<float>(T.m);
+    const float R2 = T.radius2_f, hinv = T.hinv_f;
+    const float wm = T.w_f * T.m_f;
     Kahan acc;
     for_cells<D, false>(T, c, A.k, A.cell_start,
                         [&](uint32_t s, uint32_t en, int, int, int) {
@@ -828,10 +907,17 @@ __global__ void __launch_bounds__(256) k_commit(StageArgs<D, F> A) {
   A.X.rho[j] = A.Y.rho[j];
   A.X.drho[j] = A.Y.drho[j];
   A.X.id[j] = id;
-  A.X.tank[j] = A.Y.tank[j];
+  A.X.key[j] = A.skey[j];
+  if constexpr (F == TG_FP32C) {
+    float o[3] = {0.f, 0.f, 0.f};
+    load_pos(A.posrec, static_cast<uint32_t>(j), o);
+#pragma unroll
+    for (int k = 0; k < D; ++k) A.X.off[k][j] = o[k];
+  }
 }
 
-// Upload: AoS doubles in upload order into the SoA home state.
+// Upload: AoS doubles in upload order into the SoA home state (keys follow
+// from k_keys).
 template<int D, class R>
 __global__ void __launch_bounds__(256)
     k_unpack(StateBuf<R> X, const double* __restrict__ r,
@@ -856,19 +942,18 @@ __global__ void __launch_bounds__(256)
   }
   X.drho[i] = R(0);
   X.id[i] = static_cast<uint32_t>(i) | (wall ? kWallBit : 0u);
-  X.tank[i] = tk;
 }
 
 // Download: one field of the home state into upload order (AoS for vectors).
 template<int D, class R>
 __global__ void __launch_bounds__(256)
-    k_pack(StateBuf<R> X, const TankDev* tanks, PhysDev phys, int field,
+    k_pack(StateBuf<R> X, const uint32_t* __restrict__ tank_of,
+           const TankDev* tanks, PhysDev phys, int field,
            double* __restrict__ out, int64_t n) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t id = X.id[i] & kIdMask;
-  const uint32_t tk = X.tank[i];
-  const TankDev& T = tanks[tk];
+  const TankDev& T = tanks[tank_of[id]];
   switch (field) {
     case TG_FIELD_R:
 #pragma unroll
@@ -903,7 +988,7 @@ __global__ void __launch_bounds__(256)
 
 // End of step: advance per-tank time, keep dt, reset the dt reduction.
 static __global__ void k_step_end(double* dt, double* dt_last, double* time,
-                           uint32_t* err, int ntanks) {
+                                  uint32_t* err, int ntanks) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntanks) return;
   const double d = dt[t];
@@ -916,17 +1001,15 @@ static __global__ void k_step_end(double* dt, double* dt_last, double* time,
 }
 
 // Cloud records for the summation density: absolute positions in cell order
-// (FP64, or rounded once to FP32), ids and tanks.
+// (FP64, or rounded once to FP32) and ids.
 template<int D, bool F32>
 __global__ void __launch_bounds__(256)
     k_cloud_records(const double* __restrict__ px,
                     const double* __restrict__ py,
                     const double* __restrict__ pz,
                     const uint32_t* __restrict__ id_in,
-                    const uint32_t* __restrict__ tank_in,
                     const uint32_t* __restrict__ perm, void* rec,
-                    uint32_t* __restrict__ id_out,
-                    uint32_t* __restrict__ tank_out, int64_t n) {
+                    uint32_t* __restrict__ id_out, int64_t n) {
   const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const uint32_t s = perm[j];
@@ -945,7 +1028,6 @@ __global__ void __launch_bounds__(256)
     }
   }
   id_out[j] = id_in[s];
-  tank_out[j] = tank_in[s];
 }
 
 }  // namespace tg

@@ -35,15 +35,17 @@ constexpr size_t kOffKeysB = kOffKeysA + align256(kU32);
 constexpr size_t kOffValsA = kOffKeysB + align256(kU32);
 constexpr size_t kOffValsB = kOffValsA + align256(kU32);
 constexpr size_t kOffIds = kOffValsB + align256(kU32);
-constexpr size_t kOffTanks = kOffIds + align256(kU32);
 constexpr size_t kHistBytes =
     sizeof(uint32_t) * kRadixBins * ((kMaxPoints + kSortTile - 1) / kSortTile + 1) + 256;
-constexpr size_t kOffHist = kOffTanks + align256(kU32);
+constexpr size_t kOffHist = kOffIds + align256(kU32);
 constexpr size_t kOffCells = kOffHist + align256(kHistBytes);
 constexpr size_t kOffRecs = kOffCells + align256(sizeof(uint32_t) * (kMaxCells + 1));
-constexpr size_t kOffTank = kOffRecs + align256(sizeof(Pos64_3) * kMaxPoints);
+constexpr size_t kOffBounds = kOffRecs + align256(sizeof(Pos64_3) * kMaxPoints);
+constexpr size_t kBoundsBytes = sizeof(uint32_t) * ((kMaxCells + 256) / 256 + 2);
+constexpr size_t kOffTank = kOffBounds + align256(kBoundsBytes);
 constexpr size_t kOffIdBase = kOffTank + align256(sizeof(TankDev));
 constexpr size_t kScratchBytes = kOffIdBase + 256;
+static_assert(kBoundsBytes >= 4 * ((kMaxCells + 256) / 256 + 2), "coarse bounds");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -164,7 +166,7 @@ template<int D>
 __global__ void __launch_bounds__(256)
     k_na_records(const double* __restrict__ r, const uint32_t* __restrict__ perm,
                  int64_t n, Pos64_3* __restrict__ rec3, Pos64_2* __restrict__ rec2,
-                 uint32_t* __restrict__ ids, uint32_t* __restrict__ tank) {
+                 uint32_t* __restrict__ ids) {
   const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const uint32_t s = perm[j];
@@ -174,7 +176,6 @@ __global__ void __launch_bounds__(256)
     rec3[j] = Pos64_3{r[int64_t(s) * 3], r[int64_t(s) * 3 + 1], r[int64_t(s) * 3 + 2], 0.0};
   }
   ids[j] = s;
-  tank[j] = 0;
 }
 
 template<int D, int K>
@@ -186,7 +187,6 @@ cudaError_t run(unsigned char* base, int64_t n, const double* r, double h,
   auto* vals_a = reinterpret_cast<uint32_t*>(base + kOffValsA);
   auto* vals_b = reinterpret_cast<uint32_t*>(base + kOffValsB);
   auto* ids = reinterpret_cast<uint32_t*>(base + kOffIds);
-  auto* tank = reinterpret_cast<uint32_t*>(base + kOffTanks);
   auto* cells = reinterpret_cast<uint32_t*>(base + kOffCells);
   auto* recs = base + kOffRecs;
   auto* T = reinterpret_cast<TankDev*>(base + kOffTank);
@@ -204,11 +204,14 @@ cudaError_t run(unsigned char* base, int64_t n, const double* r, double h,
   if (e != cudaSuccess) return e;
   const uint32_t* sorted = in_b ? keys_b : keys_a;
   const uint32_t* perm = in_b ? vals_b : vals_a;
-  e = build_cell_table(sorted, n, kMaxCells, cells, s, &launches);
+  e = build_cell_table(sorted, n, kMaxCells, cells, base + kOffBounds, s, &launches);
   if (e != cudaSuccess) return e;
   k_na_records<D><<<g, 256, 0, s>>>(r, perm, n, reinterpret_cast<Pos64_3*>(recs),
-                                    reinterpret_cast<Pos64_2*>(recs), ids, tank);
-  CloudArgs<D> a{recs, ids, tank, cells, T, n, 1, rho, counts, hashes, id_base};
+                                    reinterpret_cast<Pos64_2*>(recs), ids);
+  // One tank whose first cell (and first id) is 0: id_base doubles as the
+  // tank cell-offset table.
+  CloudArgs<D> a{recs, ids, sorted, cells, T, id_base, 1, n, 1, rho, counts, hashes,
+                 id_base};
   k_sumdens<D, K, false><<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(a);
   return cudaGetLastError();
 }

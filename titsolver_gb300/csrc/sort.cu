@@ -161,15 +161,19 @@ __global__ void __launch_bounds__(kSortThreads)
   }
 }
 
-// One thread per cell: cell_start[c] = lower_bound(keys, c).  Every cell
-// costs the same (log2 n probes), so long runs of empty cells (air above
-// the water, the grid margins) do not serialise on one thread.
-__global__ void __launch_bounds__(256)
-    k_cell_table(const uint32_t* __restrict__ keys, int64_t n,
-                 uint32_t total_cells, uint32_t* __restrict__ cell_start) {
-  const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (c > static_cast<int64_t>(total_cells)) return;
-  int64_t lo = 0, hi = n;
+// cell_start[c] = lower_bound(keys, c) for every cell, in two passes:
+//   k_coarse_bounds  one warp per block of kTableCells cells finds
+//                    lower_bound(keys, first cell of the block) with 32-way
+//                    probes (about log32(n) dependent loads)
+//   k_cell_table     one thread per cell; the keys between the block's two
+//                    coarse bounds are staged in shared memory (when they
+//                    fit) and each thread searches there.
+// Long runs of empty cells cost the same as full ones.
+constexpr int kTableCells = 256;
+constexpr int kTableStage = 2048;
+
+__device__ __forceinline__ int64_t lower_bound_global(
+    const uint32_t* __restrict__ keys, int64_t lo, int64_t hi, int64_t c) {
   while (lo < hi) {
     const int64_t mid = (lo + hi) >> 1;
     if (static_cast<int64_t>(__ldg(keys + mid)) < c) {
@@ -178,7 +182,69 @@ __global__ void __launch_bounds__(256)
       hi = mid;
     }
   }
-  cell_start[c] = static_cast<uint32_t>(lo);
+  return lo;
+}
+
+__global__ void __launch_bounds__(256)
+    k_coarse_bounds(const uint32_t* __restrict__ keys, int64_t n,
+                    int64_t nblocks, uint32_t* __restrict__ bounds) {
+  const int64_t b = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (b > nblocks) return;  // whole warps exit together
+  const int64_t c = b * kTableCells;
+  int64_t lo = 0, hi = n;  // answer in [lo, hi]
+  while (hi - lo > 32) {
+    const int64_t step = (hi - lo) / 33;
+    const int64_t probe = lo + step * (lane + 1);
+    const bool ge = static_cast<int64_t>(__ldg(keys + probe)) >= c;
+    const uint32_t mask = __ballot_sync(0xffffffffu, ge);
+    if (mask == 0) {
+      lo = lo + step * 32 + 1;
+    } else {
+      const int first = __ffs(mask) - 1;
+      const int64_t new_hi = lo + step * (first + 1);
+      lo = first == 0 ? lo : lo + step * first + 1;
+      hi = new_hi;
+    }
+  }
+  // At most 32 candidates left: one probe per lane.
+  const int64_t probe = lo + lane;
+  const bool ge = probe >= hi || static_cast<int64_t>(__ldg(keys + probe)) >= c;
+  const uint32_t mask = __ballot_sync(0xffffffffu, ge);
+  if (lane == 0) {
+    bounds[b] = static_cast<uint32_t>(mask != 0 ? lo + (__ffs(mask) - 1) : hi);
+  }
+}
+
+__global__ void __launch_bounds__(kTableCells)
+    k_cell_table(const uint32_t* __restrict__ keys, int64_t n,
+                 uint32_t total_cells, const uint32_t* __restrict__ bounds,
+                 uint32_t* __restrict__ cell_start) {
+  __shared__ uint32_t s_keys[kTableStage];
+  const int64_t lo = bounds[blockIdx.x];
+  const int64_t hi = bounds[blockIdx.x + 1];
+  const int64_t cnt = hi - lo;
+  const int64_t c = static_cast<int64_t>(blockIdx.x) * kTableCells + threadIdx.x;
+  if (cnt <= kTableStage) {
+    for (int64_t t = threadIdx.x; t < cnt; t += blockDim.x) {
+      s_keys[t] = keys[lo + t];
+    }
+    __syncthreads();
+    if (c > static_cast<int64_t>(total_cells)) return;
+    int a = 0, b = static_cast<int>(cnt);
+    while (a < b) {
+      const int mid = (a + b) >> 1;
+      if (static_cast<int64_t>(s_keys[mid]) < c) {
+        a = mid + 1;
+      } else {
+        b = mid;
+      }
+    }
+    cell_start[c] = static_cast<uint32_t>(lo + a);
+  } else {
+    if (c > static_cast<int64_t>(total_cells)) return;
+    cell_start[c] = static_cast<uint32_t>(lower_bound_global(keys, lo, hi, c));
+  }
 }
 
 }  // namespace
@@ -223,15 +289,24 @@ cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
   return cudaGetLastError();
 }
 
+size_t cell_table_scratch_bytes(uint32_t total_cells) {
+  const int64_t nblocks = (static_cast<int64_t>(total_cells) + kTableCells) / kTableCells;
+  return sizeof(uint32_t) * static_cast<size_t>(nblocks + 2);
+}
+
 cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
                              uint32_t total_cells, uint32_t* cell_start,
-                             cudaStream_t stream, int64_t* launches) {
-  const int64_t threads = static_cast<int64_t>(total_cells) + 1;
-  const int block = 256;
-  const int64_t grid = (threads + block - 1) / block;
-  k_cell_table<<<static_cast<unsigned>(grid), block, 0, stream>>>(
-      sorted_keys, n, total_cells, cell_start);
-  *launches += 1;
+                             void* scratch, cudaStream_t stream,
+                             int64_t* launches) {
+  // Cells 0..total_cells inclusive, in blocks of kTableCells.
+  const int64_t nblocks = (static_cast<int64_t>(total_cells) + kTableCells) / kTableCells;
+  uint32_t* bounds = static_cast<uint32_t*>(scratch);
+  const int64_t warps = nblocks + 1;  // bounds[0..nblocks]
+  k_coarse_bounds<<<static_cast<unsigned>((warps * 32 + 255) / 256), 256, 0, stream>>>(
+      sorted_keys, n, nblocks, bounds);
+  k_cell_table<<<static_cast<unsigned>(nblocks), kTableCells, 0, stream>>>(
+      sorted_keys, n, total_cells, bounds, cell_start);
+  *launches += 2;
   return cudaGetLastError();
 }
 

@@ -31,10 +31,14 @@ cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
                        bool identity_vals, void* scratch, bool* result_in_b,
                        cudaStream_t stream, int64_t* launches);
 
+// Scratch needed by build_cell_table (bytes).
+size_t cell_table_scratch_bytes(uint32_t total_cells);
+
 // cell_start[c] = first sorted index whose key >= c, for c in
-// [0, total_cells]; cell_start[total_cells] = n.
+// [0, total_cells]; cell_start[total_cells] = n.  Two kernels.
 cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
                              uint32_t total_cells, uint32_t* cell_start,
-                             cudaStream_t stream, int64_t* launches);
+                             void* scratch, cudaStream_t stream,
+                             int64_t* launches);
 
 }  // namespace tg

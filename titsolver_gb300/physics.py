@@ -24,7 +24,7 @@ def reference_params(dim: int = 2, precision: int = _abi.TG_FP64,
     p.viscosity = _abi.TG_VISC_MORRIS
     p.diffusion = _abi.TG_DIFF_FERRARI
     p.post_integrate = _abi.TG_POST_PREPARE
-    p.cells_per_radius = 1
+    p.cells_per_radius = 2
     p.kahan = 1
     p.device = -1
     p.xi = 7.0
