@@ -129,6 +129,10 @@ typedef struct tg_params {
   int32_t cells_per_radius; /* grid cells per support radius, 1..3 */
   int32_t kahan;            /* FP32C: 1 = compensated sums, 0 = plain */
   int32_t device;           /* CUDA device ordinal; -1 = the current one */
+  int32_t staging;          /* 2D FP32C: read neighbour windows from
+                               shared memory (1) or through L1 (0, default;
+                               measured faster on GB300) */
+  int32_t reserved1;
   double xi;      /* Tait polytropic index */
   double g;       /* gravity, acting along -axis 1 */
   double mu;      /* Morris dynamic viscosity */

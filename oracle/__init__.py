@@ -28,7 +28,8 @@ class _Params(ctypes.Structure):
     # Same layout as tg_params of include/titgpu.h.
     _fields_ = [(n, ctypes.c_int32) for n in (
         "dim", "precision", "kernel", "integrator", "viscosity", "diffusion",
-        "post_integrate", "cells_per_radius", "kahan", "device")] + [
+        "post_integrate", "cells_per_radius", "kahan", "device", "staging",
+        "reserved1")] + [
         (n, ctypes.c_double) for n in (
             "xi", "g", "mu", "alpha", "delta", "cfl", "c_force", "c_visc")]
 

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(gpu_lib):
 
 
 def test_struct_layouts_match_header():
-    assert ctypes.sizeof(_abi.TgParams) == 10 * 4 + 8 * 8
+    assert ctypes.sizeof(_abi.TgParams) == 12 * 4 + 8 * 8
     assert ctypes.sizeof(_abi.TgTank) == 2 * 8 + 4 * 8
     assert ctypes.sizeof(_abi.TgProfile) == 5 * 8 + 3 * 8
 

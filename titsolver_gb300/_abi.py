@@ -57,6 +57,8 @@ class TgParams(ctypes.Structure):
         ("cells_per_radius", ctypes.c_int32),
         ("kahan", ctypes.c_int32),
         ("device", ctypes.c_int32),
+        ("staging", ctypes.c_int32),
+        ("reserved1", ctypes.c_int32),
         ("xi", ctypes.c_double),
         ("g", ctypes.c_double),
         ("mu", ctypes.c_double),

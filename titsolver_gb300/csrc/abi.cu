@@ -198,6 +198,7 @@ void tg_params_default(tg_params* p) {
   p->cells_per_radius = 2;
   p->kahan = 1;
   p->device = -1;
+  p->staging = 0;
   p->xi = 7.0;
   p->g = 9.81;
   p->mu = 0.001;

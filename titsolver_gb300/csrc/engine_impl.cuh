@@ -14,6 +14,18 @@ inline unsigned grid_for(int64_t n, int block) {
   return static_cast<unsigned>((n + block - 1) / block);
 }
 
+// Compile-time physics preset of the compensated force kernel for params.
+inline int physics_preset(const tg_params& P) {
+  if (!P.kahan) return kPhysGeneric;
+  if (P.viscosity == TG_VISC_MONAGHAN && P.diffusion == TG_DIFF_MOLTENI) {
+    return kPhysTextbook;
+  }
+  if (P.viscosity == TG_VISC_MORRIS && P.diffusion == TG_DIFF_FERRARI) {
+    return kPhysReference;
+  }
+  return kPhysGeneric;
+}
+
 template<int D, int F, int K>
 class Engine final : public EngineBase {
  public:
@@ -262,7 +274,27 @@ class Engine final : public EngineBase {
       C.group_end(tok);
     }
     tok = C.group_begin(kGroupForces);
-    k_forces<D, F, K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+    const unsigned grid = grid_for(C.n, 128);
+    if constexpr (F == TG_FP32C) {
+      const int phys = physics_preset(C.P);
+      bool staged = false;
+      if constexpr (D == 2) {
+        if (C.P.staging) {
+          k_forces_staged2<K><<<grid, 128, 0, C.stream>>>(a);
+          staged = true;
+        }
+      }
+      if (staged) {
+      } else if (phys == kPhysTextbook) {
+        k_forces<D, F, K, kPhysTextbook><<<grid, 128, 0, C.stream>>>(a);
+      } else if (phys == kPhysReference) {
+        k_forces<D, F, K, kPhysReference><<<grid, 128, 0, C.stream>>>(a);
+      } else {
+        k_forces<D, F, K><<<grid, 128, 0, C.stream>>>(a);
+      }
+    } else {
+      k_forces<D, F, K><<<grid, 128, 0, C.stream>>>(a);
+    }
     C.launches += 1;
     C.group_end(tok);
     // k_forces and k_walls wrote the keys of the new positions.

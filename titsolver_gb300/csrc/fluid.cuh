@@ -508,6 +508,7 @@ __global__ void __launch_bounds__(128)
 // then r' = r + dt v, v' = v + dt dv, rho' = rho + dt drho and, in the later
 // SSPRK stages, u = (1 - w) u_n + w u'.  Last, the key (and FP32 offset)
 // of the new position for the next sort.
+
 // Resident 128-thread blocks per SM requested for k_forces: 8 for the 2D
 // compensated form (64 registers, latency hiding for its L1-bound loop), 6
 // in 3D (its wider state needs more registers), 4 for FP64 (its FP64 pipe
@@ -517,7 +518,172 @@ constexpr int forces_min_blocks() {
   return F == TG_FP32C ? (D == 2 ? 8 : 6) : 4;
 }
 
-template<int D, int F, int K>
+// Physics presets the compensated force kernel is specialised for (the
+// per-pair term choices become compile-time): generic reads them at run
+// time.
+enum { kPhysGeneric = 0, kPhysTextbook = 1, kPhysReference = 2 };
+
+// Pair sums of the compensated form for one target.
+template<int D, int K, int Phys = kPhysGeneric>
+struct PairF32 {
+  float va[3];
+  Dat32 a;
+  float R2, hinv, wg, m, mu2, ah, eps2, dk, rho0x2;
+  int visc, diff;
+  bool kahan;
+  Kahan drho, dv[3];
+
+  __device__ __forceinline__ void init(const PhysDev& P, const TankDev& T,
+                                       const Dat32& own, int kahan_on) {
+    a = own;
+    va[0] = own.vx;
+    va[1] = own.vy;
+    va[2] = own.vz;
+    R2 = T.radius2_f;
+    hinv = T.hinv_f;
+    wg = T.wg_f;
+    m = T.m_f;
+    mu2 = 2.f * P.mu_f;
+    ah = P.alpha_f * T.h_f;
+    eps2 = T.visc_eps2_f;
+    dk = T.diff_k_f;
+    rho0x2 = 2.f * T.rho0_f;
+    visc = P.viscosity;
+    diff = P.diffusion;
+    kahan = kahan_on != 0;
+    dv[1].s = -P.g_f;
+  }
+
+  // One neighbour at r_ab = d (|d|^2 = s2 <= R2, b != a).
+  __device__ __forceinline__ void add(const float* d, float s2, const Dat32& b) {
+    const float rinv = rsqrtf(s2);
+    const float r = s2 * rinv;
+    const float q = r * hinv;
+    const float Fk = grad_factor<K>(q, rinv, wg, hinv);
+    const float vb[3] = {b.vx, b.vy, b.vz};
+    float vd = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) vd += (va[k] - vb[k]) * d[k];
+    const float drab = a.drho - b.drho;
+    const int df = Phys == kPhysTextbook    ? TG_DIFF_MOLTENI
+                   : Phys == kPhysReference ? TG_DIFF_FERRARI
+                                            : diff;
+    const int vs = Phys == kPhysTextbook    ? TG_VISC_MONAGHAN
+                   : Phys == kPhysReference ? TG_VISC_MORRIS
+                                            : visc;
+    float cont = vd;
+    if (df == TG_DIFF_FERRARI) {
+      cont += fmaxf(a.c, b.c) * drab * r * b.invrho;
+    } else if (df == TG_DIFF_MOLTENI) {
+      cont += dk * drab * b.invrho;
+    }
+    const float dr = m * Fk * cont;
+    float Pi;
+    if (vs == TG_VISC_MORRIS) {
+      Pi = mu2 * vd * a.invrho * b.invrho * (rinv * rinv);
+    } else {
+      Pi = vd < 0.f ? __fdividef(ah * vd * (a.c + b.c),
+                                 (s2 + eps2) * (rho0x2 + a.drho + b.drho))
+                    : 0.f;
+    }
+    const float coef = m * (Pi - (a.P + b.P)) * Fk;
+    if (Phys != kPhysGeneric || kahan) {
+      drho.add(dr);
+#pragma unroll
+      for (int k = 0; k < D; ++k) dv[k].add(coef * d[k]);
+    } else {
+      drho.s += dr;
+#pragma unroll
+      for (int k = 0; k < D; ++k) dv[k].s += coef * d[k];
+    }
+  }
+};
+
+// Euler update (time_integrator.hpp:203-207), SSPRK lincomb (:212-223) and
+// the cell key (and FP32 offset) of the new position; positions in FP64,
+// the rest in the form's type.
+template<int D, int F>
+__device__ __forceinline__ void forces_epilogue(
+    const StageArgs<D, F>& A, int64_t i, uint32_t id, uint32_t tk,
+    const TankDev& T, const int* c, const typename StageArgs<D, F>::R* va,
+    typename StageArgs<D, F>::R rho_self,
+    const typename StageArgs<D, F>::R* dv_out,
+    typename StageArgs<D, F>::R drho_out) {
+  using R = typename StageArgs<D, F>::R;
+  const double dt = A.dt[tk];
+  R dtr;
+  if constexpr (F == TG_FP64) {
+    dtr = dt;
+  } else {
+    dtr = __double2float_rn(dt);
+  }
+  double pn[3] = {0.0, 0.0, 0.0};
+  R vn[3];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    pn[k] = fma(dt, static_cast<double>(va[k]), A.Y.pos[k][i]);
+    vn[k] = va[k] + dtr * dv_out[k];
+  }
+  R rn = rho_self + dtr * drho_out;
+  if (A.lincomb) {
+    const double w = A.w_new, w0 = 1.0 - A.w_new;
+    R wr, w0r;
+    if constexpr (F == TG_FP64) {
+      wr = w;
+      w0r = w0;
+    } else {
+      wr = __double2float_rn(w);
+      w0r = __double2float_rn(w0);
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      pn[k] = fma(w0, A.Udst.pos[k][i], w * pn[k]);
+      vn[k] = w0r * A.Udst.vel[k][i] + wr * vn[k];
+    }
+    rn = w0r * A.Udst.rho[i] + wr * rn;
+  }
+  int cn[3] = {0, 0, 0};
+  if constexpr (F == TG_FP64) {
+    bool outside = false;
+    cell_of<D>(T, pn, cn, outside);
+    if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
+  } else {
+    // Offset from the old cell corner (exact FP64 difference, rounded once),
+    // then a shift by whole cells in FP32, clamped at the grid border.
+    bool outside = false;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const float o = __double2float_rn(
+          pn[k] - fma(static_cast<double>(c[k]), T.cs, T.lo[k]));
+      const float f = floorf(__fdividef(o, T.cs_f));
+      int ck = c[k] + (isfinite(f) ? static_cast<int>(f) : 0);
+      if (ck < 0 || ck >= T.nc[k]) {
+        outside = true;
+        ck = min(max(ck, 0), T.nc[k] - 1);
+      }
+      cn[k] = ck;
+      A.X.off[k][i] = o - static_cast<float>(ck - c[k]) * T.cs_f;
+    }
+    if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
+  }
+  A.X.key[i] = flat_cell<D>(T, cn);
+  bool finite = true;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    A.X.pos[k][i] = pn[k];
+    A.X.vel[k][i] = vn[k];
+    A.X.dv[k][i] = dv_out[k];
+    finite = finite && finite_bits(pn[k]) && isfinite(vn[k]);
+  }
+  A.X.rho[i] = rn;
+  A.X.drho[i] = drho_out;
+  A.X.id[i] = id;
+  if (!(finite && isfinite(rn))) {
+    atomicOr(A.err, static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
+  }
+}
+
+template<int D, int F, int K, int Phys = kPhysGeneric>
 __global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(StageArgs<D, F> A) {
   using R = typename StageArgs<D, F>::R;
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -529,12 +695,12 @@ __global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(Stage
   const TankDev& T = A.tanks[tk];
   int c[3] = {0, 0, 0};
   cell_from_key<D>(T, key, c);
-  const int visc = A.phys.viscosity, diff = A.phys.diffusion;
   R dv_out[3] = {R(0), R(0), R(0)};
   R drho_out;
   R va[3];
   R rho_self;
   if constexpr (F == TG_FP64) {
+    const int visc = A.phys.viscosity, diff = A.phys.diffusion;
     double pa[3] = {0.0, 0.0, 0.0};
     load_pos(A.posrec, static_cast<uint32_t>(i), pa);
     const Dat64 a = load_dat(A.datrec, static_cast<uint32_t>(i));
@@ -589,25 +755,11 @@ __global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(Stage
     for (int k = 0; k < D; ++k) dv_out[k] = dv[k];
     drho_out = drho;
   } else {
-    const Dat32 a = load_dat(A.datrec, static_cast<uint32_t>(i));
-    va[0] = a.vx;
-    va[1] = a.vy;
-    va[2] = a.vz;
-    rho_self = a.drho;
+    PairF32<D, K, Phys> acc;
+    acc.init(A.phys, T, load_dat(A.datrec, static_cast<uint32_t>(i)), A.kahan);
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
-    const float R2 = T.radius2_f, hinv = T.hinv_f;
-    const float wg = T.wg_f, m = T.m_f;
-    const float mu2 = 2.f * A.phys.mu_f;
-    const float ah = A.phys.alpha_f * T.h_f;
-    const float eps2 = T.visc_eps2_f;
-    const float dk = T.diff_k_f;
-    const float rho0x2 = 2.f * T.rho0_f;
     const float csz = T.cs_f;
-    const bool kahan = A.kahan != 0;
-    Kahan drho;
-    Kahan dv[3];
-    dv[1].s = -A.phys.g_f;
     for_cells<D, true>(T, c, A.k, A.cell_start,
                        [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
       float oas[3];
@@ -622,123 +774,156 @@ __global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(Stage
         for (int k = 0; k < D; ++k) d[k] = oas[k] - ob[k];
         float s2 = d[0] * d[0] + d[1] * d[1];
         if constexpr (D == 3) s2 += d[2] * d[2];
-        if (s2 > R2) continue;
-        const Dat32 b = load_dat(A.datrec, j);
-        const float rinv = rsqrtf(s2);
-        const float r = s2 * rinv;
-        const float q = r * hinv;
-        const float Fk = grad_factor<K>(q, rinv, wg, hinv);
-        const float vb[3] = {b.vx, b.vy, b.vz};
-        float vd = 0.f;
-#pragma unroll
-        for (int k = 0; k < D; ++k) vd += (va[k] - vb[k]) * d[k];
-        const float drab = a.drho - b.drho;
-        float cont = vd;
-        if (diff == TG_DIFF_FERRARI) {
-          cont += fmaxf(a.c, b.c) * drab * r * b.invrho;
-        } else if (diff == TG_DIFF_MOLTENI) {
-          cont += dk * drab * b.invrho;
-        }
-        const float dr = m * Fk * cont;
-        float Pi;
-        if (visc == TG_VISC_MORRIS) {
-          Pi = mu2 * vd * a.invrho * b.invrho * (rinv * rinv);
-        } else {
-          Pi = vd < 0.f ? __fdividef(ah * vd * (a.c + b.c),
-                                     (s2 + eps2) * (rho0x2 + a.drho + b.drho))
-                        : 0.f;
-        }
-        const float coef = m * (Pi - (a.P + b.P)) * Fk;
-        if (kahan) {
-          drho.add(dr);
-#pragma unroll
-          for (int k = 0; k < D; ++k) dv[k].add(coef * d[k]);
-        } else {
-          drho.s += dr;
-#pragma unroll
-          for (int k = 0; k < D; ++k) dv[k].s += coef * d[k];
-        }
+        if (s2 > acc.R2) continue;
+        acc.add(d, s2, load_dat(A.datrec, j));
       }
     });
 #pragma unroll
-    for (int k = 0; k < D; ++k) dv_out[k] = dv[k].value();
-    drho_out = drho.value();
+    for (int k = 0; k < D; ++k) {
+      va[k] = acc.va[k];
+      dv_out[k] = acc.dv[k].value();
+    }
+    rho_self = acc.a.drho;
+    drho_out = acc.drho.value();
   }
+  forces_epilogue<D, F>(A, i, id, tk, T, c, va, rho_self, dv_out, drho_out);
+}
 
-  // Euler update (time_integrator.hpp:203-207) and SSPRK lincomb (:212-223):
-  // positions in FP64, the rest in the form's type.
-  const double dt = A.dt[tk];
-  R dtr;
-  if constexpr (F == TG_FP64) {
-    dtr = dt;
-  } else {
-    dtr = __double2float_rn(dt);
-  }
-  double pn[3] = {0.0, 0.0, 0.0};
-  R vn[3];
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    pn[k] = fma(dt, static_cast<double>(va[k]), A.Y.pos[k][i]);
-    vn[k] = va[k] + dtr * dv_out[k];
-  }
-  R rn = rho_self + dtr * drho_out;
-  if (A.lincomb) {
-    const double w = A.w_new, w0 = 1.0 - A.w_new;
-    R wr, w0r;
-    if constexpr (F == TG_FP64) {
-      wr = w;
-      w0r = w0;
-    } else {
-      wr = __double2float_rn(w);
-      w0r = __double2float_rn(w0);
-    }
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-      pn[k] = fma(w0, A.Udst.pos[k][i], w * pn[k]);
-      vn[k] = w0r * A.Udst.vel[k][i] + wr * vn[k];
-    }
-    rn = w0r * A.Udst.rho[i] + wr * rn;
-  }
-  // Cell key (and offset) of the new position.
-  int cn[3] = {0, 0, 0};
-  if constexpr (F == TG_FP64) {
-    bool outside = false;
-    cell_of<D>(T, pn, cn, outside);
-    if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
-  } else {
-    // Offset from the old cell corner (exact FP64 difference, rounded once),
-    // then a shift by whole cells in FP32, clamped at the grid border.
-    bool outside = false;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-      const float o = __double2float_rn(
-          pn[k] - fma(static_cast<double>(c[k]), T.cs, T.lo[k]));
-      const float f = floorf(__fdividef(o, T.cs_f));
-      int ck = c[k] + (isfinite(f) ? static_cast<int>(f) : 0);
-      if (ck < 0 || ck >= T.nc[k]) {
-        outside = true;
-        ck = min(max(ck, 0), T.nc[k] - 1);
+// 2D compensated form with the block's neighbour window staged in shared
+// memory.  A block of 128 consecutive (cell-ordered) targets whose first
+// and last target share a tank and a row of cells needs, for every target,
+// only the 2k+1 rows around that row over x in [x_first - k, x_last + k];
+// each of those row segments is contiguous in cell order, so the block
+// copies them (position and data records) into shared memory with coalesced
+// 16-byte loads and every target then reads its candidates from there.
+// Blocks that straddle rows or tanks, or whose window exceeds the staging
+// capacity, read from global memory as k_forces does.
+constexpr int kStageCap = 800;  // records: 800 x (8 + 32) B = 32 KB
+constexpr int kStageRows = 7;   // 2k + 1 for k <= 3
+
+template<int K>
+__global__ void __launch_bounds__(128, 7)
+    k_forces_staged2(StageArgs<2, TG_FP32C> A) {
+  __shared__ __align__(16) float2 s_pos[kStageCap];
+  __shared__ __align__(16) float4 s_dat[2 * kStageCap];
+  __shared__ uint32_t s_gbeg[kStageRows], s_goff[kStageRows + 1];
+  __shared__ int s_ok, s_rows, s_ylo;
+  const int64_t i0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
+  const int64_t i = i0 + threadIdx.x;
+  if (threadIdx.x == 0) {
+    s_ok = 0;
+    const int64_t ilast = min(i0 + static_cast<int64_t>(blockDim.x), A.n) - 1;
+    const uint32_t k0 = A.skey[i0], k1 = A.skey[ilast];
+    const uint32_t t0 = tank_of_key(k0, A.tank_off, A.ntanks);
+    const uint32_t t1 = tank_of_key(k1, A.tank_off, A.ntanks);
+    if (t0 == t1) {
+      const TankDev& T = A.tanks[t0];
+      int c0[3], c1[3];
+      cell_from_key<2>(T, k0, c0);
+      cell_from_key<2>(T, k1, c1);
+      if (c0[1] == c1[1] && 2 * A.k + 1 <= kStageRows) {
+        const int ylo = max(c0[1] - A.k, 0), yhi = min(c0[1] + A.k, T.nc[1] - 1);
+        const int xlo = max(c0[0] - A.k, 0), xhi = min(c1[0] + A.k, T.nc[0] - 1);
+        uint32_t off = 0;
+        for (int y = ylo; y <= yhi; ++y) {
+          const uint32_t row = T.cell_off + static_cast<uint32_t>(y) * T.nc[0];
+          const uint32_t gb = __ldg(A.cell_start + row + xlo);
+          const uint32_t ge = __ldg(A.cell_start + row + xhi + 1);
+          s_gbeg[y - ylo] = gb;
+          s_goff[y - ylo] = off;
+          off += ge - gb;
+        }
+        s_goff[yhi - ylo + 1] = off;
+        s_rows = yhi - ylo + 1;
+        s_ylo = ylo;
+        s_ok = off <= static_cast<uint32_t>(kStageCap) ? 1 : 0;
       }
-      cn[k] = ck;
-      A.X.off[k][i] = o - static_cast<float>(ck - c[k]) * T.cs_f;
     }
-    if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
   }
-  A.X.key[i] = flat_cell<D>(T, cn);
-  bool finite = true;
+  __syncthreads();
+  const bool staged = s_ok != 0;
+  if (staged) {
+    const float2* gpos = reinterpret_cast<const float2*>(A.posrec);
+    const float4* gdat = reinterpret_cast<const float4*>(A.datrec);
+    for (int r = 0; r < s_rows; ++r) {
+      const uint32_t gb = s_gbeg[r], off = s_goff[r];
+      const uint32_t len = s_goff[r + 1] - off;
+      for (uint32_t t = threadIdx.x; t < len; t += blockDim.x) {
+        s_pos[off + t] = __ldg(gpos + gb + t);
+      }
+      for (uint32_t t = threadIdx.x; t < 2 * len; t += blockDim.x) {
+        s_dat[2 * off + t] = __ldg(gdat + 2 * static_cast<size_t>(gb) + t);
+      }
+    }
+  }
+  __syncthreads();
+  if (i >= A.n) return;
+  const uint32_t id = A.Y.id[i];
+  if (id & kWallBit) return;
+  const uint32_t key = A.skey[i];
+  const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
+  const TankDev& T = A.tanks[tk];
+  int c[3] = {0, 0, 0};
+  cell_from_key<2>(T, key, c);
+  PairF32<2, K> acc;
+  acc.init(A.phys, T, load_dat(A.datrec, static_cast<uint32_t>(i)), A.kahan);
+  float oa[3] = {0.f, 0.f, 0.f};
+  load_pos(A.posrec, static_cast<uint32_t>(i), oa);
+  const float csz = T.cs_f;
+  if (staged) {
+    const int xlo = max(c[0] - A.k, 0), xhi = min(c[0] + A.k, T.nc[0] - 1);
+    for (int r = 0; r < s_rows; ++r) {
+      const int y = s_ylo + r;
+      const uint32_t row = T.cell_off + static_cast<uint32_t>(y) * T.nc[0];
+      const int32_t shift = static_cast<int32_t>(s_goff[r]) - static_cast<int32_t>(s_gbeg[r]);
+      float oas[3];
+      oas[1] = oa[1] - (y - c[1]) * csz;
+      uint32_t gs = __ldg(A.cell_start + row + xlo);
+      for (int x = xlo; x <= xhi; ++x) {
+        const uint32_t ge = __ldg(A.cell_start + row + x + 1);
+        oas[0] = oa[0] - (x - c[0]) * csz;
+        for (uint32_t j = gs; j < ge; ++j) {
+          if (j == static_cast<uint32_t>(i)) continue;
+          const int sj = static_cast<int>(j) + shift;
+          const float2 ob = s_pos[sj];
+          float d[3] = {oas[0] - ob.x, oas[1] - ob.y, 0.f};
+          const float s2 = d[0] * d[0] + d[1] * d[1];
+          if (s2 > acc.R2) continue;
+          const float4 b0 = s_dat[2 * sj], b1 = s_dat[2 * sj + 1];
+          acc.add(d, s2, Dat32{b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w});
+        }
+        gs = ge;
+      }
+    }
+  } else {
+    for_cells<2, true>(T, c, A.k, A.cell_start,
+                       [&](uint32_t s, uint32_t en, int dx, int dy, int) {
+      float oas[3];
+      oas[0] = oa[0] - dx * csz;
+      oas[1] = oa[1] - dy * csz;
+      for (uint32_t j = s; j < en; ++j) {
+        if (j == static_cast<uint32_t>(i)) continue;
+        float ob[3], d[3];
+        load_pos(A.posrec, j, ob);
+        d[0] = oas[0] - ob[0];
+        d[1] = oas[1] - ob[1];
+        d[2] = 0.f;
+        const float s2 = d[0] * d[0] + d[1] * d[1];
+        if (s2 > acc.R2) continue;
+        acc.add(d, s2, load_dat(A.datrec, j));
+      }
+    });
+  }
+  float va[3], dv_out[3];
 #pragma unroll
-  for (int k = 0; k < D; ++k) {
-    A.X.pos[k][i] = pn[k];
-    A.X.vel[k][i] = vn[k];
-    A.X.dv[k][i] = dv_out[k];
-    finite = finite && finite_bits(pn[k]) && isfinite(vn[k]);
+  for (int k = 0; k < 2; ++k) {
+    va[k] = acc.va[k];
+    dv_out[k] = acc.dv[k].value();
   }
-  A.X.rho[i] = rn;
-  A.X.drho[i] = drho_out;
-  A.X.id[i] = id;
-  if (!(finite && isfinite(rn))) {
-    atomicOr(A.err, static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
-  }
+  va[2] = 0.f;
+  dv_out[2] = 0.f;
+  forces_epilogue<2, TG_FP32C>(A, i, id, tk, T, c, va, acc.a.drho, dv_out,
+                               acc.drho.value());
 }
 
 // ---------------------------------------------------------------------------
