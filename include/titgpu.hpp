@@ -1,0 +1,738 @@
+/*
+ * titgpu.hpp - C++20 host mirror of TitSolver's particle-array,
+ * fluid-equation and time-integrator API, driving the GB300 path through the
+ * C ABI of titgpu.h.
+ *
+ * The reference API is header-only C++26 with closed concepts
+ * (source/tit/sph/particle_mesh.hpp:263-264, time_integrator.hpp:25-26), so a
+ * GPU backend cannot be plugged into it; this header restates the names and
+ * call shapes a titwcsph-style driver uses instead:
+ *
+ *   ParticleArray{Space<Real, Dim>{}, integrator}   particle_array.hpp:160-162
+ *   particles.append(ParticleType::fluid|fixed)     particle_array.hpp:188-199
+ *   r[a] = ..., m[a] = ..., rho[a] = ..., h[particles] = h_0
+ *                                                   field.hpp:172-218
+ *   particles.all() / fluid() / fixed()             particle_array.hpp:203-228
+ *   TaitEquationOfState{cs_0, rho_0[, xi]}          equation_of_state.hpp:19-72
+ *   FluidEquations{g, mu, domain, containment, eos, kernel}
+ *                                                   fluid_equations.hpp:61-69
+ *   SSPRKIntegrator{equations, SSPRKOrder::three}   time_integrator.hpp:153-156
+ *   SymplecticEulerIntegrator{equations}            time_integrator.hpp:31-75
+ *   VelocityVerletIntegrator{equations}             time_integrator.hpp:80-129
+ *   ParticleMesh{geom::GridSearch{h_0}, ...}        particle_mesh.hpp:53-61
+ *   equations.initialize(mesh, particles)           fluid_equations.hpp:79-89
+ *   dt = integrator.step(mesh, particles)           time_integrator.hpp:161-185
+ *
+ * The particle state lives on the GPU once initialize() has run.  Host field
+ * access after a step downloads the state first; a host write is uploaded
+ * (tg_particles_update) before the next step.  Errors throw tit::Exception,
+ * as TIT_ENSURE does (source/tit/core/exception.hpp:81).
+ *
+ * Walls are fixed particles ("particle walls, no faces"): the domain surface
+ * must be empty and every fluid particle must lie inside the containment,
+ * which then gives gamma = 1 and no face terms in the reference equations
+ * (fluid_equations.hpp:122-163).  A non-empty surface throws.
+ *
+ * GPU-only choices (precision form, the textbook term set, CFL constants)
+ * come in an optional trailing sph::GpuOptions argument of FluidEquations.
+ */
+#ifndef TITGPU_HPP
+#define TITGPU_HPP
+
+#include <array>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <ranges>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "titgpu.h"
+
+namespace tit {
+
+/// Error thrown for every failed call (the role of tit::Exception).
+class Exception : public std::runtime_error {
+public:
+  using std::runtime_error::runtime_error;
+};
+
+namespace gpu_detail {
+inline void ensure(int status, tg_context* ctx, const char* what) {
+  if (status == TG_OK) return;
+  std::string msg = std::string{what} + " failed: " + tg_status_string(status);
+  if (ctx != nullptr) {
+    const char* why = tg_last_error(ctx);
+    if (why != nullptr && *why != '\0') msg += " (" + std::string{why} + ")";
+  }
+  throw Exception{msg};
+}
+} // namespace gpu_detail
+
+template<class T>
+constexpr auto pow2(T x) noexcept -> T {
+  return x * x;
+}
+
+/// Small fixed-size vector with the arithmetic a driver writes.
+template<class Real, std::size_t Dim>
+class Vec {
+public:
+  constexpr Vec() noexcept = default;
+  template<class... Args>
+    requires(sizeof...(Args) == Dim && Dim > 1)
+  constexpr Vec(Args... args) noexcept : c_{static_cast<Real>(args)...} {}
+
+  constexpr auto operator[](std::size_t i) noexcept -> Real& { return c_[i]; }
+  constexpr auto operator[](std::size_t i) const noexcept -> const Real& {
+    return c_[i];
+  }
+  static constexpr auto dim() noexcept -> std::size_t { return Dim; }
+
+  constexpr auto operator+=(const Vec& o) noexcept -> Vec& {
+    for (std::size_t i = 0; i < Dim; ++i) c_[i] += o.c_[i];
+    return *this;
+  }
+  constexpr auto operator-=(const Vec& o) noexcept -> Vec& {
+    for (std::size_t i = 0; i < Dim; ++i) c_[i] -= o.c_[i];
+    return *this;
+  }
+  constexpr auto operator*=(Real s) noexcept -> Vec& {
+    for (auto& x : c_) x *= s;
+    return *this;
+  }
+  friend constexpr auto operator+(Vec a, const Vec& b) noexcept -> Vec {
+    return a += b;
+  }
+  friend constexpr auto operator-(Vec a, const Vec& b) noexcept -> Vec {
+    return a -= b;
+  }
+  friend constexpr auto operator*(Real s, Vec a) noexcept -> Vec {
+    return a *= s;
+  }
+  friend constexpr auto operator*(Vec a, Real s) noexcept -> Vec {
+    return a *= s;
+  }
+  friend constexpr auto operator/(Vec a, Real s) noexcept -> Vec {
+    for (auto& x : a.c_) x /= s;
+    return a;
+  }
+  friend constexpr auto operator==(const Vec&, const Vec&) noexcept
+      -> bool = default;
+
+private:
+  std::array<Real, Dim> c_{};
+};
+
+template<class T, class... U>
+Vec(T, U...) -> Vec<std::common_type_t<T, U...>, 1 + sizeof...(U)>;
+
+namespace geom {
+
+/// Boundary surface.  The GPU path runs with particle walls, so a surface
+/// handed to FluidEquations must stay empty; the type exists so that a
+/// driver's domain declaration compiles.
+template<class V>
+class Surface {
+public:
+  auto append_vert(const V& v) -> std::size_t {
+    verts_.push_back(v);
+    return verts_.size() - 1;
+  }
+  void append_face(std::array<std::size_t, V::dim()> face) {
+    faces_.push_back(face);
+  }
+  auto num_verts() const noexcept -> std::size_t { return verts_.size(); }
+  auto num_faces() const noexcept -> std::size_t { return faces_.size(); }
+  auto vert(std::size_t i) const -> const V& { return verts_.at(i); }
+
+private:
+  std::vector<V> verts_;
+  std::vector<std::array<std::size_t, V::dim()>> faces_;
+};
+
+/// Grid neighbour search with the given cell spacing
+/// (source/tit/geom/search/grid_search.hpp:73-113).  On the GPU the spacing
+/// picks how many grid cells span the kernel support radius (1, 2 or 3).
+struct GridSearch {
+  double spacing;
+  explicit GridSearch(double cell_spacing) : spacing{cell_spacing} {
+    if (!(cell_spacing > 0.0)) throw Exception{"GridSearch: spacing <= 0"};
+  }
+};
+
+/// Face search and partitioners of the reference mesh.  The GPU path has no
+/// faces and sums in gather form, so these only record the driver's choice.
+struct GridFaceSearch {
+  double spacing;
+  explicit GridFaceSearch(double cell_spacing) : spacing{cell_spacing} {}
+};
+struct RecursiveInertialBisection {};
+struct KMeansClustering {};
+struct PixelatedPartition {
+  template<class... Args>
+  explicit PixelatedPartition(Args&&... /*args*/) noexcept {}
+};
+
+/// Containment functor that accepts every point.
+struct AllInside {
+  template<class V>
+  constexpr auto operator()(const V& /*point*/) const noexcept -> bool {
+    return true;
+  }
+};
+
+} // namespace geom
+
+namespace sph {
+
+template<class Real, std::size_t Dim>
+struct Space {
+  using real_t = Real;
+  static constexpr std::size_t dim = Dim;
+};
+
+/// Particle types (source/tit/sph/particle_array.hpp).
+enum class ParticleType : std::uint8_t { fluid, fixed, count };
+
+// Smoothing kernels: the closed set of source/tit/sph/kernel.hpp:459-465.
+// `unit_radius` is the support radius in units of h.
+struct CubicSplineKernel {
+  static constexpr std::int32_t gpu_id = TG_KERNEL_CUBIC_SPLINE;
+  static constexpr double unit_radius = 2.0;
+};
+struct QuarticSplineKernel {
+  static constexpr std::int32_t gpu_id = TG_KERNEL_QUARTIC_SPLINE;
+  static constexpr double unit_radius = 2.5;
+};
+struct QuinticSplineKernel {
+  static constexpr std::int32_t gpu_id = TG_KERNEL_QUINTIC_SPLINE;
+  static constexpr double unit_radius = 3.0;
+};
+struct QuarticWendlandKernel {
+  static constexpr std::int32_t gpu_id = TG_KERNEL_WENDLAND_C2;
+  static constexpr double unit_radius = 2.0;
+};
+struct SixthOrderWendlandKernel {
+  static constexpr std::int32_t gpu_id = TG_KERNEL_WENDLAND_C4;
+  static constexpr double unit_radius = 2.0;
+};
+struct EighthOrderWendlandKernel {
+  static constexpr std::int32_t gpu_id = TG_KERNEL_WENDLAND_C6;
+  static constexpr double unit_radius = 2.0;
+};
+
+/// Tait equation of state (source/tit/sph/equation_of_state.hpp:19-72).
+template<class Num>
+class TaitEquationOfState {
+public:
+  constexpr explicit TaitEquationOfState(Num cs_0, Num rho_0, Num xi = Num{7})
+      : cs_0_{cs_0}, rho_0_{rho_0}, xi_{xi} {
+    if (!(cs_0 > Num{0}) || !(rho_0 > Num{0}) || !(xi > Num{1})) {
+      throw Exception{"TaitEquationOfState: need cs_0 > 0, rho_0 > 0, xi > 1"};
+    }
+  }
+  auto pressure_from_density(Num rho) const -> Num {
+    return rho_0_ * pow2(cs_0_) / xi_ * (std::pow(rho / rho_0_, xi_) - 1);
+  }
+  auto sound_speed_from_density(Num rho) const -> Num {
+    return cs_0_ * std::pow(rho / rho_0_, (xi_ - 1) / 2);
+  }
+  constexpr auto cs_0() const noexcept -> Num { return cs_0_; }
+  constexpr auto rho_0() const noexcept -> Num { return rho_0_; }
+  constexpr auto xi() const noexcept -> Num { return xi_; }
+
+private:
+  Num cs_0_;
+  Num rho_0_;
+  Num xi_;
+};
+
+/// Arithmetic form of the GPU pair sums.
+enum class Precision : std::int32_t {
+  fp64 = TG_FP64,                  ///< plain FP64
+  fp32_compensated = TG_FP32C,     ///< FP32 sums with Kahan compensation
+};
+
+/// GPU-side choices with no counterpart in the reference constructor.  The
+/// defaults are the reference's own terms: Morris viscosity with the given
+/// mu, Ferrari diffusion, CFL 0.4, C_force 0.25, C_visc 0.125
+/// (fluid_equations.hpp:518-520).
+struct GpuOptions {
+  Precision precision = Precision::fp64;
+  std::int32_t viscosity = TG_VISC_MORRIS;
+  std::int32_t diffusion = TG_DIFF_FERRARI;
+  double alpha = 0.0; ///< Monaghan artificial viscosity (TG_VISC_MONAGHAN)
+  double delta = 0.0; ///< delta-SPH coefficient (TG_DIFF_MOLTENI)
+  double cfl = 0.4;
+  double c_force = 0.25;
+  double c_visc = 0.125;
+  bool kahan = true;
+  std::int32_t device = -1; ///< CUDA ordinal; -1 = the current device
+  bool graph = true;        ///< replay each step as a CUDA graph
+  bool autotune = false;    ///< pick launch shapes with tg_autotune
+};
+
+template<class PA>
+class ParticleView;
+template<class Real, std::size_t Dim>
+class ParticleArray;
+
+/// Thin handle of the reference ParticleMesh: it keeps the search spacing
+/// (the neighbour structure itself lives on the GPU, inside the particles'
+/// context).
+class ParticleMesh {
+public:
+  template<class... Rest>
+  explicit ParticleMesh(geom::GridSearch search, Rest&&... /*rest*/) noexcept
+      : spacing_{search.spacing} {}
+  auto spacing() const noexcept -> double { return spacing_; }
+
+private:
+  double spacing_;
+};
+
+/// Fluid equations (source/tit/sph/fluid_equations.hpp:61-69), particle
+/// walls only.
+template<class Real, std::size_t Dim, class Containment, class Kernel>
+class FluidEquations {
+public:
+  FluidEquations(Real g,
+                 Real mu,
+                 geom::Surface<Vec<Real, Dim>> domain,
+                 Containment containment,
+                 TaitEquationOfState<Real> eos,
+                 Kernel /*kernel*/,
+                 GpuOptions options = {})
+      : g_{g}, mu_{mu}, containment_{std::move(containment)}, eos_{eos},
+        options_{options} {
+    if (domain.num_faces() != 0) {
+      throw Exception{"FluidEquations: the GPU path runs with particle walls; "
+                      "the domain surface must be empty"};
+    }
+  }
+
+  /// Create the GPU context and upload the particles
+  /// (FluidEquations::initialize, fluid_equations.hpp:79-89).
+  template<class PA>
+  void initialize(ParticleMesh& mesh, PA& particles) const {
+    for (const auto a : particles.fluid()) {
+      if (!containment_(std::as_const(particles).position(a.index()))) {
+        throw Exception{"FluidEquations::initialize: a fluid particle lies "
+                        "outside the containment (gamma = 0)"};
+      }
+    }
+    tg_params P;
+    tg_params_default(&P);
+    P.dim = static_cast<std::int32_t>(Dim);
+    P.precision = static_cast<std::int32_t>(options_.precision);
+    P.kernel = Kernel::gpu_id;
+    P.integrator = particles.integrator_id();
+    P.viscosity = options_.viscosity;
+    P.diffusion = options_.diffusion;
+    P.kahan = options_.kahan ? 1 : 0;
+    P.device = options_.device;
+    P.xi = static_cast<double>(eos_.xi());
+    P.g = static_cast<double>(g_);
+    P.mu = static_cast<double>(mu_);
+    P.alpha = options_.alpha;
+    P.delta = options_.delta;
+    P.cfl = options_.cfl;
+    P.c_force = options_.c_force;
+    P.c_visc = options_.c_visc;
+    // Cells of the grid search's spacing across the support radius.
+    const double radius = Kernel::unit_radius * particles.uniform_h();
+    const long k = std::lround(radius / mesh.spacing());
+    P.cells_per_radius = static_cast<std::int32_t>(k < 1 ? 1 : (k > 3 ? 3 : k));
+    particles.attach_(P,
+                      static_cast<double>(eos_.rho_0()),
+                      static_cast<double>(eos_.cs_0()),
+                      options_.graph,
+                      options_.autotune);
+  }
+
+  auto eos() const noexcept -> const TaitEquationOfState<Real>& { return eos_; }
+
+private:
+  Real g_;
+  Real mu_;
+  Containment containment_;
+  TaitEquationOfState<Real> eos_;
+  GpuOptions options_;
+};
+
+template<class Real, std::size_t Dim, class Containment, class Kernel>
+FluidEquations(Real,
+               Real,
+               geom::Surface<Vec<Real, Dim>>,
+               Containment,
+               TaitEquationOfState<Real>,
+               Kernel,
+               GpuOptions = {})
+    -> FluidEquations<Real, Dim, Containment, Kernel>;
+
+namespace gpu_detail {
+// One GPU step of a ParticleArray bound to a context.
+template<class Equations, class PA>
+auto step(const Equations& equations, ParticleMesh& mesh, PA& particles)
+    -> double {
+  if (!particles.attached()) equations.initialize(mesh, particles);
+  return particles.step_();
+}
+} // namespace gpu_detail
+
+/// SSPRK order (time_integrator.hpp).
+enum class SSPRKOrder : std::uint8_t { two, three };
+
+/// SSPRK integrator (time_integrator.hpp:140-228).
+template<class Equations>
+class SSPRKIntegrator {
+public:
+  explicit SSPRKIntegrator(Equations equations,
+                           SSPRKOrder order = SSPRKOrder::three)
+      : equations_{std::move(equations)}, order_{order} {}
+  auto gpu_integrator() const noexcept -> std::int32_t {
+    return order_ == SSPRKOrder::three ? TG_SSPRK3 : TG_SSPRK2;
+  }
+  template<class PA>
+  auto step(ParticleMesh& mesh, PA& particles) const {
+    return static_cast<typename PA::real_t>(
+        gpu_detail::step(equations_, mesh, particles));
+  }
+  auto equations() const noexcept -> const Equations& { return equations_; }
+
+private:
+  Equations equations_;
+  SSPRKOrder order_;
+};
+
+/// Symplectic Euler integrator (time_integrator.hpp:31-75).
+template<class Equations>
+class SymplecticEulerIntegrator {
+public:
+  explicit SymplecticEulerIntegrator(Equations equations)
+      : equations_{std::move(equations)} {}
+  static constexpr auto gpu_integrator() noexcept -> std::int32_t {
+    return TG_EULER;
+  }
+  template<class PA>
+  auto step(ParticleMesh& mesh, PA& particles) const {
+    return static_cast<typename PA::real_t>(
+        gpu_detail::step(equations_, mesh, particles));
+  }
+
+private:
+  Equations equations_;
+};
+
+/// Velocity Verlet integrator (time_integrator.hpp:80-129).
+template<class Equations>
+class VelocityVerletIntegrator {
+public:
+  explicit VelocityVerletIntegrator(Equations equations)
+      : equations_{std::move(equations)} {}
+  static constexpr auto gpu_integrator() noexcept -> std::int32_t {
+    return TG_VERLET;
+  }
+  template<class PA>
+  auto step(ParticleMesh& mesh, PA& particles) const {
+    return static_cast<typename PA::real_t>(
+        gpu_detail::step(equations_, mesh, particles));
+  }
+
+private:
+  Equations equations_;
+};
+
+/// A particle of a ParticleArray: the array and the particle's index, fluid
+/// particles first (particle_array.hpp:188-199).
+template<class PA>
+class ParticleView {
+public:
+  constexpr ParticleView(PA& array, std::size_t index) noexcept
+      : array_{&array}, index_{index} {}
+  constexpr auto array() const noexcept -> PA& { return *array_; }
+  constexpr auto index() const noexcept -> std::size_t { return index_; }
+  auto has_type(ParticleType type) const noexcept -> bool {
+    return array_->type_of(index_) == type;
+  }
+
+private:
+  PA* array_;
+  std::size_t index_;
+};
+
+/// Particle array (particle_array.hpp:139-293) whose state is mirrored on
+/// one GPU context.  Real is the driver's floating type; the GPU computes in
+/// FP64 or the FP32-compensated form whatever Real is.
+template<class Real, std::size_t Dim>
+class ParticleArray {
+public:
+  using real_t = Real;
+  using vec_t = Vec<Real, Dim>;
+  static constexpr std::size_t dim = Dim;
+
+  template<class Integrator>
+  ParticleArray(Space<Real, Dim> /*space*/, const Integrator& integrator)
+      : integrator_id_{integrator.gpu_integrator()} {}
+
+  ParticleArray(const ParticleArray&) = delete;
+  auto operator=(const ParticleArray&) -> ParticleArray& = delete;
+  ParticleArray(ParticleArray&&) noexcept = default;
+  auto operator=(ParticleArray&&) noexcept -> ParticleArray& = default;
+  ~ParticleArray() { detach_(); }
+
+  auto size() const noexcept -> std::size_t { return r_.size(); }
+  auto num_fluid() const noexcept -> std::size_t { return n_fluid_; }
+
+  /// Append a particle; fluid particles go before the fixed ones.
+  auto append(ParticleType type) -> ParticleView<ParticleArray> {
+    if (type != ParticleType::fluid && type != ParticleType::fixed) {
+      throw Exception{"ParticleArray::append: invalid particle type"};
+    }
+    if (ctx_ != nullptr) {
+      throw Exception{"ParticleArray::append: particles are on the GPU"};
+    }
+    const std::size_t at = type == ParticleType::fluid ? n_fluid_++ : size();
+    r_.emplace(r_.begin() + static_cast<std::ptrdiff_t>(at));
+    v_.emplace(v_.begin() + static_cast<std::ptrdiff_t>(at));
+    dv_dt_.emplace(dv_dt_.begin() + static_cast<std::ptrdiff_t>(at));
+    rho_.emplace(rho_.begin() + static_cast<std::ptrdiff_t>(at));
+    drho_dt_.emplace(drho_dt_.begin() + static_cast<std::ptrdiff_t>(at));
+    m_.emplace(m_.begin() + static_cast<std::ptrdiff_t>(at));
+    return {*this, at};
+  }
+
+  auto all() noexcept { return views_(0, size()); }
+  auto fluid() noexcept { return views_(0, n_fluid_); }
+  auto fixed() noexcept { return views_(n_fluid_, size()); }
+  auto typed(ParticleType type) noexcept {
+    return type == ParticleType::fluid ? fluid() : fixed();
+  }
+
+  auto type_of(std::size_t i) const noexcept -> ParticleType {
+    return i < n_fluid_ ? ParticleType::fluid : ParticleType::fixed;
+  }
+
+  // ---- field storage (used by the field objects below) --------------------
+  auto position(std::size_t i) -> vec_t& { return pull_mut_(r_)[i]; }
+  auto position(std::size_t i) const -> const vec_t& { return pull_(r_)[i]; }
+  auto velocity(std::size_t i) -> vec_t& { return pull_mut_(v_)[i]; }
+  auto velocity(std::size_t i) const -> const vec_t& { return pull_(v_)[i]; }
+  auto accel(std::size_t i) -> vec_t& { return pull_mut_(dv_dt_)[i]; }
+  auto accel(std::size_t i) const -> const vec_t& { return pull_(dv_dt_)[i]; }
+  auto density(std::size_t i) -> Real& { return pull_mut_(rho_)[i]; }
+  auto density(std::size_t i) const -> const Real& { return pull_(rho_)[i]; }
+  auto drho(std::size_t i) const -> const Real& { return pull_(drho_dt_)[i]; }
+  auto mass(std::size_t i) -> Real& {
+    if (ctx_ != nullptr) throw Exception{"m: masses are fixed on the GPU"};
+    return m_[i];
+  }
+  auto mass(std::size_t i) const -> const Real& { return m_[i]; }
+  auto uniform_h() -> Real& {
+    if (ctx_ != nullptr) throw Exception{"h: widths are fixed on the GPU"};
+    return h_;
+  }
+  auto uniform_h() const -> const Real& { return h_; }
+
+  // ---- GPU binding (FluidEquations::initialize and the integrators) -------
+  auto integrator_id() const noexcept -> std::int32_t { return integrator_id_; }
+  auto attached() const noexcept -> bool { return ctx_ != nullptr; }
+  auto context() const noexcept -> tg_context* { return ctx_; }
+
+  void attach_(tg_params P, double rho_0, double cs_0, bool graph,
+               bool autotune) {
+    if (n_fluid_ == 0) throw Exception{"initialize: no fluid particles"};
+    if (!(h_ > Real{0})) throw Exception{"initialize: set h[particles] first"};
+    for (std::size_t i = 1; i < size(); ++i) {
+      if (m_[i] != m_[0]) {
+        throw Exception{"initialize: the GPU path needs one uniform mass"};
+      }
+    }
+    detach_();
+    tg_context* ctx = nullptr;
+    gpu_detail::ensure(tg_context_create(&P, &ctx), nullptr,
+                       "tg_context_create");
+    ctx_ = ctx;
+    tg_tank tank{};
+    tank.n_fluid = static_cast<std::int64_t>(n_fluid_);
+    tank.n_wall = static_cast<std::int64_t>(size() - n_fluid_);
+    tank.h = static_cast<double>(h_);
+    tank.m = static_cast<double>(m_[0]);
+    tank.rho0 = rho_0;
+    tank.cs0 = cs_0;
+    std::vector<double> r, v, rho;
+    pack_(r, v, rho);
+    gpu_detail::ensure(tg_particles_upload(ctx_, 1, &tank, r.data(), v.data(),
+                                           rho.data()),
+                       ctx_, "tg_particles_upload");
+    gpu_detail::ensure(tg_set_graph(ctx_, graph ? 1 : 0), ctx_,
+                       "tg_set_graph");
+    if (autotune) {
+      tg_tuning tuned{};
+      gpu_detail::ensure(tg_autotune(ctx_, 3, &tuned), ctx_, "tg_autotune");
+    }
+    state_ = State::synced;
+  }
+
+  auto step_() -> double {
+    if (state_ == State::host_ahead) push_();
+    double dt = 0.0;
+    gpu_detail::ensure(tg_step(ctx_, 1, &dt), ctx_, "tg_step");
+    state_ = State::device_ahead;
+    return dt;
+  }
+
+  /// Bring the host copy up to date (downloads after GPU steps).
+  void sync() const {
+    if (state_ != State::device_ahead) return;
+    std::vector<double> buf(size() * Dim);
+    const auto get = [&](std::int32_t field, auto& dst) {
+      using T = typename std::decay_t<decltype(dst)>::value_type;
+      const std::size_t width = std::is_same_v<T, Real> ? 1 : Dim;
+      buf.resize(size() * width);
+      gpu_detail::ensure(tg_particles_download(ctx_, field, buf.data()), ctx_,
+                         "tg_particles_download");
+      for (std::size_t i = 0; i < size(); ++i) {
+        if constexpr (std::is_same_v<T, Real>) {
+          dst[i] = static_cast<Real>(buf[i]);
+        } else {
+          for (std::size_t d = 0; d < Dim; ++d) {
+            dst[i][d] = static_cast<Real>(buf[i * Dim + d]);
+          }
+        }
+      }
+    };
+    get(TG_FIELD_R, r_);
+    get(TG_FIELD_V, v_);
+    get(TG_FIELD_DV_DT, dv_dt_);
+    get(TG_FIELD_RHO, rho_);
+    get(TG_FIELD_DRHO_DT, drho_dt_);
+    state_ = State::synced;
+  }
+
+private:
+  enum class State : std::uint8_t { host_only, synced, device_ahead, host_ahead };
+
+  auto views_(std::size_t lo, std::size_t hi) noexcept {
+    return std::views::iota(lo, hi) |
+           std::views::transform([this](std::size_t i) {
+             return ParticleView<ParticleArray>{*this, i};
+           });
+  }
+
+  template<class T>
+  auto pull_(const std::vector<T>& col) const -> const std::vector<T>& {
+    sync();
+    return col;
+  }
+  template<class T>
+  auto pull_mut_(std::vector<T>& col) -> std::vector<T>& {
+    sync();
+    if (state_ == State::synced) state_ = State::host_ahead;
+    return col;
+  }
+
+  void pack_(std::vector<double>& r, std::vector<double>& v,
+             std::vector<double>& rho, std::vector<double>* dv = nullptr) const {
+    const std::size_t n = size();
+    r.resize(n * Dim);
+    v.resize(n * Dim);
+    rho.resize(n);
+    if (dv != nullptr) dv->resize(n * Dim);
+    for (std::size_t i = 0; i < n; ++i) {
+      for (std::size_t d = 0; d < Dim; ++d) {
+        r[i * Dim + d] = static_cast<double>(r_[i][d]);
+        v[i * Dim + d] = static_cast<double>(v_[i][d]);
+        if (dv != nullptr) (*dv)[i * Dim + d] = static_cast<double>(dv_dt_[i][d]);
+      }
+      rho[i] = static_cast<double>(rho_[i]);
+    }
+  }
+
+  void push_() {
+    std::vector<double> r, v, rho, dv;
+    pack_(r, v, rho, &dv);
+    gpu_detail::ensure(tg_particles_update(ctx_, r.data(), v.data(),
+                                           rho.data(), dv.data()),
+                       ctx_, "tg_particles_update");
+    state_ = State::synced;
+  }
+
+  void detach_() noexcept {
+    if (ctx_ != nullptr) tg_context_destroy(ctx_);
+    ctx_ = nullptr;
+    state_ = State::host_only;
+  }
+
+  std::int32_t integrator_id_;
+  std::size_t n_fluid_ = 0;
+  Real h_{};
+  mutable std::vector<vec_t> r_, v_, dv_dt_;
+  mutable std::vector<Real> rho_, drho_dt_;
+  std::vector<Real> m_;
+  tg_context* ctx_ = nullptr;
+  mutable State state_ = State::host_only;
+};
+
+template<class Real, std::size_t Dim, class Integrator>
+ParticleArray(Space<Real, Dim>, const Integrator&) -> ParticleArray<Real, Dim>;
+
+} // namespace sph
+
+// ---- fields (source/tit/sph/field.hpp:172-218) ------------------------------
+namespace gpu_detail {
+template<class Get>
+struct Field {
+  Get get;
+  template<class PA>
+  constexpr decltype(auto) operator[](sph::ParticleView<PA> a) const {
+    return get(a.array(), a.index());
+  }
+};
+struct UniformH {
+  template<class PA>
+  constexpr decltype(auto) operator[](sph::ParticleView<PA> a) const {
+    return std::as_const(a.array()).uniform_h();
+  }
+  template<class Real, std::size_t Dim>
+  constexpr auto operator[](sph::ParticleArray<Real, Dim>& particles) const
+      -> Real& {
+    return particles.uniform_h();
+  }
+};
+} // namespace gpu_detail
+
+namespace sph {
+/// Particle position.
+inline constexpr gpu_detail::Field r{
+    [](auto& pa, std::size_t i) -> decltype(auto) { return pa.position(i); }};
+} // namespace sph
+/// Particle velocity.
+inline constexpr gpu_detail::Field v{
+    [](auto& pa, std::size_t i) -> decltype(auto) { return pa.velocity(i); }};
+/// Particle acceleration.
+inline constexpr gpu_detail::Field dv_dt{
+    [](auto& pa, std::size_t i) -> decltype(auto) { return pa.accel(i); }};
+/// Particle density.
+inline constexpr gpu_detail::Field rho{
+    [](auto& pa, std::size_t i) -> decltype(auto) { return pa.density(i); }};
+/// Particle density time derivative (read-only on the host).
+inline constexpr gpu_detail::Field drho_dt{
+    [](auto& pa, std::size_t i) -> decltype(auto) {
+      return std::as_const(pa).drho(i);
+    }};
+/// Particle mass.
+inline constexpr gpu_detail::Field m{
+    [](auto& pa, std::size_t i) -> decltype(auto) { return pa.mass(i); }};
+/// Particle width (uniform over the array).
+inline constexpr gpu_detail::UniformH h{};
+
+} // namespace tit
+
+#endif // TITGPU_HPP

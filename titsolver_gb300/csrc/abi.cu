@@ -388,9 +388,9 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     D.inv_cs = 1.0 / cs;
     D.cell_off = static_cast<uint32_t>(total_cells);
     total_cells += cells;
-    if (total_cells >= (uint64_t{1} << 31)) {
+    if (total_cells >= (uint64_t{1} << 30)) {
       return fail(&C, TG_ERR_INVALID_ARGUMENT,
-                  "more than 2^31 grid cells; lower cells_per_radius");
+                  "more than 2^30 grid cells; lower cells_per_radius");
     }
     D.h = T.h;
     D.hinv = 1.0 / T.h;
@@ -438,7 +438,8 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   C.id_base = id_base;
   C.wall_from = wall_from;
   C.total_cells = static_cast<uint32_t>(total_cells);
-  C.key_bits = key_bits_for(C.total_cells);
+  C.total_keys = static_cast<uint32_t>(2 * total_cells);
+  C.key_bits = key_bits_for(C.total_keys);
   const int64_t nn = n > 0 ? n : 1;
   auto A = [&](auto*& p, size_t bytes) -> cudaError_t {
     return C.alloc(reinterpret_cast<void**>(&p), bytes);
@@ -458,9 +459,8 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, A(C.vals_a, sizeof(uint32_t) * nn));
   TG_CUDA(&C, A(C.vals_b, sizeof(uint32_t) * nn));
   TG_CUDA(&C, C.alloc(&C.sort_scratch, tg::radix_sort_scratch_bytes(nn)));
-  TG_CUDA(&C, A(C.cell_start, sizeof(uint32_t) * (total_cells + 1)));
-  TG_CUDA(&C, C.alloc(&C.cell_scratch,
-                      tg::cell_table_scratch_bytes(static_cast<uint32_t>(total_cells))));
+  TG_CUDA(&C, A(C.cell_start, sizeof(uint32_t) * (2 * total_cells + 1)));
+  TG_CUDA(&C, C.alloc(&C.cell_scratch, tg::cell_table_scratch_bytes(C.total_keys)));
   TG_CUDA(&C, A(C.wall_list, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
   TG_CUDA(&C, A(C.d_stage, sizeof(double) * nn * dim));
   TG_CUDA(&C, A(C.d_stage2, sizeof(double) * nn * dim));
@@ -488,7 +488,7 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, cudaMemcpyAsync(C.d_id_base, id_base.data(), sizeof(uint32_t) * n_tanks,
                               cudaMemcpyHostToDevice, s));
   std::vector<uint32_t> tank_off(static_cast<size_t>(n_tanks));
-  for (int32_t t = 0; t < n_tanks; ++t) tank_off[t] = td[t].cell_off;
+  for (int32_t t = 0; t < n_tanks; ++t) tank_off[t] = 2 * td[t].cell_off;
   TG_CUDA(&C, cudaMemcpyAsync(C.d_tank_off, tank_off.data(), sizeof(uint32_t) * n_tanks,
                               cudaMemcpyHostToDevice, s));
   TG_CUDA(&C, cudaMemcpyAsync(C.d_wall_from, wall_from.data(),

@@ -256,7 +256,16 @@ __device__ __forceinline__ void cell_of(const TankDev& T, const double* x,
   }
 }
 
-// Tank of a global cell key: the last tank whose first cell is <= key.
+// Keys: every cell owns two consecutive keys, 2 * cell for its fluid
+// particles and 2 * cell + 1 for its wall particles, so in key order a
+// cell's fluid particles precede its walls and a row of cells is still one
+// contiguous key range.
+__device__ __forceinline__ uint32_t key_of(uint32_t cell, bool wall) {
+  return (cell << 1) | (wall ? 1u : 0u);
+}
+
+// Tank of a global key: the last tank whose first key is <= key (off holds
+// each tank's first key, 2 * cell_off).
 __device__ __forceinline__ uint32_t tank_of_key(uint32_t key,
                                                 const uint32_t* __restrict__ off,
                                                 int ntanks) {
@@ -272,11 +281,11 @@ __device__ __forceinline__ uint32_t tank_of_key(uint32_t key,
   return static_cast<uint32_t>(lo);
 }
 
-// Cell coordinates of a key of tank T (inverse of flat_cell).
+// Cell coordinates of a key of tank T (inverse of key_of(flat_cell)).
 template<int D>
 __device__ __forceinline__ void cell_from_key(const TankDev& T, uint32_t key,
                                               int* c) {
-  const uint32_t f = key - T.cell_off;
+  const uint32_t f = (key >> 1) - T.cell_off;
   const uint32_t nx = static_cast<uint32_t>(T.nc[0]);
   c[0] = static_cast<int>(f % nx);
   const uint32_t rest = f / nx;

@@ -75,13 +75,14 @@ struct Context {
   std::vector<uint32_t> id_base;    // first upload index of each tank
   std::vector<uint32_t> wall_from;  // first wall upload index of each tank
   uint32_t total_cells = 0;
+  uint32_t total_keys = 0;  // 2 per cell: fluid, then walls
   int key_bits = 0;
   int k = 1;
   bool uploaded = false;
 
   // Common device buffers.
   TankDev* d_tanks = nullptr;
-  uint32_t* d_tank_off = nullptr;  // first global cell of each tank
+  uint32_t* d_tank_off = nullptr;  // first key of each tank
   uint32_t* d_id_base = nullptr;
   uint32_t* d_wall_from = nullptr;
   uint32_t* d_tank_of = nullptr;  // tank of each upload index

@@ -251,7 +251,7 @@ class Engine final : public EngineBase {
     if (e != cudaSuccess) return e;
     C.sorted_keys = in_b ? C.keys_b : C.keys_a;
     C.perm = in_b ? C.vals_b : C.vals_a;
-    e = build_cell_table(C.sorted_keys, C.n, C.total_cells, C.cell_start,
+    e = build_cell_table(C.sorted_keys, C.n, C.total_keys, C.cell_start,
                          C.cell_scratch, C.stream, &C.launches);
     C.group_end(tok);
     return e;

@@ -149,10 +149,12 @@ struct StageArgs {
 
 // ---------------------------------------------------------------------------
 // Neighbour-cell traversal over the (2k+1)^D block of cells around c,
-// clipped to the tank grid.  Merged: one [begin, end) range per row of
-// cells (rows are contiguous in cell order).  Per cell: one range per cell
-// with its cell offset (dx, dy, dz) relative to c.
-template<int D, bool PerCell, class Fn>
+// clipped to the tank grid.  cstart is indexed by key (2 per cell).
+// Merged: one [begin, end) range per row of cells (rows are contiguous in
+// key order), fluid and walls.  Per cell: one range per cell with its cell
+// offset (dx, dy, dz) relative to c; FluidOnly restricts each cell's range
+// to its fluid particles.
+template<int D, bool PerCell, class Fn, bool FluidOnly = false>
 __device__ __forceinline__ void for_cells(const TankDev& T, const int* c,
                                           int k,
                                           const uint32_t* __restrict__ cstart,
@@ -167,16 +169,50 @@ __device__ __forceinline__ void for_cells(const TankDev& T, const int* c,
       const uint32_t row =
           T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx;
       if constexpr (!PerCell) {
-        fn(__ldg(cstart + row + xlo), __ldg(cstart + row + xhi + 1), 0, 0, 0);
-      } else {
-        uint32_t s = __ldg(cstart + row + xlo);
+        fn(__ldg(cstart + 2 * (row + xlo)), __ldg(cstart + 2 * (row + xhi + 1)),
+           0, 0, 0);
+      } else if constexpr (FluidOnly) {
         for (int x = xlo; x <= xhi; ++x) {
-          const uint32_t e = __ldg(cstart + row + x + 1);
+          const uint32_t kc = 2 * (row + x);
+          fn(__ldg(cstart + kc), __ldg(cstart + kc + 1), x - c[0], y - c[1],
+             D == 3 ? z - c[2] : 0);
+        }
+      } else {
+        uint32_t s = __ldg(cstart + 2 * (row + xlo));
+        for (int x = xlo; x <= xhi; ++x) {
+          const uint32_t e = __ldg(cstart + 2 * (row + x + 1));
           fn(s, e, x - c[0], y - c[1], D == 3 ? z - c[2] : 0);
           s = e;
         }
       }
     }
+  }
+}
+
+// Fluid ranges of the (2k+1)^D cell block around c, dealt out to the lanes
+// of a team: lane l of a team of `team` lanes visits cells l, l + team, ...
+// of the block (cells, not particles, are split, so no lane repeats another
+// lane's cell-table reads).
+template<int D, class Fn>
+__device__ __forceinline__ void for_fluid_cells_team(
+    const TankDev& T, const int* c, int k,
+    const uint32_t* __restrict__ cstart, int lane, int team, Fn&& fn) {
+  const int nx = T.nc[0], ny = T.nc[1];
+  const int zlo = D == 3 ? max(c[2] - k, 0) : 0;
+  const int zhi = D == 3 ? min(c[2] + k, T.nc[2] - 1) : 0;
+  const int ylo = max(c[1] - k, 0), yhi = min(c[1] + k, ny - 1);
+  const int xlo = max(c[0] - k, 0), xhi = min(c[0] + k, nx - 1);
+  const int wx = xhi - xlo + 1, wy = yhi - ylo + 1, wz = zhi - zlo + 1;
+  const int total = wx * wy * wz;
+  for (int t = lane; t < total; t += team) {
+    const int x = xlo + t % wx;
+    const int rest = t / wx;
+    const int y = ylo + rest % wy;
+    const int z = zlo + rest / wy;
+    const uint32_t kc =
+        2 * (T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx + x);
+    fn(__ldg(cstart + kc), __ldg(cstart + kc + 1), x - c[0], y - c[1],
+       D == 3 ? z - c[2] : 0);
   }
 }
 
@@ -222,7 +258,7 @@ __global__ void __launch_bounds__(256)
   int c[3] = {0, 0, 0};
   bool outside = false;
   cell_of<D>(T, p, c, outside);
-  X.key[i] = flat_cell<D>(T, c);
+  X.key[i] = key_of(flat_cell<D>(T, c), (X.id[i] & kWallBit) != 0);
   if constexpr (F == TG_FP32C) {
 #pragma unroll
     for (int k = 0; k < D; ++k) {
@@ -382,8 +418,8 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
 // Wall extrapolation (fluid_equations.hpp:122-164) with a zero wall normal:
 //   rho_e = rho(H),  H = sum_b V_b H(rho_b) W_be / sum_b V_b W_be over fluid
 //   neighbours b (H = 0 when the Shepard sum is tiny); v_e = 0.
-// A team of kWallTeam lanes shares one wall: each lane takes every
-// kWallTeam-th candidate, then the team reduces by shuffles.
+// A team of kWallTeam lanes shares one wall: the lanes split the cells of
+// the wall's block (fluid ranges only), then the team reduces by shuffles.
 constexpr int kWallTeam = 8;
 
 template<int D, int F, int K>
@@ -407,10 +443,8 @@ __global__ void __launch_bounds__(128)
     const double R2 = T.radius2, hinv = T.hinv, w = T.w, m = T.m;
     double S = 0.0, H = 0.0;
     if (valid) {
-      for_cells<D, false>(T, c, A.k, A.cell_start,
-                          [&](uint32_t s, uint32_t en, int, int, int) {
-        for (uint32_t j = s + lane; j < en; j += kWallTeam) {
-          if (A.Y.id[j] & kWallBit) continue;
+      auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
+        for (uint32_t j = s; j < en; ++j) {
           double pb[3], d[3];
           load_pos(A.posrec, j, pb);
           const double s2 = dist2_exact<D>(pb, pe, d);
@@ -422,7 +456,8 @@ __global__ void __launch_bounds__(128)
           S += Vb * W;
           H += Vb * Hb * W;
         }
-      });
+      };
+      for_fluid_cells_team<D>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
     }
 #pragma unroll
     for (int o = kWallTeam / 2; o > 0; o >>= 1) {
@@ -444,14 +479,12 @@ __global__ void __launch_bounds__(128)
     if (valid) load_pos(A.posrec, e, oe);
     Kahan S, H;
     if (valid) {
-      for_cells<D, true>(T, c, A.k, A.cell_start,
-                         [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
         float oes[3];
         oes[0] = oe[0] - dx * csz;
         oes[1] = oe[1] - dy * csz;
         oes[2] = D == 3 ? oe[2] - dz * csz : 0.f;
-        for (uint32_t j = s + lane; j < en; j += kWallTeam) {
-          if (A.Y.id[j] & kWallBit) continue;
+        for (uint32_t j = s; j < en; ++j) {
           float ob[3], d[3];
           load_pos(A.posrec, j, ob);
           const float s2 = dist2_exact<D>(oes, ob, d);
@@ -463,7 +496,8 @@ __global__ void __launch_bounds__(128)
           S.add(Vb * W);
           H.add(Vb * Hb * W);
         }
-      });
+      };
+      for_fluid_cells_team<D>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
     }
     float Ss = S.value(), Hv = H.value();
 #pragma unroll
@@ -666,7 +700,7 @@ __device__ __forceinline__ void forces_epilogue(
     }
     if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
   }
-  A.X.key[i] = flat_cell<D>(T, cn);
+  A.X.key[i] = key_of(flat_cell<D>(T, cn), false);
   bool finite = true;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
@@ -827,8 +861,8 @@ __global__ void __launch_bounds__(128, 7)
         uint32_t off = 0;
         for (int y = ylo; y <= yhi; ++y) {
           const uint32_t row = T.cell_off + static_cast<uint32_t>(y) * T.nc[0];
-          const uint32_t gb = __ldg(A.cell_start + row + xlo);
-          const uint32_t ge = __ldg(A.cell_start + row + xhi + 1);
+          const uint32_t gb = __ldg(A.cell_start + 2 * (row + xlo));
+          const uint32_t ge = __ldg(A.cell_start + 2 * (row + xhi + 1));
           s_gbeg[y - ylo] = gb;
           s_goff[y - ylo] = off;
           off += ge - gb;
@@ -878,9 +912,9 @@ __global__ void __launch_bounds__(128, 7)
       const int32_t shift = static_cast<int32_t>(s_goff[r]) - static_cast<int32_t>(s_gbeg[r]);
       float oas[3];
       oas[1] = oa[1] - (y - c[1]) * csz;
-      uint32_t gs = __ldg(A.cell_start + row + xlo);
+      uint32_t gs = __ldg(A.cell_start + 2 * (row + xlo));
       for (int x = xlo; x <= xhi; ++x) {
-        const uint32_t ge = __ldg(A.cell_start + row + x + 1);
+        const uint32_t ge = __ldg(A.cell_start + 2 * (row + x + 1));
         oas[0] = oa[0] - (x - c[0]) * csz;
         for (uint32_t j = gs; j < ge; ++j) {
           if (j == static_cast<uint32_t>(i)) continue;

@@ -23,7 +23,7 @@ namespace tg {
 namespace {
 
 constexpr int64_t kMaxPoints = TG_NOALLOC_MAX_POINTS;
-constexpr uint32_t kMaxCells = 1u << 18;
+constexpr uint32_t kMaxCells = 1u << 17;  // keys: 2 per cell
 constexpr int kMaxCellBits = 18;
 constexpr int kMaxDevices = 64;
 
@@ -39,13 +39,13 @@ constexpr size_t kHistBytes =
     sizeof(uint32_t) * kRadixBins * ((kMaxPoints + kSortTile - 1) / kSortTile + 1) + 256;
 constexpr size_t kOffHist = kOffIds + align256(kU32);
 constexpr size_t kOffCells = kOffHist + align256(kHistBytes);
-constexpr size_t kOffRecs = kOffCells + align256(sizeof(uint32_t) * (kMaxCells + 1));
+constexpr size_t kOffRecs = kOffCells + align256(sizeof(uint32_t) * (2 * kMaxCells + 1));
 constexpr size_t kOffBounds = kOffRecs + align256(sizeof(Pos64_3) * kMaxPoints);
-constexpr size_t kBoundsBytes = sizeof(uint32_t) * ((kMaxCells + 256) / 256 + 2);
+constexpr size_t kBoundsBytes = sizeof(uint32_t) * ((2 * kMaxCells + 256) / 256 + 2);
 constexpr size_t kOffTank = kOffBounds + align256(kBoundsBytes);
 constexpr size_t kOffIdBase = kOffTank + align256(sizeof(TankDev));
 constexpr size_t kScratchBytes = kOffIdBase + 256;
-static_assert(kBoundsBytes >= 4 * ((kMaxCells + 256) / 256 + 2), "coarse bounds");
+static_assert(kBoundsBytes >= 4 * ((2 * kMaxCells + 256) / 256 + 2), "coarse bounds");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256)
   int c[3] = {0, 0, 0};
   bool outside = false;
   cell_of<D>(*T, p, c, outside);
-  keys[i] = flat_cell<D>(*T, c);
+  keys[i] = key_of(flat_cell<D>(*T, c), false);
 }
 
 template<int D>
@@ -204,7 +204,7 @@ cudaError_t run(unsigned char* base, int64_t n, const double* r, double h,
   if (e != cudaSuccess) return e;
   const uint32_t* sorted = in_b ? keys_b : keys_a;
   const uint32_t* perm = in_b ? vals_b : vals_a;
-  e = build_cell_table(sorted, n, kMaxCells, cells, base + kOffBounds, s, &launches);
+  e = build_cell_table(sorted, n, 2 * kMaxCells, cells, base + kOffBounds, s, &launches);
   if (e != cudaSuccess) return e;
   k_na_records<D><<<g, 256, 0, s>>>(r, perm, n, reinterpret_cast<Pos64_3*>(recs),
                                     reinterpret_cast<Pos64_2*>(recs), ids);
