@@ -224,11 +224,16 @@ def tune(P, args) -> None:
     P.staging = args.staging
 
 
-def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks):
+def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks,
+            autotune: bool = False):
     from titsolver_gb300 import _abi
 
     ctx = _abi.Context(params)
     ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+    if autotune:
+        # Untimed setup: the autotuner times a few steps per launch shape and
+        # leaves the context at the fastest, with the uploaded state.
+        ctx.autotune(3)
     if warmup:
         ctx.step(warmup)
     ranks.barrier()
@@ -264,8 +269,10 @@ def run_gpu(args, ranks) -> dict | None:
     tune(P32, args)
     clocks = ClockSampler(dev)
     clocks.start()
+    auto = args.cells_per_radius is None and args.autotune == 1
     ctx32, ms32, launches, prof32 = gpu_leg(scn, P32, args.warmup, args.steps,
-                                            min(args.steps, 20), ranks)
+                                            min(args.steps, 20), ranks, auto)
+    tuning32 = ctx32.get_tuning()
     clk = clocks.stop()
     sec32 = ms32 / 1e3
     value, t_max = (nf * args.steps / sec32, sec32)
@@ -278,7 +285,8 @@ def run_gpu(args, ranks) -> dict | None:
     P64.device = dev
     tune(P64, args)
     k64 = args.steps if args.fp64_steps is None else args.fp64_steps
-    ctx64, ms64, _, prof64 = gpu_leg(scn, P64, args.warmup, k64, min(k64, 20), ranks)
+    ctx64, ms64, _, prof64 = gpu_leg(scn, P64, args.warmup, k64, min(k64, 20), ranks, auto)
+    tuning64 = ctx64.get_tuning()
     value64 = nf * k64 / (ms64 / 1e3)
 
     # Error of the compensated form against FP64 after the same steps.
@@ -371,9 +379,9 @@ def run_gpu(args, ranks) -> dict | None:
                        "l2": f"inputs larger than L2 (working set ~{ws / 1e6:.0f} MB > 129 MB)"},
             "forms": {
                 "fp32c": {"value": value, "ms_per_step": ms32 / args.steps,
-                          "kernel_shares": shares(prof32)},
+                          "kernel_shares": shares(prof32), "launch_shape": tuning32},
                 "fp64": {"value": value64, "ms_per_step": ms64 / k64, "steps": k64,
-                         "kernel_shares": shares(prof64)},
+                         "kernel_shares": shares(prof64), "launch_shape": tuning64},
                 "speedup_fp32c_over_fp64": value / value64 if value64 > 0 else None,
             },
             "l2_error_vs_fp64": err,
@@ -458,14 +466,17 @@ def run_single_form(args, ranks) -> dict | None:
     P = physics.baseline_params(scn["dim"], precision=form)
     P.device = ranks.local_rank
     tune(P, args)
-    ctx, ms, launches, prof = gpu_leg(scn, P, args.warmup, args.steps, 0, ranks)
+    auto = args.cells_per_radius is None and args.autotune == 1
+    ctx, ms, launches, prof = gpu_leg(scn, P, args.warmup, args.steps, 0, ranks, auto)
+    shape = ctx.get_tuning()
     ctx.close()
     if ranks.rank != 0:
         return None
     return {"metric": METRIC, "value": nf * args.steps / (ms / 1e3), "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "form": args.only,
-            "cells_per_radius": P.cells_per_radius, "kahan": P.kahan, "staging": P.staging,
+            "ms_per_step": ms / args.steps, "form": args.only, "launch_shape": shape,
+            "cells_per_radius": shape["cells_per_radius"], "kahan": P.kahan,
+            "staging": P.staging,
             "config": {"workload": workload}, "gpu_launches": launches}
 
 
@@ -484,6 +495,9 @@ def main() -> int:
     ap.add_argument("--cells-per-radius", type=int, default=None,
                     help="grid cells per support radius (default: library default)")
     ap.add_argument("--kahan", type=int, choices=(0, 1), default=1)
+    ap.add_argument("--autotune", type=int, choices=(0, 1), default=1,
+                    help="pick the launch shape with tg_autotune before warm-up "
+                         "(skipped when --cells-per-radius is given)")
     ap.add_argument("--staging", type=int, choices=(0, 1), default=0)
     ap.add_argument("--only", choices=("fp32c", "fp64"), default=None,
                     help="time one form only (profiling runs); prints its value")

@@ -280,6 +280,35 @@ int tg_summation_density_noalloc(int32_t dim, int32_t kernel, int64_t n,
                                  double* rho, int32_t* counts, uint64_t* hashes,
                                  void* stream);
 
+/* ---- launch shape and the autotuner ----------------------------------- */
+/* Launch shape of a context: the grid's cell size (cells_per_radius cells
+ * across the kernel support radius, as GridSearch{spacing} picks the cell
+ * size in source/tit/geom/search/grid_search.hpp:73-113), the force pass's
+ * threads per block, and its lanes per fluid particle (1, 2 or 4: the lanes
+ * split the particle's neighbour cells, so a warp advances 32, 16 or 8
+ * particles; 2 and 4 exist for the Wendland C2 and C4 kernels). */
+typedef struct tg_tuning {
+  int32_t cells_per_radius;   /* 1..3 */
+  int32_t block_size;         /* 64, 128 or 256 */
+  int32_t lanes_per_particle; /* 1, 2 or 4 */
+  int32_t candidates;         /* shapes timed by the last tg_autotune */
+  double ms_per_step;         /* device ms per step of the tuned shape
+                                 (0 before any tg_autotune) */
+} tg_tuning;
+
+/* Current launch shape. */
+int tg_get_tuning(tg_context* ctx, tg_tuning* out);
+/* Set the launch shape.  A new cells_per_radius re-grids the tanks from the
+ * current positions and keeps the particle state and clocks. */
+int tg_set_tuning(tg_context* ctx, const tg_tuning* tuning);
+/* Autotuner (no reference counterpart; the reference fixes its grid cell
+ * size in the driver): times trial_steps steps of each candidate shape on
+ * the uploaded particles, by coordinate search over cells_per_radius, then
+ * lanes_per_particle, then block_size, and leaves the context at the
+ * fastest shape with the particle state and clocks of the call (the trial
+ * steps are undone).  out (may be NULL) receives the choice. */
+int tg_autotune(tg_context* ctx, int32_t trial_steps, tg_tuning* out);
+
 /* Human-readable text of a status code, and of the context's last error. */
 const char* tg_status_string(int status);
 const char* tg_last_error(tg_context* ctx);

@@ -46,6 +46,7 @@
 #include <functional>
 #include <memory>
 #include <ranges>
+#include <span>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -376,7 +377,7 @@ FluidEquations(Real,
                GpuOptions = {})
     -> FluidEquations<Real, Dim, Containment, Kernel>;
 
-namespace gpu_detail {
+namespace integrator_detail {
 // One GPU step of a ParticleArray bound to a context.
 template<class Equations, class PA>
 auto step(const Equations& equations, ParticleMesh& mesh, PA& particles)
@@ -384,7 +385,7 @@ auto step(const Equations& equations, ParticleMesh& mesh, PA& particles)
   if (!particles.attached()) equations.initialize(mesh, particles);
   return particles.step_();
 }
-} // namespace gpu_detail
+} // namespace integrator_detail
 
 /// SSPRK order (time_integrator.hpp).
 enum class SSPRKOrder : std::uint8_t { two, three };
@@ -402,7 +403,7 @@ public:
   template<class PA>
   auto step(ParticleMesh& mesh, PA& particles) const {
     return static_cast<typename PA::real_t>(
-        gpu_detail::step(equations_, mesh, particles));
+        integrator_detail::step(equations_, mesh, particles));
   }
   auto equations() const noexcept -> const Equations& { return equations_; }
 
@@ -423,7 +424,7 @@ public:
   template<class PA>
   auto step(ParticleMesh& mesh, PA& particles) const {
     return static_cast<typename PA::real_t>(
-        gpu_detail::step(equations_, mesh, particles));
+        integrator_detail::step(equations_, mesh, particles));
   }
 
 private:
@@ -442,7 +443,7 @@ public:
   template<class PA>
   auto step(ParticleMesh& mesh, PA& particles) const {
     return static_cast<typename PA::real_t>(
-        gpu_detail::step(equations_, mesh, particles));
+        integrator_detail::step(equations_, mesh, particles));
   }
 
 private:
@@ -586,6 +587,42 @@ public:
     gpu_detail::ensure(tg_step(ctx_, 1, &dt), ctx_, "tg_step");
     state_ = State::device_ahead;
     return dt;
+  }
+
+  /// Write the particle fields as a new frame of `series`
+  /// (ParticleArray::write, particle_array.hpp:165-172): r, v, dv_dt, rho,
+  /// drho_dt, p, cs and m under the reference's field names.  The fields are
+  /// copied from the device here; the storage writes them on a background
+  /// thread while the caller goes on stepping.  Include titgpu_data.hpp for
+  /// the storage.
+  template<class Series>
+  void write(double time, const Series& series) const {
+    sync();
+    auto& storage = series.storage();
+    using Blob = typename std::remove_reference_t<decltype(storage)>::blob_type;
+    std::vector<Blob> arrays;
+    arrays.push_back(Blob::of(std::string{"r"}, std::span<const vec_t>{r_}));
+    arrays.push_back(Blob::of(std::string{"v"}, std::span<const vec_t>{v_}));
+    arrays.push_back(
+        Blob::of(std::string{"dv_dt"}, std::span<const vec_t>{dv_dt_}));
+    arrays.push_back(Blob::of(std::string{"rho"}, std::span<const Real>{rho_}));
+    arrays.push_back(
+        Blob::of(std::string{"drho_dt"}, std::span<const Real>{drho_dt_}));
+    if (ctx_ != nullptr) {
+      std::vector<double> buf(size());
+      std::vector<Real> col(size());
+      for (const auto& [field, name] :
+           {std::pair{TG_FIELD_P, "p"}, std::pair{TG_FIELD_CS, "cs"}}) {
+        gpu_detail::ensure(tg_particles_download(ctx_, field, buf.data()),
+                           ctx_, "tg_particles_download");
+        for (std::size_t i = 0; i < size(); ++i) {
+          col[i] = static_cast<Real>(buf[i]);
+        }
+        arrays.push_back(Blob::of(std::string{name}, std::span<const Real>{col}));
+      }
+    }
+    arrays.push_back(Blob::of(std::string{"m"}, std::span<const Real>{m_}));
+    storage.write_frame_async(series.id(), time, std::move(arrays));
   }
 
   /// Bring the host copy up to date (downloads after GPU steps).

@@ -1,0 +1,139 @@
+// Host-only checks of the C++ mirror (titgpu.hpp) and the .ttdb writer
+// (titgpu_data.hpp); no kernel runs.  Writes a storage to argv[1] for the
+// Python side to read back.  Prints "ok" and exits 0 when every check holds.
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "titgpu.hpp"
+#include "titgpu_data.hpp"
+
+using namespace tit;
+using namespace tit::sph;
+
+#define CHECK(cond)                                                   \
+  do {                                                                \
+    if (!(cond)) {                                                    \
+      std::fprintf(stderr, "check failed at line %d: %s\n", __LINE__, \
+                   #cond);                                            \
+      return 1;                                                       \
+    }                                                                 \
+  } while (0)
+
+template<class F>
+auto throws(F&& f) -> bool {
+  try {
+    f();
+  } catch (const Exception&) {
+    return true;
+  }
+  return false;
+}
+
+auto main(int argc, char** argv) -> int {
+  if (argc < 2) return 2;
+
+  // Vec arithmetic and deduction.
+  const Vec a{1.0, 2.0};
+  const Vec b = 2.0 * a + Vec{0.5, 0.25};
+  CHECK(b[0] == 2.5 && b[1] == 4.25);
+  static_assert(std::is_same_v<decltype(Vec{1.0, 2.0, 3.0}), Vec<double, 3>>);
+
+  // Equations, integrator and array types as a driver spells them.
+  const geom::Surface<Vec<double, 2>> domain;
+  const FluidEquations equations{9.81, 0.001, domain, geom::AllInside{},
+                                 TaitEquationOfState{20.0, 1000.0},
+                                 QuarticWendlandKernel{}};
+  const SSPRKIntegrator rk3{equations, SSPRKOrder::three};
+  const SSPRKIntegrator rk2{equations, SSPRKOrder::two};
+  CHECK(rk3.gpu_integrator() == TG_SSPRK3 && rk2.gpu_integrator() == TG_SSPRK2);
+  CHECK(SymplecticEulerIntegrator{equations}.gpu_integrator() == TG_EULER);
+  CHECK(VelocityVerletIntegrator{equations}.gpu_integrator() == TG_VERLET);
+  ParticleArray particles{Space<double, 2>{}, rk3};
+  static_assert(std::is_same_v<decltype(particles), ParticleArray<double, 2>>);
+
+  // Fluid particles go before the fixed ones, whatever the append order.
+  auto w0 = particles.append(ParticleType::fixed);
+  r[w0] = Vec{-1.0, -1.0};
+  auto f0 = particles.append(ParticleType::fluid);
+  r[f0] = Vec{0.5, 0.5};
+  auto f1 = particles.append(ParticleType::fluid);
+  r[f1] = Vec{0.75, 0.5};
+  CHECK(particles.size() == 3 && particles.num_fluid() == 2);
+  CHECK(particles.position(0) == (Vec{0.5, 0.5}));
+  CHECK(particles.position(1) == (Vec{0.75, 0.5}));
+  CHECK(particles.position(2) == (Vec{-1.0, -1.0}));
+  std::size_t nfix = 0;
+  for (const auto p : particles.fixed()) {
+    CHECK(p.has_type(ParticleType::fixed));
+    ++nfix;
+  }
+  CHECK(nfix == 1);
+  h[particles] = 0.1;
+  for (const auto p : particles.all()) {
+    m[p] = 1.0;
+    rho[p] = 1000.0;
+    CHECK(h[p] == 0.1);
+  }
+
+  // A surface with faces is refused (the GPU path has particle walls only).
+  geom::Surface<Vec<double, 2>> faces;
+  faces.append_vert({0.0, 0.0});
+  faces.append_vert({1.0, 0.0});
+  faces.append_face({0, 1});
+  CHECK(throws([&] {
+    FluidEquations bad{9.81, 0.001, faces, geom::AllInside{},
+                       TaitEquationOfState{20.0, 1000.0},
+                       QuarticWendlandKernel{}};
+  }));
+  CHECK(throws([] { TaitEquationOfState{-1.0, 1000.0}; }));
+  CHECK(throws([] { geom::GridSearch{0.0}; }));
+
+  // A fluid particle outside the containment is refused before any device
+  // call; mixed masses too.
+  const auto outside = [](const Vec<double, 2>& x) { return x[0] < 0.6; };
+  const FluidEquations fenced{9.81, 0.001, domain, outside,
+                              TaitEquationOfState{20.0, 1000.0},
+                              QuarticWendlandKernel{}};
+  ParticleMesh mesh{geom::GridSearch{0.1}};
+  CHECK(throws([&] { fenced.initialize(mesh, particles); }));
+  m[f1] = 2.0;
+  CHECK(throws([&] { particles.attach_(tg_params{}, 1000.0, 20.0, true, false); }));
+  m[f1] = 1.0;
+
+  // .ttdb writer: two series with max_series 1 keeps the last one; frames
+  // and arrays of every kind the particle writer uses.
+  {
+    data::Storage storage{argv[1]};
+    storage.set_max_series(1);
+    (void)storage.create_series("first");
+    const auto series = storage.create_series("second");
+    CHECK(storage.num_series() == 1);
+    CHECK(storage.max_series() == 1);
+    const auto frame = series.create_frame(0.0);
+    const std::vector<Vec<double, 2>> rs{{1.0, 2.0}, {3.0, 4.0}, {5.0, 6.0}};
+    frame.write_array("r", std::span<const Vec<double, 2>>{rs});
+    const std::vector<double> dens{1000.0, 1001.5, 999.25};
+    frame.write_array("rho", std::span<const double>{dens});
+    const std::vector<float> f32{1.5f, -2.0f};
+    frame.write_array("f32", std::span<const float>{f32});
+    const std::vector<std::int32_t> ids{7, 8, 9, 10};
+    frame.write_array("ids", std::span<const std::int32_t>{ids});
+    // A payload over one 128 KiB block.
+    std::vector<double> big(40000);
+    for (std::size_t i = 0; i < big.size(); ++i) big[i] = 0.5 * double(i);
+    frame.write_array("big", std::span<const double>{big});
+    const std::vector<double> none;
+    frame.write_array("empty", std::span<const double>{none});
+    // Background frame write, then a time that does not increase.
+    std::vector<data::ArrayBlob> arrays;
+    arrays.push_back(data::ArrayBlob::of(std::string{"rho"},
+                                         std::span<const double>{dens}));
+    storage.write_frame_async(series.id(), 0.5, std::move(arrays));
+    CHECK(series.num_frames() == 2);
+    CHECK(throws([&] { (void)series.create_frame(0.25); }));
+  }
+  std::printf("ok\n");
+  return 0;
+}

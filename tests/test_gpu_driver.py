@@ -1,0 +1,80 @@
+"""The titwcsph-style C++ driver (titsolver_gb300/host/titwcsph_gpu.cpp) on
+the GPU through the C++ mirror: its initial state, run through the oracle,
+must give its final state (plain FP64: r 1e-9, v and rho 1e-7 relative L2
+after 20 steps; FP32-compensated: rho 1e-5, r 1e-6), and its .ttdb frames
+must hold that final state."""
+
+from __future__ import annotations
+
+import sqlite3
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import oracle_run, rel_l2
+from test_host_mirror import decode
+from titsolver_gb300 import _abi, build as gpu_build, physics
+
+pytestmark = pytest.mark.gpu
+
+
+def read_dump(path):
+    raw = path.read_bytes()
+    n, nf, steps = np.frombuffer(raw, "<i8", 3)
+    h, m, rho0, cs0, t = np.frombuffer(raw, "<f8", 5, offset=24)
+    off = 64
+
+    def state(off):
+        r = np.frombuffer(raw, "<f8", 2 * n, offset=off).reshape(n, 2)
+        off += 16 * n
+        v = np.frombuffer(raw, "<f8", 2 * n, offset=off).reshape(n, 2)
+        off += 16 * n
+        rho = np.frombuffer(raw, "<f8", n, offset=off)
+        return (r, v, rho), off + 8 * n
+
+    init, off = state(off)
+    final, off = state(off)
+    assert off == len(raw)
+    tank = dict(n_fluid=int(nf), n_wall=int(n - nf), h=float(h), m=float(m),
+                rho0=float(rho0), cs0=float(cs0))
+    return tank, init, final, float(t), int(steps)
+
+
+@pytest.mark.parametrize("fp32c", (False, True))
+def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c):
+    exe = gpu_build.build_host()["titwcsph_gpu"]
+    dump, ttdb = tmp_path / "state.bin", tmp_path / "particles.ttdb"
+    cmd = [str(exe), "--nx", "20", "--steps", "20", "--dump", str(dump), "--ttdb", str(ttdb)]
+    if fp32c:
+        cmd.append("--fp32c")
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    tank, (r0, v0, rho0), (r1, v1, rho1), t, steps = read_dump(dump)
+    assert steps == 20
+    scn = dict(dim=2, tanks=[tank], r=r0.copy(), v=v0.copy(), rho=rho0.copy())
+    # The driver's physics: the reference term set, C4 Wendland, mu = 0.001.
+    o = oracle_run(scn, physics.reference_params(2), steps)
+    f = np.arange(r0.shape[0]) < tank["n_fluid"]
+    np.testing.assert_allclose(t, o.time[0], rtol=1e-12 if not fp32c else 1e-6)
+    if fp32c:
+        assert rel_l2(rho1[f], o.rho[f]) <= 1e-5
+        assert rel_l2(r1[f], o.r[f]) <= 1e-6
+    else:
+        assert rel_l2(r1[f], o.r[f]) <= 1e-9
+        assert rel_l2(v1[f], o.v[f]) <= 1e-7
+        assert rel_l2(rho1[f], o.rho[f]) <= 1e-7
+    # The .ttdb: frame 0 is the initial state, the last one the final state.
+    con = sqlite3.connect(ttdb)
+    frames = con.execute("SELECT id, time FROM DataFrames ORDER BY id").fetchall()
+    assert len(frames) == 2 and frames[0][1] == 0.0 and frames[1][1] > 0.0
+    arrays = {name: decode(data) for name, data in con.execute(
+        "SELECT name, data FROM DataArrays WHERE frame_id = ?", (frames[1][0],))}
+    assert {"r", "v", "dv_dt", "rho", "drho_dt", "p", "cs", "m"} <= set(arrays)
+    np.testing.assert_array_equal(np.frombuffer(arrays["r"], "<f8").reshape(-1, 2), r1)
+    np.testing.assert_array_equal(np.frombuffer(arrays["rho"], "<f8"), rho1)
+    r_first = np.frombuffer(decode(con.execute(
+        "SELECT data FROM DataArrays WHERE frame_id = ? AND name = 'r'",
+        (frames[0][0],)).fetchone()[0]), "<f8").reshape(-1, 2)
+    np.testing.assert_array_equal(r_first, r0)
+    con.close()

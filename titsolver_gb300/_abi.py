@@ -94,6 +94,16 @@ class TgProfile(ctypes.Structure):
     ]
 
 
+class TgTuning(ctypes.Structure):
+    _fields_ = [
+        ("cells_per_radius", ctypes.c_int32),
+        ("block_size", ctypes.c_int32),
+        ("lanes_per_particle", ctypes.c_int32),
+        ("candidates", ctypes.c_int32),
+        ("ms_per_step", ctypes.c_double),
+    ]
+
+
 # (name, restype, argtypes) of every exported entry point.
 _P = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
@@ -128,6 +138,9 @@ SIGNATURES = [
     ("tg_summation_density_noalloc", ctypes.c_int,
      [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _P, ctypes.c_double, ctypes.c_double,
       _P, _P, _P, _P]),
+    ("tg_get_tuning", ctypes.c_int, [_P, ctypes.POINTER(TgTuning)]),
+    ("tg_set_tuning", ctypes.c_int, [_P, ctypes.POINTER(TgTuning)]),
+    ("tg_autotune", ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(TgTuning)]),
     ("tg_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("tg_last_error", ctypes.c_char_p, [_P]),
 ]
@@ -340,3 +353,20 @@ class Context:
         ms = ctypes.c_double()
         self._check(self.lib.tg_timer_stop(self.handle, ctypes.byref(ms)), "tg_timer_stop")
         return ms.value
+
+    def get_tuning(self) -> dict:
+        t = TgTuning()
+        self._check(self.lib.tg_get_tuning(self.handle, ctypes.byref(t)), "tg_get_tuning")
+        return {k: getattr(t, k) for k, _ in TgTuning._fields_}
+
+    def set_tuning(self, cells_per_radius: int, block_size: int = 128,
+                   lanes_per_particle: int = 1):
+        t = TgTuning(cells_per_radius, block_size, lanes_per_particle, 0, 0.0)
+        self._check(self.lib.tg_set_tuning(self.handle, ctypes.byref(t)), "tg_set_tuning")
+
+    def autotune(self, trial_steps: int = 3) -> dict:
+        """Time candidate launch shapes and keep the fastest (state kept)."""
+        t = TgTuning()
+        self._check(self.lib.tg_autotune(self.handle, int(trial_steps), ctypes.byref(t)),
+                    "tg_autotune")
+        return {k: getattr(t, k) for k, _ in TgTuning._fields_}

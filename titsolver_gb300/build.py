@@ -94,6 +94,32 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     return LIB
 
 
+HOST_DIR = PKG / "host"
+INCLUDE = ROOT / "include"
+
+
+def build_host(force: bool = False) -> dict[str, pathlib.Path]:
+    """Compile the C++ host programs of ``host/*.cpp`` (drivers over the C++
+    mirror of ``include/titgpu.hpp``) next to the library; returns name ->
+    executable.  Plain g++ for the build machine (no -march flags)."""
+    lib = build()
+    out = {}
+    deps = [lib, *INCLUDE.glob("*.h"), *INCLUDE.glob("*.hpp"), pathlib.Path(__file__)]
+    for src in sorted(HOST_DIR.glob("*.cpp")):
+        exe = OUT_DIR / src.stem
+        fresh = exe.exists() and all(p.stat().st_mtime <= exe.stat().st_mtime
+                                     for p in [src, *deps])
+        if force or not fresh:
+            cmd = [os.environ.get("CXX", "g++"), "-std=c++20", "-O2", "-Wall", "-Wextra",
+                   "-I", str(INCLUDE), str(src), "-L", str(OUT_DIR), "-ltitgpu",
+                   "-Wl,-rpath,$ORIGIN", "-ldl", "-pthread", "-o", str(exe)]
+            res = subprocess.run(cmd, capture_output=True, text=True)
+            if res.returncode != 0:
+                raise RuntimeError(f"g++ failed on {src.name}:\n{res.stdout}\n{res.stderr}")
+        out[src.stem] = exe
+    return out
+
+
 if __name__ == "__main__":
     import argparse
 
@@ -102,3 +128,5 @@ if __name__ == "__main__":
     ap.add_argument("--verbose", action="store_true", help="print ptxas register/spill report")
     a = ap.parse_args()
     print(build(force=a.force, verbose=a.verbose))
+    for name, exe in build_host(force=a.force).items():
+        print(exe)

@@ -817,6 +817,207 @@ int tg_timer_stop(tg_context* ctx, double* ms) {
   return TG_OK;
 }
 
+// ---- launch-shape tuning -----------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// Host copy of the whole particle state and the per-tank clocks, in upload
+// order, so that trial steps can be undone.
+struct Snapshot {
+  std::vector<double> r, v, rho, dv, time, dt_last;
+};
+
+int take_snapshot(tg_context* ctx, Snapshot* S) {
+  Context& C = ctx->c;
+  const size_t n = static_cast<size_t>(C.n), d = static_cast<size_t>(C.P.dim);
+  S->r.resize(n * d);
+  S->v.resize(n * d);
+  S->dv.resize(n * d);
+  S->rho.resize(n);
+  S->time.resize(static_cast<size_t>(C.ntanks));
+  S->dt_last.resize(static_cast<size_t>(C.ntanks));
+  int st = tg_particles_download(ctx, TG_FIELD_R, S->r.data());
+  if (st == TG_OK) st = tg_particles_download(ctx, TG_FIELD_V, S->v.data());
+  if (st == TG_OK) st = tg_particles_download(ctx, TG_FIELD_RHO, S->rho.data());
+  if (st == TG_OK) st = tg_particles_download(ctx, TG_FIELD_DV_DT, S->dv.data());
+  if (st != TG_OK) return st;
+  TG_CUDA(&C, cudaMemcpy(S->time.data(), C.d_time, sizeof(double) * C.ntanks,
+                         cudaMemcpyDeviceToHost));
+  TG_CUDA(&C, cudaMemcpy(S->dt_last.data(), C.d_dt_last,
+                         sizeof(double) * C.ntanks, cudaMemcpyDeviceToHost));
+  return TG_OK;
+}
+
+// Put a snapshot back.  A new cells_per_radius re-grids the tanks (from the
+// snapshot's positions) before the state goes back.
+int restore_snapshot(tg_context* ctx, const Snapshot& S, int k) {
+  Context& C = ctx->c;
+  if (k != C.k) {
+    const int old_k = C.k;
+    C.k = k;
+    C.P.cells_per_radius = k;
+    const std::vector<tg_tank> tanks = C.tanks;
+    const int st = tg_particles_upload(ctx, C.ntanks, tanks.data(), S.r.data(),
+                                       S.v.data(), S.rho.data());
+    if (st != TG_OK) {
+      // Back to the old grid (the same data fitted it before).
+      C.k = old_k;
+      C.P.cells_per_radius = old_k;
+      const std::string why = C.last_error;
+      tg_particles_upload(ctx, C.ntanks, tanks.data(), S.r.data(), S.v.data(),
+                          S.rho.data());
+      C.last_error = why;
+      return st;
+    }
+  }
+  const int st = tg_particles_update(ctx, S.r.data(), S.v.data(), S.rho.data(),
+                                     S.dv.data());
+  if (st != TG_OK) return st;
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_time, S.time.data(),
+                              sizeof(double) * C.ntanks,
+                              cudaMemcpyHostToDevice, C.stream));
+  TG_CUDA(&C, cudaMemcpyAsync(C.d_dt_last, S.dt_last.data(),
+                              sizeof(double) * C.ntanks,
+                              cudaMemcpyHostToDevice, C.stream));
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  return TG_OK;
+}
+
+bool valid_shape(const Context& C, const tg_tuning& t) {
+  return t.cells_per_radius >= 1 && t.cells_per_radius <= 3 &&
+         (t.block_size == 64 || t.block_size == 128 || t.block_size == 256) &&
+         (t.lanes_per_particle == 1 || t.lanes_per_particle == 2 ||
+          t.lanes_per_particle == 4) &&
+         C.engine->supports_team(t.lanes_per_particle);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tg_get_tuning(tg_context* ctx, tg_tuning* out) {
+  if (ctx == nullptr || out == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  const Context& C = ctx->c;
+  std::memset(out, 0, sizeof(*out));
+  out->cells_per_radius = C.k;
+  out->block_size = C.force_block;
+  out->lanes_per_particle = C.force_team;
+  out->ms_per_step = C.tuned_ms;
+  out->candidates = C.tuned_candidates;
+  return TG_OK;
+}
+
+int tg_set_tuning(tg_context* ctx, const tg_tuning* tuning) {
+  if (ctx == nullptr || tuning == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!valid_shape(C, *tuning)) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT,
+                "launch shape: cells_per_radius 1..3, block_size 64/128/256, "
+                "lanes_per_particle 1/2/4 (2 and 4 for Wendland C2/C4 only)");
+  }
+  if (tuning->cells_per_radius != C.k) {
+    if (C.uploaded && C.n > 0) {
+      Snapshot S;
+      int st = take_snapshot(ctx, &S);
+      if (st == TG_OK) st = restore_snapshot(ctx, S, tuning->cells_per_radius);
+      if (st != TG_OK) return st;
+    } else {
+      C.k = tuning->cells_per_radius;
+      C.P.cells_per_radius = C.k;
+    }
+  }
+  C.force_block = tuning->block_size;
+  C.force_team = tuning->lanes_per_particle;
+  C.invalidate_graph();
+  return TG_OK;
+}
+
+int tg_autotune(tg_context* ctx, int32_t trial_steps, tg_tuning* out) {
+  if (ctx == nullptr || trial_steps < 1 || trial_steps > 1000) {
+    return TG_ERR_INVALID_ARGUMENT;
+  }
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (C.n_fluid == 0) return fail(&C, TG_ERR_INVALID_ARGUMENT, "no fluid");
+  Snapshot S;
+  int st = take_snapshot(ctx, &S);
+  if (st != TG_OK) return st;
+  tg_tuning best{};
+  tg_get_tuning(ctx, &best);
+  best.ms_per_step = std::numeric_limits<double>::infinity();
+  int timed = 0;
+  // Time `trial_steps` graph-replayed steps of one shape (one untimed step
+  // first captures the graph); the state goes back afterwards.
+  auto trial = [&](tg_tuning t, double* ms) -> int {
+    *ms = std::numeric_limits<double>::infinity();
+    int s = restore_snapshot(ctx, S, t.cells_per_radius);
+    if (s == TG_ERR_INVALID_ARGUMENT) return TG_OK;  // grid too large: skip
+    if (s != TG_OK) return s;
+    C.force_block = t.block_size;
+    C.force_team = t.lanes_per_particle;
+    C.invalidate_graph();
+    s = tg_step(ctx, 1, nullptr);
+    if (s == TG_OK) s = tg_timer_start(ctx);
+    if (s == TG_OK) s = tg_step(ctx, trial_steps, nullptr);
+    double total = 0.0;
+    if (s == TG_OK) s = tg_timer_stop(ctx, &total);
+    if (s != TG_OK) return s;
+    *ms = total / trial_steps;
+    ++timed;
+    return TG_OK;
+  };
+  auto consider = [&](tg_tuning t) -> int {
+    if (!valid_shape(C, t)) return TG_OK;
+    double ms = 0.0;
+    const int s = trial(t, &ms);
+    if (s != TG_OK) return s;
+    if (ms < best.ms_per_step) {
+      best = t;
+      best.ms_per_step = ms;
+    }
+    return TG_OK;
+  };
+  // Coordinate search: cell size, then lanes per target, then block size,
+  // each with the others at their best so far.
+  tg_tuning base = best;
+  base.block_size = 128;
+  base.lanes_per_particle = 1;
+  for (int k = 1; k <= 3 && st == TG_OK; ++k) {
+    tg_tuning t = base;
+    t.cells_per_radius = k;
+    st = consider(t);
+  }
+  for (int lanes : {2, 4}) {
+    if (st != TG_OK) break;
+    tg_tuning t = best;
+    t.lanes_per_particle = lanes;
+    st = consider(t);
+  }
+  for (int block : {64, 256}) {
+    if (st != TG_OK) break;
+    tg_tuning t = best;
+    t.block_size = block;
+    st = consider(t);
+  }
+  // Leave the context at the best shape with the state of the call.
+  const int st2 = restore_snapshot(
+      ctx, S, std::isfinite(best.ms_per_step) ? best.cells_per_radius : C.k);
+  if (st != TG_OK) return st;
+  if (st2 != TG_OK) return st2;
+  if (!std::isfinite(best.ms_per_step)) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "no launch shape fits");
+  }
+  C.force_block = best.block_size;
+  C.force_team = best.lanes_per_particle;
+  C.invalidate_graph();
+  C.tuned_ms = best.ms_per_step;
+  C.tuned_candidates = timed;
+  best.candidates = timed;
+  if (out != nullptr) *out = best;
+  return TG_OK;
+}
+
 int tg_host_alloc(size_t bytes, void** out) {
   if (out == nullptr) return TG_ERR_INVALID_ARGUMENT;
   *out = nullptr;

@@ -418,6 +418,11 @@ struct Kahan {
     s = t;
   }
   __device__ __forceinline__ float value() const { return s; }
+  // Fold in another accumulator's sum s2 - c2 (two compensated adds).
+  __device__ __forceinline__ void merge(float s2, float c2) {
+    add(s2);
+    add(-c2);
+  }
 };
 
 }  // namespace tg

@@ -49,6 +49,8 @@ struct EngineBase {
                                       uint64_t* hashes) = 0;
   // Kernel launches of one step.
   virtual int64_t launches_per_step(Context& C) = 0;
+  // Whether the force pass has a variant with `team` lanes per target.
+  virtual bool supports_team(int team) const = 0;
 };
 
 std::unique_ptr<EngineBase> make_engine_2d_f64(int kernel);
@@ -79,6 +81,11 @@ struct Context {
   int key_bits = 0;
   int k = 1;
   bool uploaded = false;
+  // Launch shape of the force pass (tg_set_tuning / tg_autotune).
+  int force_block = 128;
+  int force_team = 1;
+  double tuned_ms = 0.0;  // device time per step of the tuned shape
+  int tuned_candidates = 0;
 
   // Common device buffers.
   TankDev* d_tanks = nullptr;

@@ -26,6 +26,12 @@ inline int physics_preset(const tg_params& P) {
   return kPhysGeneric;
 }
 
+// Kernels with multi-lane force variants: the two the shipped parameter
+// sets use (Wendland C2 and C4); the others run one lane per target.
+constexpr bool team_kernel(int K) {
+  return K == TG_KERNEL_WENDLAND_C2 || K == TG_KERNEL_WENDLAND_C4;
+}
+
 template<int D, int F, int K>
 class Engine final : public EngineBase {
  public:
@@ -193,6 +199,10 @@ class Engine final : public EngineBase {
     return cudaGetLastError();
   }
 
+  bool supports_team(int team) const override {
+    return team == 1 || (team_kernel(K) && (team == 2 || team == 4));
+  }
+
   int64_t launches_per_step(Context& C) override {
     const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
     const int stages = C.P.integrator == TG_SSPRK2 ? 2 : 3;
@@ -274,32 +284,50 @@ class Engine final : public EngineBase {
       C.group_end(tok);
     }
     tok = C.group_begin(kGroupForces);
-    const unsigned grid = grid_for(C.n, 128);
     if constexpr (F == TG_FP32C) {
       const int phys = physics_preset(C.P);
       bool staged = false;
       if constexpr (D == 2) {
         if (C.P.staging) {
-          k_forces_staged2<K><<<grid, 128, 0, C.stream>>>(a);
+          k_forces_staged2<K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
           staged = true;
         }
       }
       if (staged) {
       } else if (phys == kPhysTextbook) {
-        k_forces<D, F, K, kPhysTextbook><<<grid, 128, 0, C.stream>>>(a);
+        launch_forces<kPhysTextbook>(C, a);
       } else if (phys == kPhysReference) {
-        k_forces<D, F, K, kPhysReference><<<grid, 128, 0, C.stream>>>(a);
+        launch_forces<kPhysReference>(C, a);
       } else {
-        k_forces<D, F, K><<<grid, 128, 0, C.stream>>>(a);
+        launch_forces<kPhysGeneric>(C, a);
       }
     } else {
-      k_forces<D, F, K><<<grid, 128, 0, C.stream>>>(a);
+      launch_forces<kPhysGeneric>(C, a);
     }
     C.launches += 1;
     C.group_end(tok);
     // k_forces and k_walls wrote the keys of the new positions.
     C.keys_valid = true;
     return cudaGetLastError();
+  }
+
+  // The force pass at the context's launch shape: C.force_team lanes per
+  // target (team variants exist for the Wendland C2 and C4 kernels) in
+  // blocks of C.force_block threads.
+  template<int Phys>
+  void launch_forces(Context& C, const StageArgs<D, F>& a) {
+    const int block = C.force_block;
+    if constexpr (team_kernel(K)) {
+      if (C.force_team == 4) {
+        k_forces<D, F, K, Phys, 4><<<grid_for(C.n * 4, block), block, 0, C.stream>>>(a);
+        return;
+      }
+      if (C.force_team == 2) {
+        k_forces<D, F, K, Phys, 2><<<grid_for(C.n * 2, block), block, 0, C.stream>>>(a);
+        return;
+      }
+    }
+    k_forces<D, F, K, Phys, 1><<<grid_for(C.n, block), block, 0, C.stream>>>(a);
   }
 
   StateBuf<R> X_{}, Y_{};

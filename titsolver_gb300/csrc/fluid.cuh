@@ -189,12 +189,13 @@ __device__ __forceinline__ void for_cells(const TankDev& T, const int* c,
   }
 }
 
-// Fluid ranges of the (2k+1)^D cell block around c, dealt out to the lanes
-// of a team: lane l of a team of `team` lanes visits cells l, l + team, ...
-// of the block (cells, not particles, are split, so no lane repeats another
-// lane's cell-table reads).
-template<int D, class Fn>
-__device__ __forceinline__ void for_fluid_cells_team(
+// The (2k+1)^D cell block around c, dealt out to the lanes of a team: lane
+// l of a team of `team` lanes visits cells l, l + team, ... of the block
+// (cells, not particles, are split, so no lane repeats another lane's
+// cell-table reads).  Each visit gets the cell's fluid range (FluidOnly) or
+// its whole range, fluid then walls, with the cell offset (dx, dy, dz).
+template<int D, bool FluidOnly, class Fn>
+__device__ __forceinline__ void for_cells_team(
     const TankDev& T, const int* c, int k,
     const uint32_t* __restrict__ cstart, int lane, int team, Fn&& fn) {
   const int nx = T.nc[0], ny = T.nc[1];
@@ -211,8 +212,19 @@ __device__ __forceinline__ void for_fluid_cells_team(
     const int z = zlo + rest / wy;
     const uint32_t kc =
         2 * (T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx + x);
-    fn(__ldg(cstart + kc), __ldg(cstart + kc + 1), x - c[0], y - c[1],
-       D == 3 ? z - c[2] : 0);
+    fn(__ldg(cstart + kc), __ldg(cstart + kc + (FluidOnly ? 1 : 2)),
+       x - c[0], y - c[1], D == 3 ? z - c[2] : 0);
+  }
+}
+
+// Mask of the `team` lanes (aligned, a power of two) that hold this lane.
+template<int Team>
+__device__ __forceinline__ unsigned team_mask() {
+  if constexpr (Team >= 32) {
+    return 0xffffffffu;
+  } else {
+    const unsigned base = (threadIdx.x & 31u) & ~static_cast<unsigned>(Team - 1);
+    return ((1u << Team) - 1u) << base;
   }
 }
 
@@ -457,7 +469,7 @@ __global__ void __launch_bounds__(128)
           H += Vb * Hb * W;
         }
       };
-      for_fluid_cells_team<D>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
+      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
     }
 #pragma unroll
     for (int o = kWallTeam / 2; o > 0; o >>= 1) {
@@ -497,7 +509,7 @@ __global__ void __launch_bounds__(128)
           H.add(Vb * Hb * W);
         }
       };
-      for_fluid_cells_team<D>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
+      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
     }
     float Ss = S.value(), Hv = H.value();
 #pragma unroll
@@ -717,10 +729,19 @@ __device__ __forceinline__ void forces_epilogue(
   }
 }
 
-template<int D, int F, int K, int Phys = kPhysGeneric>
-__global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(StageArgs<D, F> A) {
+// Team lanes share one target: each takes every Team-th cell of the block
+// and the team merges its partial sums by shuffles (compensated merges in
+// the FP32 form), so a warp advances 32 / Team targets.  The block size is
+// a run-time choice (a multiple of 32, at most 256) at the register budget
+// of forces_min_blocks 128-thread blocks per SM.
+template<int D, int F, int K, int Phys = kPhysGeneric, int Team = 1>
+__global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
+    k_forces(StageArgs<D, F> A) {
   using R = typename StageArgs<D, F>::R;
-  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t gt = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t i = gt / Team;
+  const int lane = Team == 1 ? 0 : static_cast<int>(threadIdx.x % Team);
+  // Every exit below is uniform over a team (its lanes share i).
   if (i >= A.n) return;
   const uint32_t id = A.Y.id[i];
   if (id & kWallBit) return;
@@ -746,9 +767,8 @@ __global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(Stage
     const double mu2 = 2.0 * A.phys.mu, ah = A.phys.alpha * T.h;
     const double eps2 = T.visc_eps2, dk = T.diff_k;
     double drho = 0.0;
-    double dv[3] = {0.0, -A.phys.g, 0.0};
-    for_cells<D, false>(T, c, A.k, A.cell_start,
-                        [&](uint32_t s, uint32_t en, int, int, int) {
+    double dv[3] = {0.0, lane == 0 ? -A.phys.g : 0.0, 0.0};
+    auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
       for (uint32_t j = s; j < en; ++j) {
         if (j == static_cast<uint32_t>(i)) continue;
         double pb[3], d[3];
@@ -784,18 +804,31 @@ __global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(Stage
 #pragma unroll
         for (int k = 0; k < D; ++k) dv[k] += coef * d[k];
       }
-    });
+    };
+    if constexpr (Team == 1) {
+      for_cells<D, false>(T, c, A.k, A.cell_start, visit);
+    } else {
+      for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, visit);
+      const unsigned mask = team_mask<Team>();
+#pragma unroll
+      for (int o = Team / 2; o > 0; o >>= 1) {
+        drho += __shfl_xor_sync(mask, drho, o, Team);
+#pragma unroll
+        for (int k = 0; k < D; ++k) dv[k] += __shfl_xor_sync(mask, dv[k], o, Team);
+      }
+      if (lane != 0) return;
+    }
 #pragma unroll
     for (int k = 0; k < D; ++k) dv_out[k] = dv[k];
     drho_out = drho;
   } else {
     PairF32<D, K, Phys> acc;
     acc.init(A.phys, T, load_dat(A.datrec, static_cast<uint32_t>(i)), A.kahan);
+    if (lane != 0) acc.dv[1].s = 0.f;  // gravity once per target
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
     const float csz = T.cs_f;
-    for_cells<D, true>(T, c, A.k, A.cell_start,
-                       [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+    auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
       float oas[3];
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
@@ -811,7 +844,24 @@ __global__ void __launch_bounds__(128, forces_min_blocks<D, F>()) k_forces(Stage
         if (s2 > acc.R2) continue;
         acc.add(d, s2, load_dat(A.datrec, j));
       }
-    });
+    };
+    if constexpr (Team == 1) {
+      for_cells<D, true>(T, c, A.k, A.cell_start, visit);
+    } else {
+      for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, visit);
+      const unsigned mask = team_mask<Team>();
+#pragma unroll
+      for (int o = Team / 2; o > 0; o >>= 1) {
+        acc.drho.merge(__shfl_xor_sync(mask, acc.drho.s, o, Team),
+                       __shfl_xor_sync(mask, acc.drho.c, o, Team));
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          acc.dv[k].merge(__shfl_xor_sync(mask, acc.dv[k].s, o, Team),
+                          __shfl_xor_sync(mask, acc.dv[k].c, o, Team));
+        }
+      }
+      if (lane != 0) return;
+    }
 #pragma unroll
     for (int k = 0; k < D; ++k) {
       va[k] = acc.va[k];

@@ -1,0 +1,256 @@
+// titwcsph_gpu.cpp - the titwcsph dam break (source/titwcsph/wcsph.cpp:37-193)
+// driven through the C++ mirror of titgpu.hpp: the same setup expressions,
+// API calls and loop, with three layers of fixed wall particles in place of
+// the tessellated boundary faces (the GPU path runs particle walls).
+//
+// Usage: titwcsph_gpu [--nx N] [--steps S] [--end-time T] [--fp32c]
+//                     [--ttdb FILE] [--dump FILE]
+//   --nx       particles per column height H (default 80, as wcsph.cpp:42)
+//   --steps    stop after S steps (default: run to scaled time T)
+//   --end-time scaled end time t sqrt(g/H) (default 10, as wcsph.cpp:183)
+//   --fp32c    FP32-compensated pair sums instead of plain FP64
+//   --ttdb     write frames every 100 steps to this .ttdb file
+//   --dump     write the initial and final state as raw binary (see below)
+//
+// Dump layout (little-endian): int64 n, n_fluid, steps; float64 h, m, rho_0,
+// cs_0, time; then r (n x 2), v (n x 2), rho (n) of the initial state and
+// the same of the final state.
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <numbers>
+#include <optional>
+#include <string>
+#include <vector>
+
+#include "titgpu.hpp"
+#include "titgpu_data.hpp"
+
+namespace tit::sph::wcsph {
+namespace {
+
+struct Options {
+  int nx = 80;
+  long steps = -1;
+  double end_time = 10.0;
+  bool fp32c = false;
+  std::string ttdb;
+  std::string dump;
+};
+
+auto parse(int argc, char** argv) -> Options {
+  Options o;
+  for (int i = 1; i < argc; ++i) {
+    const std::string a = argv[i];
+    const auto next = [&]() -> std::string {
+      if (i + 1 >= argc) throw Exception{"missing value after " + a};
+      return argv[++i];
+    };
+    if (a == "--nx") o.nx = std::stoi(next());
+    else if (a == "--steps") o.steps = std::stol(next());
+    else if (a == "--end-time") o.end_time = std::stod(next());
+    else if (a == "--fp32c") o.fp32c = true;
+    else if (a == "--ttdb") o.ttdb = next();
+    else if (a == "--dump") o.dump = next();
+    else throw Exception{"unknown option " + a};
+  }
+  if (o.nx < 4) throw Exception{"--nx must be at least 4"};
+  return o;
+}
+
+template<class PA>
+void dump_state(std::ofstream& out, PA& particles) {
+  const auto& cp = std::as_const(particles);
+  for (std::size_t i = 0; i < cp.size(); ++i) {
+    const auto& x = cp.position(i);
+    out.write(reinterpret_cast<const char*>(&x[0]), 2 * sizeof(double));
+  }
+  for (std::size_t i = 0; i < cp.size(); ++i) {
+    const auto& x = cp.velocity(i);
+    out.write(reinterpret_cast<const char*>(&x[0]), 2 * sizeof(double));
+  }
+  for (std::size_t i = 0; i < cp.size(); ++i) {
+    const double d = cp.density(i);
+    out.write(reinterpret_cast<const char*>(&d), sizeof(double));
+  }
+}
+
+template<class Real>
+auto sph_main(int argc, char** argv) -> int {
+  const Options opt = parse(argc, argv);
+
+  constexpr Real H = 0.6;   // Water column height.
+  constexpr Real L = 2 * H; // Water column length.
+
+  constexpr Real POOL_WIDTH = 5.366 * H; // Pool width.
+  constexpr Real POOL_HEIGHT = 4.0 * H;  // Pool height.
+
+  const Real dr = H / opt.nx; // Initial particle spacing.
+  const auto WATER_M = int(std::round(L / dr));
+  const auto WATER_N = int(std::round(H / dr));
+
+  constexpr Real g = 9.81;
+  constexpr Real rho_0 = 1000.0;
+  const Real cs_0 = 20 * std::sqrt(g * H);
+  const Real h_0 = 2.0 * dr;
+  const Real m_0 = rho_0 * pow2(dr);
+  constexpr Real mu = 0.001;
+
+  // Particle walls: the domain surface stays empty and every point is
+  // inside the containment (gamma = 1, no face terms).
+  const geom::Surface<Vec<Real, 2>> domain;
+  GpuOptions gpu;
+  gpu.precision = opt.fp32c ? Precision::fp32_compensated : Precision::fp64;
+  const FluidEquations equations{
+      // Constants.
+      g,
+      mu,
+      // Wall boundary.
+      domain,
+      geom::AllInside{},
+      // Weakly compressible equation of state.
+      TaitEquationOfState{cs_0, rho_0},
+      // C4 Wendland's spline kernel.
+      SixthOrderWendlandKernel{},
+      gpu,
+  };
+
+  // Setup the time integrator.
+  const SSPRKIntegrator time_integrator{equations, SSPRKOrder::three};
+
+  // Setup the particles array:
+  ParticleArray particles{
+      // 2D space.
+      Space<Real, 2>{},
+      // Set of fields is inferred from the time integrator.
+      time_integrator,
+  };
+
+  // Generate individual particles.
+  for (auto i = 0; i < WATER_M; ++i) {
+    for (auto j = 0; j < WATER_N; ++j) {
+      auto a = particles.append(ParticleType::fluid);
+      r[a] = dr * Vec{i + Real{1.0}, j + Real{1.0}};
+    }
+  }
+  // Three layers of fixed particles on the dr lattice: bottom and both
+  // sides of the pool, open top.
+  const auto nW = int(std::round(POOL_WIDTH / dr));
+  const auto nH = int(std::round(POOL_HEIGHT / dr));
+  for (auto j = -2; j <= nH; ++j) {
+    for (auto i = -2; i <= nW + 2; ++i) {
+      if (i > 0 && i < nW && j > 0) continue;
+      auto a = particles.append(ParticleType::fixed);
+      r[a] = dr * Vec{Real(i), Real(j)};
+    }
+  }
+
+  // Set global particle constants.
+  h[particles] = h_0;
+  for (const auto a : particles.all()) {
+    m[a] = m_0;
+    rho[a] = rho_0;
+  }
+
+  // Density hydrostatic initialization.
+  for (const auto a : particles.all()) {
+    if (a.has_type(ParticleType::fixed)) {
+      rho[a] = rho_0;
+      continue;
+    }
+
+    // Compute pressure from Poisson problem.
+    const auto x = r[a][0];
+    const auto y = r[a][1];
+    auto p_a = rho_0 * g * (H - y);
+    for (std::size_t k = 1; k < 100; k += 2) {
+      constexpr auto pi = std::numbers::pi_v<Real>;
+      const auto k_pi = static_cast<Real>(k) * pi;
+      p_a -= 8 * rho_0 * g * H / pow2(k_pi) *
+             (std::exp(k_pi * (x - L) / (2 * H)) * std::cos(k_pi * y / (2 * H)));
+    }
+
+    // Recalculate density.
+    rho[a] = rho_0 + p_a / pow2(cs_0);
+  }
+
+  std::ofstream dump;
+  if (!opt.dump.empty()) {
+    dump.open(opt.dump, std::ios::binary);
+    if (!dump) throw Exception{"cannot open " + opt.dump};
+    const std::int64_t head[3] = {static_cast<std::int64_t>(particles.size()),
+                                  static_cast<std::int64_t>(particles.num_fluid()),
+                                  opt.steps};
+    dump.write(reinterpret_cast<const char*>(head), sizeof(head));
+    const double consts[5] = {h_0, m_0, rho_0, cs_0, 0.0};
+    dump.write(reinterpret_cast<const char*>(consts), sizeof(consts));
+    dump_state(dump, particles);
+  }
+
+  // Setup the particle mesh structure.
+  ParticleMesh mesh{
+      // Search for the particles using the grid search.
+      geom::GridSearch{h_0},
+      // Search for the boundary faces using the grid search.
+      geom::GridFaceSearch{h_0},
+      // Use RIB as the primary partitioning method.
+      geom::RecursiveInertialBisection{},
+      // Use pixelated K-means as the interface partitioning method.
+      geom::PixelatedPartition{2 * h_0, geom::KMeansClustering{}},
+  };
+
+  // Initialize the particles.
+  equations.initialize(mesh, particles);
+
+  // Store only the last run, as the reference driver does.
+  std::optional<data::Storage> storage;
+  std::optional<data::SeriesView> series;
+  if (!opt.ttdb.empty()) {
+    storage.emplace(opt.ttdb);
+    storage->set_max_series(1);
+    series.emplace(storage->create_series());
+    particles.write(0.0, *series);
+  }
+
+  // Run the simulation.
+  Real time{};
+  std::size_t step = 1;
+  for (;; ++step) {
+    const auto scaled_time = time * std::sqrt(g / H);
+    const Real dt = time_integrator.step(mesh, particles);
+    const bool end = opt.steps >= 0 ? static_cast<long>(step) >= opt.steps
+                                    : scaled_time >= opt.end_time;
+    if (series && ((step % 100 == 0) || end)) {
+      particles.write(scaled_time + dt * std::sqrt(g / H), *series);
+    }
+    time += dt;
+    if (end) break;
+  }
+  if (storage) storage->wait();
+
+  if (dump) {
+    dump_state(dump, particles);
+    dump.seekp(3 * sizeof(std::int64_t) + 4 * sizeof(double));
+    const double t = time;
+    dump.write(reinterpret_cast<const char*>(&t), sizeof(t));
+  }
+  std::printf("titwcsph_gpu: %zu steps, time %.6f, %zu particles (%zu fluid)\n",
+              step, static_cast<double>(time), particles.size(),
+              particles.num_fluid());
+  return 0;
+}
+
+} // namespace
+} // namespace tit::sph::wcsph
+
+auto main(int argc, char** argv) -> int {
+  try {
+    return tit::sph::wcsph::sph_main<double>(argc, argv);
+  } catch (const tit::Exception& e) {
+    std::fprintf(stderr, "titwcsph_gpu: %s\n", e.what());
+    return 1;
+  }
+}
