@@ -95,6 +95,10 @@ def make_config(name: str):
     if name == "c4q":
         return ("3D dam break 2Hx1Hx1H, dx=H/100 (2,000,000 fluid + 3-layer walls), "
                 "Wendland C2 h=1.3dx, same physics"), lambda: scenarios.dam_break_3d(nx_per_H=100)
+    if name == "c5":
+        return ("64 independent 3D dam breaks, column height N~U{12..40} particles, "
+                "length and depth U[0.5,2] N, dx=1/100, Wendland C2 h=1.3dx, same physics"), \
+            lambda: scenarios.batched_tanks_3d(64)
     if name == "c4half":
         return ("3D dam break 2Hx1HxH/2, dx=H/200 (8,000,000 fluid + 3-layer walls), "
                 "Wendland C2 h=1.3dx, same physics"), \

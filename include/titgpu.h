@@ -98,8 +98,11 @@ enum {
 };
 /* Post-integration stage (fluid_equations.hpp:315-321). */
 enum {
-  TG_POST_PREPARE = 0, /* refresh mesh and wall state only */
-  TG_POST_SHIFTING = 1 /* + apply_shifts + free-surface density correction */
+  TG_POST_PREPARE = 0, /* refresh mesh and wall state only (the next step's
+                          prepare does this anyway: no extra pass) */
+  TG_POST_SHIFTING = 1 /* + apply_shifts + free-surface density correction
+                          (fluid_equations.hpp:331-512): one more search,
+                          wall extrapolation and five passes per step */
 };
 /* Fields for tg_particles_download (names of source/tit/sph/field.hpp). */
 enum {
@@ -117,7 +120,9 @@ enum {
  * values: SixthOrderWendlandKernel (wcsph.cpp:89), xi = 7
  * (equation_of_state.hpp:29), g = 9.81 and mu = 0.001 (wcsph.cpp:47,52),
  * Morris viscosity, Ferrari diffusion, CFL 0.4, C_force 0.25, C_visc 0.125
- * (fluid_equations.hpp:518-520), SSPRK3, FP64. */
+ * (fluid_equations.hpp:518-520), SSPRK3, post-integration with shifting and
+ * the free-surface correction (FluidEquations::post_integrate always runs
+ * them, fluid_equations.hpp:315-321), FP64. */
 typedef struct tg_params {
   int32_t dim;              /* 2 or 3 */
   int32_t precision;        /* TG_FP64 | TG_FP32C */

@@ -263,7 +263,7 @@ enum class Precision : std::int32_t {
 /// GPU-side choices with no counterpart in the reference constructor.  The
 /// defaults are the reference's own terms: Morris viscosity with the given
 /// mu, Ferrari diffusion, CFL 0.4, C_force 0.25, C_visc 0.125
-/// (fluid_equations.hpp:518-520).
+/// (fluid_equations.hpp:518-520), shifting after every step.
 struct GpuOptions {
   Precision precision = Precision::fp64;
   std::int32_t viscosity = TG_VISC_MORRIS;
@@ -277,6 +277,10 @@ struct GpuOptions {
   std::int32_t device = -1; ///< CUDA ordinal; -1 = the current device
   bool graph = true;        ///< replay each step as a CUDA graph
   bool autotune = false;    ///< pick launch shapes with tg_autotune
+  /// Particle shifting and the free-surface density correction after each
+  /// step; FluidEquations::post_integrate always runs them
+  /// (fluid_equations.hpp:315-321).
+  bool shifting = true;
 };
 
 template<class PA>
@@ -334,6 +338,7 @@ public:
     P.precision = static_cast<std::int32_t>(options_.precision);
     P.kernel = Kernel::gpu_id;
     P.integrator = particles.integrator_id();
+    P.post_integrate = options_.shifting ? TG_POST_SHIFTING : TG_POST_PREPARE;
     P.viscosity = options_.viscosity;
     P.diffusion = options_.diffusion;
     P.kahan = options_.kahan ? 1 : 0;

@@ -1,8 +1,9 @@
 """The titwcsph-style C++ driver (titsolver_gb300/host/titwcsph_gpu.cpp) on
-the GPU through the C++ mirror: its initial state, run through the oracle,
-must give its final state (plain FP64: r 1e-9, v and rho 1e-7 relative L2
-after 20 steps; FP32-compensated: rho 1e-5, r 1e-6), and its .ttdb frames
-must hold that final state."""
+the GPU through the C++ mirror: its initial state, run through the oracle
+(the reference term set, with or without the post-step shifting as the
+driver ran), must give its final state (plain FP64: r 1e-9, v and rho 1e-7
+relative L2 after 20 steps; FP32-compensated: rho 1e-5, r 1e-6), and its
+.ttdb frames must hold that final state."""
 
 from __future__ import annotations
 
@@ -41,20 +42,32 @@ def read_dump(path):
     return tank, init, final, float(t), int(steps)
 
 
-@pytest.mark.parametrize("fp32c", (False, True))
-def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c):
+INTEGRATORS = {"ssprk3": _abi.TG_SSPRK3, "ssprk2": _abi.TG_SSPRK2,
+               "euler": _abi.TG_EULER, "verlet": _abi.TG_VERLET}
+
+
+@pytest.mark.parametrize("fp32c,integrator,shifting", [
+    (False, "ssprk3", True), (True, "ssprk3", True), (False, "ssprk3", False),
+    (False, "ssprk2", True), (False, "euler", True), (False, "verlet", False)])
+def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting):
     exe = gpu_build.build_host()["titwcsph_gpu"]
     dump, ttdb = tmp_path / "state.bin", tmp_path / "particles.ttdb"
-    cmd = [str(exe), "--nx", "20", "--steps", "20", "--dump", str(dump), "--ttdb", str(ttdb)]
+    cmd = [str(exe), "--nx", "20", "--steps", "20", "--dump", str(dump), "--ttdb", str(ttdb),
+           "--integrator", integrator]
     if fp32c:
         cmd.append("--fp32c")
+    if not shifting:
+        cmd.append("--no-shifting")
     res = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr
     tank, (r0, v0, rho0), (r1, v1, rho1), t, steps = read_dump(dump)
     assert steps == 20
     scn = dict(dim=2, tanks=[tank], r=r0.copy(), v=v0.copy(), rho=rho0.copy())
     # The driver's physics: the reference term set, C4 Wendland, mu = 0.001.
-    o = oracle_run(scn, physics.reference_params(2), steps)
+    P = physics.reference_params(2)
+    P.integrator = INTEGRATORS[integrator]
+    P.post_integrate = _abi.TG_POST_SHIFTING if shifting else _abi.TG_POST_PREPARE
+    o = oracle_run(scn, P, steps)
     f = np.arange(r0.shape[0]) < tank["n_fluid"]
     np.testing.assert_allclose(t, o.time[0], rtol=1e-12 if not fp32c else 1e-6)
     if fp32c:

@@ -231,3 +231,99 @@ def test_fp32_compensated_presets_vs_fp64_oracle(gpu_lib, term_set):
             g = gpu_state(ctx)
         assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5, (term_set, kahan)
         assert rel_l2(g["r"][f], o.r[f]) <= 1e-6, (term_set, kahan)
+
+
+@pytest.mark.parametrize("integrator", (_abi.TG_EULER, _abi.TG_VERLET))
+@pytest.mark.parametrize("term_set", ("baseline", "reference"))
+def test_euler_and_verlet_fp64(gpu_lib, integrator, term_set):
+    # SymplecticEulerIntegrator and VelocityVerletIntegrator
+    # (time_integrator.hpp:31-129): split passes, one sum each.
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    P = getattr(physics, f"{term_set}_params")(2)
+    P.integrator = integrator
+    _compare(scn, P, 1, 1e-12, 1e-9)
+    _compare(scn, P, 5, 1e-11)
+
+
+@pytest.mark.parametrize("integrator", (_abi.TG_EULER, _abi.TG_VERLET))
+def test_euler_and_verlet_3d_and_batched(gpu_lib, integrator):
+    P = physics.baseline_params(3)
+    P.integrator = integrator
+    _compare(scenarios.dam_break_3d(nx_per_H=8), P, 2, 1e-12)
+    P = physics.baseline_params(2)
+    P.integrator = integrator
+    _compare(scenarios.batched_tanks(n_tanks=6, n_range=(6, 12), seed=5), P, 2, 1e-12)
+
+
+@pytest.mark.parametrize("integrator", (_abi.TG_EULER, _abi.TG_VERLET))
+def test_euler_and_verlet_fp32c_vs_fp64_oracle(gpu_lib, integrator):
+    scn = scenarios.dam_break_2d(nx_per_H=40)
+    P64 = physics.baseline_params(2)
+    P64.integrator = integrator
+    o = oracle_run(scn, P64, 30)
+    f = fluid_mask(scn)
+    for lanes in (1, 2):
+        P32 = physics.baseline_params(2, precision=_abi.TG_FP32C)
+        P32.integrator = integrator
+        with gpu_context(scn, P32) as ctx:
+            ctx.set_tuning(2, 128, lanes)
+            ctx.step(30)
+            g = gpu_state(ctx)
+        assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5, lanes
+        assert rel_l2(g["r"][f], o.r[f]) <= 1e-6, lanes
+
+
+@pytest.mark.parametrize("integrator", (_abi.TG_EULER, _abi.TG_VERLET))
+def test_split_pass_launch_counts(gpu_lib, integrator):
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    P = physics.baseline_params(2)
+    P.integrator = integrator
+    with gpu_context(scn, P) as ctx:
+        ctx.profile_enable(True)
+        ctx.step(2)
+        prof = ctx.profile_read()
+    passes = 2 if integrator == _abi.TG_EULER else 3
+    assert prof["forces_launches"] == 2 * passes
+
+
+@pytest.mark.parametrize("term_set", ("baseline", "reference"))
+def test_post_integrate_shifting_fp64(gpu_lib, term_set):
+    # FluidEquations::post_integrate with apply_shifts and the free-surface
+    # density correction (fluid_equations.hpp:315-512).
+    scn = scenarios.dam_break_2d(nx_per_H=20)
+    P = getattr(physics, f"{term_set}_params")(2)
+    P.post_integrate = _abi.TG_POST_SHIFTING
+    g, o = _compare(scn, P, 1, 1e-12)
+    g, o = _compare(scn, P, 5, 1e-11)
+    # Shifting and the correction change the state: the plain run differs.
+    P0 = getattr(physics, f"{term_set}_params")(2)
+    o0 = oracle_run(scn, P0, 5)
+    f = fluid_mask(scn)
+    assert rel_l2(o0.rho[f], o.rho[f]) > 1e-9
+    assert rel_l2(o0.r[f], o.r[f]) > 1e-12
+
+
+def test_post_integrate_shifting_3d_batched_and_integrators(gpu_lib):
+    P = physics.baseline_params(3)
+    P.post_integrate = _abi.TG_POST_SHIFTING
+    _compare(scenarios.dam_break_3d(nx_per_H=8), P, 2, 1e-11)
+    for integ in (_abi.TG_SSPRK2, _abi.TG_EULER, _abi.TG_VERLET):
+        P = physics.baseline_params(2)
+        P.post_integrate = _abi.TG_POST_SHIFTING
+        P.integrator = integ
+        _compare(scenarios.batched_tanks(n_tanks=5, n_range=(8, 14), seed=9), P, 2, 1e-11)
+
+
+def test_post_integrate_shifting_fp32c_vs_fp64_oracle(gpu_lib):
+    scn = scenarios.dam_break_2d(nx_per_H=40)
+    P64 = physics.baseline_params(2)
+    P64.post_integrate = _abi.TG_POST_SHIFTING
+    o = oracle_run(scn, P64, 30)
+    P32 = physics.baseline_params(2, precision=_abi.TG_FP32C)
+    P32.post_integrate = _abi.TG_POST_SHIFTING
+    f = fluid_mask(scn)
+    with gpu_context(scn, P32) as ctx:
+        ctx.step(30)
+        g = gpu_state(ctx)
+    assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5
+    assert rel_l2(g["r"][f], o.r[f]) <= 1e-6

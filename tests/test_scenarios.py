@@ -3,6 +3,7 @@
 from __future__ import annotations
 
 import numpy as np
+import pytest
 
 from titsolver_gb300 import scenarios
 
@@ -62,3 +63,18 @@ def test_batched_tanks_sizes():
     nf = np.array([t["n_fluid"] for t in s["tanks"]])
     assert nf.min() >= 200 and nf.max() <= 29_000
     assert s["r"].shape[0] == sum(t["n_fluid"] + t["n_wall"] for t in s["tanks"])
+
+
+def test_batched_tanks_3d_layout():
+    scn = scenarios.batched_tanks_3d(n_tanks=5, n_range=(6, 9), seed=3)
+    assert scn["dim"] == 3 and len(scn["tanks"]) == 5
+    n = sum(t["n_fluid"] + t["n_wall"] for t in scn["tanks"])
+    assert scn["r"].shape == (n, 3) and scn["rho"].shape == (n,)
+    base = 0
+    for t in scn["tanks"]:
+        assert t["h"] == pytest.approx(1.3 * scn["dx"])
+        assert t["m"] == pytest.approx(1000.0 * scn["dx"] ** 3)
+        fl = scn["r"][base:base + t["n_fluid"]]
+        # Fluid on the dx lattice from dx, walls after it.
+        assert np.all(fl.min(axis=0) == pytest.approx(scn["dx"]))
+        base += t["n_fluid"] + t["n_wall"]

@@ -39,6 +39,7 @@ void Context::release_all() {
   d_id_base = d_wall_from = d_tank_of = nullptr;
   d_dt = d_dt_last = d_time = nullptr;
   d_err = d_wall_count = nullptr;
+  d_fbox = nullptr;
   keys_a = keys_b = vals_a = vals_b = nullptr;
   sort_scratch = nullptr;
   cell_start = wall_list = nullptr;
@@ -140,8 +141,8 @@ bool valid_params(const tg_params* P, std::string* why) {
     *why = "unknown kernel";
     return false;
   }
-  if (P->integrator != TG_SSPRK3 && P->integrator != TG_SSPRK2) {
-    *why = "this build runs the SSPRK integrators (TG_SSPRK3, TG_SSPRK2)";
+  if (P->integrator < TG_SSPRK3 || P->integrator > TG_VERLET) {
+    *why = "unknown integrator";
     return false;
   }
   if (P->viscosity != TG_VISC_MORRIS && P->viscosity != TG_VISC_MONAGHAN) {
@@ -152,8 +153,9 @@ bool valid_params(const tg_params* P, std::string* why) {
     *why = "unknown diffusion model";
     return false;
   }
-  if (P->post_integrate != TG_POST_PREPARE) {
-    *why = "this build runs post_integrate = TG_POST_PREPARE";
+  if (P->post_integrate != TG_POST_PREPARE &&
+      P->post_integrate != TG_POST_SHIFTING) {
+    *why = "unknown post_integrate mode";
     return false;
   }
   if (P->cells_per_radius < 1 || P->cells_per_radius > 3) {
@@ -194,7 +196,7 @@ void tg_params_default(tg_params* p) {
   p->integrator = TG_SSPRK3;
   p->viscosity = TG_VISC_MORRIS;
   p->diffusion = TG_DIFF_FERRARI;
-  p->post_integrate = TG_POST_PREPARE;
+  p->post_integrate = TG_POST_SHIFTING;
   p->cells_per_radius = 2;
   p->kahan = 1;
   p->device = -1;
@@ -270,6 +272,11 @@ int tg_context_create(const tg_params* params, tg_context** out) {
   C.phys.c_force_f = static_cast<float>(params->c_force);
   C.phys.c_visc_f = static_cast<float>(params->c_visc);
   C.k = params->cells_per_radius;
+  {
+    const double cos_fov = std::cos(3.14159265358979323846 / 4.0);
+    C.post_cos2_fov = cos_fov * cos_fov;
+    C.post_k_fs = -std::log(0.05) / (0.01 * 0.01);
+  }
   const bool f64 = params->precision == TG_FP64;
   if (params->dim == 2) {
     C.engine = f64 ? tg::make_engine_2d_f64(params->kernel)
@@ -421,6 +428,10 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     D.diff_k_f = static_cast<float>(D.diff_k);
     D.visc_eps2_f = static_cast<float>(D.visc_eps2);
     D.c02_f = static_cast<float>(D.cs0 * D.cs0);
+    {
+      const double rc = R * (1.0 + 1.0 / 4096.0);
+      D.cull_r2_f = static_cast<float>(rc * rc);
+    }
     id_base[t] = static_cast<uint32_t>(base);
     wall_from[t] = static_cast<uint32_t>(base + T.n_fluid);
     base += nt;
@@ -454,6 +465,7 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, A(C.d_time, sizeof(double) * n_tanks));
   TG_CUDA(&C, A(C.d_err, sizeof(uint32_t)));
   TG_CUDA(&C, A(C.d_wall_count, sizeof(uint32_t)));
+  TG_CUDA(&C, A(C.d_fbox, sizeof(unsigned) * 6 * n_tanks));
   TG_CUDA(&C, A(C.keys_a, sizeof(uint32_t) * nn));
   TG_CUDA(&C, A(C.keys_b, sizeof(uint32_t) * nn));
   TG_CUDA(&C, A(C.vals_a, sizeof(uint32_t) * nn));
@@ -585,12 +597,15 @@ int tg_step(tg_context* ctx, int32_t n_steps, double* dt_out) {
     } else {
       for (int32_t i = 0; i < n_steps; ++i) {
         TG_CUDA(&C, C.engine->enqueue_step(C));
-        C.prof.stages += C.P.integrator == TG_SSPRK2 ? 2 : 3;
-        C.prof.forces_launches += C.P.integrator == TG_SSPRK2 ? 2 : 3;
+        C.prof.stages += tg::force_passes(C.P.integrator);
+        C.prof.forces_launches += tg::force_passes(C.P.integrator);
       }
     }
     C.prof.steps += n_steps;
-    C.walls_fresh = false;
+    // With shifting, the post-integration prepare left the walls as the
+    // reference leaves them (extrapolated before the shift); otherwise the
+    // reference's closing prepare runs on the next density download.
+    C.walls_fresh = C.P.post_integrate == TG_POST_SHIFTING;
   }
   TG_CUDA(&C, cudaStreamSynchronize(C.stream));
   C.drain_profile();

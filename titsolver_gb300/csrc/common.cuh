@@ -53,7 +53,8 @@ struct TankDev {
   uint32_t pad;
   // FP32 copies for the compensated form (no FP64 conversions in kernels).
   float h_f, hinv_f, w_f, wg_f, m_f, rho0_f, cs0_f, B_f, diff_k_f;
-  float visc_eps2_f, c02_f, pad_f;
+  float visc_eps2_f, c02_f;
+  float cull_r2_f;  // (R (1 + 2^-12))^2: cell clipping radius, squared
 };
 
 struct PhysDev {

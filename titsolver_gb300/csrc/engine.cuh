@@ -15,6 +15,15 @@ namespace tg {
 
 struct Context;
 
+// Force passes per step of an integrator.
+inline int force_passes(int integrator) {
+  switch (integrator) {
+    case TG_SSPRK2: return 2;
+    case TG_EULER: return 2;
+    default: return 3;  // SSPRK3, velocity Verlet
+  }
+}
+
 // Kernel groups timed by the profiler.
 enum Group { kGroupSort = 0, kGroupReorder, kGroupWalls, kGroupForces,
              kGroupPost, kGroupCount };
@@ -84,6 +93,8 @@ struct Context {
   // Launch shape of the force pass (tg_set_tuning / tg_autotune).
   int force_block = 128;
   int force_team = 1;
+  double post_cos2_fov = 0.0;  // cos(pi/4)^2 of the visibility cone
+  double post_k_fs = 0.0;      // -log(0.05) / 0.01^2
   double tuned_ms = 0.0;  // device time per step of the tuned shape
   int tuned_candidates = 0;
 
@@ -98,6 +109,9 @@ struct Context {
   double* d_time = nullptr;
   uint32_t* d_err = nullptr;
   uint32_t* d_wall_count = nullptr;
+  // Per tank: order-preserving encodings of the fluid bounding box of the
+  // current stage (FP32, rounded outwards), mins [ntanks x 3] then maxes.
+  unsigned* d_fbox = nullptr;
   uint32_t* keys_a = nullptr;
   uint32_t* keys_b = nullptr;
   uint32_t* vals_a = nullptr;

@@ -6,6 +6,7 @@
 
 #include "engine.cuh"
 #include "fluid.cuh"
+#include "post.cuh"
 #include "sort.cuh"
 
 namespace tg {
@@ -75,6 +76,17 @@ class Engine final : public EngineBase {
     }
     A(posrec_, n);
     A(datrec_, n);
+    post_ = PostArgs<D, F>{};
+    if (C.P.post_integrate == TG_POST_SHIFTING) {
+      A(post_.N, n * D);
+      A(post_.dr, n * D);
+      A(post_.gv, n * D * D);
+      A(post_.grho, n * D);
+      A(post_.count, n);
+      A(post_.phi, n);
+      A(post_.phi2, n);
+      A(post_.rho_raw, n);
+    }
     return e;
   }
 
@@ -101,11 +113,55 @@ class Engine final : public EngineBase {
     if (C.n == 0) return cudaSuccess;
     static const double w3[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
     static const double w2[2] = {1.0, 1.0 / 2.0};
-    const bool rk2 = C.P.integrator == TG_SSPRK2;
-    const int stages = rk2 ? 2 : 3;
-    const double* w = rk2 ? w2 : w3;
-    for (int s = 0; s < stages; ++s) {
-      cudaError_t e = enqueue_stage(C, s, w[s]);
+    const int integ = C.P.integrator;
+    if (integ == TG_SSPRK2 || integ == TG_SSPRK3) {
+      // SSPRKIntegrator::step (time_integrator.hpp:161-185): every stage a
+      // prepare (search + walls) and both sums, then the lincomb.
+      const bool rk2 = integ == TG_SSPRK2;
+      const double* w = rk2 ? w2 : w3;
+      for (int s = 0; s < (rk2 ? 2 : 3); ++s) {
+        Pass p;
+        p.stage = s;
+        p.w = w[s];
+        cudaError_t e = enqueue_stage(C, p);
+        if (e != cudaSuccess) return e;
+      }
+    } else if (integ == TG_EULER) {
+      // SymplecticEulerIntegrator::step (:50-69): prepare, dt, continuity
+      // and rho update, then momentum on the new rho (walls as prepared)
+      // with v += dt dv, r += dt v.
+      Pass a;
+      a.mode = kPassContinuity;
+      a.carry = 1;
+      Pass b = a;
+      b.stage = 1;
+      b.mode = kPassKickDrift;
+      b.walls_keep = 1;
+      b.lincomb = 0;
+      cudaError_t e = enqueue_stage(C, a);
+      if (e == cudaSuccess) e = enqueue_stage(C, b);
+      if (e != cudaSuccess) return e;
+    } else {
+      // VelocityVerletIntegrator::step (:99-123): prepare, dt, momentum with
+      // v += dt/2 dv, r += dt v; prepare, continuity and rho update;
+      // momentum on the new rho with v += dt/2 dv.
+      Pass a;
+      a.mode = kPassHalfKickDrift;
+      a.carry = 1;
+      Pass b = a;
+      b.stage = 1;
+      b.mode = kPassContinuity;
+      b.lincomb = 0;
+      Pass c = b;
+      c.mode = kPassHalfKick;
+      c.walls_keep = 1;
+      cudaError_t e = enqueue_stage(C, a);
+      if (e == cudaSuccess) e = enqueue_stage(C, b);
+      if (e == cudaSuccess) e = enqueue_stage(C, c);
+      if (e != cudaSuccess) return e;
+    }
+    if (C.P.post_integrate == TG_POST_SHIFTING) {
+      cudaError_t e = enqueue_post(C);
       if (e != cudaSuccess) return e;
     }
     const int tok = C.group_begin(kGroupForces);
@@ -205,9 +261,12 @@ class Engine final : public EngineBase {
 
   int64_t launches_per_step(Context& C) override {
     const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
-    const int stages = C.P.integrator == TG_SSPRK2 ? 2 : 3;
+    const int stages = force_passes(C.P.integrator);
     const int per_stage = 3 * passes + 2 + 2 + (C.n_wall > 0 ? 1 : 0);
-    return static_cast<int64_t>(stages) * per_stage + 1;
+    const int post = C.P.post_integrate == TG_POST_SHIFTING
+                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 : 0) + 5
+                         : 0;
+    return static_cast<int64_t>(stages) * per_stage + post + 1;
   }
 
  private:
@@ -229,6 +288,9 @@ class Engine final : public EngineBase {
     a.dt = C.d_dt;
     a.wall_list = C.wall_list;
     a.wall_count = C.d_wall_count;
+    // The wall pass's fluid-box early-out pays when walls are a sizeable
+    // share of the particles (it costs a fold in every reorder).
+    a.fbox = C.n_wall > 0 && 4 * C.n_wall >= C.n_fluid ? C.d_fbox : nullptr;
     a.err = C.d_err;
     a.n = C.n;
     a.k = C.k;
@@ -238,12 +300,23 @@ class Engine final : public EngineBase {
     a.w_new = 1.0;
     a.kahan = C.P.kahan;
     a.carry = 0;
+    a.mode = kPassRK;
+    a.walls_keep = 0;
     return a;
   }
 
   cudaError_t reorder(Context& C, const StageArgs<D, F>& a) {
     cudaError_t e = cudaMemsetAsync(C.d_wall_count, 0, sizeof(uint32_t), C.stream);
     if (e != cudaSuccess) return e;
+    if (a.fbox != nullptr) {
+      // Empty fluid boxes: mins at the top encoding, maxes at the bottom.
+      const size_t half = sizeof(unsigned) * 3 * C.ntanks;
+      e = cudaMemsetAsync(C.d_fbox, 0xff, half, C.stream);
+      if (e == cudaSuccess) {
+        e = cudaMemsetAsync(C.d_fbox + 3 * C.ntanks, 0, half, C.stream);
+      }
+      if (e != cudaSuccess) return e;
+    }
     k_reorder<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
     C.launches += 1;
     return cudaGetLastError();
@@ -267,11 +340,63 @@ class Engine final : public EngineBase {
     return e;
   }
 
-  cudaError_t enqueue_stage(Context& C, int s, double w) {
+  // FluidEquations::post_integrate with shifting (fluid_equations.hpp:
+  // 315-512): a prepare (sort, reorder carrying every field, wall
+  // extrapolation), then the five post kernels, which leave the shifted and
+  // corrected state and its keys in the home buffers.
+  cudaError_t enqueue_post(Context& C) {
     cudaError_t e = enqueue_sort(C);
     if (e != cudaSuccess) return e;
-    StageArgs<D, F> a = args(C, s);
-    a.w_new = w;
+    StageArgs<D, F> a = args(C, 0);
+    a.compute_dt = 0;
+    a.copy_start = 0;
+    a.carry = 1;
+    int tok = C.group_begin(kGroupPost);
+    e = reorder(C, a);
+    if (e != cudaSuccess) return e;
+    if (C.n_wall > 0) {
+      k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
+          a, C.n_wall);
+      C.launches += 1;
+    }
+    PostArgs<D, F> p = post_;
+    p.S = a;
+    p.cos2_fov = C.post_cos2_fov;
+    p.k_fs = C.post_k_fs;
+    p.shift = -C.P.cfl * 0.2;
+    const unsigned grid = grid_for(C.n, 128);
+    k_post_sums<D, F, K><<<grid, 128, 0, C.stream>>>(p);
+    k_post_phi<D, F><<<grid, 128, 0, C.stream>>>(p);
+    k_post_near<D, F, K><<<grid, 128, 0, C.stream>>>(p);
+    k_post_shift<D, F><<<grid, 128, 0, C.stream>>>(p);
+    k_post_fs<D, F, K><<<grid, 128, 0, C.stream>>>(p);
+    C.launches += 5;
+    C.group_end(tok);
+    C.keys_valid = true;
+    return cudaGetLastError();
+  }
+
+  // One force pass of a step: its index (stage 0 copies the start state
+  // and reduces dt), lincomb weight, update rule, whether Y carries every
+  // field, and whether the walls keep their carried densities.
+  struct Pass {
+    int stage = 0;
+    double w = 1.0;
+    int mode = kPassRK;
+    int carry = 0;
+    int walls_keep = 0;
+    int lincomb = -1;  // -1: the SSPRK rule (stages after the first)
+  };
+
+  cudaError_t enqueue_stage(Context& C, const Pass& p) {
+    cudaError_t e = enqueue_sort(C);
+    if (e != cudaSuccess) return e;
+    StageArgs<D, F> a = args(C, p.stage);
+    a.w_new = p.w;
+    a.mode = p.mode;
+    a.carry = p.carry;
+    a.walls_keep = p.walls_keep;
+    if (p.lincomb >= 0) a.lincomb = p.lincomb;
     int tok = C.group_begin(kGroupReorder);
     e = reorder(C, a);
     C.group_end(tok);
@@ -332,6 +457,7 @@ class Engine final : public EngineBase {
 
   StateBuf<R> X_{}, Y_{};
   StartBuf<R> U_[2]{};
+  PostArgs<D, F> post_{};
   PosRec* posrec_ = nullptr;
   DatRec* datrec_ = nullptr;
 };

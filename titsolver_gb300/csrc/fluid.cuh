@@ -31,6 +31,7 @@ struct alignas(16) Pos64_2 { double x, y; };
 struct alignas(32) Pos64_3 { double x, y, z, w; };
 struct alignas(32) Dat64 { double vx, vy, vz, rho, P, c, invrho, pad; };
 struct alignas(8) Pos32_2 { float x, y; };
+
 struct alignas(16) Pos32_3 { float x, y, z, w; };
 struct alignas(32) Dat32 { float vx, vy, vz, drho, P, c, invrho, pad; };
 
@@ -144,21 +145,200 @@ struct StageArgs {
   int lincomb;       // apply (1 - w) Udst + w new
   double w_new;
   int kahan;
-  int carry;         // prepare pass: gather every field into Y
+  int carry;         // gather every field into Y (prepare and split passes)
+  int mode;          // update rule of the force pass (kPass*)
+  int walls_keep;    // k_walls: keep the carried wall densities
+  unsigned* fbox;     // per-tank fluid bounding box (k_reorder)
+};
+
+// Order-preserving map of floats to unsigned 32-bit integers (and back),
+// for atomic min/max of coordinates of either sign.
+__device__ __forceinline__ unsigned order_enc(float x) {
+  const unsigned b = __float_as_uint(x);
+  return (b >> 31) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float order_dec(unsigned e) {
+  return __uint_as_float((e >> 31) ? (e & 0x7fffffffu) : ~e);
+}
+
+// Fold a lane's fluid position into its tank's bounding box, rounded
+// outwards to FP32 (so the box only grows).  Each warp reduces its lanes
+// (one instruction per bound) when they share a tank; the block then merges
+// its warps and issues at most one atomic per bound and tank run, and only
+// when it would move the box (cell order makes the slowest axis grow block
+// after block, so per-warp atomics would queue on one address).  Warps that
+// straddle tanks fold lane by lane.  Called by every thread of the block.
+template<int D>
+__device__ __forceinline__ void fold_fluid_box(unsigned* box, int ntanks,
+                                               uint32_t tk, bool fluid,
+                                               const double* p) {
+  constexpr uint32_t kEmpty = 0xffffffffu, kMixed = 0xfffffffeu;
+  __shared__ unsigned s_lo[32][3], s_hi[32][3];
+  __shared__ uint32_t s_tk[32];
+  unsigned lo[3], hi[3];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    lo[k] = fluid ? order_enc(__double2float_rd(p[k])) : 0xffffffffu;
+    hi[k] = fluid ? order_enc(__double2float_ru(p[k])) : 0u;
+  }
+  const uint32_t key_tk = fluid ? tk : kEmpty;
+  const uint32_t t0 = __reduce_min_sync(0xffffffffu, key_tk);
+  const bool one_tank = __all_sync(0xffffffffu, key_tk == t0 || key_tk == kEmpty);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto push = [&](uint32_t t, const unsigned* l, const unsigned* h) {
+    unsigned* mins = box + 3 * t;
+    unsigned* maxs = box + 3 * (ntanks + t);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      if (l[k] < *reinterpret_cast<volatile unsigned*>(mins + k)) atomicMin(mins + k, l[k]);
+      if (h[k] > *reinterpret_cast<volatile unsigned*>(maxs + k)) atomicMax(maxs + k, h[k]);
+    }
+  };
+  if (one_tank) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      lo[k] = __reduce_min_sync(0xffffffffu, lo[k]);
+      hi[k] = __reduce_max_sync(0xffffffffu, hi[k]);
+    }
+  } else if (fluid) {
+    push(tk, lo, hi);
+  }
+  if (lane == 0) {
+    s_tk[warp] = one_tank ? t0 : kMixed;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      s_lo[warp][k] = lo[k];
+      s_hi[warp][k] = hi[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    uint32_t cur = kEmpty;
+    unsigned clo[3] = {0u, 0u, 0u}, chi[3] = {0u, 0u, 0u};
+    for (int w = 0; w < nw; ++w) {
+      const uint32_t t = s_tk[w];
+      if (t == kEmpty || t == kMixed) continue;
+      if (t != cur) {
+        if (cur != kEmpty) push(cur, clo, chi);
+        cur = t;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          clo[k] = s_lo[w][k];
+          chi[k] = s_hi[w][k];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          clo[k] = min(clo[k], s_lo[w][k]);
+          chi[k] = max(chi[k], s_hi[w][k]);
+        }
+      }
+    }
+    if (cur != kEmpty) push(cur, clo, chi);
+  }
+}
+
+// True when no fluid particle of the tank can lie within the support radius
+// of point p: p is farther than R from the tank's fluid bounding box (or the
+// tank has no fluid this stage).  The margin 2^-20 on R^2 only makes the
+// test stricter.
+template<int D>
+__device__ __forceinline__ bool beyond_fluid(const unsigned* box, int ntanks,
+                                             uint32_t tk, const TankDev& T,
+                                             const double* p) {
+  if (box == nullptr) return false;  // no box this stage: walk every wall
+  double g2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const unsigned elo = box[3 * tk + k];
+    const unsigned ehi = box[3 * (ntanks + tk) + k];
+    if (elo > ehi) return true;  // empty box
+    const double lo = order_dec(elo), hi = order_dec(ehi);
+    const double g = fmax(fmax(lo - p[k], p[k] - hi), 0.0);
+    g2 += g * g;
+  }
+  return g2 > T.radius2 * (1.0 + 1.0 / 1048576.0);
+}
+
+// Update rules of a force pass.  The SSPRK stage uses both sums; the split
+// passes of the symplectic Euler and velocity Verlet integrators
+// (time_integrator.hpp:50-69, 99-123) use one sum each and carry the other
+// field through unchanged.
+enum {
+  kPassRK = 0,         // r += dt v, v += dt dv, rho += dt drho (+ lincomb)
+  kPassContinuity,     // rho += dt drho
+  kPassKickDrift,      // v += dt dv, then r += dt v
+  kPassHalfKickDrift,  // v += dt/2 dv, then r += dt v
+  kPassHalfKick        // v += dt/2 dv
 };
 
 // ---------------------------------------------------------------------------
 // Neighbour-cell traversal over the (2k+1)^D block of cells around c,
 // clipped to the tank grid.  cstart is indexed by key (2 per cell).
 // Merged: one [begin, end) range per row of cells (rows are contiguous in
-// key order), fluid and walls.  Per cell: one range per cell with its cell
+// key order), fluid and walls, with the row offset (0, dy, dz).  Per cell: one range per cell with its cell
 // offset (dx, dy, dz) relative to c; FluidOnly restricts each cell's range
 // to its fluid particles.
+//
+// With the target's offset o from its own cell's corner (o == nullptr: no
+// clipping), rows and cells that cannot hold a point within the cull radius
+// (the support radius widened by 2^-12, far above the FP32 rounding of the
+// offsets) are skipped: a row whose y/z gap to the target exceeds it, and
+// cells beyond the row's half-width.  Skipped cells hold no neighbour, so
+// every sum is bit-identical to the unclipped traversal.  Rows and columns
+// on the grid border are never clipped (particles clamped into border
+// cells may lie outside their cell's box).
+
+// Distance from offset o to the cell box [d cs, (d + 1) cs) along one axis.
+__device__ __forceinline__ float cell_gap(int d, float o, float cs) {
+  if (d > 0) return fmaxf(static_cast<float>(d) * cs - o, 0.f);
+  if (d < 0) return fmaxf(o - static_cast<float>(d + 1) * cs, 0.f);
+  return 0.f;
+}
+
+// FP32 offset of an FP64 position from the corner of its cell c.
+template<int D>
+__device__ __forceinline__ void cell_offset(const TankDev& T, const int* c,
+                                            const double* p, float* o) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    o[k] = __double2float_rn(p[k] - fma(static_cast<double>(c[k]), T.cs, T.lo[k]));
+  }
+}
+
+// Clipped x-range of one row: [x0, x1] within [xlo, xhi]; false when the
+// row holds no reachable cell.
+template<int D>
+__device__ __forceinline__ bool clip_row(const TankDev& T, const int* c,
+                                         const float* o, int y, int z,
+                                         int xlo, int xhi, int& x0, int& x1) {
+  x0 = xlo;
+  x1 = xhi;
+  if (o == nullptr) return true;
+  const float cs = T.cs_f;
+  const float gy = (y == 0 || y == T.nc[1] - 1) ? 0.f : cell_gap(y - c[1], o[1], cs);
+  float gz = 0.f;
+  if constexpr (D == 3) {
+    gz = (z == 0 || z == T.nc[2] - 1) ? 0.f : cell_gap(z - c[2], o[2], cs);
+  }
+  const float rem = T.cull_r2_f - gy * gy - gz * gz;
+  if (rem < 0.f) return false;
+  if (xlo == 0 || xhi == T.nc[0] - 1) return true;
+  const float w = sqrtf(rem);
+  // dx > 0 reachable iff dx cs - o0 <= w; dx < 0 iff o0 - (dx + 1) cs <= w.
+  const float hi = floorf(__fdiv_rn(o[0] + w, cs));
+  const float lo = ceilf(__fdiv_rn(o[0] - w, cs)) - 1.f;
+  x1 = min(xhi, c[0] + static_cast<int>(fminf(fmaxf(hi, 0.f), 64.f)));
+  x0 = max(xlo, c[0] + static_cast<int>(fmaxf(fminf(lo, 0.f), -64.f)));
+  return true;
+}
+
 template<int D, bool PerCell, class Fn, bool FluidOnly = false>
 __device__ __forceinline__ void for_cells(const TankDev& T, const int* c,
                                           int k,
                                           const uint32_t* __restrict__ cstart,
-                                          Fn&& fn) {
+                                          Fn&& fn, const float* o = nullptr) {
   const int nx = T.nc[0], ny = T.nc[1];
   const int zlo = D == 3 ? max(c[2] - k, 0) : 0;
   const int zhi = D == 3 ? min(c[2] + k, T.nc[2] - 1) : 0;
@@ -166,20 +346,22 @@ __device__ __forceinline__ void for_cells(const TankDev& T, const int* c,
   const int xlo = max(c[0] - k, 0), xhi = min(c[0] + k, nx - 1);
   for (int z = zlo; z <= zhi; ++z) {
     for (int y = ylo; y <= yhi; ++y) {
+      int x0, x1;
+      if (!clip_row<D>(T, c, o, y, z, xlo, xhi, x0, x1)) continue;
       const uint32_t row =
           T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx;
       if constexpr (!PerCell) {
-        fn(__ldg(cstart + 2 * (row + xlo)), __ldg(cstart + 2 * (row + xhi + 1)),
-           0, 0, 0);
+        fn(__ldg(cstart + 2 * (row + x0)), __ldg(cstart + 2 * (row + x1 + 1)),
+           0, y - c[1], D == 3 ? z - c[2] : 0);
       } else if constexpr (FluidOnly) {
-        for (int x = xlo; x <= xhi; ++x) {
+        for (int x = x0; x <= x1; ++x) {
           const uint32_t kc = 2 * (row + x);
           fn(__ldg(cstart + kc), __ldg(cstart + kc + 1), x - c[0], y - c[1],
              D == 3 ? z - c[2] : 0);
         }
       } else {
-        uint32_t s = __ldg(cstart + 2 * (row + xlo));
-        for (int x = xlo; x <= xhi; ++x) {
+        uint32_t s = __ldg(cstart + 2 * (row + x0));
+        for (int x = x0; x <= x1; ++x) {
           const uint32_t e = __ldg(cstart + 2 * (row + x + 1));
           fn(s, e, x - c[0], y - c[1], D == 3 ? z - c[2] : 0);
           s = e;
@@ -197,7 +379,8 @@ __device__ __forceinline__ void for_cells(const TankDev& T, const int* c,
 template<int D, bool FluidOnly, class Fn>
 __device__ __forceinline__ void for_cells_team(
     const TankDev& T, const int* c, int k,
-    const uint32_t* __restrict__ cstart, int lane, int team, Fn&& fn) {
+    const uint32_t* __restrict__ cstart, int lane, int team, Fn&& fn,
+    const float* o = nullptr) {
   const int nx = T.nc[0], ny = T.nc[1];
   const int zlo = D == 3 ? max(c[2] - k, 0) : 0;
   const int zhi = D == 3 ? min(c[2] + k, T.nc[2] - 1) : 0;
@@ -210,6 +393,20 @@ __device__ __forceinline__ void for_cells_team(
     const int rest = t / wx;
     const int y = ylo + rest % wy;
     const int z = zlo + rest / wy;
+    if (o != nullptr) {
+      // Skip a cell whose box lies beyond the cull radius (border cells
+      // are always visited; see for_cells).
+      const float cs = T.cs_f;
+      const float gx = (x == 0 || x == nx - 1) ? 0.f : cell_gap(x - c[0], o[0], cs);
+      const float gy = (y == 0 || y == ny - 1) ? 0.f : cell_gap(y - c[1], o[1], cs);
+      float g2 = gx * gx + gy * gy;
+      if constexpr (D == 3) {
+        const float gz =
+            (z == 0 || z == T.nc[2] - 1) ? 0.f : cell_gap(z - c[2], o[2], cs);
+        g2 += gz * gz;
+      }
+      if (g2 > T.cull_r2_f) continue;
+    }
     const uint32_t kc =
         2 * (T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx + x);
     fn(__ldg(cstart + kc), __ldg(cstart + kc + (FluidOnly ? 1 : 2)),
@@ -294,6 +491,8 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
   const bool valid = j < A.n;
   double dt_a = __longlong_as_double(0x7ff0000000000000ll);
   uint32_t tk = 0xffffffffu;
+  double box_p[3] = {0.0, 0.0, 0.0};  // fluid position for the bounding box
+  bool box_fluid = false;
   if (valid) {
     const uint32_t src = A.perm[j];
     const uint32_t key = A.skey[j];
@@ -308,6 +507,9 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
     }
     const R rho = A.X.rho[src];
     const uint32_t id = A.X.id[src];
+    box_fluid = !(id & kWallBit);
+#pragma unroll
+    for (int k = 0; k < D; ++k) box_p[k] = p[k];
 #pragma unroll
     for (int k = 0; k < D; ++k) A.Y.pos[k][j] = p[k];
     A.Y.id[j] = id;
@@ -349,7 +551,11 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
       if constexpr (D == 2) {
         A.posrec[j] = Pos32_2{o[0], o[1]};
       } else {
-        A.posrec[j] = Pos32_3{o[0], o[1], o[2], 0.f};
+        // w: the cell's x index (bit pattern), so that a whole row of cells
+        // can be read as one range (k_forces, 3D compensated form).
+        int cc[3] = {0, 0, 0};
+        cell_from_key<D>(T, key, cc);
+        A.posrec[j] = Pos32_3{o[0], o[1], o[2], __int_as_float(cc[0])};
       }
     }
     if (id & kWallBit) {
@@ -407,6 +613,7 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
       }
     }
   }
+  if (A.fbox != nullptr) fold_fluid_box<D>(A.fbox, A.ntanks, tk, box_fluid, box_p);
   if (A.compute_dt) {
     // Warp-level min when the whole warp is in one tank, else per lane.
     const uint32_t t0 = __shfl_sync(0xffffffffu, tk, 0);
@@ -430,6 +637,10 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
 // Wall extrapolation (fluid_equations.hpp:122-164) with a zero wall normal:
 //   rho_e = rho(H),  H = sum_b V_b H(rho_b) W_be / sum_b V_b W_be over fluid
 //   neighbours b (H = 0 when the Shepard sum is tiny); v_e = 0.
+// With walls_keep (a split pass with no prepare before it) the wall keeps
+// its carried density and only its records and home state are written.
+// A wall farther than the support radius from its tank's fluid bounding
+// box skips the neighbour walk: its sums are empty either way.
 // A team of kWallTeam lanes shares one wall: the lanes split the cells of
 // the wall's block (fluid ranges only), then the team reduces by shuffles.
 constexpr int kWallTeam = 8;
@@ -454,7 +665,8 @@ __global__ void __launch_bounds__(128)
     if (valid) load_pos(A.posrec, e, pe);
     const double R2 = T.radius2, hinv = T.hinv, w = T.w, m = T.m;
     double S = 0.0, H = 0.0;
-    if (valid) {
+    if (valid && !A.walls_keep &&
+        !beyond_fluid<D>(A.fbox, A.ntanks, tk, T, pe)) {
       auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
         for (uint32_t j = s; j < en; ++j) {
           double pb[3], d[3];
@@ -469,7 +681,9 @@ __global__ void __launch_bounds__(128)
           H += Vb * Hb * W;
         }
       };
-      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
+      float oc[3] = {0.f, 0.f, 0.f};
+      cell_offset<D>(T, c, pe, oc);
+      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit, oc);
     }
 #pragma unroll
     for (int o = kWallTeam / 2; o > 0; o >>= 1) {
@@ -477,8 +691,12 @@ __global__ void __launch_bounds__(128)
       H += __shfl_xor_sync(0xffffffffu, H, o, kWallTeam);
     }
     if (!valid || lane != 0) return;
-    const double Hs = fabs(S) <= 6.0554544523933395e-06 ? 0.0 : H / S;
-    rho_e = density_from_potential_f64(A.phys, T, Hs);
+    if (A.walls_keep) {
+      rho_e = A.Y.rho[e];
+    } else {
+      const double Hs = fabs(S) <= 6.0554544523933395e-06 ? 0.0 : H / S;
+      rho_e = density_from_potential_f64(A.phys, T, Hs);
+    }
     double pr, cc;
     tait_f64(A.phys, T, rho_e, pr, cc);
     const double inv = 1.0 / rho_e;
@@ -490,7 +708,13 @@ __global__ void __launch_bounds__(128)
     float oe[3] = {0.f, 0.f, 0.f};
     if (valid) load_pos(A.posrec, e, oe);
     Kahan S, H;
+    double pw[3] = {0.0, 0.0, 0.0};
     if (valid) {
+#pragma unroll
+      for (int k = 0; k < D; ++k) pw[k] = A.Y.pos[k][e];
+    }
+    if (valid && !A.walls_keep &&
+        !beyond_fluid<D>(A.fbox, A.ntanks, tk, T, pw)) {
       auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
         float oes[3];
         oes[0] = oe[0] - dx * csz;
@@ -509,7 +733,7 @@ __global__ void __launch_bounds__(128)
           H.add(Vb * Hb * W);
         }
       };
-      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit);
+      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit, oe);
     }
     float Ss = S.value(), Hv = H.value();
 #pragma unroll
@@ -518,8 +742,12 @@ __global__ void __launch_bounds__(128)
       Hv += __shfl_xor_sync(0xffffffffu, Hv, o, kWallTeam);
     }
     if (!valid || lane != 0) return;
-    const float Hs = fabsf(Ss) <= 6.0554544523933395e-06f ? 0.f : Hv / Ss;
-    rho_e = deviation_from_potential_f32(A.phys, T, Hs);
+    if (A.walls_keep) {
+      rho_e = A.Y.rho[e];
+    } else {
+      const float Hs = fabsf(Ss) <= 6.0554544523933395e-06f ? 0.f : Hv / Ss;
+      rho_e = deviation_from_potential_f32(A.phys, T, Hs);
+    }
     float pr, cc;
     tait_f32(A.phys, T, rho_e, pr, cc);
     const float inv = 1.f / (T.rho0_f + rho_e);
@@ -657,20 +885,49 @@ __device__ __forceinline__ void forces_epilogue(
     typename StageArgs<D, F>::R drho_out) {
   using R = typename StageArgs<D, F>::R;
   const double dt = A.dt[tk];
-  R dtr;
+  const int mode = A.mode;
+  const bool half = mode == kPassHalfKickDrift || mode == kPassHalfKick;
+  const double dt_v = half ? 0.5 * dt : dt;  // velocity kick
+  R dtr, dtr_v;
   if constexpr (F == TG_FP64) {
     dtr = dt;
+    dtr_v = dt_v;
   } else {
     dtr = __double2float_rn(dt);
+    dtr_v = __double2float_rn(dt_v);
   }
   double pn[3] = {0.0, 0.0, 0.0};
   R vn[3];
+  R dv_keep[3];
+  R rn = rho_self;
+  R drho_keep = drho_out;
+  if (mode == kPassRK) {
 #pragma unroll
-  for (int k = 0; k < D; ++k) {
-    pn[k] = fma(dt, static_cast<double>(va[k]), A.Y.pos[k][i]);
-    vn[k] = va[k] + dtr * dv_out[k];
+    for (int k = 0; k < D; ++k) {
+      pn[k] = fma(dt, static_cast<double>(va[k]), A.Y.pos[k][i]);
+      vn[k] = va[k] + dtr * dv_out[k];
+      dv_keep[k] = dv_out[k];
+    }
+    rn = rho_self + dtr * drho_out;
+  } else if (mode == kPassContinuity) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      pn[k] = A.Y.pos[k][i];
+      vn[k] = va[k];
+      dv_keep[k] = A.Y.dv[k][i];
+    }
+    rn = rho_self + dtr * drho_out;
+  } else {
+    const bool drift = mode != kPassHalfKick;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      vn[k] = va[k] + dtr_v * dv_out[k];
+      pn[k] = drift ? fma(dt, static_cast<double>(vn[k]), A.Y.pos[k][i])
+                    : A.Y.pos[k][i];
+      dv_keep[k] = dv_out[k];
+    }
+    drho_keep = A.Y.drho[i];
   }
-  R rn = rho_self + dtr * drho_out;
   if (A.lincomb) {
     const double w = A.w_new, w0 = 1.0 - A.w_new;
     R wr, w0r;
@@ -718,11 +975,11 @@ __device__ __forceinline__ void forces_epilogue(
   for (int k = 0; k < D; ++k) {
     A.X.pos[k][i] = pn[k];
     A.X.vel[k][i] = vn[k];
-    A.X.dv[k][i] = dv_out[k];
+    A.X.dv[k][i] = dv_keep[k];
     finite = finite && finite_bits(pn[k]) && isfinite(vn[k]);
   }
   A.X.rho[i] = rn;
-  A.X.drho[i] = drho_out;
+  A.X.drho[i] = drho_keep;
   A.X.id[i] = id;
   if (!(finite && isfinite(rn))) {
     atomicOr(A.err, static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
@@ -805,10 +1062,12 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
         for (int k = 0; k < D; ++k) dv[k] += coef * d[k];
       }
     };
+    float oc[3] = {0.f, 0.f, 0.f};
+    cell_offset<D>(T, c, pa, oc);
     if constexpr (Team == 1) {
-      for_cells<D, false>(T, c, A.k, A.cell_start, visit);
+      for_cells<D, false>(T, c, A.k, A.cell_start, visit, oc);
     } else {
-      for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, visit);
+      for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, visit, oc);
       const unsigned mask = team_mask<Team>();
 #pragma unroll
       for (int o = Team / 2; o > 0; o >>= 1) {
@@ -845,10 +1104,35 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
         acc.add(d, s2, load_dat(A.datrec, j));
       }
     };
-    if constexpr (Team == 1) {
-      for_cells<D, true>(T, c, A.k, A.cell_start, visit);
+    // 3D: one range per row of cells; each candidate's x offset is moved
+    // to the target's cell by its cell's x index (record word w).  Same
+    // candidates in the same order as the per-cell walk.
+    auto visit_row = [&](uint32_t s, uint32_t en, int, int dy, int dz) {
+      if constexpr (D == 3) {
+        const float oay = oa[1] - dy * csz;
+        const float oaz = oa[2] - dz * csz;
+        for (uint32_t j = s; j < en; ++j) {
+          if (j == static_cast<uint32_t>(i)) continue;
+          const Pos32_3 b = A.posrec[j];
+          const int dxc = __float_as_int(b.w) - c[0];
+          float d[3];
+          d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
+          d[1] = oay - b.y;
+          d[2] = oaz - b.z;
+          const float s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          if (s2 > acc.R2) continue;
+          acc.add(d, s2, load_dat(A.datrec, j));
+        }
+      }
+    };
+    if constexpr (Team == 1 && D == 3) {
+      for_cells<D, false>(T, c, A.k, A.cell_start, visit_row, oa);
+    } else if constexpr (Team == 1) {
+      // 2D: per cell (8-byte records; measured faster than row ranges over
+      // 16-byte records).
+      for_cells<D, true>(T, c, A.k, A.cell_start, visit, oa);
     } else {
-      for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, visit);
+      for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, visit, oa);
       const unsigned mask = team_mask<Team>();
 #pragma unroll
       for (int o = Team / 2; o > 0; o >>= 1) {
@@ -1118,6 +1402,11 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
     load_pos(pr, static_cast<uint32_t>(i), pa);
     const double R2 = T.radius2, hinv = T.hinv, wm = T.w * T.m;
     double acc = 0.0;
+    // Cell clipping where the grid carries its FP32 geometry (not in the
+    // allocation-free pass, whose grid leaves it unset).
+    float oc[3] = {0.f, 0.f, 0.f};
+    cell_offset<D>(T, c, pa, oc);
+    const float* clip = T.cull_r2_f > 0.f ? oc : nullptr;
     for_cells<D, false>(T, c, A.k, A.cell_start,
                         [&](uint32_t s, uint32_t en, int, int, int) {
       for (uint32_t j = s; j < en; ++j) {
@@ -1129,7 +1418,7 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
         ++cnt;
         hs += splitmix64(static_cast<uint64_t>((A.id[j] & kIdMask) - base) + 1u);
       }
-    });
+    }, clip);
     rho = acc;
   } else {
     using P = std::conditional_t<D == 2, Pos32_2, Pos32_3>;
@@ -1139,6 +1428,10 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
     const float R2 = T.radius2_f, hinv = T.hinv_f;
     const float wm = T.w_f * T.m_f;
     Kahan acc;
+    double pd[3] = {pa[0], pa[1], pa[2]};
+    float oc[3] = {0.f, 0.f, 0.f};
+    cell_offset<D>(T, c, pd, oc);
+    const float* clip = T.cull_r2_f > 0.f ? oc : nullptr;
     for_cells<D, false>(T, c, A.k, A.cell_start,
                         [&](uint32_t s, uint32_t en, int, int, int) {
       for (uint32_t j = s; j < en; ++j) {
@@ -1150,7 +1443,7 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
         ++cnt;
         hs += splitmix64(static_cast<uint64_t>((A.id[j] & kIdMask) - base) + 1u);
       }
-    });
+    }, clip);
     rho = static_cast<double>(acc.value());
   }
   if (A.rho != nullptr) A.rho[id] = rho;

@@ -165,15 +165,15 @@ __global__ void __launch_bounds__(256)
 template<int D>
 __global__ void __launch_bounds__(256)
     k_na_records(const double* __restrict__ r, const uint32_t* __restrict__ perm,
-                 int64_t n, Pos64_3* __restrict__ rec3, Pos64_2* __restrict__ rec2,
-                 uint32_t* __restrict__ ids) {
+                 int64_t n, void* __restrict__ recs, uint32_t* __restrict__ ids) {
   const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const uint32_t s = perm[j];
   if constexpr (D == 2) {
-    rec2[j] = Pos64_2{r[int64_t(s) * 2], r[int64_t(s) * 2 + 1]};
+    static_cast<Pos64_2*>(recs)[j] = Pos64_2{r[int64_t(s) * 2], r[int64_t(s) * 2 + 1]};
   } else {
-    rec3[j] = Pos64_3{r[int64_t(s) * 3], r[int64_t(s) * 3 + 1], r[int64_t(s) * 3 + 2], 0.0};
+    static_cast<Pos64_3*>(recs)[j] =
+        Pos64_3{r[int64_t(s) * 3], r[int64_t(s) * 3 + 1], r[int64_t(s) * 3 + 2], 0.0};
   }
   ids[j] = s;
 }
@@ -206,8 +206,7 @@ cudaError_t run(unsigned char* base, int64_t n, const double* r, double h,
   const uint32_t* perm = in_b ? vals_b : vals_a;
   e = build_cell_table(sorted, n, 2 * kMaxCells, cells, base + kOffBounds, s, &launches);
   if (e != cudaSuccess) return e;
-  k_na_records<D><<<g, 256, 0, s>>>(r, perm, n, reinterpret_cast<Pos64_3*>(recs),
-                                    reinterpret_cast<Pos64_2*>(recs), ids);
+  k_na_records<D><<<g, 256, 0, s>>>(r, perm, n, recs, ids);
   // One tank whose first cell (and first id) is 0: id_base doubles as the
   // tank cell-offset table.
   CloudArgs<D> a{recs, ids, sorted, cells, T, id_base, 1, n, 1, rho, counts, hashes,

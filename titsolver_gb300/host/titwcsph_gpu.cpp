@@ -4,11 +4,15 @@
 // the tessellated boundary faces (the GPU path runs particle walls).
 //
 // Usage: titwcsph_gpu [--nx N] [--steps S] [--end-time T] [--fp32c]
-//                     [--ttdb FILE] [--dump FILE]
+//                     [--integrator ssprk3|ssprk2|euler|verlet]
+//                     [--no-shifting] [--ttdb FILE] [--dump FILE]
 //   --nx       particles per column height H (default 80, as wcsph.cpp:42)
 //   --steps    stop after S steps (default: run to scaled time T)
 //   --end-time scaled end time t sqrt(g/H) (default 10, as wcsph.cpp:183)
 //   --fp32c    FP32-compensated pair sums instead of plain FP64
+//   --integrator  time integrator (default ssprk3, as wcsph.cpp:92)
+//   --no-shifting skip the post-step shifting and free-surface correction
+//                 (the reference always runs them)
 //   --ttdb     write frames every 100 steps to this .ttdb file
 //   --dump     write the initial and final state as raw binary (see below)
 //
@@ -37,6 +41,8 @@ struct Options {
   long steps = -1;
   double end_time = 10.0;
   bool fp32c = false;
+  std::string integrator = "ssprk3";
+  bool shifting = true;
   std::string ttdb;
   std::string dump;
 };
@@ -53,11 +59,17 @@ auto parse(int argc, char** argv) -> Options {
     else if (a == "--steps") o.steps = std::stol(next());
     else if (a == "--end-time") o.end_time = std::stod(next());
     else if (a == "--fp32c") o.fp32c = true;
+    else if (a == "--integrator") o.integrator = next();
+    else if (a == "--no-shifting") o.shifting = false;
     else if (a == "--ttdb") o.ttdb = next();
     else if (a == "--dump") o.dump = next();
     else throw Exception{"unknown option " + a};
   }
   if (o.nx < 4) throw Exception{"--nx must be at least 4"};
+  if (o.integrator != "ssprk3" && o.integrator != "ssprk2" &&
+      o.integrator != "euler" && o.integrator != "verlet") {
+    throw Exception{"unknown integrator " + o.integrator};
+  }
   return o;
 }
 
@@ -78,25 +90,19 @@ void dump_state(std::ofstream& out, PA& particles) {
   }
 }
 
+template<class Real, class Equations, class Integrator>
+auto simulate(const Options& opt, const Equations& equations,
+              const Integrator& time_integrator) -> int;
+
 template<class Real>
 auto sph_main(int argc, char** argv) -> int {
   const Options opt = parse(argc, argv);
 
-  constexpr Real H = 0.6;   // Water column height.
-  constexpr Real L = 2 * H; // Water column length.
-
-  constexpr Real POOL_WIDTH = 5.366 * H; // Pool width.
-  constexpr Real POOL_HEIGHT = 4.0 * H;  // Pool height.
-
-  const Real dr = H / opt.nx; // Initial particle spacing.
-  const auto WATER_M = int(std::round(L / dr));
-  const auto WATER_N = int(std::round(H / dr));
+  constexpr Real H = 0.6; // Water column height.
 
   constexpr Real g = 9.81;
   constexpr Real rho_0 = 1000.0;
   const Real cs_0 = 20 * std::sqrt(g * H);
-  const Real h_0 = 2.0 * dr;
-  const Real m_0 = rho_0 * pow2(dr);
   constexpr Real mu = 0.001;
 
   // Particle walls: the domain surface stays empty and every point is
@@ -104,6 +110,7 @@ auto sph_main(int argc, char** argv) -> int {
   const geom::Surface<Vec<Real, 2>> domain;
   GpuOptions gpu;
   gpu.precision = opt.fp32c ? Precision::fp32_compensated : Precision::fp64;
+  gpu.shifting = opt.shifting;
   const FluidEquations equations{
       // Constants.
       g,
@@ -119,7 +126,38 @@ auto sph_main(int argc, char** argv) -> int {
   };
 
   // Setup the time integrator.
-  const SSPRKIntegrator time_integrator{equations, SSPRKOrder::three};
+  if (opt.integrator == "ssprk2") {
+    return simulate<Real>(opt, equations,
+                          SSPRKIntegrator{equations, SSPRKOrder::two});
+  }
+  if (opt.integrator == "euler") {
+    return simulate<Real>(opt, equations, SymplecticEulerIntegrator{equations});
+  }
+  if (opt.integrator == "verlet") {
+    return simulate<Real>(opt, equations, VelocityVerletIntegrator{equations});
+  }
+  return simulate<Real>(opt, equations,
+                        SSPRKIntegrator{equations, SSPRKOrder::three});
+}
+
+template<class Real, class Equations, class Integrator>
+auto simulate(const Options& opt, const Equations& equations,
+              const Integrator& time_integrator) -> int {
+  constexpr Real H = 0.6;   // Water column height.
+  constexpr Real L = 2 * H; // Water column length.
+
+  constexpr Real POOL_WIDTH = 5.366 * H; // Pool width.
+  constexpr Real POOL_HEIGHT = 4.0 * H;  // Pool height.
+
+  const Real dr = H / opt.nx; // Initial particle spacing.
+  const auto WATER_M = int(std::round(L / dr));
+  const auto WATER_N = int(std::round(H / dr));
+
+  constexpr Real g = 9.81;
+  constexpr Real rho_0 = 1000.0;
+  const Real cs_0 = 20 * std::sqrt(g * H);
+  const Real h_0 = 2.0 * dr;
+  const Real m_0 = rho_0 * pow2(dr);
 
   // Setup the particles array:
   ParticleArray particles{

@@ -176,5 +176,33 @@ def batched_tanks(n_tanks: int = 512, nx_per_unit: int = 80, n_range=(20, 120),
                 dx=dx, seed=seed, name=f"batched_{n_tanks}_tanks")
 
 
+def batched_tanks_3d(n_tanks: int = 64, nx_per_unit: int = 100, n_range=(12, 40),
+                     aspect_range=(0.5, 2.0), seed: int = 20261204, layers: int = 3,
+                     cs0_factor: float = 10.0, h_factor: float = 1.3, g: float = G,
+                     rho0: float = RHO0) -> dict:
+    """Independent 3D dam breaks: column height N ~ U{n_range} particles,
+    length round(a N) and depth round(b N) with a, b ~ U[aspect_range],
+    spacing dx = 1/nx_per_unit, H = N dx; each tank is dam_break_3d's layout
+    (tank 5.366 H x 3 H x (depth + dx), 3 wall layers, h = 1.3 dx)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dx = 1.0 / nx_per_unit
+    tanks, rs, rhos = [], [], []
+    for _ in range(n_tanks):
+        N = int(rng.integers(n_range[0], n_range[1] + 1))
+        a = float(rng.uniform(*aspect_range))
+        b = float(rng.uniform(*aspect_range))
+        H = N * dx
+        one = dam_break_3d(H=H, nx_per_H=N, column=(max(1, round(a * N)) / N,
+                                                    1.0, max(1, round(b * N)) / N),
+                           layers=layers, cs0_factor=cs0_factor, h_factor=h_factor,
+                           g=g, rho0=rho0)
+        tanks.extend(one["tanks"])
+        rs.append(one["r"])
+        rhos.append(one["rho"])
+    r = np.ascontiguousarray(np.concatenate(rs))
+    return dict(dim=3, tanks=tanks, r=r, v=np.zeros_like(r), rho=np.concatenate(rhos),
+                dx=dx, seed=seed, name=f"batched_3d_{n_tanks}_tanks")
+
+
 def n_fluid(scn: dict) -> int:
     return int(sum(t["n_fluid"] for t in scn["tanks"]))
