@@ -431,6 +431,10 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     {
       const double rc = R * (1.0 + 1.0 / 4096.0);
       D.cull_r2_f = static_cast<float>(rc * rc);
+      double extent = 0.0;
+      for (int k = 0; k < dim; ++k) extent = std::max(extent, D.nc[k] * cs);
+      const double rs = rc + extent / 524288.0;
+      D.wall_skip_r2_f = static_cast<float>(rs * rs);
     }
     id_base[t] = static_cast<uint32_t>(base);
     wall_from[t] = static_cast<uint32_t>(base + T.n_fluid);

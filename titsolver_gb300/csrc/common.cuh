@@ -55,6 +55,9 @@ struct TankDev {
   float h_f, hinv_f, w_f, wg_f, m_f, rho0_f, cs0_f, B_f, diff_k_f;
   float visc_eps2_f, c02_f;
   float cull_r2_f;  // (R (1 + 2^-12))^2: cell clipping radius, squared
+  // (R (1 + 2^-12) + 2^-19 extent)^2: the wall pass's fluid-box test radius
+  // in tank-local FP32 coordinates (extent = the grid's largest side).
+  float wall_skip_r2_f;
 };
 
 struct PhysDev {

@@ -161,25 +161,25 @@ __device__ __forceinline__ float order_dec(unsigned e) {
   return __uint_as_float((e >> 31) ? (e & 0x7fffffffu) : ~e);
 }
 
-// Fold a lane's fluid position into its tank's bounding box, rounded
-// outwards to FP32 (so the box only grows).  Each warp reduces its lanes
-// (one instruction per bound) when they share a tank; the block then merges
-// its warps and issues at most one atomic per bound and tank run, and only
-// when it would move the box (cell order makes the slowest axis grow block
-// after block, so per-warp atomics would queue on one address).  Warps that
-// straddle tanks fold lane by lane.  Called by every thread of the block.
+// Fold a lane's fluid position (tank-local FP32 coordinates, x - lo) into
+// its tank's bounding box.  Each warp reduces its lanes (one instruction
+// per bound) when they share a tank; the block then merges its warps and
+// issues at most one atomic per bound and tank run, and only when it would
+// move the box (cell order makes the slowest axis grow block after block,
+// so per-warp atomics would queue on one address).  Warps that straddle
+// tanks fold lane by lane.  Called by every thread of the block.
 template<int D>
 __device__ __forceinline__ void fold_fluid_box(unsigned* box, int ntanks,
                                                uint32_t tk, bool fluid,
-                                               const double* p) {
+                                               const float* xl) {
   constexpr uint32_t kEmpty = 0xffffffffu, kMixed = 0xfffffffeu;
   __shared__ unsigned s_lo[32][3], s_hi[32][3];
   __shared__ uint32_t s_tk[32];
   unsigned lo[3], hi[3];
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    lo[k] = fluid ? order_enc(__double2float_rd(p[k])) : 0xffffffffu;
-    hi[k] = fluid ? order_enc(__double2float_ru(p[k])) : 0u;
+    lo[k] = fluid ? order_enc(xl[k]) : 0xffffffffu;
+    hi[k] = fluid ? order_enc(xl[k]) : 0u;
   }
   const uint32_t key_tk = fluid ? tk : kEmpty;
   const uint32_t t0 = __reduce_min_sync(0xffffffffu, key_tk);
@@ -240,25 +240,41 @@ __device__ __forceinline__ void fold_fluid_box(unsigned* box, int ntanks,
 }
 
 // True when no fluid particle of the tank can lie within the support radius
-// of point p: p is farther than R from the tank's fluid bounding box (or the
-// tank has no fluid this stage).  The margin 2^-20 on R^2 only makes the
-// test stricter.
+// of a point with tank-local FP32 coordinates xl: its distance to the
+// tank's fluid bounding box exceeds R plus a margin that covers the FP32
+// rounding of both coordinates (wall_skip_r2_f), or the tank has no fluid
+// this stage.
 template<int D>
 __device__ __forceinline__ bool beyond_fluid(const unsigned* box, int ntanks,
                                              uint32_t tk, const TankDev& T,
-                                             const double* p) {
+                                             const float* xl) {
   if (box == nullptr) return false;  // no box this stage: walk every wall
-  double g2 = 0.0;
+  float g2 = 0.f;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     const unsigned elo = box[3 * tk + k];
     const unsigned ehi = box[3 * (ntanks + tk) + k];
     if (elo > ehi) return true;  // empty box
-    const double lo = order_dec(elo), hi = order_dec(ehi);
-    const double g = fmax(fmax(lo - p[k], p[k] - hi), 0.0);
+    const float g = fmaxf(fmaxf(order_dec(elo) - xl[k], xl[k] - order_dec(ehi)), 0.f);
     g2 += g * g;
   }
-  return g2 > T.radius2 * (1.0 + 1.0 / 1048576.0);
+  return g2 > T.wall_skip_r2_f;
+}
+
+// Tank-local FP32 coordinates: from the FP64 position (FP64 form) or from
+// the cell index and the FP32 offset from the cell corner (compensated
+// form, FP32 only).
+template<int D>
+__device__ __forceinline__ void local_coords(const TankDev& T, const double* p,
+                                             float* xl) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) xl[k] = __double2float_rn(p[k] - T.lo[k]);
+}
+template<int D>
+__device__ __forceinline__ void local_coords(const TankDev& T, const int* c,
+                                             const float* o, float* xl) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) xl[k] = fmaf(static_cast<float>(c[k]), T.cs_f, o[k]);
 }
 
 // Update rules of a force pass.  The SSPRK stage uses both sums; the split
@@ -491,7 +507,7 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
   const bool valid = j < A.n;
   double dt_a = __longlong_as_double(0x7ff0000000000000ll);
   uint32_t tk = 0xffffffffu;
-  double box_p[3] = {0.0, 0.0, 0.0};  // fluid position for the bounding box
+  float box_xl[3] = {0.f, 0.f, 0.f};  // fluid position for the bounding box
   bool box_fluid = false;
   if (valid) {
     const uint32_t src = A.perm[j];
@@ -508,8 +524,18 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
     const R rho = A.X.rho[src];
     const uint32_t id = A.X.id[src];
     box_fluid = !(id & kWallBit);
+    if (A.fbox != nullptr && box_fluid) {
+      if constexpr (F == TG_FP64) {
+        local_coords<D>(T, p, box_xl);
+      } else {
+        int cc[3] = {0, 0, 0};
+        float oo[3] = {0.f, 0.f, 0.f};
+        cell_from_key<D>(T, key, cc);
 #pragma unroll
-    for (int k = 0; k < D; ++k) box_p[k] = p[k];
+        for (int k = 0; k < D; ++k) oo[k] = A.X.off[k][src];
+        local_coords<D>(T, cc, oo, box_xl);
+      }
+    }
 #pragma unroll
     for (int k = 0; k < D; ++k) A.Y.pos[k][j] = p[k];
     A.Y.id[j] = id;
@@ -613,7 +639,7 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
       }
     }
   }
-  if (A.fbox != nullptr) fold_fluid_box<D>(A.fbox, A.ntanks, tk, box_fluid, box_p);
+  if (A.fbox != nullptr) fold_fluid_box<D>(A.fbox, A.ntanks, tk, box_fluid, box_xl);
   if (A.compute_dt) {
     // Warp-level min when the whole warp is in one tank, else per lane.
     const uint32_t t0 = __shfl_sync(0xffffffffu, tk, 0);
@@ -665,8 +691,15 @@ __global__ void __launch_bounds__(128)
     if (valid) load_pos(A.posrec, e, pe);
     const double R2 = T.radius2, hinv = T.hinv, w = T.w, m = T.m;
     double S = 0.0, H = 0.0;
-    if (valid && !A.walls_keep &&
-        !beyond_fluid<D>(A.fbox, A.ntanks, tk, T, pe)) {
+    // The box test once per team (FP64 conversions are scarce), shared.
+    bool skip = false;
+    if (valid && lane == 0) {
+      float xl[3] = {0.f, 0.f, 0.f};
+      local_coords<D>(T, pe, xl);
+      skip = beyond_fluid<D>(A.fbox, A.ntanks, tk, T, xl);
+    }
+    skip = __shfl_sync(0xffffffffu, skip, 0, kWallTeam);
+    if (valid && !A.walls_keep && !skip) {
       auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
         for (uint32_t j = s; j < en; ++j) {
           double pb[3], d[3];
@@ -708,13 +741,14 @@ __global__ void __launch_bounds__(128)
     float oe[3] = {0.f, 0.f, 0.f};
     if (valid) load_pos(A.posrec, e, oe);
     Kahan S, H;
-    double pw[3] = {0.0, 0.0, 0.0};
-    if (valid) {
-#pragma unroll
-      for (int k = 0; k < D; ++k) pw[k] = A.Y.pos[k][e];
+    bool skip = false;
+    if (valid && lane == 0) {
+      float xl[3] = {0.f, 0.f, 0.f};
+      local_coords<D>(T, c, oe, xl);
+      skip = beyond_fluid<D>(A.fbox, A.ntanks, tk, T, xl);
     }
-    if (valid && !A.walls_keep &&
-        !beyond_fluid<D>(A.fbox, A.ntanks, tk, T, pw)) {
+    skip = __shfl_sync(0xffffffffu, skip, 0, kWallTeam);
+    if (valid && !A.walls_keep && !skip) {
       auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
         float oes[3];
         oes[0] = oe[0] - dx * csz;
@@ -789,7 +823,7 @@ __global__ void __launch_bounds__(128)
 // is the limit).
 template<int D, int F>
 constexpr int forces_min_blocks() {
-  return F == TG_FP32C ? (D == 2 ? 8 : 6) : 4;
+  return F == TG_FP32C ? 8 : 4;
 }
 
 // Physics presets the compensated force kernel is specialised for (the
