@@ -430,6 +430,33 @@ __device__ __forceinline__ void for_cells_team(
   }
 }
 
+// Rows of the (2k+1)^D cell block around c (3D), dealt out to the lanes of
+// a team: lane l visits rows l, l + team, ...; each visit gets the row's
+// whole record range (fluid and walls, clipped as in for_cells) and its
+// offset (0, dy, dz).
+template<int D, class Fn>
+__device__ __forceinline__ void for_rows_team(
+    const TankDev& T, const int* c, int k,
+    const uint32_t* __restrict__ cstart, int lane, int team, Fn&& fn,
+    const float* o) {
+  const int nx = T.nc[0], ny = T.nc[1];
+  const int zlo = D == 3 ? max(c[2] - k, 0) : 0;
+  const int zhi = D == 3 ? min(c[2] + k, T.nc[2] - 1) : 0;
+  const int ylo = max(c[1] - k, 0), yhi = min(c[1] + k, ny - 1);
+  const int xlo = max(c[0] - k, 0), xhi = min(c[0] + k, nx - 1);
+  const int wy = yhi - ylo + 1;
+  const int rows = wy * (zhi - zlo + 1);
+  for (int t = lane; t < rows; t += team) {
+    const int y = ylo + t % wy;
+    const int z = zlo + t / wy;
+    int x0, x1;
+    if (!clip_row<D>(T, c, o, y, z, xlo, xhi, x0, x1)) continue;
+    const uint32_t row = T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx;
+    fn(__ldg(cstart + 2 * (row + x0)), __ldg(cstart + 2 * (row + x1 + 1)), 0,
+       y - c[1], D == 3 ? z - c[2] : 0);
+  }
+}
+
 // Mask of the `team` lanes (aligned, a power of two) that hold this lane.
 template<int Team>
 __device__ __forceinline__ unsigned team_mask() {
@@ -577,11 +604,13 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
       if constexpr (D == 2) {
         A.posrec[j] = Pos32_2{o[0], o[1]};
       } else {
-        // w: the cell's x index (bit pattern), so that a whole row of cells
-        // can be read as one range (k_forces, 3D compensated form).
+        // w: the cell's x index, and bit 31 for a wall (bit pattern), so
+        // that a whole row of cells can be read as one range (k_forces and
+        // k_walls, 3D compensated form).
         int cc[3] = {0, 0, 0};
         cell_from_key<D>(T, key, cc);
-        A.posrec[j] = Pos32_3{o[0], o[1], o[2], __int_as_float(cc[0])};
+        const unsigned wbits = static_cast<unsigned>(cc[0]) | (id & kWallBit ? kWallBit : 0u);
+        A.posrec[j] = Pos32_3{o[0], o[1], o[2], __uint_as_float(wbits)};
       }
     }
     if (id & kWallBit) {
@@ -767,7 +796,35 @@ __global__ void __launch_bounds__(128)
           H.add(Vb * Hb * W);
         }
       };
-      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit, oe);
+      if constexpr (D == 3) {
+        // One range per row of cells (records carry the cell's x index and
+        // the wall bit), fluid records only.
+        auto visit_row = [&](uint32_t s, uint32_t en, int, int dy, int dz) {
+          const float oey = oe[1] - dy * csz;
+          const float oez = oe[2] - dz * csz;
+          for (uint32_t j = s; j < en; ++j) {
+            const Pos32_3 b = A.posrec[j];
+            const unsigned wb = __float_as_uint(b.w);
+            if (wb & kWallBit) continue;
+            const int dxc = static_cast<int>(wb) - c[0];
+            float d[3];
+            d[0] = (oe[0] - static_cast<float>(dxc) * csz) - b.x;
+            d[1] = oey - b.y;
+            d[2] = oez - b.z;
+            const float s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (s2 > R2) continue;
+            const Dat32 bd = load_dat_coherent(A.datrec, j);
+            const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
+            const float Vb = m * bd.invrho;
+            const float Hb = potential_f32(A.phys, T, bd.drho);
+            S.add(Vb * W);
+            H.add(Vb * Hb * W);
+          }
+        };
+        for_rows_team<D>(T, c, A.k, A.cell_start, lane, kWallTeam, visit_row, oe);
+      } else {
+        for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit, oe);
+      }
     }
     float Ss = S.value(), Hv = H.value();
 #pragma unroll
@@ -1148,7 +1205,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
         for (uint32_t j = s; j < en; ++j) {
           if (j == static_cast<uint32_t>(i)) continue;
           const Pos32_3 b = A.posrec[j];
-          const int dxc = __float_as_int(b.w) - c[0];
+          const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
           float d[3];
           d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
           d[1] = oay - b.y;
