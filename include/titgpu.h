@@ -285,6 +285,28 @@ int tg_summation_density_noalloc(int32_t dim, int32_t kernel, int64_t n,
                                  double* rho, int32_t* counts, uint64_t* hashes,
                                  void* stream);
 
+/* ---- boundary faces ------------------------------------------------------ */
+/* The reference's semi-analytical wall mode for one tank: FluidEquations
+ * with a non-empty domain surface and a containment function
+ * (fluid_equations.hpp:122-193 gamma, grad gamma and the wall extrapolation
+ * with the wall normal; :241-247 and :276-292 the face terms of continuity
+ * and momentum; :335-349, :465-467, :491-511 the face terms of shifting and
+ * the free-surface correction; kernel.hpp:194-221 the kernel flux and
+ * antigradient flux of a face).  2D and the FP64 form only.
+ *
+ * face_verts: 2 per face, indices into the tank's fixed particles (0 = the
+ * tank's first fixed particle), which are the face vertices and stay fixed
+ * (titwcsph appends one fixed particle per vertex of the tessellated
+ * domain, wcsph.cpp:109-112).  poly: the containment polygon, n_poly (x, y)
+ * vertices of a closed loop; a point is inside when its winding number
+ * exceeds 1/2 (the reference passes a FastWinding of the domain,
+ * fast_winding.hpp:80-95).  n_faces = 0 returns the tank to particle walls.
+ * Call after tg_particles_upload (a new upload drops the faces); applies to
+ * the following steps. */
+int tg_tank_faces(tg_context* ctx, int32_t tank, int32_t n_faces,
+                  const int32_t* face_verts, int32_t n_poly,
+                  const double* poly);
+
 /* ---- launch shape and the autotuner ----------------------------------- */
 /* Launch shape of a context: the grid's cell size (cells_per_radius cells
  * across the kernel support radius, as GridSearch{spacing} picks the cell

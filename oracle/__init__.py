@@ -34,6 +34,11 @@ class _Params(ctypes.Structure):
             "xi", "g", "mu", "alpha", "delta", "cfl", "c_force", "c_visc")]
 
 
+class _Faces(ctypes.Structure):
+    _fields_ = [("n_faces", ctypes.c_int32), ("face_verts", ctypes.POINTER(ctypes.c_int32)),
+                ("n_poly", ctypes.c_int32), ("poly", ctypes.POINTER(ctypes.c_double))]
+
+
 class _Tank(ctypes.Structure):
     _fields_ = [("n_fluid", ctypes.c_int64), ("n_wall", ctypes.c_int64),
                 ("h", ctypes.c_double), ("m", ctypes.c_double),
@@ -70,6 +75,14 @@ def lib():
             "or_wcsph_step": (ctypes.c_int32, [ctypes.POINTER(_Params), ctypes.c_int32,
                                                ctypes.POINTER(_Tank), _D, _D, _D, _D, _D,
                                                ctypes.c_int32, _D, _D, ctypes.c_int32]),
+            "or_wcsph_step_faces": (ctypes.c_int32, [ctypes.POINTER(_Params), ctypes.c_int32,
+                                                     ctypes.POINTER(_Tank), _D, _D, _D, _D, _D,
+                                                     ctypes.c_int32, _D, _D, ctypes.c_int32,
+                                                     ctypes.POINTER(_Faces)]),
+            "or_kernel_flux2": (None, [ctypes.c_int32, _D, _D, _D, ctypes.c_double, _D]),
+            "or_kernel_antigrad_flux2": (ctypes.c_double, [ctypes.c_int32, _D, _D, _D,
+                                                           ctypes.c_double]),
+            "or_winding_number2": (ctypes.c_double, [ctypes.c_int32, _D, _D]),
             "or_tank_neighbour_counts": (ctypes.c_int32, [ctypes.POINTER(_Params), ctypes.c_int32,
                                                           ctypes.POINTER(_Tank), _D, _I32, _U64,
                                                           ctypes.c_int32]),
@@ -218,20 +231,62 @@ class State:
         self.dv_dt = np.zeros((n, self.dim))
         self.time = np.zeros(len(self.tanks))
         self.dt = np.zeros(len(self.tanks))
+        # Per-tank boundary faces (face-boundary scenarios): face_verts
+        # (n, 2) indices into the tank's fixed particles, poly (m, 2).
+        self.faces = None
+        if scn.get("faces") is not None:
+            self.faces = [None if fc is None else
+                          (np.ascontiguousarray(fc["face_verts"], dtype=np.int32),
+                           np.ascontiguousarray(fc["poly"], dtype=np.float64))
+                          for fc in scn["faces"]]
 
 
 def step(params, state: State, n_steps: int = 1, nthreads: int = 0) -> np.ndarray:
     P = _params(params)
     T = _tanks(state.tanks)
-    st = lib().or_wcsph_step(ctypes.byref(P), len(state.tanks), T,
-                             _p(state.r, ctypes.c_double), _p(state.v, ctypes.c_double),
-                             _p(state.rho, ctypes.c_double), _p(state.drho_dt, ctypes.c_double),
-                             _p(state.dv_dt, ctypes.c_double), n_steps,
-                             _p(state.dt, ctypes.c_double), _p(state.time, ctypes.c_double),
-                             nthreads or default_threads())
+    args = (ctypes.byref(P), len(state.tanks), T,
+            _p(state.r, ctypes.c_double), _p(state.v, ctypes.c_double),
+            _p(state.rho, ctypes.c_double), _p(state.drho_dt, ctypes.c_double),
+            _p(state.dv_dt, ctypes.c_double), n_steps,
+            _p(state.dt, ctypes.c_double), _p(state.time, ctypes.c_double),
+            nthreads or default_threads())
+    if state.faces is None:
+        st = lib().or_wcsph_step(*args)
+    else:
+        F = (_Faces * len(state.tanks))()
+        for t, fc in enumerate(state.faces):
+            if fc is None:
+                continue
+            fv, poly = fc
+            F[t].n_faces = fv.shape[0]
+            F[t].face_verts = _p(fv, ctypes.c_int32)
+            F[t].n_poly = poly.shape[0]
+            F[t].poly = _p(poly, ctypes.c_double)
+        st = lib().or_wcsph_step_faces(*args, F)
     if st != 0:
         raise RuntimeError(f"or_wcsph_step: status {st}")
     return state.dt.copy()
+
+
+def kernel_flux2(kernel: int, a, b, x, h: float) -> np.ndarray:
+    """Kernel flux of segment a-b at x (kernel.hpp:194-206)."""
+    out = np.zeros(2)
+    A, B, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (a, b, x))
+    lib().or_kernel_flux2(kernel, _p(A, ctypes.c_double), _p(B, ctypes.c_double),
+                          _p(X, ctypes.c_double), h, _p(out, ctypes.c_double))
+    return out
+
+
+def kernel_antigrad_flux2(kernel: int, a, b, x, h: float) -> float:
+    """Antigradient flux of segment a-b at x (kernel.hpp:209-221)."""
+    A, B, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (a, b, x))
+    return lib().or_kernel_antigrad_flux2(kernel, _p(A, ctypes.c_double),
+                                          _p(B, ctypes.c_double), _p(X, ctypes.c_double), h)
+
+
+def winding_number2(poly, x) -> float:
+    P, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (poly, x))
+    return lib().or_winding_number2(P.shape[0], _p(P, ctypes.c_double), _p(X, ctypes.c_double))
 
 
 def tank_neighbour_counts(params, tanks, r: np.ndarray, nthreads: int = 0):

@@ -200,6 +200,191 @@ double kernel_weight(int k, int d) {
   return 1.0 / (kernel_table[k].moment[d - 1] * area);
 }
 
+// ---------------------------------------------------------------------------
+// Semi-analytical face boundaries in 2D: kernel flux and antigradient flux
+// over a segment (kernel.hpp:194-221, 286-314; kernel.gen.cpp:313-395).
+// Each kernel is a sum of support pieces w_i(q) = sum_p c_p q^p for
+// q < cutoff_i (the pieces of kernel.gen.cpp:520-553, expanded; t_p are the
+// coefficients of the piece's 2D tail moment T(q) = cutoff^2 P(cutoff) -
+// q^2 P(q), P(q) = sum_p c_p q^p / (p + 2)).  Over a segment at wall
+// distance eta and along-segment coordinates [z_min, z_max] (units of h):
+//   unit_flux          = sum over pieces of [sum_p c_p J_p]
+//   unit_antigrad_flux = sum over pieces of [t_0 A + t_1 eta L +
+//                                            sum_{p>=2} t_p eta J_{p-2}]
+// each clipped to |z| <= sqrt(cutoff^2 - eta^2), with rho^2 = z^2 + eta^2,
+// A = atan2(z, eta), L = copysign(log1p((|z| + z^2/(rho + eta))/eta), z)
+// (0 when eta is tiny), J_0 = z, J_1 = (z rho + eta^2 L)/2,
+// J_p = (z rho^p + p eta^2 J_{p-2})/(p + 1).  The reference evaluates A and
+// L with Highway's fast_atan2/fast_log1p; this restatement uses the libm
+// functions.
+
+struct KernelPiece {
+  double cutoff;
+  int deg;
+  double c[12];
+  int tdeg;
+  double t[14];
+};
+struct KernelPieces {
+  int n;
+  KernelPiece p[3];
+};
+
+constexpr KernelPieces kPieces[6] = {
+  // cubic
+  {2, {{2.0, 3, {2.0, -3.0, 3.0 / 2.0, -1.0 / 4.0}, 5, {2.0 / 5.0, 0.0, -1.0, 1.0, -3.0 / 8.0, 1.0 / 20.0}},
+   {1.0, 3, {-1.0, 3.0, -3.0, 1.0}, 5, {-1.0 / 20.0, 0.0, 1.0 / 2.0, -1.0, 3.0 / 4.0, -1.0 / 5.0}}}},
+  // quartic
+  {3, {{5.0 / 2.0, 4, {625.0 / 16.0, -125.0 / 2.0, 75.0 / 2.0, -10.0, 1.0}, 6, {3125.0 / 384.0, 0.0, -625.0 / 32.0, 125.0 / 6.0, -75.0 / 8.0, 2.0, -1.0 / 6.0}},
+   {3.0 / 2.0, 4, {-405.0 / 16.0, 135.0 / 2.0, -135.0 / 2.0, 30.0, -5.0}, 6, {-243.0 / 128.0, 0.0, 405.0 / 32.0, -45.0 / 2.0, 135.0 / 8.0, -6.0, 5.0 / 6.0}},
+   {1.0 / 2.0, 4, {5.0 / 8.0, -5.0, 15.0, -20.0, 10.0}, 6, {1.0 / 192.0, 0.0, -5.0 / 16.0, 5.0 / 3.0, -15.0 / 4.0, 4.0, -5.0 / 3.0}}}},
+  // quintic
+  {3, {{3.0, 5, {243.0, -405.0, 270.0, -90.0, 15.0, -1.0}, 7, {729.0 / 14.0, 0.0, -243.0 / 2.0, 135.0, -135.0 / 2.0, 18.0, -5.0 / 2.0, 1.0 / 7.0}},
+   {2.0, 5, {-192.0, 480.0, -480.0, 240.0, -60.0, 6.0}, 7, {-128.0 / 7.0, 0.0, 96.0, -160.0, 120.0, -48.0, 10.0, -6.0 / 7.0}},
+   {1.0, 5, {15.0, -75.0, 150.0, -150.0, 75.0, -15.0}, 7, {5.0 / 14.0, 0.0, -15.0 / 2.0, 25.0, -75.0 / 2.0, 30.0, -25.0 / 2.0, 15.0 / 7.0}}}},
+  // wc2
+  {1, {{2.0, 5, {1.0, 0.0, -5.0 / 2.0, 5.0 / 2.0, -15.0 / 16.0, 1.0 / 8.0}, 7, {2.0 / 7.0, 0.0, -1.0 / 2.0, 0.0, 5.0 / 8.0, -1.0 / 2.0, 5.0 / 32.0, -1.0 / 56.0}}}},
+  // wc4
+  {1, {{2.0, 8, {1.0, 0.0, -7.0 / 3.0, 0.0, 35.0 / 8.0, -14.0 / 3.0, 35.0 / 16.0, -1.0 / 2.0, 35.0 / 768.0}, 10, {2.0 / 9.0, 0.0, -1.0 / 2.0, 0.0, 7.0 / 12.0, 0.0, -35.0 / 48.0, 2.0 / 3.0, -35.0 / 128.0, 1.0 / 18.0, -7.0 / 1536.0}}}},
+  // wc6
+  {1, {{2.0, 11, {1.0, 0.0, -11.0 / 4.0, 0.0, 33.0 / 8.0, 0.0, -231.0 / 32.0, 33.0 / 4.0, -1155.0 / 256.0, 11.0 / 8.0, -231.0 / 1024.0, 1.0 / 64.0}, 13, {7.0 / 39.0, 0.0, -1.0 / 2.0, 0.0, 11.0 / 16.0, 0.0, -11.0 / 16.0, 0.0, 231.0 / 256.0, -11.0 / 12.0, 231.0 / 512.0, -1.0 / 8.0, 77.0 / 4096.0, -1.0 / 832.0}}}},
+};
+
+
+
+void line_integrals(double eta, double z, double rho, double L, int pmax,
+                    double* J) {
+  J[0] = z;
+  if (pmax >= 1) J[1] = (z * rho + eta * eta * L) / 2.0;
+  double rp = rho;
+  for (int p = 2; p <= pmax; ++p) {
+    rp *= rho;
+    J[p] = (z * rp + p * eta * eta * J[p - 2]) / (p + 1);
+  }
+}
+
+double piece_primitive(const KernelPiece& kp, bool antigrad, double eta,
+                       double z) {
+  const double rho = std::sqrt(z * z + eta * eta);
+  const double A = std::atan2(z, eta);
+  const double L =
+      std::abs(eta) <= tiny_d
+          ? 0.0
+          : std::copysign(std::log1p((std::abs(z) + z * z / (rho + eta)) / eta), z);
+  double J[16];
+  double s = 0.0;
+  if (!antigrad) {
+    line_integrals(eta, z, rho, L, kp.deg, J);
+    for (int p = 0; p <= kp.deg; ++p) s += kp.c[p] * J[p];
+    return s;
+  }
+  line_integrals(eta, z, rho, L, std::max(kp.tdeg - 2, 0), J);
+  for (int p = 0; p <= kp.tdeg; ++p) {
+    if (p == 0) s += kp.t[0] * A;
+    else if (p == 1) s += kp.t[1] * eta * L;
+    else s += kp.t[p] * eta * J[p - 2];
+  }
+  return s;
+}
+
+// unit_segment_integral (kernel.hpp:286-314) summed over the pieces.
+double unit_segment(int k, bool antigrad, double eta, double zmin, double zmax) {
+  double total = 0.0;
+  for (int i = 0; i < kPieces[k].n; ++i) {
+    const KernelPiece& kp = kPieces[k].p[i];
+    if (eta >= kp.cutoff) continue;
+    const double zc = std::sqrt(kp.cutoff * kp.cutoff - eta * eta);
+    const double lo = std::max(zmin, -zc), hi = std::min(zmax, zc);
+    if (lo >= hi) continue;
+    total += piece_primitive(kp, antigrad, eta, hi) -
+             piece_primitive(kp, antigrad, eta, lo);
+  }
+  return total;
+}
+
+// Segment geometry (geom/segment.hpp): normal = normalize(cross(b - a)),
+// cross((x, y)) = (y, -x) (core/_vec/vec.hpp:692-694); project(x) =
+// (dot(a - x, e), dot(b - x, e)), e = normalize(b - a).
+struct SegFrame {
+  double n[2], d, za, zb;
+};
+SegFrame seg_frame(const double* a, const double* b, const double* x,
+                   double h) {
+  const double ba[2] = {b[0] - a[0], b[1] - a[1]};
+  const double cr[2] = {ba[1], -ba[0]};
+  SegFrame F;
+  normalize(cr, 2, F.n);
+  double e[2];
+  normalize(ba, 2, e);
+  const double hinv = 1.0 / h;
+  const double xa[2] = {x[0] - a[0], x[1] - a[1]};
+  F.d = dot(xa, F.n, 2) * hinv;
+  const double ax[2] = {a[0] - x[0], a[1] - x[1]};
+  const double bx[2] = {b[0] - x[0], b[1] - x[1]};
+  F.za = dot(ax, e, 2) * hinv;
+  F.zb = dot(bx, e, 2) * hinv;
+  return F;
+}
+
+// Kernel::flux (kernel.hpp:194-206): n w h^-1 unit_flux(|d|, z_a, z_b).
+void face_flux(int k, const double* a, const double* b, const double* x,
+               double h, double* out) {
+  const SegFrame F = seg_frame(a, b, x, h);
+  const double w = kernel_weight(k, 2) * (1.0 / h);
+  const double s = w * unit_segment(k, false, std::abs(F.d), F.za, F.zb);
+  out[0] = F.n[0] * s;
+  out[1] = F.n[1] * s;
+}
+
+// Kernel::antigrad_flux (kernel.hpp:209-221).
+double face_antigrad_flux(int k, const double* a, const double* b,
+                          const double* x, double h) {
+  const SegFrame F = seg_frame(a, b, x, h);
+  return std::copysign(kernel_weight(k, 2), F.d) *
+         unit_segment(k, true, std::abs(F.d), F.za, F.zb);
+}
+
+// Segment::intersects(BSphere) (geom/segment.hpp:108-112): boxes overlap
+// and the closest point of the segment (clamp, :91-106) is in the sphere.
+bool face_in_sphere(const double* a, const double* b, const double* c,
+                    double radius) {
+  for (int k = 0; k < 2; ++k) {
+    const double lo = std::min(a[k], b[k]), hi = std::max(a[k], b[k]);
+    if (!(c[k] - radius <= hi && lo <= c[k] + radius)) return false;
+  }
+  const double ba[2] = {b[0] - a[0], b[1] - a[1]};
+  const double len2 = norm2(ba, 2);
+  double q[2] = {a[0], a[1]};
+  if (!is_tiny(len2)) {
+    const double pa[2] = {c[0] - a[0], c[1] - a[1]};
+    const double t = dot(pa, ba, 2) / len2;
+    if (t > 1.0) {
+      q[0] = b[0];
+      q[1] = b[1];
+    } else if (!(t < 0.0)) {
+      q[0] = a[0] + t * ba[0];
+      q[1] = a[1] + t * ba[1];
+    }
+  }
+  const double d[2] = {q[0] - c[0], q[1] - c[1]};
+  return norm2(d, 2) <= radius * radius;
+}
+
+// Exact generalized winding number of a closed polygon at x
+// (Segment::winding_number, geom/segment.hpp:74-79, summed over the loop).
+double winding_number(int32_t n_poly, const double* poly, const double* x) {
+  double w = 0.0;
+  for (int32_t i = 0; i < n_poly; ++i) {
+    const double* a = poly + 2 * i;
+    const double* b = poly + 2 * ((i + 1) % n_poly);
+    const double ap[2] = {a[0] - x[0], a[1] - x[1]};
+    const double bp[2] = {b[0] - x[0], b[1] - x[1]};
+    w += std::atan2(ap[0] * bp[1] - ap[1] * bp[0], dot(ap, bp, 2)) /
+         (2.0 * std::numbers::pi);
+  }
+  return w;
+}
+
 template<class Num>
 struct Kern {
   int id;
@@ -397,9 +582,11 @@ int64_t export_csr(const Adjacency& adj, int64_t n, int64_t* offsets,
 }
 
 // ---------------------------------------------------------------------------
-// FluidEquations with particle walls: no boundary faces and an always-true
-// containment, so gamma = 1 and grad_gamma = 0 everywhere
-// (fluid_equations.hpp:171-193), and every face term vanishes.
+// FluidEquations (fluid_equations.hpp:79-512).  With particle walls (no
+// boundary faces, an always-true containment) gamma = 1 and grad_gamma = 0
+// everywhere (:166-193) and every face term vanishes.  With faces (2D), the
+// tank's fixed particles are the face vertices; gamma, grad_gamma, the face
+// terms and the gamma-divided pair sums follow the reference.
 
 struct TankView {
   int64_t nf = 0, nw = 0, n = 0;
@@ -410,6 +597,12 @@ struct TankView {
   double* rho = nullptr;
   double* drho = nullptr;
   double* dv = nullptr;
+  // Boundary faces (2D): vertex pairs as indices into the tank's fixed
+  // particles, and the containment polygon (closed loop of vertices).
+  int32_t n_faces = 0;
+  const int32_t* face_verts = nullptr;
+  int32_t n_poly = 0;
+  const double* poly = nullptr;
 };
 
 struct Solver {
@@ -420,12 +613,76 @@ struct Solver {
   Kern<double> K;
   Adjacency adj;
   std::vector<double> p, cs;
+  std::vector<double> gamma, ggam;           // gamma and grad gamma
+  std::vector<std::vector<int32_t>> fadj;    // adjacent faces, ascending
 
   Solver(const tg_params& params, TankView& tank, int32_t nt)
       : P{params}, dim{params.dim}, nthreads{nt}, T{tank},
         K{params.kernel, params.dim, tank.h} {
     p.assign(static_cast<size_t>(T.n), 0.0);
     cs.assign(static_cast<size_t>(T.n), 0.0);
+    gamma.assign(static_cast<size_t>(T.n), 1.0);
+    ggam.assign(static_cast<size_t>(T.n * dim), 0.0);
+    fadj.assign(static_cast<size_t>(T.n), {});
+  }
+
+  bool faces() const { return T.n_faces > 0; }
+  const double* vert(int32_t f, int i) const {
+    return T.r + (T.nf + T.face_verts[2 * f + i]) * dim;
+  }
+  int64_t vert_index(int32_t f, int i) const {
+    return T.nf + T.face_verts[2 * f + i];
+  }
+  // Field of a face's vertex pair: avg (field.hpp:59-64, core/math.hpp:130).
+  double face_avg(const std::vector<double>& fld, int32_t f) const {
+    return (fld[vert_index(f, 0)] + fld[vert_index(f, 1)]) / 2.0;
+  }
+  double face_avg(const double* fld, int32_t f) const {
+    return (fld[vert_index(f, 0)] + fld[vert_index(f, 1)]) / 2.0;
+  }
+
+  double face_avg_vec(const double* fld, int32_t f, int k) const {
+    return (fld[vert_index(f, 0) * dim + k] + fld[vert_index(f, 1) * dim + k]) / 2.0;
+  }
+
+  // ParticleMesh face adjacency (particle_mesh.hpp:149-161): faces within
+  // the search sphere, sorted.
+  void index_faces() {
+    parallel_for(T.n, nthreads, [&](int64_t a) {
+      auto& out = fadj[a];
+      out.clear();
+      for (int32_t fi = 0; fi < T.n_faces; ++fi) {
+        if (face_in_sphere(vert(fi, 0), vert(fi, 1), T.r + a * dim, K.radius)) {
+          out.push_back(fi);
+        }
+      }
+    });
+  }
+
+  // FluidEquations::compute_gamma (fluid_equations.hpp:166-193).
+  void compute_gamma() {
+    parallel_for(T.n, nthreads, [&](int64_t a) {
+      double* g = &ggam[a * dim];
+      g[0] = g[1] = 0.0;
+      for (int32_t fi : fadj[a]) {
+        double fl[2];
+        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * dim, T.h, fl);
+        g[0] += fl[0];
+        g[1] += fl[1];
+      }
+      double ga = winding_number(T.n_poly, T.poly, T.r + a * dim) > 0.5 ? 1.0 : 0.0;
+      const double ng = norm(g, 2);
+      if (!is_tiny(ng)) {
+        const double n_a[2] = {g[0] / ng, g[1] / ng};
+        const double s = (2.0 * ga - 1.0);
+        const double r_a[2] = {T.r[a * dim] + s * n_a[0] * pow2(T.h),
+                               T.r[a * dim + 1] + s * n_a[1] * pow2(T.h)};
+        for (int32_t fi : fadj[a]) {
+          ga -= face_antigrad_flux(P.kernel, vert(fi, 0), vert(fi, 1), r_a, T.h);
+        }
+      }
+      gamma[a] = ga;
+    });
   }
 
   bool is_fluid(int64_t a) const { return a < T.nf; }
@@ -437,12 +694,15 @@ struct Solver {
   }
 
   // FluidEquations::setup_boundary (fluid_equations.hpp:122-164).  With
-  // grad_gamma = 0 the normal n_e is zero and the hydrostatic term vanishes.
+  // particle walls grad_gamma = 0, so the normal n_e is zero and the
+  // hydrostatic term vanishes.
   void setup_boundary() {
     parallel_for(T.nw, nthreads, [&](int64_t i) {
       const int64_t e = T.nf + i;
       for (int k = 0; k < dim; ++k) T.v[e * dim + k] = 0.0;
       double S_e = 0.0, H_e = 0.0;
+      double n_e[3] = {0.0, 0.0, 0.0};
+      normalize(&ggam[e * dim], dim, n_e);
       for (int64_t j = adj.off[e]; j < adj.off[e + 1]; ++j) {
         const int64_t b = adj.idx[j];
         if (!is_fluid(b)) continue;
@@ -454,7 +714,7 @@ struct Solver {
         const double W_be = K.value(r_be);
         const double H_b = T.eos.potential(T.rho[b]);
         S_e += V_b * W_be;
-        H_e += V_b * H_b * W_be;
+        H_e += V_b * (H_b + P.g * dot(r_be, n_e, dim) * n_e[1]) * W_be;
       }
       T.rho[e] = T.eos.density_from_potential(is_tiny(S_e) ? 0.0 : H_e / S_e);
     });
@@ -463,6 +723,10 @@ struct Solver {
   // FluidEquations::prepare (fluid_equations.hpp:99-105).
   void prepare() {
     index();
+    if (faces()) {
+      index_faces();
+      compute_gamma();
+    }
     setup_boundary();
   }
 
@@ -496,6 +760,15 @@ struct Solver {
     compute_eos();
     parallel_for(T.nf, nthreads, [&](int64_t a) {
       double acc = 0.0;
+      // Face terms (fluid_equations.hpp:241-247).
+      for (int32_t fi : fadj[a]) {
+        double gg[2];
+        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * dim, T.h, gg);
+        const double v_as[2] = {
+            T.v[a * dim] - face_avg_vec(T.v, fi, 0),
+            T.v[a * dim + 1] - face_avg_vec(T.v, fi, 1)};
+        acc -= face_avg(T.rho, fi) * dot(v_as, gg, 2) / gamma[a];
+      }
       for (int64_t j = adj.off[a]; j < adj.off[a + 1]; ++j) {
         const int64_t b = adj.idx[j];
         if (b == a) continue;
@@ -514,13 +787,13 @@ struct Solver {
             const double Psi = cs_ab * rho_ab * r_ab[k] / nr;
             w[k] = v_ab[k] + Psi / T.rho[b];
           }
-          acc += T.m / 1.0 * dot(w, gW, dim);
+          acc += T.m / gamma[a] * dot(w, gW, dim);
         } else if (P.diffusion == TG_DIFF_MOLTENI) {
           const double D = 2.0 * P.delta * T.h * T.eos.cs0 * rho_ab / T.rho[b] *
                            dot(r_ab, gW, dim) / norm2(r_ab, dim);
-          acc += T.m / 1.0 * (dot(v_ab, gW, dim) + D);
+          acc += T.m / gamma[a] * (dot(v_ab, gW, dim) + D);
         } else {
-          acc += T.m / 1.0 * dot(v_ab, gW, dim);
+          acc += T.m / gamma[a] * dot(v_ab, gW, dim);
         }
       }
       T.drho[a] = acc;
@@ -537,6 +810,31 @@ struct Solver {
     parallel_for(T.nf, nthreads, [&](int64_t a) {
       double acc[3] = {0.0, 0.0, 0.0};
       acc[1] = -P.g;  // unit<1>(r[a], -g)
+      // Face terms: wall pressure and wall shear (fluid_equations.hpp:278-291).
+      for (int32_t fi : fadj[a]) {
+        double gg[2];
+        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * dim, T.h, gg);
+        const double rho_s = face_avg(T.rho, fi);
+        const double p_s = face_avg(p, fi);
+        const double P_as =
+            rho_s * (p[a] / pow2(T.rho[a]) + p_s / pow2(rho_s));
+        double n_s[2], t_as[2];
+        normalize(gg, 2, n_s);
+        const double v_as[2] = {T.v[a * dim] - face_avg_vec(T.v, fi, 0),
+                                T.v[a * dim + 1] - face_avg_vec(T.v, fi, 1)};
+        const double vn = dot(v_as, n_s, 2);
+        const double vt[2] = {v_as[0] - vn * n_s[0], v_as[1] - vn * n_s[1]};
+        normalize(vt, 2, t_as);
+        const double r_as[2] = {T.r[a * dim] - face_avg_vec(T.r, fi, 0),
+                                T.r[a * dim + 1] - face_avg_vec(T.r, fi, 1)};
+        const double dr_as = std::max(T.h / 2.0, dot(r_as, n_s, 2));
+        const double Pi_s =
+            2.0 * P.mu / (T.rho[a] * dr_as) * dot(v_as, t_as, 2);
+        const double ng = norm(gg, 2);
+        for (int k = 0; k < 2; ++k) {
+          acc[k] += (P_as * gg[k] - Pi_s * t_as[k] * ng) / gamma[a];
+        }
+      }
       for (int64_t j = adj.off[a]; j < adj.off[a + 1]; ++j) {
         const int64_t b = adj.idx[j];
         if (b == a) continue;
@@ -562,7 +860,7 @@ struct Solver {
             Pi_ab = P.alpha * c_ab * mu_ab / rho_m;
           }
         }
-        const double s = T.m / 1.0 * (Pi_ab - P_ab);
+        const double s = T.m / gamma[a] * (Pi_ab - P_ab);
         for (int k = 0; k < dim; ++k) acc[k] += s * gW[k];
       }
       for (int k = 0; k < dim; ++k) T.dv[a * dim + k] = acc[k];
@@ -624,6 +922,25 @@ struct Solver {
       double* La = &L[a * d * d];
       double* gva = &gv[a * d * d];
       double* gra = &gr[a * d];
+      // Face terms (fluid_equations.hpp:340-349).
+      for (int32_t fi : fadj[a]) {
+        double gg[2];
+        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * d, T.h, gg);
+        double r_sa[2], v_sa[2];
+        for (int k = 0; k < 2; ++k) {
+          r_sa[k] = face_avg_vec(T.r, fi, k) - T.r[a * d + k];
+          v_sa[k] = face_avg_vec(T.v, fi, k) - T.v[a * d + k];
+        }
+        const double rho_sa = face_avg(T.rho, fi) - T.rho[a];
+        for (int i = 0; i < d; ++i) {
+          Na[i] -= gg[i] / gamma[a];
+          for (int k = 0; k < d; ++k) {
+            La[i * d + k] -= r_sa[i] * gg[k] / gamma[a];
+            gva[i * d + k] -= v_sa[i] * gg[k] / gamma[a];
+          }
+          gra[i] -= rho_sa * gg[i] / gamma[a];
+        }
+      }
       for (int64_t j = adj.off[a]; j < adj.off[a + 1]; ++j) {
         const int64_t b = adj.idx[j];
         if (b == a) continue;
@@ -635,7 +952,7 @@ struct Solver {
         }
         K.grad(r_ab, gW);
         const double V_b = T.m / T.rho[b];
-        const double s = V_b / 1.0;
+        const double s = V_b / gamma[a];
         const double rho_ba = T.rho[b] - T.rho[a];
         for (int i = 0; i < d; ++i) {
           Na[i] += s * gW[i];
@@ -750,11 +1067,14 @@ struct Solver {
       const double c = -P.cfl * 0.2 * pow2(T.h);
       for (int i = 0; i < d; ++i) dra[i] *= c;
       for (int i = 0; i < d; ++i) T.r[a * d + i] += dra[i];
-      double dv[3];
-      for (int i = 0; i < d; ++i) {
-        dv[i] = dot(&gv[a * d * d + i * d], dra, d);
+      // Velocity correction only where gamma ~ 1 (:465-467).
+      if (is_tiny(gamma[a] - 1.0)) {
+        double dv[3];
+        for (int i = 0; i < d; ++i) {
+          dv[i] = dot(&gv[a * d * d + i * d], dra, d);
+        }
+        for (int i = 0; i < d; ++i) T.v[a * d + i] += dv[i];
       }
-      for (int i = 0; i < d; ++i) T.v[a * d + i] += dv[i];
       T.rho[a] += dot(&gr[a * d], dra, d);
     });
     phi_.swap(phi);
@@ -778,10 +1098,10 @@ struct Solver {
         alpha += T.m / rho_raw[b] * W_ab;
         rho_t += T.m * W_ab;
       }
-      const double ratio = std::min(1.0, alpha / 1.0);
+      const double ratio = std::min(1.0, alpha / gamma[a]);
       if (ratio > 0.99) return;
       const double beta = std::exp(-K_fs * pow2(ratio - 1.0));
-      const double corr = beta * 1.0 + (1.0 - beta) * alpha;
+      const double corr = beta * gamma[a] + (1.0 - beta) * alpha;
       if (!is_tiny(corr)) T.rho[a] = rho_t / corr;
     });
   }
@@ -1042,8 +1362,32 @@ int32_t or_wcsph_step(const tg_params* params, int32_t n_tanks,
                       const tg_tank* tanks, double* r, double* v, double* rho,
                       double* drho_dt, double* dv_dt, int32_t n_steps,
                       double* dt_out, double* time_io, int32_t nthreads) {
+  return or_wcsph_step_faces(params, n_tanks, tanks, r, v, rho, drho_dt, dv_dt,
+                             n_steps, dt_out, time_io, nthreads, nullptr);
+}
+
+int32_t or_wcsph_step_faces(const tg_params* params, int32_t n_tanks,
+                            const tg_tank* tanks, double* r, double* v,
+                            double* rho, double* drho_dt, double* dv_dt,
+                            int32_t n_steps, double* dt_out, double* time_io,
+                            int32_t nthreads, const or_tank_faces* faces) {
   if (!valid_params(params) || n_tanks < 0 || n_steps < 0) {
     return TG_ERR_INVALID_ARGUMENT;
+  }
+  if (faces != nullptr) {
+    for (int32_t t = 0; t < n_tanks; ++t) {
+      const or_tank_faces& F = faces[t];
+      if (F.n_faces == 0) continue;
+      if (params->dim != 2 || F.n_faces < 0 || F.face_verts == nullptr ||
+          F.n_poly < 3 || F.poly == nullptr) {
+        return TG_ERR_INVALID_ARGUMENT;
+      }
+      for (int32_t i = 0; i < 2 * F.n_faces; ++i) {
+        if (F.face_verts[i] < 0 || F.face_verts[i] >= tanks[t].n_wall) {
+          return TG_ERR_INVALID_ARGUMENT;
+        }
+      }
+    }
   }
   const int dim = params->dim;
   int64_t base = 0;
@@ -1060,6 +1404,12 @@ int32_t or_wcsph_step(const tg_params* params, int32_t n_tanks,
     T.rho = rho + base;
     T.drho = drho_dt + base;
     T.dv = dv_dt + base * dim;
+    if (faces != nullptr) {
+      T.n_faces = faces[t].n_faces;
+      T.face_verts = faces[t].face_verts;
+      T.n_poly = faces[t].n_poly;
+      T.poly = faces[t].poly;
+    }
     Solver S(*params, T, nthreads);
     double dt = 0.0;
     for (int32_t s = 0; s < n_steps; ++s) {
@@ -1070,6 +1420,20 @@ int32_t or_wcsph_step(const tg_params* params, int32_t n_tanks,
     base += T.n;
   }
   return TG_OK;
+}
+
+void or_kernel_flux2(int32_t kernel, const double* a, const double* b,
+                     const double* x, double h, double* out) {
+  face_flux(kernel, a, b, x, h, out);
+}
+
+double or_kernel_antigrad_flux2(int32_t kernel, const double* a,
+                                const double* b, const double* x, double h) {
+  return face_antigrad_flux(kernel, a, b, x, h);
+}
+
+double or_winding_number2(int32_t n_poly, const double* poly, const double* x) {
+  return winding_number(n_poly, poly, x);
 }
 
 int32_t or_tank_neighbour_counts(const tg_params* params, int32_t n_tanks,

@@ -85,6 +85,33 @@ int32_t or_wcsph_step(const tg_params* params, int32_t n_tanks,
                       double* drho_dt, double* dv_dt, int32_t n_steps,
                       double* dt_out, double* time_io, int32_t nthreads);
 
+/* Boundary faces of one tank (2D semi-analytical walls): n_faces segments
+ * as index pairs into the tank's fixed particles (the face vertices), and
+ * the containment polygon, a closed loop of n_poly vertices (x, y); a point
+ * is inside when the polygon's winding number around it exceeds 1/2.
+ * n_faces = 0: particle walls. */
+typedef struct or_tank_faces {
+  int32_t n_faces;
+  const int32_t* face_verts;
+  int32_t n_poly;
+  const double* poly;
+} or_tank_faces;
+
+/* or_wcsph_step with per-tank boundary faces (faces may be NULL). */
+int32_t or_wcsph_step_faces(const tg_params* params, int32_t n_tanks,
+                            const tg_tank* tanks, double* r, double* v,
+                            double* rho, double* drho_dt, double* dv_dt,
+                            int32_t n_steps, double* dt_out, double* time_io,
+                            int32_t nthreads, const or_tank_faces* faces);
+
+/* Kernel flux (2 components) and antigradient flux of segment a-b at x with
+ * width h (kernel.hpp:194-221), and the polygon winding number at x. */
+void or_kernel_flux2(int32_t kernel, const double* a, const double* b,
+                     const double* x, double h, double* out);
+double or_kernel_antigrad_flux2(int32_t kernel, const double* a,
+                                const double* b, const double* x, double h);
+double or_winding_number2(int32_t n_poly, const double* poly, const double* x);
+
 /* Neighbour counts and hashes of every particle in its tank (tank-local ids),
  * via or_grid_search with radius = unit_radius * h. */
 int32_t or_tank_neighbour_counts(const tg_params* params, int32_t n_tanks,

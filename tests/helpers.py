@@ -12,6 +12,9 @@ from titsolver_gb300 import _abi
 def gpu_context(scn: dict, params) -> _abi.Context:
     ctx = _abi.Context(params)
     ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+    for t, fc in enumerate(scn.get("faces") or []):
+        if fc is not None:
+            ctx.set_faces(t, fc["face_verts"], fc["poly"])
     return ctx
 
 

@@ -1,0 +1,95 @@
+"""Semi-analytical face boundaries on the GPU (2D, FP64) against the
+oracle, on the titwcsph scenario itself (source/titwcsph/wcsph.cpp:37-142:
+tessellated pool faces with one fixed particle per vertex, containment by
+the pool polygon).  Tolerances (relative L2 over the fluid): 1 step r, v,
+rho <= 1e-11 and dv/dt, drho/dt <= 1e-9; 5 steps <= 1e-10."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import fluid_mask, gpu_context, gpu_state, oracle_run, rel_l2
+from titsolver_gb300 import _abi, physics, scenarios
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(scn, P, steps, tol, tol_deriv=None):
+    with gpu_context(scn, P) as ctx:
+        dt = ctx.step(steps)
+        g = gpu_state(ctx)
+    o = oracle_run(scn, P, steps)
+    f = fluid_mask(scn)
+    np.testing.assert_allclose(dt, o.dt, rtol=1e-12)
+    assert rel_l2(g["r"][f], o.r[f]) <= tol
+    assert rel_l2(g["v"][f], o.v[f]) <= tol * 1e2
+    assert rel_l2(g["rho"][f], o.rho[f]) <= tol
+    assert rel_l2(g["rho"][~f], o.rho[~f]) <= tol
+    if tol_deriv is not None:
+        assert rel_l2(g["dv_dt"][f], o.dv_dt[f]) <= tol_deriv
+        assert rel_l2(g["drho_dt"][f], o.drho_dt[f]) <= tol_deriv
+    return g, o
+
+
+@pytest.mark.parametrize("shifting", (False, True))
+def test_titwcsph_faces_vs_oracle(gpu_lib, shifting):
+    scn = scenarios.dam_break_2d_faces(nx_per_H=20)
+    P = physics.reference_params(2)
+    P.post_integrate = _abi.TG_POST_SHIFTING if shifting else _abi.TG_POST_PREPARE
+    _compare(scn, P, 1, 1e-11, 1e-9)
+    _compare(scn, P, 5, 1e-10)
+
+
+@pytest.mark.parametrize("kernel", (_abi.TG_KERNEL_WENDLAND_C2, _abi.TG_KERNEL_CUBIC_SPLINE,
+                                    _abi.TG_KERNEL_QUINTIC_SPLINE))
+def test_faces_other_kernels_and_term_sets(gpu_lib, kernel):
+    scn = scenarios.dam_break_2d_faces(nx_per_H=16)
+    _compare(scn, physics.reference_params(2, kernel=kernel), 2, 1e-10)
+    _compare(scn, physics.baseline_params(2, kernel=kernel), 2, 1e-10)
+
+
+@pytest.mark.parametrize("integrator", (_abi.TG_EULER, _abi.TG_VERLET, _abi.TG_SSPRK2))
+def test_faces_other_integrators(gpu_lib, integrator):
+    scn = scenarios.dam_break_2d_faces(nx_per_H=16)
+    P = physics.reference_params(2)
+    P.integrator = integrator
+    _compare(scn, P, 3, 1e-10)
+
+
+def test_faces_batched_with_a_particle_wall_tank(gpu_lib):
+    a = scenarios.dam_break_2d_faces(nx_per_H=12)
+    b = scenarios.dam_break_2d(nx_per_H=10)
+    c = scenarios.dam_break_2d_faces(nx_per_H=16)
+    scn = dict(dim=2, tanks=a["tanks"] + b["tanks"] + c["tanks"],
+               r=np.concatenate([a["r"], b["r"], c["r"]]),
+               v=np.concatenate([a["v"], b["v"], c["v"]]),
+               rho=np.concatenate([a["rho"], b["rho"], c["rho"]]),
+               faces=[a["faces"][0], None, c["faces"][0]])
+    _compare(scn, physics.reference_params(2), 3, 1e-10)
+
+
+def test_faces_survive_autotune_and_reject_other_forms(gpu_lib):
+    scn = scenarios.dam_break_2d_faces(nx_per_H=16)
+    P = physics.reference_params(2)
+    f = fluid_mask(scn)
+    with gpu_context(scn, P) as ctx, gpu_context(scn, P) as ref:
+        ctx.step(2)
+        ref.step(2)
+        ctx.autotune(2)
+        ctx.step(3)
+        ref.step(3)
+        a, b = gpu_state(ctx), gpu_state(ref)
+    assert rel_l2(a["rho"][f], b["rho"][f]) <= 1e-11
+    assert rel_l2(a["r"][f], b["r"][f]) <= 1e-11
+    P32 = physics.reference_params(2, precision=_abi.TG_FP32C)
+    with _abi.Context(P32) as ctx:
+        ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+        with pytest.raises(_abi.TgError) as ei:
+            ctx.set_faces(0, scn["faces"][0]["face_verts"], scn["faces"][0]["poly"])
+        assert ei.value.status == _abi.TG_ERR_INVALID_ARGUMENT
+    with _abi.Context(P) as ctx:
+        ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+        bad = np.array([[0, 10**6]], dtype=np.int32)
+        with pytest.raises(_abi.TgError):
+            ctx.set_faces(0, bad, scn["faces"][0]["poly"])

@@ -138,6 +138,8 @@ SIGNATURES = [
     ("tg_summation_density_noalloc", ctypes.c_int,
      [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _P, ctypes.c_double, ctypes.c_double,
       _P, _P, _P, _P]),
+    ("tg_tank_faces", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _I32,
+                                     ctypes.c_int32, _D]),
     ("tg_get_tuning", ctypes.c_int, [_P, ctypes.POINTER(TgTuning)]),
     ("tg_set_tuning", ctypes.c_int, [_P, ctypes.POINTER(TgTuning)]),
     ("tg_autotune", ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(TgTuning)]),
@@ -370,3 +372,12 @@ class Context:
         self._check(self.lib.tg_autotune(self.handle, int(trial_steps), ctypes.byref(t)),
                     "tg_autotune")
         return {k: getattr(t, k) for k, _ in TgTuning._fields_}
+
+    def set_faces(self, tank: int, face_verts, poly):
+        """Boundary faces of a tank (2D, FP64): vertex index pairs into the
+        tank's fixed particles and the containment polygon."""
+        fv = np.ascontiguousarray(face_verts, dtype=np.int32).reshape(-1, 2)
+        pl = np.ascontiguousarray(poly, dtype=np.float64).reshape(-1, 2)
+        self._check(self.lib.tg_tank_faces(self.handle, int(tank), fv.shape[0],
+                                           _ptr(fv, ctypes.c_int32), pl.shape[0],
+                                           _ptr(pl, ctypes.c_double)), "tg_tank_faces")

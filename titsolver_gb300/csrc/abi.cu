@@ -40,6 +40,7 @@ void Context::release_all() {
   d_dt = d_dt_last = d_time = nullptr;
   d_err = d_wall_count = nullptr;
   d_fbox = nullptr;
+  faces = FaceArgs{};
   keys_a = keys_b = vals_a = vals_b = nullptr;
   sort_scratch = nullptr;
   cell_start = wall_list = nullptr;
@@ -127,6 +128,10 @@ int cuda_fail(Context* C, cudaError_t e, const char* where) {
     const cudaError_t e_ = (call);                         \
     if (e_ != cudaSuccess) return cuda_fail((C), e_, #call); \
   } while (0)
+
+int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
+                     const double* r, const double* v, const double* rho);
+int build_faces(tg_context* ctx);
 
 bool valid_params(const tg_params* P, std::string* why) {
   if (P->dim != 2 && P->dim != 3) {
@@ -313,6 +318,16 @@ int tg_context_destroy(tg_context* ctx) {
 int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
                         const double* r, const double* v, const double* rho) {
   if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  ctx->c.face_host.clear();  // faces index the previous particles
+  return upload_particles(ctx, n_tanks, tanks, r, v, rho);
+}
+
+}  // extern "C"
+
+namespace {
+
+int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
+                     const double* r, const double* v, const double* rho) {
   Context& C = ctx->c;
   const int dim = C.P.dim;
   if (n_tanks < 1 || tanks == nullptr) {
@@ -532,6 +547,10 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   C.walls_fresh = false;
   return TG_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int tg_particles_update(tg_context* ctx, const double* r, const double* v,
                         const double* rho, const double* dv_dt) {
@@ -836,6 +855,165 @@ int tg_timer_stop(tg_context* ctx, double* ms) {
   return TG_OK;
 }
 
+// ---- boundary faces ------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// Device tables of the boundary faces of every tank (face_host): segments
+// and vertex ids, per-cell face lists (each face registered in every cell of
+// its bounding box grown by the support radius, so a cell's list holds
+// every face within reach of its points, ascending), per-row containment
+// edge lists, and the per-particle gamma buffers.
+int build_faces(tg_context* ctx) {
+  Context& C = ctx->c;
+  C.faces = tg::FaceArgs{};
+  bool any = false;
+  for (const auto& t : C.face_host) any = any || !t.face_verts.empty();
+  if (!any) return TG_OK;
+  const int32_t nt = C.ntanks;
+  // Fixed-particle positions (the face vertices).
+  std::vector<double> r(static_cast<size_t>(C.n) * 2);
+  int st = tg_particles_download(ctx, TG_FIELD_R, r.data());
+  if (st != TG_OK) return st;
+  const double unit_radius = tg::kernel_unit_radius(C.P.kernel);
+  std::vector<double> seg, edges;
+  std::vector<uint32_t> vert;
+  std::vector<uint32_t> cell_count(static_cast<size_t>(C.total_cells) + 1, 0);
+  std::vector<std::pair<uint32_t, uint32_t>> cell_pairs;  // (cell, face)
+  std::vector<uint32_t> row_off(static_cast<size_t>(nt), 0), tank_edges(static_cast<size_t>(nt), 0);
+  uint32_t total_rows = 0;
+  for (int32_t t = 0; t < nt; ++t) {
+    row_off[t] = total_rows;
+    total_rows += static_cast<uint32_t>(C.tankdev[t].nc[1]);
+  }
+  std::vector<std::vector<uint32_t>> row_lists(total_rows);
+  for (int32_t t = 0; t < nt; ++t) {
+    if (static_cast<size_t>(t) >= C.face_host.size()) break;
+    const auto& F = C.face_host[t];
+    if (F.face_verts.empty()) continue;
+    const tg::TankDev& T = C.tankdev[t];
+    const double R = unit_radius * C.tanks[t].h;
+    auto cell_index = [&](double x, int k) {
+      const double f = std::floor((x - T.lo[k]) * T.inv_cs);
+      return static_cast<int>(std::min(std::max(f, 0.0), static_cast<double>(T.nc[k] - 1)));
+    };
+    for (size_t f = 0; f < F.face_verts.size() / 2; ++f) {
+      const uint32_t u0 = C.wall_from[t] + static_cast<uint32_t>(F.face_verts[2 * f]);
+      const uint32_t u1 = C.wall_from[t] + static_cast<uint32_t>(F.face_verts[2 * f + 1]);
+      const double ax = r[2 * u0], ay = r[2 * u0 + 1], bx = r[2 * u1], by = r[2 * u1 + 1];
+      const uint32_t gf = static_cast<uint32_t>(vert.size() / 2);
+      seg.insert(seg.end(), {ax, ay, bx, by});
+      vert.insert(vert.end(), {u0, u1});
+      const int x0 = cell_index(std::min(ax, bx) - R, 0), x1 = cell_index(std::max(ax, bx) + R, 0);
+      const int y0 = cell_index(std::min(ay, by) - R, 1), y1 = cell_index(std::max(ay, by) + R, 1);
+      for (int y = y0; y <= y1; ++y) {
+        for (int x = x0; x <= x1; ++x) {
+          const uint32_t gc = T.cell_off + static_cast<uint32_t>(y) * T.nc[0] + x;
+          cell_pairs.emplace_back(gc, gf);
+          ++cell_count[gc];
+        }
+      }
+    }
+    const size_t np = F.poly.size() / 2;
+    for (size_t e = 0; e < np; ++e) {
+      const size_t e1 = (e + 1) % np;
+      const double x0 = F.poly[2 * e], y0 = F.poly[2 * e + 1];
+      const double x1 = F.poly[2 * e1], y1 = F.poly[2 * e1 + 1];
+      const uint32_t ge = static_cast<uint32_t>(edges.size() / 4);
+      edges.insert(edges.end(), {x0, y0, x1, y1});
+      const int r0 = cell_index(std::min(y0, y1), 1), r1 = cell_index(std::max(y0, y1), 1);
+      for (int y = r0; y <= r1; ++y) row_lists[row_off[t] + y].push_back(ge);
+      ++tank_edges[t];
+    }
+  }
+  // CSR of the per-cell face lists (faces ascending within each cell).
+  std::vector<uint32_t> cell_start(static_cast<size_t>(C.total_cells) + 1, 0);
+  for (uint32_t c = 0; c < C.total_cells; ++c) cell_start[c + 1] = cell_start[c] + cell_count[c];
+  std::vector<uint32_t> cell_face(cell_pairs.size() > 0 ? cell_pairs.size() : 1);
+  {
+    std::vector<uint32_t> fill(cell_start.begin(), cell_start.end() - 1);
+    for (const auto& [gc, gf] : cell_pairs) cell_face[fill[gc]++] = gf;
+  }
+  std::vector<uint32_t> row_start(static_cast<size_t>(total_rows) + 1, 0), row_edge;
+  for (uint32_t y = 0; y < total_rows; ++y) {
+    row_start[y + 1] = row_start[y] + static_cast<uint32_t>(row_lists[y].size());
+    row_edge.insert(row_edge.end(), row_lists[y].begin(), row_lists[y].end());
+  }
+  if (row_edge.empty()) row_edge.push_back(0);
+  if (edges.empty()) edges.assign(4, 0.0);
+  tg::FaceArgs fa{};
+  auto up = [&](auto*& dst, const auto& src) -> cudaError_t {
+    using T = std::remove_const_t<std::remove_pointer_t<std::remove_reference_t<decltype(dst)>>>;
+    void* p = nullptr;
+    cudaError_t e = C.alloc(&p, sizeof(T) * src.size());
+    if (e == cudaSuccess) {
+      e = cudaMemcpyAsync(p, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, C.stream);
+    }
+    dst = static_cast<T*>(p);
+    return e;
+  };
+  TG_CUDA(&C, up(fa.seg, seg));
+  TG_CUDA(&C, up(fa.vert, vert));
+  TG_CUDA(&C, up(fa.cell_start, cell_start));
+  TG_CUDA(&C, up(fa.cell_face, cell_face));
+  TG_CUDA(&C, up(fa.poly_edge, edges));
+  TG_CUDA(&C, up(fa.row_start, row_start));
+  TG_CUDA(&C, up(fa.row_edge, row_edge));
+  TG_CUDA(&C, up(fa.row_off, row_off));
+  TG_CUDA(&C, up(fa.tank_edges, tank_edges));
+  const int64_t nn = C.n > 0 ? C.n : 1;
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.slot_of), sizeof(uint32_t) * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.gamma), sizeof(double) * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.ggam), sizeof(double) * 2 * nn));
+  fa.weight = kernel_weight(C.P.kernel, 2);
+  fa.on = 1;
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  C.faces = fa;
+  C.invalidate_graph();
+  C.walls_fresh = false;
+  return TG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tg_tank_faces(tg_context* ctx, int32_t tank, int32_t n_faces,
+                  const int32_t* face_verts, int32_t n_poly,
+                  const double* poly) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (C.P.dim != 2 || C.P.precision != TG_FP64) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT,
+                "boundary faces run in 2D with the FP64 form");
+  }
+  if (tank < 0 || tank >= C.ntanks || n_faces < 0) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "bad tank or face count");
+  }
+  if (n_faces > 0 && (face_verts == nullptr || n_poly < 3 || poly == nullptr)) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT,
+                "faces need vertex pairs and a containment polygon");
+  }
+  for (int32_t i = 0; i < 2 * n_faces; ++i) {
+    if (face_verts[i] < 0 || face_verts[i] >= C.tanks[tank].n_wall) {
+      return fail(&C, TG_ERR_INVALID_ARGUMENT,
+                  "face vertex is not a fixed particle of the tank");
+    }
+  }
+  for (int32_t i = 0; i < 2 * n_poly; ++i) {
+    if (!std::isfinite(poly[i])) {
+      return fail(&C, TG_ERR_INVALID_ARGUMENT, "non-finite containment polygon");
+    }
+  }
+  if (C.face_host.size() < static_cast<size_t>(C.ntanks)) C.face_host.resize(C.ntanks);
+  auto& F = C.face_host[tank];
+  F.face_verts.assign(face_verts, face_verts + 2 * static_cast<size_t>(n_faces));
+  F.poly.assign(poly, poly + (n_faces > 0 ? 2 * static_cast<size_t>(n_poly) : 0));
+  return build_faces(ctx);
+}
+
 // ---- launch-shape tuning -----------------------------------------------
 }  // extern "C"
 
@@ -877,18 +1055,22 @@ int restore_snapshot(tg_context* ctx, const Snapshot& S, int k) {
     C.k = k;
     C.P.cells_per_radius = k;
     const std::vector<tg_tank> tanks = C.tanks;
-    const int st = tg_particles_upload(ctx, C.ntanks, tanks.data(), S.r.data(),
-                                       S.v.data(), S.rho.data());
+    int st = upload_particles(ctx, C.ntanks, tanks.data(), S.r.data(),
+                              S.v.data(), S.rho.data());
     if (st != TG_OK) {
       // Back to the old grid (the same data fitted it before).
       C.k = old_k;
       C.P.cells_per_radius = old_k;
       const std::string why = C.last_error;
-      tg_particles_upload(ctx, C.ntanks, tanks.data(), S.r.data(), S.v.data(),
-                          S.rho.data());
+      upload_particles(ctx, C.ntanks, tanks.data(), S.r.data(), S.v.data(),
+                       S.rho.data());
+      build_faces(ctx);
       C.last_error = why;
       return st;
     }
+    // The new grid needs new face tables.
+    st = build_faces(ctx);
+    if (st != TG_OK) return st;
   }
   const int st = tg_particles_update(ctx, S.r.data(), S.v.data(), S.rho.data(),
                                      S.dv.data());

@@ -9,7 +9,7 @@
 
 #include <cuda_runtime.h>
 
-#include "common.cuh"
+#include "faces.cuh"
 
 namespace tg {
 
@@ -93,6 +93,16 @@ struct Context {
   // Launch shape of the force pass (tg_set_tuning / tg_autotune).
   int force_block = 128;
   int force_team = 1;
+  // Boundary faces (tg_tank_faces): host copies per tank and the device
+  // view; faces.on = 0 with particle walls.
+  struct TankFaces {
+    std::vector<int32_t> face_verts;  // 2 per face, tank-local fixed index
+    std::vector<double> poly;         // 2 per containment vertex
+  };
+  std::vector<TankFaces> face_host;
+  FaceArgs faces{};
+  std::vector<void*> face_allocations;
+
   double post_cos2_fov = 0.0;  // cos(pi/4)^2 of the visibility cone
   double post_k_fs = 0.0;      // -log(0.05) / 0.01^2
   double tuned_ms = 0.0;  // device time per step of the tuned shape

@@ -185,6 +185,7 @@ class Engine final : public EngineBase {
     if (e != cudaSuccess) return e;
     tok = C.group_begin(kGroupWalls);
     if (C.n_wall > 0) {
+      enqueue_gamma(C, a);
       k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
           a, C.n_wall);
       C.launches += 1;
@@ -263,10 +264,11 @@ class Engine final : public EngineBase {
     const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
     const int stages = force_passes(C.P.integrator);
     const int per_stage = 3 * passes + 2 + 2 + (C.n_wall > 0 ? 1 : 0);
+    const int gam = C.faces.on ? 1 : 0;
     const int post = C.P.post_integrate == TG_POST_SHIFTING
-                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 : 0) + 5
+                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + gam : 0) + 5
                          : 0;
-    return static_cast<int64_t>(stages) * per_stage + post + 1;
+    return static_cast<int64_t>(stages) * (per_stage + gam) + post + 1;
   }
 
  private:
@@ -291,6 +293,7 @@ class Engine final : public EngineBase {
     // The wall pass's fluid-box early-out pays when walls are a sizeable
     // share of the particles (it costs a fold in every reorder).
     a.fbox = C.n_wall > 0 && 4 * C.n_wall >= C.n_fluid ? C.d_fbox : nullptr;
+    a.fc = C.faces;
     a.err = C.d_err;
     a.n = C.n;
     a.k = C.k;
@@ -355,6 +358,7 @@ class Engine final : public EngineBase {
     e = reorder(C, a);
     if (e != cudaSuccess) return e;
     if (C.n_wall > 0) {
+      enqueue_gamma(C, a);
       k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
           a, C.n_wall);
       C.launches += 1;
@@ -374,6 +378,17 @@ class Engine final : public EngineBase {
     C.group_end(tok);
     C.keys_valid = true;
     return cudaGetLastError();
+  }
+
+  // Face boundaries: gamma and grad gamma of every particle at the positions
+  // of this prepare (before the wall pass, which reads grad gamma).
+  void enqueue_gamma(Context& C, const StageArgs<D, F>& a) {
+    if constexpr (D == 2 && F == TG_FP64) {
+      if (a.fc.on) {
+        k_gamma<K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+        C.launches += 1;
+      }
+    }
   }
 
   // One force pass of a step: its index (stage 0 copies the start state
@@ -403,6 +418,7 @@ class Engine final : public EngineBase {
     if (e != cudaSuccess) return e;
     if (C.n_wall > 0) {
       tok = C.group_begin(kGroupWalls);
+      enqueue_gamma(C, a);
       k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
           a, C.n_wall);
       C.launches += 1;

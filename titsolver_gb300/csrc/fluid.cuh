@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "faces.cuh"
 
 namespace tg {
 
@@ -149,6 +150,7 @@ struct StageArgs {
   int mode;          // update rule of the force pass (kPass*)
   int walls_keep;    // k_walls: keep the carried wall densities
   unsigned* fbox;     // per-tank fluid bounding box (k_reorder)
+  FaceArgs fc;        // boundary faces (fc.on = 0: particle walls)
 };
 
 // Order-preserving map of floats to unsigned 32-bit integers (and back),
@@ -728,6 +730,13 @@ __global__ void __launch_bounds__(128)
       skip = beyond_fluid<D>(A.fbox, A.ntanks, tk, T, xl);
     }
     skip = __shfl_sync(0xffffffffu, skip, 0, kWallTeam);
+    // Face boundaries: the wall normal n_e = normalize(grad gamma) and the
+    // hydrostatic term g (r_be . n_e) n_e[1] (fluid_equations.hpp:146-160);
+    // zero with particle walls.
+    double ne[3] = {0.0, 0.0, 0.0};
+    if constexpr (D == 2) {
+      if (A.fc.on && valid) normalize2(A.fc.ggam + 2 * static_cast<size_t>(e), ne);
+    }
     if (valid && !A.walls_keep && !skip) {
       auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
         for (uint32_t j = s; j < en; ++j) {
@@ -738,7 +747,10 @@ __global__ void __launch_bounds__(128)
           const Dat64 b = load_dat_coherent(A.datrec, j);
           const double W = w * KernelPoly<K>::value(sqrt(s2) * hinv);
           const double Vb = m * b.invrho;
-          const double Hb = potential_f64(A.phys, T, b.rho);
+          double Hb = potential_f64(A.phys, T, b.rho);
+          if constexpr (D == 2) {
+            if (A.fc.on) Hb += A.phys.g * (d[0] * ne[0] + d[1] * ne[1]) * ne[1];
+          }
           S += Vb * W;
           H += Vb * Hb * W;
         }
@@ -1077,6 +1089,56 @@ __device__ __forceinline__ void forces_epilogue(
   }
 }
 
+// Face boundaries, FP64 form (fluid_equations.hpp:241-247, 276-292): the
+// pair sums divided by gamma_a, then per adjacent face s (vertex pair, whose
+// fields are averages; vertices have zero velocity)
+//   drho_a -= rho_s (v_as . grad gamma_as) / gamma_a
+//   dv_a   += (P_as grad gamma_as - Pi_as |grad gamma_as|) / gamma_a,
+//   P_as = rho_s (p_a / rho_a^2 + p_s / rho_s^2),
+//   Pi_as = 2 mu / (rho_a dr_as) (v_as . t_as) t_as,
+//   dr_as = max(h / 2, (r_a - r_s) . n_s), n_s = normalize(grad gamma_as),
+//   t_as = normalize(v_as - (v_as . n_s) n_s),
+// and gravity -g e_1.
+template<int K, int F>
+__device__ __forceinline__ void face_terms(const StageArgs<2, F>& A,
+                                           const TankDev& T, const int* c,
+                                           int64_t i, const double* pa,
+                                           const Dat64& a, double& drho,
+                                           double* dv) {
+  const double gam = A.fc.gamma[i];
+  drho /= gam;
+  dv[0] /= gam;
+  dv[1] /= gam;
+  const uint32_t gcell = T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
+  const double radius = KernelPoly<K>::unit_radius * T.h;
+  const double va[2] = {a.vx, a.vy};
+  for_adjacent_faces(A.fc, gcell, pa, radius, [&](uint32_t f, const double* ab) {
+    double gg[2];
+    face_flux<K>(ab, pa, T.h, A.fc.weight, gg);
+    const Dat64 v0 = load_dat(A.datrec, A.fc.slot_of[A.fc.vert[2 * f]]);
+    const Dat64 v1 = load_dat(A.datrec, A.fc.slot_of[A.fc.vert[2 * f + 1]]);
+    const double rho_s = (v0.rho + v1.rho) / 2.0;
+    double p0, p1, c0, c1;
+    tait_f64(A.phys, T, v0.rho, p0, c0);
+    tait_f64(A.phys, T, v1.rho, p1, c1);
+    const double p_s = (p0 + p1) / 2.0;
+    drho -= rho_s * (va[0] * gg[0] + va[1] * gg[1]) / gam;
+    const double P_as = rho_s * (a.P + p_s / (rho_s * rho_s));
+    double n_s[2], t_as[2];
+    normalize2(gg, n_s);
+    const double vn = va[0] * n_s[0] + va[1] * n_s[1];
+    const double vt[2] = {va[0] - vn * n_s[0], va[1] - vn * n_s[1]};
+    normalize2(vt, t_as);
+    const double r_as[2] = {pa[0] - (ab[0] + ab[2]) / 2.0, pa[1] - (ab[1] + ab[3]) / 2.0};
+    const double dr_as = fmax(T.h / 2.0, r_as[0] * n_s[0] + r_as[1] * n_s[1]);
+    const double Pi_s = 2.0 * A.phys.mu / (a.rho * dr_as) * (va[0] * t_as[0] + va[1] * t_as[1]);
+    const double ng = sqrt(gg[0] * gg[0] + gg[1] * gg[1]);
+    dv[0] += (P_as * gg[0] - Pi_s * t_as[0] * ng) / gam;
+    dv[1] += (P_as * gg[1] - Pi_s * t_as[1] * ng) / gam;
+  });
+  dv[1] += -A.phys.g;
+}
+
 // Team lanes share one target: each takes every Team-th cell of the block
 // and the team merges its partial sums by shuffles (compensated merges in
 // the FP32 form), so a warp advances 32 / Team targets.  The block size is
@@ -1115,7 +1177,9 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     const double mu2 = 2.0 * A.phys.mu, ah = A.phys.alpha * T.h;
     const double eps2 = T.visc_eps2, dk = T.diff_k;
     double drho = 0.0;
-    double dv[3] = {0.0, lane == 0 ? -A.phys.g : 0.0, 0.0};
+    // Face boundaries: gravity is added after the gamma division.
+    const bool faces = D == 2 && A.fc.on;
+    double dv[3] = {0.0, (lane == 0 && !faces) ? -A.phys.g : 0.0, 0.0};
     auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
       for (uint32_t j = s; j < en; ++j) {
         if (j == static_cast<uint32_t>(i)) continue;
@@ -1167,6 +1231,9 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
         for (int k = 0; k < D; ++k) dv[k] += __shfl_xor_sync(mask, dv[k], o, Team);
       }
       if (lane != 0) return;
+    }
+    if constexpr (D == 2) {
+      if (faces) face_terms<K>(A, T, c, i, pa, a, drho, dv);
     }
 #pragma unroll
     for (int k = 0; k < D; ++k) dv_out[k] = dv[k];
@@ -1540,6 +1607,48 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
   if (A.rho != nullptr) A.rho[id] = rho;
   if (A.counts != nullptr) A.counts[id] = cnt;
   if (A.hashes != nullptr) A.hashes[id] = hs;
+}
+
+// ---------------------------------------------------------------------------
+// gamma and grad gamma of every particle (FluidEquations::compute_gamma,
+// fluid_equations.hpp:166-193); also records the cell-order slot of each
+// fixed particle for the face terms' vertex lookups.
+template<int K>
+__global__ void __launch_bounds__(128) k_gamma(StageArgs<2, TG_FP64> A) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const FaceArgs& fc = A.fc;
+  const uint32_t id = A.Y.id[i];
+  if (id & kWallBit) fc.slot_of[id & kIdMask] = static_cast<uint32_t>(i);
+  const uint32_t key = A.skey[i];
+  const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
+  const TankDev& T = A.tanks[tk];
+  int c[3] = {0, 0, 0};
+  cell_from_key<2>(T, key, c);
+  const uint32_t gcell = T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
+  const double x[2] = {A.Y.pos[0][i], A.Y.pos[1][i]};
+  const double radius = KernelPoly<K>::unit_radius * T.h;
+  const double wd = fc.weight;
+  double g[2] = {0.0, 0.0};
+  for_adjacent_faces(fc, gcell, x, radius, [&](uint32_t, const double* ab) {
+    double fl[2];
+    face_flux<K>(ab, x, T.h, wd, fl);
+    g[0] += fl[0];
+    g[1] += fl[1];
+  });
+  double ga = face_contains(fc, tk, fc.row_off[tk] + c[1], x) ? 1.0 : 0.0;
+  const double ng = sqrt(g[0] * g[0] + g[1] * g[1]);
+  if (!(ng <= kTiny)) {
+    const double s = 2.0 * ga - 1.0;
+    const double h2 = T.h * T.h;
+    const double xs[2] = {x[0] + s * (g[0] / ng) * h2, x[1] + s * (g[1] / ng) * h2};
+    for_adjacent_faces(fc, gcell, x, radius, [&](uint32_t, const double* ab) {
+      ga -= face_antigrad_flux<K>(ab, xs, T.h, wd);
+    });
+  }
+  fc.gamma[i] = ga;
+  fc.ggam[2 * i] = g[0];
+  fc.ggam[2 * i + 1] = g[1];
 }
 
 // ---------------------------------------------------------------------------

@@ -22,6 +22,7 @@
 //                 the prepare's neighbours at the shifted positions
 #pragma once
 
+#include "faces.cuh"
 #include "fluid.cuh"
 
 namespace tg {
@@ -165,6 +166,34 @@ __global__ void __launch_bounds__(128) k_post_sums(PostArgs<D, F> A) {
   double N[D] = {}, L[D * D] = {}, gv[D * D] = {}, gr[D] = {};
   int32_t count = 0;
   const double tiny2 = 6.0554544523933395e-06 * 6.0554544523933395e-06;
+  // Face boundaries (fluid_equations.hpp:335-349): face terms first, and
+  // every sum divided by gamma_a.
+  double gam = 1.0;
+  if constexpr (D == 2 && F == TG_FP64) {
+    if (A.S.fc.on) {
+      gam = A.S.fc.gamma[i];
+      const uint32_t gcell =
+          T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
+      const double radius = KernelPoly<K>::unit_radius * T.h;
+      for_adjacent_faces(A.S.fc, gcell, pa, radius, [&](uint32_t f, const double* ab) {
+        double gg[2];
+        face_flux<K>(ab, pa, T.h, A.S.fc.weight, gg);
+        const Dat64 v0 = load_dat(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f]]);
+        const Dat64 v1 = load_dat(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f + 1]]);
+        const double r_sa[2] = {(ab[0] + ab[2]) / 2.0 - pa[0], (ab[1] + ab[3]) / 2.0 - pa[1]};
+        const double v_sa[2] = {-va[0], -va[1]};
+        const double rho_sa = (v0.rho + v1.rho) / 2.0 - rho_a;
+        for (int a2 = 0; a2 < 2; ++a2) {
+          N[a2] -= gg[a2] / gam;
+          for (int b2 = 0; b2 < 2; ++b2) {
+            L[a2 * D + b2] -= r_sa[a2] * gg[b2] / gam;
+            gv[a2 * D + b2] -= v_sa[a2] * gg[b2] / gam;
+          }
+          gr[a2] -= rho_sa * gg[a2] / gam;
+        }
+      });
+    }
+  }
   for_cells<D, false>(T, c, A.S.k, A.S.cell_start,
                       [&](uint32_t s, uint32_t en, int, int, int) {
     for (uint32_t j = s; j < en; ++j) {
@@ -185,7 +214,7 @@ __global__ void __launch_bounds__(128) k_post_sums(PostArgs<D, F> A) {
       for (int k = 0; k < D; ++k) gW[k] = f * ((d[k] * sc) * T.hinv);
       double rho_b, vb[3];
       post_neighbour<D>(A.S.datrec, j, T, rho_b, vb);
-      const double V = T.m / rho_b;
+      const double V = T.m / rho_b / gam;
       const double drb = rho_b - rho_a;
 #pragma unroll
       for (int a = 0; a < D; ++a) {
@@ -368,11 +397,15 @@ __global__ void __launch_bounds__(128) k_post_shift(PostArgs<D, F> A) {
     for (int k = 0; k < D; ++k) dr[k] = A.dr[i * D + k] * sc;
 #pragma unroll
     for (int k = 0; k < D; ++k) p[k] += dr[k];
-    double dv[D];
+    // The velocity correction applies where gamma ~ 1 (:465-467).
+    const double gam = A.S.fc.on ? A.S.fc.gamma[i] : 1.0;
+    if (fabs(gam - 1.0) <= 6.0554544523933395e-06) {
+      double dv[D];
 #pragma unroll
-    for (int a = 0; a < D; ++a) dv[a] = dot_rn(A.gv + (i * D + a) * D, dr, D);
+      for (int a = 0; a < D; ++a) dv[a] = dot_rn(A.gv + (i * D + a) * D, dr, D);
 #pragma unroll
-    for (int k = 0; k < D; ++k) v[k] += dv[k];
+      for (int k = 0; k < D; ++k) v[k] += dv[k];
+    }
     rho += dot_rn(A.grho + i * D, dr, D);
   }
   A.rho_raw[i] = rho;
@@ -439,10 +472,11 @@ __global__ void __launch_bounds__(128) k_post_fs(PostArgs<D, F> A) {
       rho_t += T.m * W;
     }
   });
-  const double ratio = fmin(1.0, alpha / 1.0);
+  const double gam = A.S.fc.on ? A.S.fc.gamma[i] : 1.0;
+  const double ratio = fmin(1.0, alpha / gam);
   if (ratio > 0.99) return;
   const double beta = exp(-A.k_fs * ((ratio - 1.0) * (ratio - 1.0)));
-  const double corr = beta * 1.0 + (1.0 - beta) * alpha;
+  const double corr = beta * gam + (1.0 - beta) * alpha;
   if (fabs(corr) <= 6.0554544523933395e-06) return;
   const double rho = rho_t / corr;
   if constexpr (F == TG_FP64) {

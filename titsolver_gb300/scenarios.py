@@ -73,6 +73,60 @@ def dam_break_2d(H: float = 1.0, nx_per_H: int = 80, column=(2.0, 1.0),
                 H=H, width=nW * dx, name=f"dam_break_2d_H{H}_dx1/{nx_per_H}")
 
 
+def rectangle_faces(width: float, height: float, dx: float):
+    """The titwcsph domain (source/titwcsph/wcsph.cpp:55-65): a rectangle
+    with vertices (0, Ht), (W, Ht), (W, 0), (0, 0) and faces 0-1, 1-2, 2-3,
+    3-0, tessellated as geom::tessellate does (geom/tessellation.hpp:30-60:
+    the original vertices first, then each face split into
+    max(1, ceil(len / dx)) pieces with the new vertices appended in order).
+    Returns (vertices (n, 2), faces (m, 2))."""
+    verts = [(0.0, height), (width, height), (width, 0.0), (0.0, 0.0)]
+    faces_in = [(0, 1), (1, 2), (2, 3), (3, 0)]
+    out_v = list(verts)
+    out_f = []
+    for a, b in faces_in:
+        pa, pb = np.array(verts[a]), np.array(verts[b])
+        length = float(np.hypot(*(pb - pa)))
+        n = max(1, int(math.ceil(length / dx)))
+        prev = a
+        for i in range(1, n):
+            t = i / n
+            out_v.append(tuple(pa + t * (pb - pa)))
+            out_f.append((prev, len(out_v) - 1))
+            prev = len(out_v) - 1
+        out_f.append((prev, b))
+    return np.array(out_v, dtype=np.float64), np.array(out_f, dtype=np.int32)
+
+
+def dam_break_2d_faces(nx_per_H: int = 80, H: float = 0.6, g: float = G,
+                       rho0: float = RHO0) -> dict:
+    """The titwcsph scenario itself (source/titwcsph/wcsph.cpp:37-142):
+    H = 0.6, column 2H x H at dr (i + 1, j + 1), pool 5.366H x 4H whose
+    tessellated boundary faces carry one fixed particle per vertex,
+    cs0 = 20 sqrt(gH), h = 2 dr, m = rho0 dr^2, hydrostatic density; the
+    containment polygon is the pool rectangle counter-clockwise (domain2 of
+    wcsph.cpp:67-77).  Returns a scenario with "faces"."""
+    dx = H / nx_per_H
+    L = 2.0 * H
+    M = int(round(L / dx))
+    N = int(round(H / dx))
+    i, j = np.meshgrid(np.arange(M), np.arange(N), indexing="ij")
+    fluid = np.stack([dx * (i.ravel() + 1.0), dx * (j.ravel() + 1.0)], axis=1)
+    W, Ht = 5.366 * H, 4.0 * H
+    walls, faces = rectangle_faces(W, Ht, dx)
+    cs0 = 20.0 * math.sqrt(g * H)
+    p = hydrostatic_pressure(fluid[:, 0], fluid[:, 1], H, L, g, rho0)
+    rho_f = rho0 + p / (cs0 * cs0)
+    r = np.concatenate([fluid, walls])
+    rho = np.concatenate([rho_f, np.full(walls.shape[0], rho0)])
+    tank = dict(n_fluid=fluid.shape[0], n_wall=walls.shape[0], h=2.0 * dx,
+                m=rho0 * dx * dx, rho0=rho0, cs0=cs0)
+    poly = np.array([(0.0, 0.0), (W, 0.0), (W, Ht), (0.0, Ht)])
+    return dict(dim=2, tanks=[tank], r=r, v=np.zeros_like(r), rho=rho, dx=dx, H=H,
+                faces=[dict(face_verts=faces, poly=poly)],
+                name=f"titwcsph_faces_dx=H/{nx_per_H}")
+
+
 def dam_break_3d(H: float = 1.0, nx_per_H: int = 200, column=(2.0, 1.0, 1.0),
                  tank=(5.366, 3.0), layers: int = 3, cs0_factor: float = 10.0,
                  h_factor: float = 1.3, g: float = G, rho0: float = RHO0) -> dict:
