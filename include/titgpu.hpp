@@ -28,10 +28,13 @@
  * (tg_particles_update) before the next step.  Errors throw tit::Exception,
  * as TIT_ENSURE does (source/tit/core/exception.hpp:81).
  *
- * Walls are fixed particles ("particle walls, no faces"): the domain surface
- * must be empty and every fluid particle must lie inside the containment,
- * which then gives gamma = 1 and no face terms in the reference equations
- * (fluid_equations.hpp:122-163).  A non-empty surface throws.
+ * Walls: either fixed particles with an empty domain surface ("particle
+ * walls": gamma = 1 and no face terms, fluid_equations.hpp:122-163), or,
+ * in 2D with the FP64 form, the reference's semi-analytical face walls: a
+ * tessellated domain surface whose vertices are the fixed particles and a
+ * winding-number containment (geom::MakeFastWinding), as titwcsph sets up
+ * (wcsph.cpp:55-77, 109-112).  Every fluid particle must lie inside the
+ * containment.
  *
  * GPU-only choices (precision form, the textbook term set, CFL constants)
  * come in an optional trailing sph::GpuOptions argument of FluidEquations.
@@ -39,6 +42,7 @@
 #ifndef TITGPU_HPP
 #define TITGPU_HPP
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstddef>
@@ -135,9 +139,10 @@ Vec(T, U...) -> Vec<std::common_type_t<T, U...>, 1 + sizeof...(U)>;
 
 namespace geom {
 
-/// Boundary surface.  The GPU path runs with particle walls, so a surface
-/// handed to FluidEquations must stay empty; the type exists so that a
-/// driver's domain declaration compiles.
+/// Boundary surface (source/tit/geom/surface.hpp): vertices and faces
+/// (segments in 2D).  An empty surface means particle walls; a 2D surface
+/// with faces selects the semi-analytical wall mode, whose fixed particles
+/// are the surface's vertices in order (wcsph.cpp:109-112).
 template<class V>
 class Surface {
 public:
@@ -151,10 +156,86 @@ public:
   auto num_verts() const noexcept -> std::size_t { return verts_.size(); }
   auto num_faces() const noexcept -> std::size_t { return faces_.size(); }
   auto vert(std::size_t i) const -> const V& { return verts_.at(i); }
+  auto face_verts(std::size_t i) const -> const std::array<std::size_t, V::dim()>& {
+    return faces_.at(i);
+  }
 
 private:
   std::vector<V> verts_;
   std::vector<std::array<std::size_t, V::dim()>> faces_;
+};
+
+/// Split every face into max(1, ceil(length / d_max)) segments: the
+/// original vertices first, then each face's new vertices in order
+/// (source/tit/geom/tessellation.hpp:30-60).
+template<class V>
+auto tessellate(const Surface<V>& surf, double d_max) -> Surface<V> {
+  if (!(d_max > 0.0)) throw Exception{"tessellate: d_max <= 0"};
+  Surface<V> out;
+  for (std::size_t i = 0; i < surf.num_verts(); ++i) out.append_vert(surf.vert(i));
+  using Num = std::remove_cvref_t<decltype(surf.vert(0)[0])>;
+  for (std::size_t fi = 0; fi < surf.num_faces(); ++fi) {
+    const auto [ia, ib] = surf.face_verts(fi);
+    const V a = surf.vert(ia), b = surf.vert(ib);
+    const V ba = b - a;
+    const double len = std::sqrt(static_cast<double>(ba[0] * ba[0] + ba[1] * ba[1]));
+    const auto n = std::max<std::size_t>(
+        1, static_cast<std::size_t>(std::ceil(len / d_max)));
+    std::size_t prev = ia;
+    for (std::size_t i = 1; i < n; ++i) {
+      const Num t = static_cast<Num>(i) / static_cast<Num>(n);
+      out.append_vert(a + t * ba);
+      const std::size_t vi = out.num_verts() - 1;
+      out.append_face({prev, vi});
+      prev = vi;
+    }
+    out.append_face({prev, ib});
+  }
+  return out;
+}
+
+/// Containment by the winding number of a closed polygon (> 1/2 inside),
+/// the role of the reference's FastWinding (fast_winding.hpp:80-95); the
+/// GPU receives the polygon itself.
+template<class V>
+class Winding {
+public:
+  explicit Winding(const Surface<V>& surf) {
+    for (std::size_t fi = 0; fi < surf.num_faces(); ++fi) {
+      loop_.push_back(surf.vert(surf.face_verts(fi)[0]));
+    }
+  }
+  auto operator()(const V& x) const -> double {
+    double w = 0.0;
+    for (std::size_t i = 0; i < loop_.size(); ++i) {
+      const V a = loop_[i] - x, b = loop_[(i + 1) % loop_.size()] - x;
+      w += std::atan2(static_cast<double>(a[0] * b[1] - a[1] * b[0]),
+                      static_cast<double>(a[0] * b[0] + a[1] * b[1]));
+    }
+    return w / (2.0 * 3.14159265358979323846);
+  }
+  auto contains(const V& x) const -> bool { return (*this)(x) > 0.5; }
+  auto polygon() const -> std::vector<double> {
+    std::vector<double> out;
+    for (const V& v : loop_) {
+      out.push_back(static_cast<double>(v[0]));
+      out.push_back(static_cast<double>(v[1]));
+    }
+    return out;
+  }
+
+private:
+  std::vector<V> loop_;
+};
+
+/// Maker of winding-number containment functions (the reference's
+/// MakeFastWinding, fast_winding.hpp).
+template<class Num>
+struct MakeFastWinding {
+  template<class V>
+  auto operator()(const Surface<V>& surf) const -> Winding<V> {
+    return Winding<V>{surf};
+  }
 };
 
 /// Grid neighbour search with the given cell spacing
@@ -314,11 +395,16 @@ public:
                  TaitEquationOfState<Real> eos,
                  Kernel /*kernel*/,
                  GpuOptions options = {})
-      : g_{g}, mu_{mu}, containment_{std::move(containment)}, eos_{eos},
-        options_{options} {
-    if (domain.num_faces() != 0) {
-      throw Exception{"FluidEquations: the GPU path runs with particle walls; "
-                      "the domain surface must be empty"};
+      : g_{g}, mu_{mu}, domain_{std::move(domain)},
+        containment_{std::move(containment)}, eos_{eos}, options_{options} {
+    if (domain_.num_faces() != 0) {
+      if constexpr (Dim != 2 || !has_polygon_) {
+        throw Exception{"FluidEquations: boundary faces need 2D and a "
+                        "winding-number containment (geom::MakeFastWinding)"};
+      }
+      if (options_.precision != Precision::fp64) {
+        throw Exception{"FluidEquations: boundary faces run in the FP64 form"};
+      }
     }
   }
 
@@ -327,7 +413,7 @@ public:
   template<class PA>
   void initialize(ParticleMesh& mesh, PA& particles) const {
     for (const auto a : particles.fluid()) {
-      if (!containment_(std::as_const(particles).position(a.index()))) {
+      if (!contains_(std::as_const(particles).position(a.index()))) {
         throw Exception{"FluidEquations::initialize: a fluid particle lies "
                         "outside the containment (gamma = 0)"};
       }
@@ -359,14 +445,62 @@ public:
                       static_cast<double>(eos_.rho_0()),
                       static_cast<double>(eos_.cs_0()),
                       options_.graph,
-                      options_.autotune);
+                      options_.autotune && domain_.num_faces() == 0);
+    if constexpr (Dim == 2 && has_polygon_) {
+      if (domain_.num_faces() != 0) attach_faces_(particles);
+    }
   }
 
   auto eos() const noexcept -> const TaitEquationOfState<Real>& { return eos_; }
 
 private:
+  auto contains_(const Vec<Real, Dim>& x) const -> bool {
+    if constexpr (requires { containment_.contains(x); }) {
+      return containment_.contains(x);
+    } else {
+      return static_cast<bool>(containment_(x));
+    }
+  }
+
+  static constexpr bool has_polygon_ =
+      requires(const Containment& c) { c.polygon(); };
+
+  // The tank's fixed particles must be the domain's vertices, in order
+  // (wcsph.cpp:109-112); the faces index them.
+  template<class PA>
+  void attach_faces_(PA& particles) const {
+    const auto& cp = std::as_const(particles);
+    if (cp.size() - cp.num_fluid() < domain_.num_verts()) {
+      throw Exception{"initialize: fewer fixed particles than domain vertices"};
+    }
+    for (std::size_t i = 0; i < domain_.num_verts(); ++i) {
+      if (!(cp.position(cp.num_fluid() + i) == domain_.vert(i))) {
+        throw Exception{"initialize: fixed particle " + std::to_string(i) +
+                        " is not domain vertex " + std::to_string(i)};
+      }
+    }
+    std::vector<std::int32_t> fv;
+    for (std::size_t fi = 0; fi < domain_.num_faces(); ++fi) {
+      for (const auto v : domain_.face_verts(fi)) {
+        fv.push_back(static_cast<std::int32_t>(v));
+      }
+    }
+    const std::vector<double> poly = containment_.polygon();
+    gpu_detail::ensure(
+        tg_tank_faces(particles.context(), 0,
+                      static_cast<std::int32_t>(domain_.num_faces()), fv.data(),
+                      static_cast<std::int32_t>(poly.size() / 2), poly.data()),
+        particles.context(), "tg_tank_faces");
+    if (options_.autotune) {
+      tg_tuning tuned{};
+      gpu_detail::ensure(tg_autotune(particles.context(), 3, &tuned),
+                         particles.context(), "tg_autotune");
+    }
+  }
+
   Real g_;
   Real mu_;
+  geom::Surface<Vec<Real, Dim>> domain_;
   Containment containment_;
   TaitEquationOfState<Real> eos_;
   GpuOptions options_;

@@ -88,6 +88,43 @@ auto main(int argc, char** argv) -> int {
                        QuarticWendlandKernel{}};
   }));
   CHECK(throws([] { TaitEquationOfState{-1.0, 1000.0}; }));
+
+  // Face walls: tessellation as the reference splits faces, winding-number
+  // containment, and the FP32 form refused with faces.
+  {
+    geom::Surface<Vec<double, 2>> pool;
+    pool.append_vert({0.0, 1.0});
+    pool.append_vert({2.0, 1.0});
+    pool.append_vert({2.0, 0.0});
+    pool.append_vert({0.0, 0.0});
+    pool.append_face({0, 1});
+    pool.append_face({1, 2});
+    pool.append_face({2, 3});
+    pool.append_face({3, 0});
+    const auto t = geom::tessellate(pool, 0.25);
+    CHECK(t.num_verts() == 24 && t.num_faces() == 24);
+    CHECK(t.vert(4) == (Vec{0.25, 1.0}));  // first new vertex of face 0-1
+    geom::Surface<Vec<double, 2>> ccw;
+    ccw.append_vert({0.0, 0.0});
+    ccw.append_vert({2.0, 0.0});
+    ccw.append_vert({2.0, 1.0});
+    ccw.append_vert({0.0, 1.0});
+    for (std::size_t i = 0; i < 4; ++i) ccw.append_face({i, (i + 1) % 4});
+    const geom::MakeFastWinding<double> make_winding;
+    const auto inside = make_winding(ccw);
+    CHECK(inside.contains(Vec{1.0, 0.5}) && !inside.contains(Vec{3.0, 0.5}));
+    CHECK(inside.polygon().size() == 8);
+    const FluidEquations faced{9.81, 0.001, t, inside,
+                               TaitEquationOfState{20.0, 1000.0},
+                               SixthOrderWendlandKernel{}};
+    (void)faced;
+    GpuOptions f32;
+    f32.precision = Precision::fp32_compensated;
+    CHECK(throws([&] {
+      FluidEquations bad{9.81, 0.001, t, inside, TaitEquationOfState{20.0, 1000.0},
+                         SixthOrderWendlandKernel{}, f32};
+    }));
+  }
   CHECK(throws([] { geom::GridSearch{0.0}; }));
 
   // A fluid particle outside the containment is refused before any device

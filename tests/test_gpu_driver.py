@@ -1,7 +1,8 @@
 """The titwcsph-style C++ driver (titsolver_gb300/host/titwcsph_gpu.cpp) on
 the GPU through the C++ mirror: its initial state, run through the oracle
-(the reference term set, with or without the post-step shifting as the
-driver ran), must give its final state (plain FP64: r 1e-9, v and rho 1e-7
+(the reference term set, with or without the post-step shifting, with
+particle walls or the reference's face walls, as the driver ran), must give
+its final state (plain FP64: r 1e-9, v and rho 1e-7
 relative L2 after 20 steps; FP32-compensated: rho 1e-5, r 1e-6), and its
 .ttdb frames must hold that final state."""
 
@@ -36,20 +37,33 @@ def read_dump(path):
 
     init, off = state(off)
     final, off = state(off)
+    faces = None
+    if off < len(raw):  # --faces: face vertex pairs and containment polygon
+        nfaces = int(np.frombuffer(raw, "<i8", 1, offset=off)[0])
+        off += 8
+        fv = np.frombuffer(raw, "<i4", 2 * nfaces, offset=off).reshape(nfaces, 2)
+        off += 8 * nfaces
+        npoly = int(np.frombuffer(raw, "<i8", 1, offset=off)[0])
+        off += 8
+        poly = np.frombuffer(raw, "<f8", 2 * npoly, offset=off).reshape(npoly, 2)
+        off += 16 * npoly
+        faces = [dict(face_verts=fv.copy(), poly=poly.copy())]
     assert off == len(raw)
     tank = dict(n_fluid=int(nf), n_wall=int(n - nf), h=float(h), m=float(m),
                 rho0=float(rho0), cs0=float(cs0))
-    return tank, init, final, float(t), int(steps)
+    return tank, init, final, float(t), int(steps), faces
 
 
 INTEGRATORS = {"ssprk3": _abi.TG_SSPRK3, "ssprk2": _abi.TG_SSPRK2,
                "euler": _abi.TG_EULER, "verlet": _abi.TG_VERLET}
 
 
-@pytest.mark.parametrize("fp32c,integrator,shifting", [
-    (False, "ssprk3", True), (True, "ssprk3", True), (False, "ssprk3", False),
-    (False, "ssprk2", True), (False, "euler", True), (False, "verlet", False)])
-def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting):
+@pytest.mark.parametrize("fp32c,integrator,shifting,faces", [
+    (False, "ssprk3", True, False), (True, "ssprk3", True, False),
+    (False, "ssprk3", False, False), (False, "ssprk2", True, False),
+    (False, "euler", True, False), (False, "verlet", False, False),
+    (False, "ssprk3", True, True), (False, "verlet", True, True)])
+def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting, faces):
     exe = gpu_build.build_host()["titwcsph_gpu"]
     dump, ttdb = tmp_path / "state.bin", tmp_path / "particles.ttdb"
     cmd = [str(exe), "--nx", "20", "--steps", "20", "--dump", str(dump), "--ttdb", str(ttdb),
@@ -58,11 +72,14 @@ def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting):
         cmd.append("--fp32c")
     if not shifting:
         cmd.append("--no-shifting")
+    if faces:
+        cmd.append("--faces")
     res = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr
-    tank, (r0, v0, rho0), (r1, v1, rho1), t, steps = read_dump(dump)
+    tank, (r0, v0, rho0), (r1, v1, rho1), t, steps, fc = read_dump(dump)
     assert steps == 20
-    scn = dict(dim=2, tanks=[tank], r=r0.copy(), v=v0.copy(), rho=rho0.copy())
+    assert (fc is not None) == faces
+    scn = dict(dim=2, tanks=[tank], r=r0.copy(), v=v0.copy(), rho=rho0.copy(), faces=fc)
     # The driver's physics: the reference term set, C4 Wendland, mu = 0.001.
     P = physics.reference_params(2)
     P.integrator = INTEGRATORS[integrator]

@@ -137,3 +137,7 @@ def test_driver_builds_and_fails_cleanly_without_device(gpu_lib):
     assert "no CUDA device" in res.stderr
     bad = subprocess.run([str(exe), "--bogus"], capture_output=True, text=True, timeout=60)
     assert bad.returncode == 1 and "unknown option" in bad.stderr
+    # Face walls need the FP64 form: refused before any device call.
+    f32 = subprocess.run([str(exe), "--faces", "--fp32c"], capture_output=True, text=True,
+                         timeout=60)
+    assert f32.returncode == 1 and "FP64" in f32.stderr

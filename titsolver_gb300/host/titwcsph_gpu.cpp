@@ -1,11 +1,13 @@
 // titwcsph_gpu.cpp - the titwcsph dam break (source/titwcsph/wcsph.cpp:37-193)
 // driven through the C++ mirror of titgpu.hpp: the same setup expressions,
-// API calls and loop, with three layers of fixed wall particles in place of
-// the tessellated boundary faces (the GPU path runs particle walls).
+// API calls and loop.  With --faces the walls are the reference's own: the
+// tessellated pool surface, one fixed particle per vertex and a
+// winding-number containment; by default three layers of fixed wall
+// particles with an empty surface (particle walls).
 //
 // Usage: titwcsph_gpu [--nx N] [--steps S] [--end-time T] [--fp32c]
 //                     [--integrator ssprk3|ssprk2|euler|verlet]
-//                     [--no-shifting] [--ttdb FILE] [--dump FILE]
+//                     [--no-shifting] [--faces] [--ttdb FILE] [--dump FILE]
 //   --nx       particles per column height H (default 80, as wcsph.cpp:42)
 //   --steps    stop after S steps (default: run to scaled time T)
 //   --end-time scaled end time t sqrt(g/H) (default 10, as wcsph.cpp:183)
@@ -13,12 +15,15 @@
 //   --integrator  time integrator (default ssprk3, as wcsph.cpp:92)
 //   --no-shifting skip the post-step shifting and free-surface correction
 //                 (the reference always runs them)
+//   --faces    the reference's face walls (2D FP64 only)
 //   --ttdb     write frames every 100 steps to this .ttdb file
 //   --dump     write the initial and final state as raw binary (see below)
 //
 // Dump layout (little-endian): int64 n, n_fluid, steps; float64 h, m, rho_0,
 // cs_0, time; then r (n x 2), v (n x 2), rho (n) of the initial state and
-// the same of the final state.
+// the same of the final state; with --faces then int64 n_faces, n_faces
+// pairs of int32 fixed-particle indices, int64 n_poly and n_poly (x, y)
+// float64 containment vertices.
 
 #include <cmath>
 #include <cstdio>
@@ -43,6 +48,7 @@ struct Options {
   bool fp32c = false;
   std::string integrator = "ssprk3";
   bool shifting = true;
+  bool faces = false;
   std::string ttdb;
   std::string dump;
 };
@@ -61,6 +67,7 @@ auto parse(int argc, char** argv) -> Options {
     else if (a == "--fp32c") o.fp32c = true;
     else if (a == "--integrator") o.integrator = next();
     else if (a == "--no-shifting") o.shifting = false;
+    else if (a == "--faces") o.faces = true;
     else if (a == "--ttdb") o.ttdb = next();
     else if (a == "--dump") o.dump = next();
     else throw Exception{"unknown option " + a};
@@ -92,7 +99,11 @@ void dump_state(std::ofstream& out, PA& particles) {
 
 template<class Real, class Equations, class Integrator>
 auto simulate(const Options& opt, const Equations& equations,
-              const Integrator& time_integrator) -> int;
+              const Integrator& time_integrator,
+              const geom::Surface<Vec<Real, 2>>* domain) -> int;
+template<class Real, class Equations>
+auto run_integrator(const Options& opt, const Equations& equations,
+                    const geom::Surface<Vec<Real, 2>>* domain) -> int;
 
 template<class Real>
 auto sph_main(int argc, char** argv) -> int {
@@ -105,12 +116,45 @@ auto sph_main(int argc, char** argv) -> int {
   const Real cs_0 = 20 * std::sqrt(g * H);
   constexpr Real mu = 0.001;
 
-  // Particle walls: the domain surface stays empty and every point is
-  // inside the containment (gamma = 1, no face terms).
-  const geom::Surface<Vec<Real, 2>> domain;
   GpuOptions gpu;
   gpu.precision = opt.fp32c ? Precision::fp32_compensated : Precision::fp64;
   gpu.shifting = opt.shifting;
+  if (opt.faces) {
+    // The reference's walls (wcsph.cpp:55-77): the pool surface tessellated
+    // at dr, and a winding-number containment of the pool.
+    constexpr Real POOL_WIDTH = 5.366 * H;
+    constexpr Real POOL_HEIGHT = 4.0 * H;
+    const Real dr = H / opt.nx;
+    geom::Surface<Vec<Real, 2>> domain;
+    domain.append_vert({0.0, POOL_HEIGHT});
+    domain.append_vert({POOL_WIDTH, POOL_HEIGHT});
+    domain.append_vert({POOL_WIDTH, 0.0});
+    domain.append_vert({0.0, 0.0});
+    domain.append_face({0, 1});
+    domain.append_face({1, 2});
+    domain.append_face({2, 3});
+    domain.append_face({3, 0});
+    domain = geom::tessellate(domain, dr);
+    geom::Surface<Vec<Real, 2>> domain2;
+    domain2.append_vert({0.0, 0.0});
+    domain2.append_vert({POOL_WIDTH, 0.0});
+    domain2.append_vert({POOL_WIDTH, POOL_HEIGHT});
+    domain2.append_vert({0.0, POOL_HEIGHT});
+    domain2.append_face({0, 1});
+    domain2.append_face({1, 2});
+    domain2.append_face({2, 3});
+    domain2.append_face({3, 0});
+    const geom::MakeFastWinding<Real> make_winding;
+    const auto containment = make_winding(domain2);
+    const FluidEquations equations{
+        g, mu, domain, containment, TaitEquationOfState{cs_0, rho_0},
+        SixthOrderWendlandKernel{}, gpu,
+    };
+    return run_integrator<Real>(opt, equations, &domain);
+  }
+  // Particle walls: the domain surface stays empty and every point is
+  // inside the containment (gamma = 1, no face terms).
+  const geom::Surface<Vec<Real, 2>> domain;
   const FluidEquations equations{
       // Constants.
       g,
@@ -124,25 +168,34 @@ auto sph_main(int argc, char** argv) -> int {
       SixthOrderWendlandKernel{},
       gpu,
   };
+  return run_integrator<Real>(opt, equations, nullptr);
+}
+
+template<class Real, class Equations>
+auto run_integrator(const Options& opt, const Equations& equations,
+                    const geom::Surface<Vec<Real, 2>>* domain) -> int {
 
   // Setup the time integrator.
   if (opt.integrator == "ssprk2") {
     return simulate<Real>(opt, equations,
-                          SSPRKIntegrator{equations, SSPRKOrder::two});
+                          SSPRKIntegrator{equations, SSPRKOrder::two}, domain);
   }
   if (opt.integrator == "euler") {
-    return simulate<Real>(opt, equations, SymplecticEulerIntegrator{equations});
+    return simulate<Real>(opt, equations, SymplecticEulerIntegrator{equations},
+                          domain);
   }
   if (opt.integrator == "verlet") {
-    return simulate<Real>(opt, equations, VelocityVerletIntegrator{equations});
+    return simulate<Real>(opt, equations, VelocityVerletIntegrator{equations},
+                          domain);
   }
   return simulate<Real>(opt, equations,
-                        SSPRKIntegrator{equations, SSPRKOrder::three});
+                        SSPRKIntegrator{equations, SSPRKOrder::three}, domain);
 }
 
 template<class Real, class Equations, class Integrator>
 auto simulate(const Options& opt, const Equations& equations,
-              const Integrator& time_integrator) -> int {
+              const Integrator& time_integrator,
+              const geom::Surface<Vec<Real, 2>>* domain) -> int {
   constexpr Real H = 0.6;   // Water column height.
   constexpr Real L = 2 * H; // Water column length.
 
@@ -174,15 +227,23 @@ auto simulate(const Options& opt, const Equations& equations,
       r[a] = dr * Vec{i + Real{1.0}, j + Real{1.0}};
     }
   }
-  // Three layers of fixed particles on the dr lattice: bottom and both
-  // sides of the pool, open top.
-  const auto nW = int(std::round(POOL_WIDTH / dr));
-  const auto nH = int(std::round(POOL_HEIGHT / dr));
-  for (auto j = -2; j <= nH; ++j) {
-    for (auto i = -2; i <= nW + 2; ++i) {
-      if (i > 0 && i < nW && j > 0) continue;
+  if (domain != nullptr) {
+    // One fixed particle per domain vertex (wcsph.cpp:109-112).
+    for (std::size_t i = 0; i < domain->num_verts(); ++i) {
       auto a = particles.append(ParticleType::fixed);
-      r[a] = dr * Vec{Real(i), Real(j)};
+      r[a] = domain->vert(i);
+    }
+  } else {
+    // Three layers of fixed particles on the dr lattice: bottom and both
+    // sides of the pool, open top.
+    const auto nW = int(std::round(POOL_WIDTH / dr));
+    const auto nH = int(std::round(POOL_HEIGHT / dr));
+    for (auto j = -2; j <= nH; ++j) {
+      for (auto i = -2; i <= nW + 2; ++i) {
+        if (i > 0 && i < nW && j > 0) continue;
+        auto a = particles.append(ParticleType::fixed);
+        r[a] = dr * Vec{Real(i), Real(j)};
+      }
     }
   }
 
@@ -271,6 +332,21 @@ auto simulate(const Options& opt, const Equations& equations,
 
   if (dump) {
     dump_state(dump, particles);
+    if (domain != nullptr) {
+      const std::int64_t nfaces = static_cast<std::int64_t>(domain->num_faces());
+      dump.write(reinterpret_cast<const char*>(&nfaces), sizeof(nfaces));
+      for (std::size_t fi = 0; fi < domain->num_faces(); ++fi) {
+        for (const auto v : domain->face_verts(fi)) {
+          const std::int32_t vi = static_cast<std::int32_t>(v);
+          dump.write(reinterpret_cast<const char*>(&vi), sizeof(vi));
+        }
+      }
+      const double poly[8] = {0.0, 0.0, POOL_WIDTH, 0.0, POOL_WIDTH, POOL_HEIGHT,
+                              0.0, POOL_HEIGHT};
+      const std::int64_t npoly = 4;
+      dump.write(reinterpret_cast<const char*>(&npoly), sizeof(npoly));
+      dump.write(reinterpret_cast<const char*>(poly), sizeof(poly));
+    }
     dump.seekp(3 * sizeof(std::int64_t) + 4 * sizeof(double));
     const double t = time;
     dump.write(reinterpret_cast<const char*>(&t), sizeof(t));
