@@ -30,7 +30,7 @@
  *
  * Walls: either fixed particles with an empty domain surface ("particle
  * walls": gamma = 1 and no face terms, fluid_equations.hpp:122-163), or,
- * in 2D with the FP64 form, the reference's semi-analytical face walls: a
+ * in 2D, the reference's semi-analytical face walls: a
  * tessellated domain surface whose vertices are the fixed particles and a
  * winding-number containment (geom::MakeFastWinding), as titwcsph sets up
  * (wcsph.cpp:55-77, 109-112).  Every fluid particle must lie inside the
@@ -401,9 +401,6 @@ public:
       if constexpr (Dim != 2 || !has_polygon_) {
         throw Exception{"FluidEquations: boundary faces need 2D and a "
                         "winding-number containment (geom::MakeFastWinding)"};
-      }
-      if (options_.precision != Precision::fp64) {
-        throw Exception{"FluidEquations: boundary faces run in the FP64 form"};
       }
     }
   }

@@ -118,11 +118,10 @@ auto main(int argc, char** argv) -> int {
                                TaitEquationOfState{20.0, 1000.0},
                                SixthOrderWendlandKernel{}};
     (void)faced;
-    GpuOptions f32;
-    f32.precision = Precision::fp32_compensated;
+    // Faces need a polygon containment: an all-inside functor is refused.
     CHECK(throws([&] {
-      FluidEquations bad{9.81, 0.001, t, inside, TaitEquationOfState{20.0, 1000.0},
-                         SixthOrderWendlandKernel{}, f32};
+      FluidEquations bad{9.81, 0.001, t, geom::AllInside{},
+                         TaitEquationOfState{20.0, 1000.0}, SixthOrderWendlandKernel{}};
     }));
   }
   CHECK(throws([] { geom::GridSearch{0.0}; }));

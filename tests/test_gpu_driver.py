@@ -62,7 +62,7 @@ INTEGRATORS = {"ssprk3": _abi.TG_SSPRK3, "ssprk2": _abi.TG_SSPRK2,
     (False, "ssprk3", True, False), (True, "ssprk3", True, False),
     (False, "ssprk3", False, False), (False, "ssprk2", True, False),
     (False, "euler", True, False), (False, "verlet", False, False),
-    (False, "ssprk3", True, True), (False, "verlet", True, True)])
+    (False, "ssprk3", True, True), (False, "verlet", True, True), (True, "ssprk3", True, True)])
 def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting, faces):
     exe = gpu_build.build_host()["titwcsph_gpu"]
     dump, ttdb = tmp_path / "state.bin", tmp_path / "particles.ttdb"

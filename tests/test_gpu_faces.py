@@ -1,4 +1,5 @@
-"""Semi-analytical face boundaries on the GPU (2D, FP64) against the
+"""Semi-analytical face boundaries on the GPU (2D; FP64 and the compensated
+form) against the
 oracle, on the titwcsph scenario itself (source/titwcsph/wcsph.cpp:37-142:
 tessellated pool faces with one fixed particle per vertex, containment by
 the pool polygon).  Tolerances (relative L2 over the fluid): 1 step r, v,
@@ -69,7 +70,7 @@ def test_faces_batched_with_a_particle_wall_tank(gpu_lib):
     _compare(scn, physics.reference_params(2), 3, 1e-10)
 
 
-def test_faces_survive_autotune_and_reject_other_forms(gpu_lib):
+def test_faces_survive_autotune_and_reject_3d_and_bad_vertices(gpu_lib):
     scn = scenarios.dam_break_2d_faces(nx_per_H=16)
     P = physics.reference_params(2)
     f = fluid_mask(scn)
@@ -82,14 +83,32 @@ def test_faces_survive_autotune_and_reject_other_forms(gpu_lib):
         a, b = gpu_state(ctx), gpu_state(ref)
     assert rel_l2(a["rho"][f], b["rho"][f]) <= 1e-11
     assert rel_l2(a["r"][f], b["r"][f]) <= 1e-11
-    P32 = physics.reference_params(2, precision=_abi.TG_FP32C)
-    with _abi.Context(P32) as ctx:
-        ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+    s3 = scenarios.dam_break_3d(nx_per_H=6)
+    with _abi.Context(physics.reference_params(3)) as ctx:
+        ctx.upload(s3["tanks"], s3["r"], s3["v"], s3["rho"])
         with pytest.raises(_abi.TgError) as ei:
-            ctx.set_faces(0, scn["faces"][0]["face_verts"], scn["faces"][0]["poly"])
+            ctx.set_faces(0, np.array([[0, 1]], dtype=np.int32), scn["faces"][0]["poly"])
         assert ei.value.status == _abi.TG_ERR_INVALID_ARGUMENT
     with _abi.Context(P) as ctx:
         ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
         bad = np.array([[0, 10**6]], dtype=np.int32)
         with pytest.raises(_abi.TgError):
             ctx.set_faces(0, bad, scn["faces"][0]["poly"])
+
+
+@pytest.mark.parametrize("shifting", (False, True))
+def test_faces_fp32_compensated_vs_fp64_oracle(gpu_lib, shifting):
+    # The compensated form with face walls: face integrals in FP64, pair sums
+    # in FP32 with Kahan sums, against the FP64 oracle after 30 steps.
+    scn = scenarios.dam_break_2d_faces(nx_per_H=20)
+    P64 = physics.reference_params(2)
+    P32 = physics.reference_params(2, precision=_abi.TG_FP32C)
+    for P in (P64, P32):
+        P.post_integrate = _abi.TG_POST_SHIFTING if shifting else _abi.TG_POST_PREPARE
+    o = oracle_run(scn, P64, 30)
+    f = fluid_mask(scn)
+    with gpu_context(scn, P32) as ctx:
+        ctx.step(30)
+        g = gpu_state(ctx)
+    assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5
+    assert rel_l2(g["r"][f], o.r[f]) <= 1e-6

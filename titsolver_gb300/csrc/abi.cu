@@ -966,6 +966,8 @@ int build_faces(tg_context* ctx) {
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.slot_of), sizeof(uint32_t) * nn));
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.gamma), sizeof(double) * nn));
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.ggam), sizeof(double) * 2 * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_drho), sizeof(double) * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_dv), sizeof(double) * 2 * nn));
   fa.weight = kernel_weight(C.P.kernel, 2);
   fa.on = 1;
   TG_CUDA(&C, cudaStreamSynchronize(C.stream));
@@ -985,9 +987,8 @@ int tg_tank_faces(tg_context* ctx, int32_t tank, int32_t n_faces,
   if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
   Context& C = ctx->c;
   if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
-  if (C.P.dim != 2 || C.P.precision != TG_FP64) {
-    return fail(&C, TG_ERR_INVALID_ARGUMENT,
-                "boundary faces run in 2D with the FP64 form");
+  if (C.P.dim != 2) {
+    return fail(&C, TG_ERR_INVALID_ARGUMENT, "boundary faces run in 2D");
   }
   if (tank < 0 || tank >= C.ntanks || n_faces < 0) {
     return fail(&C, TG_ERR_INVALID_ARGUMENT, "bad tank or face count");

@@ -264,9 +264,9 @@ class Engine final : public EngineBase {
     const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
     const int stages = force_passes(C.P.integrator);
     const int per_stage = 3 * passes + 2 + 2 + (C.n_wall > 0 ? 1 : 0);
-    const int gam = C.faces.on ? 1 : 0;
+    const int gam = C.faces.on ? 2 : 0;  // k_gamma, k_face_terms
     const int post = C.P.post_integrate == TG_POST_SHIFTING
-                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + gam : 0) + 5
+                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + (gam > 0 ? 1 : 0) : 0) + 5
                          : 0;
     return static_cast<int64_t>(stages) * (per_stage + gam) + post + 1;
   }
@@ -383,9 +383,9 @@ class Engine final : public EngineBase {
   // Face boundaries: gamma and grad gamma of every particle at the positions
   // of this prepare (before the wall pass, which reads grad gamma).
   void enqueue_gamma(Context& C, const StageArgs<D, F>& a) {
-    if constexpr (D == 2 && F == TG_FP64) {
+    if constexpr (D == 2) {
       if (a.fc.on) {
-        k_gamma<K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+        k_gamma<K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
         C.launches += 1;
       }
     }
@@ -423,6 +423,12 @@ class Engine final : public EngineBase {
           a, C.n_wall);
       C.launches += 1;
       C.group_end(tok);
+    }
+    if constexpr (D == 2) {
+      if (a.fc.on) {
+        k_face_terms<K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+        C.launches += 1;
+      }
     }
     tok = C.group_begin(kGroupForces);
     if constexpr (F == TG_FP32C) {

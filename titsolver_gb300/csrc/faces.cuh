@@ -43,6 +43,8 @@ struct FaceArgs {
   uint32_t* slot_of;          // upload index -> cell-order slot (walls)
   double* gamma;              // per particle, cell order
   double* ggam;               // grad gamma, 2 per particle
+  double* face_drho;          // face terms of continuity, per particle
+  double* face_dv;            // face terms of momentum, 2 per particle
   const uint32_t* tank_edges; // per tank: containment edges (0: all inside)
   double weight;              // the kernel's 2D weight
   int on;

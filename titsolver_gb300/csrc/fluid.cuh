@@ -789,6 +789,17 @@ __global__ void __launch_bounds__(128)
       skip = beyond_fluid<D>(A.fbox, A.ntanks, tk, T, xl);
     }
     skip = __shfl_sync(0xffffffffu, skip, 0, kWallTeam);
+    // Face boundaries: wall normal and hydrostatic term (see the FP64 path);
+    // here r_be = -d.
+    float nef[2] = {0.f, 0.f};
+    if constexpr (D == 2) {
+      if (A.fc.on && valid) {
+        double ne[2];
+        normalize2(A.fc.ggam + 2 * static_cast<size_t>(e), ne);
+        nef[0] = static_cast<float>(ne[0]);
+        nef[1] = static_cast<float>(ne[1]);
+      }
+    }
     if (valid && !A.walls_keep && !skip) {
       auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
         float oes[3];
@@ -803,7 +814,10 @@ __global__ void __launch_bounds__(128)
           const Dat32 b = load_dat_coherent(A.datrec, j);
           const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
           const float Vb = m * b.invrho;
-          const float Hb = potential_f32(A.phys, T, b.drho);
+          float Hb = potential_f32(A.phys, T, b.drho);
+          if constexpr (D == 2) {
+            if (A.fc.on) Hb -= A.phys.g_f * (d[0] * nef[0] + d[1] * nef[1]) * nef[1];
+          }
           S.add(Vb * W);
           H.add(Vb * Hb * W);
         }
@@ -1089,54 +1103,102 @@ __device__ __forceinline__ void forces_epilogue(
   }
 }
 
-// Face boundaries, FP64 form (fluid_equations.hpp:241-247, 276-292): the
-// pair sums divided by gamma_a, then per adjacent face s (vertex pair, whose
-// fields are averages; vertices have zero velocity)
+// Face boundaries (fluid_equations.hpp:241-247, 276-292): per adjacent face
+// s (a vertex pair, whose fields are averages; vertices have zero velocity)
 //   drho_a -= rho_s (v_as . grad gamma_as) / gamma_a
 //   dv_a   += (P_as grad gamma_as - Pi_as |grad gamma_as|) / gamma_a,
 //   P_as = rho_s (p_a / rho_a^2 + p_s / rho_s^2),
 //   Pi_as = 2 mu / (rho_a dr_as) (v_as . t_as) t_as,
 //   dr_as = max(h / 2, (r_a - r_s) . n_s), n_s = normalize(grad gamma_as),
-//   t_as = normalize(v_as - (v_as . n_s) n_s),
-// and gravity -g e_1.
+//   t_as = normalize(v_as - (v_as . n_s) n_s).
+// k_face_terms stores these per particle (FP64, both forms) before the
+// force pass, which divides its pair sums by gamma_a, adds them and adds
+// gravity; the face integrals stay out of the force loop's registers.
+
+// Density of a face vertex from its data record (either form).
+__device__ __forceinline__ double vertex_rho(const Dat64* dat, uint32_t j,
+                                             const TankDev&) {
+  return load_dat(dat, j).rho;
+}
+__device__ __forceinline__ double vertex_rho(const Dat32* dat, uint32_t j,
+                                             const TankDev& T) {
+  return T.rho0 + static_cast<double>(load_dat(dat, j).drho);
+}
+
+// Target fields from a data record: velocity, density, P = p / rho^2.
+__device__ __forceinline__ void target_fields(const Dat64& a, const TankDev&,
+                                              double* v, double& rho, double& P) {
+  v[0] = a.vx;
+  v[1] = a.vy;
+  rho = a.rho;
+  P = a.P;
+}
+__device__ __forceinline__ void target_fields(const Dat32& a, const TankDev& T,
+                                              double* v, double& rho, double& P) {
+  v[0] = a.vx;
+  v[1] = a.vy;
+  rho = T.rho0 + static_cast<double>(a.drho);
+  P = a.P;
+}
+
 template<int K, int F>
-__device__ __forceinline__ void face_terms(const StageArgs<2, F>& A,
-                                           const TankDev& T, const int* c,
-                                           int64_t i, const double* pa,
-                                           const Dat64& a, double& drho,
-                                           double* dv) {
+__global__ void __launch_bounds__(128) k_face_terms(StageArgs<2, F> A) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const FaceArgs& fc = A.fc;
+  double drho = 0.0, dv[2] = {0.0, 0.0};
+  if (!(A.Y.id[i] & kWallBit)) {
+    const uint32_t key = A.skey[i];
+    const TankDev& T = A.tanks[tank_of_key(key, A.tank_off, A.ntanks)];
+    int c[3] = {0, 0, 0};
+    cell_from_key<2>(T, key, c);
+    const uint32_t gcell = T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
+    const double pa[2] = {A.Y.pos[0][i], A.Y.pos[1][i]};
+    const double radius = KernelPoly<K>::unit_radius * T.h;
+    const double gam = fc.gamma[i];
+    double va[2], rho_a, P_a;
+    target_fields(load_dat(A.datrec, static_cast<uint32_t>(i)), T, va, rho_a, P_a);
+    for_adjacent_faces(fc, gcell, pa, radius, [&](uint32_t f, const double* ab) {
+      double gg[2];
+      face_flux<K>(ab, pa, T.h, fc.weight, gg);
+      const double rho_v0 = vertex_rho(A.datrec, fc.slot_of[fc.vert[2 * f]], T);
+      const double rho_v1 = vertex_rho(A.datrec, fc.slot_of[fc.vert[2 * f + 1]], T);
+      const double rho_s = (rho_v0 + rho_v1) / 2.0;
+      double p0, p1, c0, c1;
+      tait_f64(A.phys, T, rho_v0, p0, c0);
+      tait_f64(A.phys, T, rho_v1, p1, c1);
+      const double p_s = (p0 + p1) / 2.0;
+      drho -= rho_s * (va[0] * gg[0] + va[1] * gg[1]) / gam;
+      const double P_as = rho_s * (P_a + p_s / (rho_s * rho_s));
+      double n_s[2], t_as[2];
+      normalize2(gg, n_s);
+      const double vn = va[0] * n_s[0] + va[1] * n_s[1];
+      const double vt[2] = {va[0] - vn * n_s[0], va[1] - vn * n_s[1]};
+      normalize2(vt, t_as);
+      const double r_as[2] = {pa[0] - (ab[0] + ab[2]) / 2.0, pa[1] - (ab[1] + ab[3]) / 2.0};
+      const double dr_as = fmax(T.h / 2.0, r_as[0] * n_s[0] + r_as[1] * n_s[1]);
+      const double Pi_s =
+          2.0 * A.phys.mu / (rho_a * dr_as) * (va[0] * t_as[0] + va[1] * t_as[1]);
+      const double ng = sqrt(gg[0] * gg[0] + gg[1] * gg[1]);
+      dv[0] += (P_as * gg[0] - Pi_s * t_as[0] * ng) / gam;
+      dv[1] += (P_as * gg[1] - Pi_s * t_as[1] * ng) / gam;
+    });
+  }
+  fc.face_drho[i] = drho;
+  fc.face_dv[2 * i] = dv[0];
+  fc.face_dv[2 * i + 1] = dv[1];
+}
+
+// The force pass's share: pair sums over gamma, plus the stored face terms
+// and gravity.
+template<int F>
+__device__ __forceinline__ void apply_face_terms(const StageArgs<2, F>& A,
+                                                 int64_t i, double& drho,
+                                                 double* dv) {
   const double gam = A.fc.gamma[i];
-  drho /= gam;
-  dv[0] /= gam;
-  dv[1] /= gam;
-  const uint32_t gcell = T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
-  const double radius = KernelPoly<K>::unit_radius * T.h;
-  const double va[2] = {a.vx, a.vy};
-  for_adjacent_faces(A.fc, gcell, pa, radius, [&](uint32_t f, const double* ab) {
-    double gg[2];
-    face_flux<K>(ab, pa, T.h, A.fc.weight, gg);
-    const Dat64 v0 = load_dat(A.datrec, A.fc.slot_of[A.fc.vert[2 * f]]);
-    const Dat64 v1 = load_dat(A.datrec, A.fc.slot_of[A.fc.vert[2 * f + 1]]);
-    const double rho_s = (v0.rho + v1.rho) / 2.0;
-    double p0, p1, c0, c1;
-    tait_f64(A.phys, T, v0.rho, p0, c0);
-    tait_f64(A.phys, T, v1.rho, p1, c1);
-    const double p_s = (p0 + p1) / 2.0;
-    drho -= rho_s * (va[0] * gg[0] + va[1] * gg[1]) / gam;
-    const double P_as = rho_s * (a.P + p_s / (rho_s * rho_s));
-    double n_s[2], t_as[2];
-    normalize2(gg, n_s);
-    const double vn = va[0] * n_s[0] + va[1] * n_s[1];
-    const double vt[2] = {va[0] - vn * n_s[0], va[1] - vn * n_s[1]};
-    normalize2(vt, t_as);
-    const double r_as[2] = {pa[0] - (ab[0] + ab[2]) / 2.0, pa[1] - (ab[1] + ab[3]) / 2.0};
-    const double dr_as = fmax(T.h / 2.0, r_as[0] * n_s[0] + r_as[1] * n_s[1]);
-    const double Pi_s = 2.0 * A.phys.mu / (a.rho * dr_as) * (va[0] * t_as[0] + va[1] * t_as[1]);
-    const double ng = sqrt(gg[0] * gg[0] + gg[1] * gg[1]);
-    dv[0] += (P_as * gg[0] - Pi_s * t_as[0] * ng) / gam;
-    dv[1] += (P_as * gg[1] - Pi_s * t_as[1] * ng) / gam;
-  });
-  dv[1] += -A.phys.g;
+  drho = drho / gam + A.fc.face_drho[i];
+  dv[0] = dv[0] / gam + A.fc.face_dv[2 * i];
+  dv[1] = dv[1] / gam + A.fc.face_dv[2 * i + 1] - A.phys.g;
 }
 
 // Team lanes share one target: each takes every Team-th cell of the block
@@ -1233,7 +1295,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
       if (lane != 0) return;
     }
     if constexpr (D == 2) {
-      if (faces) face_terms<K>(A, T, c, i, pa, a, drho, dv);
+      if (faces) apply_face_terms(A, i, drho, dv);
     }
 #pragma unroll
     for (int k = 0; k < D; ++k) dv_out[k] = dv[k];
@@ -1241,7 +1303,9 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
   } else {
     PairF32<D, K, Phys> acc;
     acc.init(A.phys, T, load_dat(A.datrec, static_cast<uint32_t>(i)), A.kahan);
-    if (lane != 0) acc.dv[1].s = 0.f;  // gravity once per target
+    // Gravity once per target; with face boundaries after the gamma division.
+    const bool faces = D == 2 && A.fc.on;
+    if (lane != 0 || faces) acc.dv[1].s = 0.f;
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
     const float csz = T.cs_f;
@@ -1311,6 +1375,16 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     }
     rho_self = acc.a.drho;
     drho_out = acc.drho.value();
+    if constexpr (D == 2) {
+      if (faces) {
+        double drho = drho_out;
+        double dv[2] = {dv_out[0], dv_out[1]};
+        apply_face_terms(A, i, drho, dv);
+        drho_out = static_cast<float>(drho);
+        dv_out[0] = static_cast<float>(dv[0]);
+        dv_out[1] = static_cast<float>(dv[1]);
+      }
+    }
   }
   forces_epilogue<D, F>(A, i, id, tk, T, c, va, rho_self, dv_out, drho_out);
 }
@@ -1613,8 +1687,8 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
 // gamma and grad gamma of every particle (FluidEquations::compute_gamma,
 // fluid_equations.hpp:166-193); also records the cell-order slot of each
 // fixed particle for the face terms' vertex lookups.
-template<int K>
-__global__ void __launch_bounds__(128) k_gamma(StageArgs<2, TG_FP64> A) {
+template<int K, int F>
+__global__ void __launch_bounds__(128) k_gamma(StageArgs<2, F> A) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   const FaceArgs& fc = A.fc;

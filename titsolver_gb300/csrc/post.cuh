@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(128) k_post_sums(PostArgs<D, F> A) {
   // Face boundaries (fluid_equations.hpp:335-349): face terms first, and
   // every sum divided by gamma_a.
   double gam = 1.0;
-  if constexpr (D == 2 && F == TG_FP64) {
+  if constexpr (D == 2) {
     if (A.S.fc.on) {
       gam = A.S.fc.gamma[i];
       const uint32_t gcell =
@@ -178,11 +178,11 @@ __global__ void __launch_bounds__(128) k_post_sums(PostArgs<D, F> A) {
       for_adjacent_faces(A.S.fc, gcell, pa, radius, [&](uint32_t f, const double* ab) {
         double gg[2];
         face_flux<K>(ab, pa, T.h, A.S.fc.weight, gg);
-        const Dat64 v0 = load_dat(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f]]);
-        const Dat64 v1 = load_dat(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f + 1]]);
+        const double rho_v0 = vertex_rho(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f]], T);
+        const double rho_v1 = vertex_rho(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f + 1]], T);
         const double r_sa[2] = {(ab[0] + ab[2]) / 2.0 - pa[0], (ab[1] + ab[3]) / 2.0 - pa[1]};
         const double v_sa[2] = {-va[0], -va[1]};
-        const double rho_sa = (v0.rho + v1.rho) / 2.0 - rho_a;
+        const double rho_sa = (rho_v0 + rho_v1) / 2.0 - rho_a;
         for (int a2 = 0; a2 < 2; ++a2) {
           N[a2] -= gg[a2] / gam;
           for (int b2 = 0; b2 < 2; ++b2) {

@@ -15,7 +15,7 @@
 //   --integrator  time integrator (default ssprk3, as wcsph.cpp:92)
 //   --no-shifting skip the post-step shifting and free-surface correction
 //                 (the reference always runs them)
-//   --faces    the reference's face walls (2D FP64 only)
+//   --faces    the reference's face walls
 //   --ttdb     write frames every 100 steps to this .ttdb file
 //   --dump     write the initial and final state as raw binary (see below)
 //
