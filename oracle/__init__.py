@@ -83,6 +83,11 @@ def lib():
             "or_kernel_antigrad_flux2": (ctypes.c_double, [ctypes.c_int32, _D, _D, _D,
                                                            ctypes.c_double]),
             "or_winding_number2": (ctypes.c_double, [ctypes.c_int32, _D, _D]),
+            "or_kernel_flux3": (None, [ctypes.c_int32, _D, _D, _D, _D, ctypes.c_double, _D]),
+            "or_kernel_antigrad_flux3": (ctypes.c_double, [ctypes.c_int32, _D, _D, _D, _D,
+                                                           ctypes.c_double]),
+            "or_winding_number3": (ctypes.c_double, [ctypes.c_int32, _D, _D]),
+            "or_triangle_in_sphere": (ctypes.c_int32, [_D, _D, _D, _D, ctypes.c_double]),
             "or_tank_neighbour_counts": (ctypes.c_int32, [ctypes.POINTER(_Params), ctypes.c_int32,
                                                           ctypes.POINTER(_Tank), _D, _I32, _U64,
                                                           ctypes.c_int32]),
@@ -287,6 +292,37 @@ def kernel_antigrad_flux2(kernel: int, a, b, x, h: float) -> float:
 def winding_number2(poly, x) -> float:
     P, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (poly, x))
     return lib().or_winding_number2(P.shape[0], _p(P, ctypes.c_double), _p(X, ctypes.c_double))
+
+
+def kernel_flux3(kernel: int, a, b, c, x, h: float) -> np.ndarray:
+    """Kernel flux of triangle a-b-c at x (kernel.hpp:194-206)."""
+    out = np.zeros(3)
+    A, B, C, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (a, b, c, x))
+    lib().or_kernel_flux3(kernel, _p(A, ctypes.c_double), _p(B, ctypes.c_double),
+                          _p(C, ctypes.c_double), _p(X, ctypes.c_double), h,
+                          _p(out, ctypes.c_double))
+    return out
+
+
+def kernel_antigrad_flux3(kernel: int, a, b, c, x, h: float) -> float:
+    """Antigradient flux of triangle a-b-c at x (kernel.hpp:209-221)."""
+    A, B, C, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (a, b, c, x))
+    return lib().or_kernel_antigrad_flux3(kernel, _p(A, ctypes.c_double),
+                                          _p(B, ctypes.c_double), _p(C, ctypes.c_double),
+                                          _p(X, ctypes.c_double), h)
+
+
+def winding_number3(tris, x) -> float:
+    """Generalized winding number of a triangle mesh (n, 3, 3) at x."""
+    T, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (tris, x))
+    return lib().or_winding_number3(T.shape[0], _p(T, ctypes.c_double), _p(X, ctypes.c_double))
+
+
+def triangle_in_sphere(a, b, c, x, radius: float) -> bool:
+    A, B, C, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (a, b, c, x))
+    return bool(lib().or_triangle_in_sphere(_p(A, ctypes.c_double), _p(B, ctypes.c_double),
+                                            _p(C, ctypes.c_double), _p(X, ctypes.c_double),
+                                            radius))
 
 
 def tank_neighbour_counts(params, tanks, r: np.ndarray, nthreads: int = 0):

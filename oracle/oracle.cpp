@@ -385,6 +385,340 @@ double winding_number(int32_t n_poly, const double* poly, const double* x) {
   return w;
 }
 
+// ---------------------------------------------------------------------------
+// Semi-analytical face boundaries in 3D: kernel flux and antigradient flux
+// over a triangle (kernel.hpp:194-221, 316-399; kernel.gen.cpp:321-466).
+// The triangle is projected into its plane around x (Triangle::project,
+// geom/triangle.hpp) and scaled by 1/h; for each support piece at wall
+// distance eta < cutoff the integral over the triangle is a sum over its
+// edges.  Edge p0 -> p1 with unit tangent t: delta = det(p0, t),
+// beta^2 = eta^2 + delta^2, z from dot(p0, t) to dot(p0, t) + |p1 - p0|,
+// split where the edge crosses the circle of radius sqrt(cutoff^2 - eta^2);
+// a sub-interval inside the circle adds the difference of the line
+// primitive, one outside adds the sector value times the arc angle
+// atan2(delta (z_hi - z_lo), z_lo z_hi + delta^2).  Line primitive at z:
+// rho^2 = z^2 + beta^2, A = atan2(delta z (rho - eta), delta^2 rho +
+// z^2 eta) (0 for tiny delta), L = copysign(log1p((|z| + z^2/(rho + beta))
+// / beta), z) (0 for tiny beta), J_0 = z, J_1 = (z rho + beta^2 L)/2,
+// J_k = (z rho^k + k beta^2 J_{k-2})/(k + 1), K_0 = A, K_1 = delta L,
+// K_k = delta J_{k-2} + eta^2 K_{k-2}, and
+//   flux line       = sum_p c_p/(p+2) K_{p+2} - K_0 sum_p c_p eta^{p+2}/(p+2)
+//   flux sector     = sum_p c_p (cutoff^{p+2} - eta^{p+2})/(p+2)
+//   antigrad line   = s_0 K_0 + sum_{p>=3} s_p (eta K_{p-1} - eta^p K_0)/(p-1)
+//   antigrad sector = s_0 (1 - eta/cutoff)
+//                     + sum_{p>=3} s_p (eta cutoff^{p-1} - eta^p)/(p-1)
+// where s_p are the coefficients of the piece's 3D tail moment
+// cutoff^3 Q(cutoff) - q^3 Q(q), Q(q) = sum_p c_p q^p/(p + 3) (its q and q^2
+// coefficients are zero).
+
+struct TailPiece3 {
+  int deg;
+  double s[15];
+};
+
+// 3D tail moments of the pieces of kPieces, in the same order.
+constexpr TailPiece3 kTail3[6][3] = {
+  // cubic
+  {{6, {4.0 / 15.0, 0.0, 0.0, -2.0 / 3.0, 3.0 / 4.0, -3.0 / 10.0, 1.0 / 24.0}},
+   {6, {-1.0 / 60.0, 0.0, 0.0, 1.0 / 3.0, -3.0 / 4.0, 3.0 / 5.0, -1.0 / 6.0}}},
+  // quartic
+  {{7, {15625.0 / 2688.0, 0.0, 0.0, -625.0 / 48.0, 125.0 / 8.0, -15.0 / 2.0, 5.0 / 3.0, -1.0 / 7.0}},
+   {7, {-729.0 / 896.0, 0.0, 0.0, 135.0 / 16.0, -135.0 / 8.0, 27.0 / 2.0, -5.0, 5.0 / 7.0}},
+   {7, {1.0 / 1344.0, 0.0, 0.0, -5.0 / 24.0, 5.0 / 4.0, -3.0, 10.0 / 3.0, -10.0 / 7.0}}},
+  // quintic
+  {{8, {2187.0 / 56.0, 0.0, 0.0, -81.0, 405.0 / 4.0, -54.0, 15.0, -15.0 / 7.0, 1.0 / 8.0}},
+   {8, {-64.0 / 7.0, 0.0, 0.0, 64.0, -120.0, 96.0, -40.0, 60.0 / 7.0, -3.0 / 4.0}},
+   {8, {5.0 / 56.0, 0.0, 0.0, -5.0, 75.0 / 4.0, -30.0, 25.0, -75.0 / 7.0, 15.0 / 8.0}}},
+  // wc2
+  {{8, {4.0 / 21.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 1.0 / 2.0, -5.0 / 12.0, 15.0 / 112.0, -1.0 / 64.0}}},
+  // wc4
+  {{11, {64.0 / 495.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 7.0 / 15.0, 0.0, -5.0 / 8.0, 7.0 / 12.0, -35.0 / 144.0, 1.0 / 20.0, -35.0 / 8448.0}}},
+  // wc6
+  {{14, {128.0 / 1365.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 11.0 / 20.0, 0.0, -33.0 / 56.0, 0.0, 77.0 / 96.0, -33.0 / 40.0, 105.0 / 256.0, -11.0 / 96.0, 231.0 / 13312.0, -1.0 / 896.0}}},
+};
+
+// Edge primitives J_0..J_kmax and K_0..K_kmax at z.
+void edge_integrals(double eta, double delta, double beta2, double z,
+                    double rho, double A, double L, int kmax, double* J,
+                    double* K) {
+  J[0] = z;
+  J[1] = (z * rho + beta2 * L) / 2.0;
+  double rp = rho;
+  for (int k = 2; k <= kmax; ++k) {
+    rp *= rho;
+    J[k] = (z * rp + k * beta2 * J[k - 2]) / (k + 1);
+  }
+  K[0] = A;
+  K[1] = delta * L;
+  for (int k = 2; k <= kmax; ++k) K[k] = delta * J[k - 2] + eta * eta * K[k - 2];
+}
+
+double edge_primitive(const KernelPiece& kp, const TailPiece3& tp,
+                      bool antigrad, double eta, double delta, double beta2,
+                      double beta, double z) {
+  const double rho = std::sqrt(z * z + beta2);
+  const double A =
+      is_tiny(delta)
+          ? 0.0
+          : std::atan2(delta * z * (rho - eta), delta * delta * rho + z * z * eta);
+  const double L =
+      is_tiny(beta)
+          ? 0.0
+          : std::copysign(std::log1p((std::abs(z) + z * z / (rho + beta)) / beta), z);
+  double J[16], K[16];
+  double s = 0.0;
+  if (!antigrad) {
+    edge_integrals(eta, delta, beta2, z, rho, A, L, kp.deg + 2, J, K);
+    double c0 = 0.0;
+    for (int p = 0; p <= kp.deg; ++p) {
+      if (kp.c[p] == 0.0) continue;
+      s += kp.c[p] / (p + 2) * K[p + 2];
+      c0 -= kp.c[p] * ipow(eta, p + 2) / (p + 2);
+    }
+    return s + c0 * K[0];
+  }
+  edge_integrals(eta, delta, beta2, z, rho, A, L, std::max(tp.deg - 1, 1), J, K);
+  for (int p = 0; p <= tp.deg; ++p) {
+    if (tp.s[p] == 0.0) continue;
+    if (p == 0) s += tp.s[0] * K[0];
+    else s += tp.s[p] * (eta * K[p - 1] - ipow(eta, p) * K[0]) / (p - 1);
+  }
+  return s;
+}
+
+double sector_value(const KernelPiece& kp, const TailPiece3& tp, bool antigrad,
+                    double eta) {
+  double s = 0.0;
+  if (!antigrad) {
+    for (int p = 0; p <= kp.deg; ++p) {
+      if (kp.c[p] == 0.0) continue;
+      s += kp.c[p] * (ipow(kp.cutoff, p + 2) - ipow(eta, p + 2)) / (p + 2);
+    }
+    return s;
+  }
+  for (int p = 0; p <= tp.deg; ++p) {
+    if (tp.s[p] == 0.0) continue;
+    if (p == 0) s += tp.s[0] * (1.0 - eta / kp.cutoff);
+    else s += tp.s[p] * (eta * ipow(kp.cutoff, p - 1) - ipow(eta, p)) / (p - 1);
+  }
+  return s;
+}
+
+// unit_triangle_integral (kernel.hpp:316-399) for one piece; v = the three
+// projected vertices (2 doubles each).
+double unit_triangle_piece(const KernelPiece& kp, const TailPiece3& tp,
+                           bool antigrad, double eta, const double* v) {
+  if (eta >= kp.cutoff) return 0.0;
+  const double radius2 = kp.cutoff * kp.cutoff - eta * eta;
+  const double sector = sector_value(kp, tp, antigrad, eta);
+  double total = 0.0;
+  for (int e = 0; e < 3; ++e) {
+    const double* p0 = v + 2 * e;
+    const double* p1 = v + 2 * ((e + 1) % 3);
+    const double edge[2] = {p1[0] - p0[0], p1[1] - p0[1]};
+    const double len2 = norm2(edge, 2);
+    if (len2 <= tiny_d * tiny_d) continue;
+    const double len = std::sqrt(len2);
+    const double t[2] = {edge[0] / len, edge[1] / len};
+    const double delta = p0[0] * t[1] - p0[1] * t[0];
+    const double delta2 = delta * delta;
+    const double beta2 = eta * eta + delta2;
+    const double beta = std::sqrt(beta2);
+    const double z0 = dot(p0, t, 2);
+    const double z1 = z0 + len;
+    double zs[4];
+    int nz = 0;
+    zs[nz++] = z0;
+    if (radius2 > delta2) {
+      const double zc = std::sqrt(radius2 - delta2);
+      if (z0 < -zc && -zc < z1) zs[nz++] = -zc;
+      if (z0 < zc && zc < z1) zs[nz++] = zc;
+    }
+    zs[nz++] = z1;
+    for (int i = 0; i + 1 < nz; ++i) {
+      const double lo = zs[i], hi = zs[i + 1];
+      if (is_tiny(hi - lo)) continue;
+      const double mid = (lo + hi) / 2.0;
+      if (mid * mid + delta2 < radius2) {
+        total += edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, hi) -
+                 edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, lo);
+      } else {
+        total += sector * std::atan2(delta * (hi - lo), lo * hi + delta2);
+      }
+    }
+  }
+  return total;
+}
+
+double unit_triangle(int k, bool antigrad, double eta, const double* v) {
+  double total = 0.0;
+  for (int i = 0; i < kPieces[k].n; ++i) {
+    total += unit_triangle_piece(kPieces[k].p[i], kTail3[k][i], antigrad, eta, v);
+  }
+  return total;
+}
+
+void cross3(const double* a, const double* b, double* out) {
+  out[0] = a[1] * b[2] - a[2] * b[1];
+  out[1] = a[2] * b[0] - a[0] * b[2];
+  out[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Triangle geometry (geom/triangle.hpp): wnormal = cross(b - a, c - a)/2,
+// normal = normalize(wnormal); project(x): e1 = normalize(b - a),
+// e2 = normalize(cross(wnormal, e1)), p_i = (dot(v_i - x, e1),
+// dot(v_i - x, e2)).
+struct TriFrame {
+  double n[3], d, p[6];
+};
+TriFrame tri_frame(const double* a, const double* b, const double* c,
+                   const double* x, double h) {
+  const double ba[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+  const double ca[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+  double wn[3];
+  cross3(ba, ca, wn);
+  for (double& w : wn) w /= 2.0;
+  TriFrame F;
+  normalize(wn, 3, F.n);
+  double e1[3], e2[3], t[3];
+  normalize(ba, 3, e1);
+  cross3(wn, e1, t);
+  normalize(t, 3, e2);
+  const double hinv = 1.0 / h;
+  const double xa[3] = {x[0] - a[0], x[1] - a[1], x[2] - a[2]};
+  F.d = dot(xa, F.n, 3) * hinv;
+  const double* vs[3] = {a, b, c};
+  for (int i = 0; i < 3; ++i) {
+    const double vx[3] = {vs[i][0] - x[0], vs[i][1] - x[1], vs[i][2] - x[2]};
+    F.p[2 * i] = dot(vx, e1, 3) * hinv;
+    F.p[2 * i + 1] = dot(vx, e2, 3) * hinv;
+  }
+  return F;
+}
+
+// Kernel::flux over a triangle: n w h^-1 unit_flux(|d|, p_a, p_b, p_c).
+void tri_flux(int k, const double* a, const double* b, const double* c,
+              const double* x, double h, double* out) {
+  const TriFrame F = tri_frame(a, b, c, x, h);
+  const double w = kernel_weight(k, 3) * (1.0 / h);
+  const double s = w * unit_triangle(k, false, std::abs(F.d), F.p);
+  for (int i = 0; i < 3; ++i) out[i] = F.n[i] * s;
+}
+
+// Kernel::antigrad_flux over a triangle.
+double tri_antigrad_flux(int k, const double* a, const double* b,
+                         const double* c, const double* x, double h) {
+  const TriFrame F = tri_frame(a, b, c, x, h);
+  return std::copysign(kernel_weight(k, 3), F.d) *
+         unit_triangle(k, true, std::abs(F.d), F.p);
+}
+
+// Closest point of a segment to x (Segment::clamp, geom/segment.hpp:91-106).
+void seg_clamp(const double* a, const double* b, const double* x, int d,
+               double* q) {
+  double ba[3], xa[3];
+  for (int k = 0; k < d; ++k) {
+    ba[k] = b[k] - a[k];
+    xa[k] = x[k] - a[k];
+    q[k] = a[k];
+  }
+  const double len2 = norm2(ba, d);
+  if (is_tiny(len2)) return;
+  const double t = dot(xa, ba, d) / len2;
+  if (t > 1.0) {
+    for (int k = 0; k < d; ++k) q[k] = b[k];
+  } else if (!(t < 0.0)) {
+    for (int k = 0; k < d; ++k) q[k] = a[k] + t * ba[k];
+  }
+}
+
+// Closest point of a triangle to x (Triangle::clamp, geom/triangle.hpp):
+// the Voronoi-region walk of Ericson, Real-Time Collision Detection 5.1.5,
+// with the degenerate triangle clamped to its longest edge.
+void tri_clamp(const double* a, const double* b, const double* c,
+               const double* x, double* q) {
+  const double ba[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+  const double ca[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+  const double cb[3] = {c[0] - b[0], c[1] - b[1], c[2] - b[2]};
+  double wn[3];
+  cross3(ba, ca, wn);
+  for (double& w : wn) w /= 2.0;
+  if (is_tiny(norm(wn, 3))) {
+    const double l_ab = norm2(ba, 3), l_bc = norm2(cb, 3), l_ca = norm2(ca, 3);
+    if (l_ab >= l_bc && l_ab >= l_ca) return seg_clamp(a, b, x, 3, q);
+    if (l_bc >= l_ca) return seg_clamp(b, c, x, 3, q);
+    return seg_clamp(a, c, x, 3, q);
+  }
+  auto set = [q](const double* p) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; };
+  const double pa[3] = {x[0] - a[0], x[1] - a[1], x[2] - a[2]};
+  const double d1 = dot(ba, pa, 3), d2 = dot(ca, pa, 3);
+  if (d1 <= 0.0 && d2 <= 0.0) return set(a);
+  const double pb[3] = {x[0] - b[0], x[1] - b[1], x[2] - b[2]};
+  const double d3 = dot(ba, pb, 3), d4 = dot(ca, pb, 3);
+  if (d3 >= 0.0 && d4 <= d3) return set(b);
+  const double pc[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+  const double d5 = dot(ba, pc, 3), d6 = dot(ca, pc, 3);
+  if (d6 >= 0.0 && d5 <= d6) return set(c);
+  const double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+    const double t = d1 / (d1 - d3);
+    for (int k = 0; k < 3; ++k) q[k] = a[k] + t * ba[k];
+    return;
+  }
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+    const double t = d2 / (d2 - d6);
+    for (int k = 0; k < 3; ++k) q[k] = a[k] + t * ca[k];
+    return;
+  }
+  const double va = d3 * d6 - d5 * d4;
+  if (va <= 0.0 && d4 >= d3 && d5 >= d6) {
+    const double t = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    for (int k = 0; k < 3; ++k) q[k] = b[k] + t * cb[k];
+    return;
+  }
+  const double v = vb / (va + vb + vc);
+  const double w = vc / (va + vb + vc);
+  for (int k = 0; k < 3; ++k) q[k] = a[k] + v * ba[k] + w * ca[k];
+}
+
+// Triangle::intersects(BSphere): boxes overlap and the closest point of the
+// triangle is in the sphere.
+bool tri_in_sphere(const double* a, const double* b, const double* c,
+                   const double* x, double radius) {
+  for (int k = 0; k < 3; ++k) {
+    const double lo = std::min(std::min(a[k], b[k]), c[k]);
+    const double hi = std::max(std::max(a[k], b[k]), c[k]);
+    if (!(x[k] - radius <= hi && lo <= x[k] + radius)) return false;
+  }
+  double q[3];
+  tri_clamp(a, b, c, x, q);
+  const double d[3] = {q[0] - x[0], q[1] - x[1], q[2] - x[2]};
+  return norm2(d, 3) <= radius * radius;
+}
+
+// Exact generalized winding number of a closed triangle mesh at x
+// (Triangle::winding_number, geom/triangle.hpp, summed over the mesh):
+// per triangle atan2(det(a', b', c'), |a'||b'||c'| + (a'.b')|c'| +
+// (b'.c')|a'| + (c'.a')|b'|) / (2 pi), primes = vertex - x (the solid
+// angle formula of Van Oosterom and Strackee).  tris: 9 doubles each.
+double winding_number3(int32_t n_tris, const double* tris, const double* x) {
+  double w = 0.0;
+  for (int32_t i = 0; i < n_tris; ++i) {
+    const double* t = tris + 9 * static_cast<int64_t>(i);
+    const double ap[3] = {t[0] - x[0], t[1] - x[1], t[2] - x[2]};
+    const double bp[3] = {t[3] - x[0], t[4] - x[1], t[5] - x[2]};
+    const double cp[3] = {t[6] - x[0], t[7] - x[1], t[8] - x[2]};
+    const double na = norm(ap, 3), nb = norm(bp, 3), nc = norm(cp, 3);
+    const double den = na * nb * nc + dot(ap, bp, 3) * nc +
+                       dot(bp, cp, 3) * na + dot(cp, ap, 3) * nb;
+    double bc[3];
+    cross3(bp, cp, bc);
+    w += std::atan2(dot(ap, bc, 3), den) / (2.0 * std::numbers::pi);
+  }
+  return w;
+}
+
 template<class Num>
 struct Kern {
   int id;
@@ -584,9 +918,10 @@ int64_t export_csr(const Adjacency& adj, int64_t n, int64_t* offsets,
 // ---------------------------------------------------------------------------
 // FluidEquations (fluid_equations.hpp:79-512).  With particle walls (no
 // boundary faces, an always-true containment) gamma = 1 and grad_gamma = 0
-// everywhere (:166-193) and every face term vanishes.  With faces (2D), the
-// tank's fixed particles are the face vertices; gamma, grad_gamma, the face
-// terms and the gamma-divided pair sums follow the reference.
+// everywhere (:166-193) and every face term vanishes.  With faces
+// (segments in 2D, triangles in 3D) the tank's fixed particles are the face
+// vertices; gamma, grad_gamma, the face terms and the gamma-divided pair
+// sums follow the reference.
 
 struct TankView {
   int64_t nf = 0, nw = 0, n = 0;
@@ -597,8 +932,9 @@ struct TankView {
   double* rho = nullptr;
   double* drho = nullptr;
   double* dv = nullptr;
-  // Boundary faces (2D): vertex pairs as indices into the tank's fixed
-  // particles, and the containment polygon (closed loop of vertices).
+  // Boundary faces: dim vertex indices per face into the tank's fixed
+  // particles.  Containment: in 2D a closed loop of n_poly vertices, in 3D
+  // n_poly triangles (9 doubles each) of a closed, outward-oriented mesh.
   int32_t n_faces = 0;
   const int32_t* face_verts = nullptr;
   int32_t n_poly = 0;
@@ -628,21 +964,45 @@ struct Solver {
 
   bool faces() const { return T.n_faces > 0; }
   const double* vert(int32_t f, int i) const {
-    return T.r + (T.nf + T.face_verts[2 * f + i]) * dim;
+    return T.r + (T.nf + T.face_verts[dim * f + i]) * dim;
   }
   int64_t vert_index(int32_t f, int i) const {
-    return T.nf + T.face_verts[2 * f + i];
+    return T.nf + T.face_verts[dim * f + i];
   }
-  // Field of a face's vertex pair: avg (field.hpp:59-64, core/math.hpp:130).
-  double face_avg(const std::vector<double>& fld, int32_t f) const {
-    return (fld[vert_index(f, 0)] + fld[vert_index(f, 1)]) / 2.0;
-  }
+  // Field of a face's vertices: avg (field.hpp:59-64, core/math.hpp:130),
+  // (a + b)/2 or (a + b + c)/3.
   double face_avg(const double* fld, int32_t f) const {
-    return (fld[vert_index(f, 0)] + fld[vert_index(f, 1)]) / 2.0;
+    if (dim == 2) return (fld[vert_index(f, 0)] + fld[vert_index(f, 1)]) / 2.0;
+    return (fld[vert_index(f, 0)] + fld[vert_index(f, 1)] + fld[vert_index(f, 2)]) / 3.0;
   }
-
+  double face_avg(const std::vector<double>& fld, int32_t f) const {
+    return face_avg(fld.data(), f);
+  }
   double face_avg_vec(const double* fld, int32_t f, int k) const {
-    return (fld[vert_index(f, 0) * dim + k] + fld[vert_index(f, 1) * dim + k]) / 2.0;
+    if (dim == 2) {
+      return (fld[vert_index(f, 0) * dim + k] + fld[vert_index(f, 1) * dim + k]) / 2.0;
+    }
+    return (fld[vert_index(f, 0) * dim + k] + fld[vert_index(f, 1) * dim + k] +
+            fld[vert_index(f, 2) * dim + k]) / 3.0;
+  }
+  // Kernel::flux / antigrad_flux of face f at x, and face-sphere overlap.
+  void flux(int32_t f, const double* x, double* out) const {
+    if (dim == 2) return face_flux(P.kernel, vert(f, 0), vert(f, 1), x, T.h, out);
+    tri_flux(P.kernel, vert(f, 0), vert(f, 1), vert(f, 2), x, T.h, out);
+  }
+  double antigrad_flux(int32_t f, const double* x) const {
+    if (dim == 2) return face_antigrad_flux(P.kernel, vert(f, 0), vert(f, 1), x, T.h);
+    return tri_antigrad_flux(P.kernel, vert(f, 0), vert(f, 1), vert(f, 2), x, T.h);
+  }
+  bool in_sphere(int32_t f, const double* x) const {
+    if (dim == 2) return face_in_sphere(vert(f, 0), vert(f, 1), x, K.radius);
+    return tri_in_sphere(vert(f, 0), vert(f, 1), vert(f, 2), x, K.radius);
+  }
+  // FastWindingFunc::contains (fast_winding.hpp:80-95): winding > 1/2, here
+  // with the exact winding number.
+  bool contains(const double* x) const {
+    if (dim == 2) return winding_number(T.n_poly, T.poly, x) > 0.5;
+    return winding_number3(T.n_poly, T.poly, x) > 0.5;
   }
 
   // ParticleMesh face adjacency (particle_mesh.hpp:149-161): faces within
@@ -652,9 +1012,7 @@ struct Solver {
       auto& out = fadj[a];
       out.clear();
       for (int32_t fi = 0; fi < T.n_faces; ++fi) {
-        if (face_in_sphere(vert(fi, 0), vert(fi, 1), T.r + a * dim, K.radius)) {
-          out.push_back(fi);
-        }
+        if (in_sphere(fi, T.r + a * dim)) out.push_back(fi);
       }
     });
   }
@@ -663,23 +1021,21 @@ struct Solver {
   void compute_gamma() {
     parallel_for(T.n, nthreads, [&](int64_t a) {
       double* g = &ggam[a * dim];
-      g[0] = g[1] = 0.0;
+      for (int k = 0; k < dim; ++k) g[k] = 0.0;
       for (int32_t fi : fadj[a]) {
-        double fl[2];
-        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * dim, T.h, fl);
-        g[0] += fl[0];
-        g[1] += fl[1];
+        double fl[3];
+        flux(fi, T.r + a * dim, fl);
+        for (int k = 0; k < dim; ++k) g[k] += fl[k];
       }
-      double ga = winding_number(T.n_poly, T.poly, T.r + a * dim) > 0.5 ? 1.0 : 0.0;
-      const double ng = norm(g, 2);
+      double ga = contains(T.r + a * dim) ? 1.0 : 0.0;
+      const double ng = norm(g, dim);
       if (!is_tiny(ng)) {
-        const double n_a[2] = {g[0] / ng, g[1] / ng};
         const double s = (2.0 * ga - 1.0);
-        const double r_a[2] = {T.r[a * dim] + s * n_a[0] * pow2(T.h),
-                               T.r[a * dim + 1] + s * n_a[1] * pow2(T.h)};
-        for (int32_t fi : fadj[a]) {
-          ga -= face_antigrad_flux(P.kernel, vert(fi, 0), vert(fi, 1), r_a, T.h);
+        double r_a[3];
+        for (int k = 0; k < dim; ++k) {
+          r_a[k] = T.r[a * dim + k] + s * (g[k] / ng) * pow2(T.h);
         }
+        for (int32_t fi : fadj[a]) ga -= antigrad_flux(fi, r_a);
       }
       gamma[a] = ga;
     });
@@ -762,12 +1118,10 @@ struct Solver {
       double acc = 0.0;
       // Face terms (fluid_equations.hpp:241-247).
       for (int32_t fi : fadj[a]) {
-        double gg[2];
-        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * dim, T.h, gg);
-        const double v_as[2] = {
-            T.v[a * dim] - face_avg_vec(T.v, fi, 0),
-            T.v[a * dim + 1] - face_avg_vec(T.v, fi, 1)};
-        acc -= face_avg(T.rho, fi) * dot(v_as, gg, 2) / gamma[a];
+        double gg[3], v_as[3];
+        flux(fi, T.r + a * dim, gg);
+        for (int k = 0; k < dim; ++k) v_as[k] = T.v[a * dim + k] - face_avg_vec(T.v, fi, k);
+        acc -= face_avg(T.rho, fi) * dot(v_as, gg, dim) / gamma[a];
       }
       for (int64_t j = adj.off[a]; j < adj.off[a + 1]; ++j) {
         const int64_t b = adj.idx[j];
@@ -812,26 +1166,24 @@ struct Solver {
       acc[1] = -P.g;  // unit<1>(r[a], -g)
       // Face terms: wall pressure and wall shear (fluid_equations.hpp:278-291).
       for (int32_t fi : fadj[a]) {
-        double gg[2];
-        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * dim, T.h, gg);
+        double gg[3];
+        flux(fi, T.r + a * dim, gg);
         const double rho_s = face_avg(T.rho, fi);
         const double p_s = face_avg(p, fi);
         const double P_as =
             rho_s * (p[a] / pow2(T.rho[a]) + p_s / pow2(rho_s));
-        double n_s[2], t_as[2];
-        normalize(gg, 2, n_s);
-        const double v_as[2] = {T.v[a * dim] - face_avg_vec(T.v, fi, 0),
-                                T.v[a * dim + 1] - face_avg_vec(T.v, fi, 1)};
-        const double vn = dot(v_as, n_s, 2);
-        const double vt[2] = {v_as[0] - vn * n_s[0], v_as[1] - vn * n_s[1]};
-        normalize(vt, 2, t_as);
-        const double r_as[2] = {T.r[a * dim] - face_avg_vec(T.r, fi, 0),
-                                T.r[a * dim + 1] - face_avg_vec(T.r, fi, 1)};
-        const double dr_as = std::max(T.h / 2.0, dot(r_as, n_s, 2));
+        double n_s[3], t_as[3], v_as[3], vt[3], r_as[3];
+        normalize(gg, dim, n_s);
+        for (int k = 0; k < dim; ++k) v_as[k] = T.v[a * dim + k] - face_avg_vec(T.v, fi, k);
+        const double vn = dot(v_as, n_s, dim);
+        for (int k = 0; k < dim; ++k) vt[k] = v_as[k] - vn * n_s[k];
+        normalize(vt, dim, t_as);
+        for (int k = 0; k < dim; ++k) r_as[k] = T.r[a * dim + k] - face_avg_vec(T.r, fi, k);
+        const double dr_as = std::max(T.h / 2.0, dot(r_as, n_s, dim));
         const double Pi_s =
-            2.0 * P.mu / (T.rho[a] * dr_as) * dot(v_as, t_as, 2);
-        const double ng = norm(gg, 2);
-        for (int k = 0; k < 2; ++k) {
+            2.0 * P.mu / (T.rho[a] * dr_as) * dot(v_as, t_as, dim);
+        const double ng = norm(gg, dim);
+        for (int k = 0; k < dim; ++k) {
           acc[k] += (P_as * gg[k] - Pi_s * t_as[k] * ng) / gamma[a];
         }
       }
@@ -924,10 +1276,10 @@ struct Solver {
       double* gra = &gr[a * d];
       // Face terms (fluid_equations.hpp:340-349).
       for (int32_t fi : fadj[a]) {
-        double gg[2];
-        face_flux(P.kernel, vert(fi, 0), vert(fi, 1), T.r + a * d, T.h, gg);
-        double r_sa[2], v_sa[2];
-        for (int k = 0; k < 2; ++k) {
+        double gg[3];
+        flux(fi, T.r + a * d, gg);
+        double r_sa[3], v_sa[3];
+        for (int k = 0; k < d; ++k) {
           r_sa[k] = face_avg_vec(T.r, fi, k) - T.r[a * d + k];
           v_sa[k] = face_avg_vec(T.v, fi, k) - T.v[a * d + k];
         }
@@ -1378,11 +1730,12 @@ int32_t or_wcsph_step_faces(const tg_params* params, int32_t n_tanks,
     for (int32_t t = 0; t < n_tanks; ++t) {
       const or_tank_faces& F = faces[t];
       if (F.n_faces == 0) continue;
-      if (params->dim != 2 || F.n_faces < 0 || F.face_verts == nullptr ||
-          F.n_poly < 3 || F.poly == nullptr) {
+      const int32_t min_poly = params->dim == 2 ? 3 : 4;
+      if (F.n_faces < 0 || F.face_verts == nullptr || F.n_poly < min_poly ||
+          F.poly == nullptr) {
         return TG_ERR_INVALID_ARGUMENT;
       }
-      for (int32_t i = 0; i < 2 * F.n_faces; ++i) {
+      for (int32_t i = 0; i < params->dim * F.n_faces; ++i) {
         if (F.face_verts[i] < 0 || F.face_verts[i] >= tanks[t].n_wall) {
           return TG_ERR_INVALID_ARGUMENT;
         }
@@ -1434,6 +1787,26 @@ double or_kernel_antigrad_flux2(int32_t kernel, const double* a,
 
 double or_winding_number2(int32_t n_poly, const double* poly, const double* x) {
   return winding_number(n_poly, poly, x);
+}
+
+void or_kernel_flux3(int32_t kernel, const double* a, const double* b,
+                     const double* c, const double* x, double h, double* out) {
+  tri_flux(kernel, a, b, c, x, h, out);
+}
+
+double or_kernel_antigrad_flux3(int32_t kernel, const double* a,
+                                const double* b, const double* c,
+                                const double* x, double h) {
+  return tri_antigrad_flux(kernel, a, b, c, x, h);
+}
+
+double or_winding_number3(int32_t n_tris, const double* tris, const double* x) {
+  return winding_number3(n_tris, tris, x);
+}
+
+int32_t or_triangle_in_sphere(const double* a, const double* b, const double* c,
+                              const double* x, double radius) {
+  return tri_in_sphere(a, b, c, x, radius) ? 1 : 0;
 }
 
 int32_t or_tank_neighbour_counts(const tg_params* params, int32_t n_tanks,

@@ -85,11 +85,12 @@ int32_t or_wcsph_step(const tg_params* params, int32_t n_tanks,
                       double* drho_dt, double* dv_dt, int32_t n_steps,
                       double* dt_out, double* time_io, int32_t nthreads);
 
-/* Boundary faces of one tank (2D semi-analytical walls): n_faces segments
- * as index pairs into the tank's fixed particles (the face vertices), and
- * the containment polygon, a closed loop of n_poly vertices (x, y); a point
- * is inside when the polygon's winding number around it exceeds 1/2.
- * n_faces = 0: particle walls. */
+/* Boundary faces of one tank (semi-analytical walls): n_faces faces as dim
+ * indices each into the tank's fixed particles (the face vertices; segments
+ * in 2D, triangles in 3D), and the containment surface: in 2D a closed loop
+ * of n_poly vertices (x, y), in 3D n_poly triangles (9 doubles each) of a
+ * closed mesh with outward normals.  A point is inside when the surface's
+ * winding number around it exceeds 1/2.  n_faces = 0: particle walls. */
 typedef struct or_tank_faces {
   int32_t n_faces;
   const int32_t* face_verts;
@@ -111,6 +112,18 @@ void or_kernel_flux2(int32_t kernel, const double* a, const double* b,
 double or_kernel_antigrad_flux2(int32_t kernel, const double* a,
                                 const double* b, const double* x, double h);
 double or_winding_number2(int32_t n_poly, const double* poly, const double* x);
+
+/* Kernel flux (3 components) and antigradient flux of triangle a-b-c at x
+ * with width h, the triangle mesh winding number at x, and the
+ * triangle-sphere overlap test of the face adjacency. */
+void or_kernel_flux3(int32_t kernel, const double* a, const double* b,
+                     const double* c, const double* x, double h, double* out);
+double or_kernel_antigrad_flux3(int32_t kernel, const double* a,
+                                const double* b, const double* c,
+                                const double* x, double h);
+double or_winding_number3(int32_t n_tris, const double* tris, const double* x);
+int32_t or_triangle_in_sphere(const double* a, const double* b, const double* c,
+                              const double* x, double radius);
 
 /* Neighbour counts and hashes of every particle in its tank (tank-local ids),
  * via or_grid_search with radius = unit_radius * h. */

@@ -164,6 +164,84 @@ def dam_break_3d(H: float = 1.0, nx_per_H: int = 200, column=(2.0, 1.0, 1.0),
                 H=H, name=f"dam_break_3d_H{H}_dx1/{nx_per_H}")
 
 
+def box_mesh(lo, hi) -> np.ndarray:
+    """The 12 outward-oriented triangles (12, 3, 3) of an axis-aligned box:
+    a containment surface whose winding number is 1 inside."""
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], dtype=np.float64)
+    quads = [(0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (2, 3, 7, 6), (1, 2, 6, 5), (0, 4, 7, 3)]
+    tris = []
+    for a, b, c, d in quads:
+        tris += [(a, b, c), (a, c, d)]
+    return v[np.array(tris)]
+
+
+def box_faces(width: float, height: float, depth: float, dx: float):
+    """Boundary faces of the box [0, W] x [0, Ht] x [0, D]: each side split
+    into a grid of max(1, ceil(len / dx)) intervals per axis, each cell into
+    two triangles, normals cross(b - a, c - a) pointing into the box (as the
+    2D pool's faces do); vertices shared between sides.  Returns
+    (vertices (n, 3), faces (m, 3))."""
+    ext = (width, height, depth)
+    n = [max(1, int(math.ceil(e / dx))) for e in ext]
+    index: dict = {}
+    verts = []
+
+    def vid(ijk):
+        if ijk not in index:
+            index[ijk] = len(verts)
+            verts.append(tuple(ext[k] * ijk[k] / n[k] for k in range(3)))
+        return index[ijk]
+
+    faces = []
+    # (fixed axis, fixed side, u axis, v axis) with cross(u, v) inward.
+    sides = [(1, 0, 2, 0), (1, 1, 0, 2), (0, 0, 1, 2), (0, 1, 2, 1), (2, 0, 0, 1), (2, 1, 1, 0)]
+    for ax, side, u, v in sides:
+        for i in range(n[u]):
+            for j in range(n[v]):
+                def corner(di, dj):
+                    ijk = [0, 0, 0]
+                    ijk[ax] = side * n[ax]
+                    ijk[u] = i + di
+                    ijk[v] = j + dj
+                    return vid(tuple(ijk))
+                p00, p10, p01, p11 = corner(0, 0), corner(1, 0), corner(0, 1), corner(1, 1)
+                faces += [(p00, p10, p11), (p00, p11, p01)]
+    return np.array(verts, dtype=np.float64), np.array(faces, dtype=np.int32)
+
+
+def dam_break_3d_faces(nx_per_H: int = 80, H: float = 0.6, column=(2.0, 1.0, 1.0),
+                       tank=(5.366, 4.0), h_factor: float = 1.3, g: float = G,
+                       rho0: float = RHO0) -> dict:
+    """The titwcsph scenario extruded to 3D with triangle faces: column
+    column * H at dr (i + 1, j + 1, k + 1), pool tank[0] H x tank[1] H x
+    (K + 1) dr whose triangulated sides (box_faces) carry one fixed particle
+    per vertex, cs0 = 20 sqrt(gH), h = h_factor dr, m = rho0 dr^3,
+    hydrostatic density; the containment is the pool box (box_mesh)."""
+    dx = H / nx_per_H
+    L = column[0] * H
+    M = int(round(L / dx))
+    N = int(round(column[1] * H / dx))
+    K = int(round(column[2] * H / dx))
+    i, j, k = np.meshgrid(np.arange(M), np.arange(N), np.arange(K), indexing="ij")
+    fluid = np.stack([dx * (i.ravel() + 1.0), dx * (j.ravel() + 1.0),
+                      dx * (k.ravel() + 1.0)], axis=1)
+    W, Ht, D = tank[0] * H, tank[1] * H, (K + 1) * dx
+    walls, faces = box_faces(W, Ht, D, dx)
+    cs0 = 20.0 * math.sqrt(g * H)
+    p = hydrostatic_pressure(fluid[:, 0], fluid[:, 1], H, L, g, rho0)
+    rho_f = rho0 + p / (cs0 * cs0)
+    r = np.concatenate([fluid, walls])
+    rho = np.concatenate([rho_f, np.full(walls.shape[0], rho0)])
+    tank_d = dict(n_fluid=fluid.shape[0], n_wall=walls.shape[0], h=h_factor * dx,
+                  m=rho0 * dx ** 3, rho0=rho0, cs0=cs0)
+    return dict(dim=3, tanks=[tank_d], r=r, v=np.zeros_like(r), rho=rho, dx=dx, H=H,
+                faces=[dict(face_verts=faces, poly=box_mesh((0.0, 0.0, 0.0), (W, Ht, D)))],
+                name=f"dam_break_3d_faces_dx=H/{nx_per_H}")
+
+
 def cloud_3d(n_total: int = 4_000_000, lattice_fraction: float = 0.7,
              n_clusters: int = 8, sigma: float = 0.05, jitter: float = 0.25,
              h_factor: float = 1.3, seed: int = 20261203, rho0: float = RHO0) -> dict:
