@@ -292,17 +292,24 @@ int tg_summation_density_noalloc(int32_t dim, int32_t kernel, int64_t n,
  * with the wall normal; :241-247 and :276-292 the face terms of continuity
  * and momentum; :335-349, :465-467, :491-511 the face terms of shifting and
  * the free-surface correction; kernel.hpp:194-221 the kernel flux and
- * antigradient flux of a face).  2D and the FP64 form only.
+ * antigradient flux of a face).  Segments in 2D, triangles in 3D; both
+ * arithmetic forms (the face sums run in FP64 either way).
  *
- * face_verts: 2 per face, indices into the tank's fixed particles (0 = the
+ * face_verts: dim per face, indices into the tank's fixed particles (0 = the
  * tank's first fixed particle), which are the face vertices and stay fixed
  * (titwcsph appends one fixed particle per vertex of the tessellated
- * domain, wcsph.cpp:109-112).  poly: the containment polygon, n_poly (x, y)
- * vertices of a closed loop; a point is inside when its winding number
- * exceeds 1/2 (the reference passes a FastWinding of the domain,
- * fast_winding.hpp:80-95).  n_faces = 0 returns the tank to particle walls.
- * Call after tg_particles_upload (a new upload drops the faces); applies to
- * the following steps. */
+ * domain, wcsph.cpp:109-112).  A face's normal, normalize(cross(b - a)) in
+ * 2D and normalize(cross(b - a, c - a)) in 3D, points into the fluid.
+ * poly: the containment surface; in 2D n_poly (x, y) vertices of a closed
+ * loop, in 3D n_poly triangles (9 doubles each: a, b, c) of a closed mesh
+ * with outward normals.  A point is inside when the surface's winding number
+ * around it exceeds 1/2 (the reference passes a FastWinding of the domain,
+ * fast_winding.hpp:80-95).  In 3D every particle near the surface evaluates
+ * the exact winding number over all n_poly triangles, so a coarse
+ * containment mesh (as titwcsph's separate containment domain) keeps that
+ * cheap.  n_faces = 0 returns the tank to particle walls.  Call after
+ * tg_particles_upload (a new upload drops the faces); applies to the
+ * following steps. */
 int tg_tank_faces(tg_context* ctx, int32_t tank, int32_t n_faces,
                   const int32_t* face_verts, int32_t n_poly,
                   const double* poly);

@@ -1,9 +1,10 @@
-"""Semi-analytical face boundaries on the GPU (2D; FP64 and the compensated
-form) against the
-oracle, on the titwcsph scenario itself (source/titwcsph/wcsph.cpp:37-142:
-tessellated pool faces with one fixed particle per vertex, containment by
-the pool polygon).  Tolerances (relative L2 over the fluid): 1 step r, v,
-rho <= 1e-11 and dv/dt, drho/dt <= 1e-9; 5 steps <= 1e-10."""
+"""Semi-analytical face boundaries on the GPU (FP64 and the compensated
+form) against the oracle: in 2D on the titwcsph scenario itself
+(source/titwcsph/wcsph.cpp:37-142: tessellated pool faces with one fixed
+particle per vertex, containment by the pool polygon), in 3D on the same
+pool extruded, with triangulated sides and a box containment mesh.
+Tolerances (relative L2 over the fluid): 1 step r, v, rho <= 1e-11 and
+dv/dt, drho/dt <= 1e-9; 5 steps <= 1e-10."""
 
 from __future__ import annotations
 
@@ -70,7 +71,7 @@ def test_faces_batched_with_a_particle_wall_tank(gpu_lib):
     _compare(scn, physics.reference_params(2), 3, 1e-10)
 
 
-def test_faces_survive_autotune_and_reject_3d_and_bad_vertices(gpu_lib):
+def test_faces_survive_autotune_and_reject_bad_vertices(gpu_lib):
     scn = scenarios.dam_break_2d_faces(nx_per_H=16)
     P = physics.reference_params(2)
     f = fluid_mask(scn)
@@ -83,17 +84,62 @@ def test_faces_survive_autotune_and_reject_3d_and_bad_vertices(gpu_lib):
         a, b = gpu_state(ctx), gpu_state(ref)
     assert rel_l2(a["rho"][f], b["rho"][f]) <= 1e-11
     assert rel_l2(a["r"][f], b["r"][f]) <= 1e-11
-    s3 = scenarios.dam_break_3d(nx_per_H=6)
-    with _abi.Context(physics.reference_params(3)) as ctx:
-        ctx.upload(s3["tanks"], s3["r"], s3["v"], s3["rho"])
-        with pytest.raises(_abi.TgError) as ei:
-            ctx.set_faces(0, np.array([[0, 1]], dtype=np.int32), scn["faces"][0]["poly"])
-        assert ei.value.status == _abi.TG_ERR_INVALID_ARGUMENT
     with _abi.Context(P) as ctx:
         ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
         bad = np.array([[0, 10**6]], dtype=np.int32)
         with pytest.raises(_abi.TgError):
             ctx.set_faces(0, bad, scn["faces"][0]["poly"])
+    s3 = _scn3()
+    with _abi.Context(physics.reference_params(3)) as ctx:
+        ctx.upload(s3["tanks"], s3["r"], s3["v"], s3["rho"])
+        fv = s3["faces"][0]["face_verts"]
+        with pytest.raises(_abi.TgError) as ei:
+            ctx.set_faces(0, np.array([[0, 1, 10**6]], dtype=np.int32), s3["faces"][0]["poly"])
+        assert ei.value.status == _abi.TG_ERR_INVALID_ARGUMENT
+        with pytest.raises(_abi.TgError):
+            ctx.set_faces(0, fv, s3["faces"][0]["poly"][:3])
+
+
+def _scn3(nx_per_H=6):
+    return scenarios.dam_break_3d_faces(nx_per_H=nx_per_H, tank=(3.0, 1.5))
+
+
+@pytest.mark.parametrize("shifting", (False, True))
+def test_3d_faces_vs_oracle(gpu_lib, shifting):
+    scn = _scn3()
+    P = physics.reference_params(3)
+    P.post_integrate = _abi.TG_POST_SHIFTING if shifting else _abi.TG_POST_PREPARE
+    _compare(scn, P, 1, 1e-11, 1e-9)
+    _compare(scn, P, 4, 1e-10)
+
+
+@pytest.mark.parametrize("kernel", (_abi.TG_KERNEL_WENDLAND_C2, _abi.TG_KERNEL_CUBIC_SPLINE))
+def test_3d_faces_other_kernels_and_term_sets(gpu_lib, kernel):
+    scn = _scn3()
+    _compare(scn, physics.reference_params(3, kernel=kernel), 2, 1e-10)
+    _compare(scn, physics.baseline_params(3, kernel=kernel), 2, 1e-10)
+
+
+def test_3d_faces_batched_with_a_particle_wall_tank(gpu_lib):
+    a = _scn3()
+    b = scenarios.dam_break_3d(nx_per_H=6)
+    scn = dict(dim=3, tanks=a["tanks"] + b["tanks"],
+               r=np.concatenate([a["r"], b["r"]]), v=np.concatenate([a["v"], b["v"]]),
+               rho=np.concatenate([a["rho"], b["rho"]]), faces=[a["faces"][0], None])
+    _compare(scn, physics.reference_params(3), 2, 1e-10)
+
+
+def test_3d_faces_fp32_compensated_vs_fp64_oracle(gpu_lib):
+    scn = _scn3()
+    P64 = physics.reference_params(3)
+    P32 = physics.reference_params(3, precision=_abi.TG_FP32C)
+    o = oracle_run(scn, P64, 20)
+    f = fluid_mask(scn)
+    with gpu_context(scn, P32) as ctx:
+        ctx.step(20)
+        g = gpu_state(ctx)
+    assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5
+    assert rel_l2(g["r"][f], o.r[f]) <= 1e-6
 
 
 @pytest.mark.parametrize("shifting", (False, True))

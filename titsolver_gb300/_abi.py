@@ -374,10 +374,12 @@ class Context:
         return {k: getattr(t, k) for k, _ in TgTuning._fields_}
 
     def set_faces(self, tank: int, face_verts, poly):
-        """Boundary faces of a tank (2D, FP64): vertex index pairs into the
-        tank's fixed particles and the containment polygon."""
-        fv = np.ascontiguousarray(face_verts, dtype=np.int32).reshape(-1, 2)
-        pl = np.ascontiguousarray(poly, dtype=np.float64).reshape(-1, 2)
+        """Boundary faces of a tank: dim vertex indices per face into the
+        tank's fixed particles, and the containment surface (2D: a closed
+        polygon, (n, 2); 3D: outward-oriented triangles, (n, 3, 3))."""
+        d = self.params.dim
+        fv = np.ascontiguousarray(face_verts, dtype=np.int32).reshape(-1, d)
+        pl = np.ascontiguousarray(poly, dtype=np.float64).reshape(-1, 2 if d == 2 else 9)
         self._check(self.lib.tg_tank_faces(self.handle, int(tank), fv.shape[0],
                                            _ptr(fv, ctypes.c_int32), pl.shape[0],
                                            _ptr(pl, ctypes.c_double)), "tg_tank_faces")

@@ -860,11 +860,45 @@ int tg_timer_stop(tg_context* ctx, double* ms) {
 
 namespace {
 
-// Device tables of the boundary faces of every tank (face_host): segments
-// and vertex ids, per-cell face lists (each face registered in every cell of
-// its bounding box grown by the support radius, so a cell's list holds
-// every face within reach of its points, ascending), per-row containment
-// edge lists, and the per-particle gamma buffers.
+// Exact generalized winding number of a closed triangle mesh at x (9
+// doubles per triangle; the solid-angle sum of the device's
+// face_contains3).
+double winding_number3(const std::vector<double>& tris, size_t first, size_t count,
+                       const double* x) {
+  double w = 0.0;
+  for (size_t i = first; i < first + count; ++i) {
+    const double* t = tris.data() + 9 * i;
+    double ap[3], bp[3], cp[3];
+    for (int k = 0; k < 3; ++k) {
+      ap[k] = t[k] - x[k];
+      bp[k] = t[3 + k] - x[k];
+      cp[k] = t[6 + k] - x[k];
+    }
+    auto dot = [](const double* a, const double* b) {
+      return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+    };
+    const double na = std::sqrt(dot(ap, ap)), nb = std::sqrt(dot(bp, bp)),
+                 nc = std::sqrt(dot(cp, cp));
+    const double den = na * nb * nc + dot(ap, bp) * nc + dot(bp, cp) * na + dot(cp, ap) * nb;
+    const double bc[3] = {bp[1] * cp[2] - bp[2] * cp[1], bp[2] * cp[0] - bp[0] * cp[2],
+                          bp[0] * cp[1] - bp[1] * cp[0]};
+    w += std::atan2(dot(ap, bc), den) / (2.0 * 3.141592653589793);
+  }
+  return w;
+}
+
+// Device tables of the boundary faces of every tank (face_host): face
+// coordinates and vertex ids, per-cell face lists (each face registered in
+// every cell of its bounding box grown by the support radius, so a cell's
+// list holds every face within reach of its points, ascending), the
+// containment tables (2D: per-row polygon edge lists; 3D: per-cell answers
+// and the surface's triangles), and the per-particle gamma buffers.
+//
+// 3D containment per tank: every cell that a containment triangle's
+// bounding box (grown by a hair) reaches is marked for the exact test; the
+// remaining cells split into face-connected components that the surface
+// does not cross, so the winding number is constant on each, and one exact
+// evaluation at a cell centre answers for the whole component.
 int build_faces(tg_context* ctx) {
   Context& C = ctx->c;
   C.faces = tg::FaceArgs{};
@@ -872,24 +906,29 @@ int build_faces(tg_context* ctx) {
   for (const auto& t : C.face_host) any = any || !t.face_verts.empty();
   if (!any) return TG_OK;
   const int32_t nt = C.ntanks;
+  const int D = C.P.dim;
   // Fixed-particle positions (the face vertices).
-  std::vector<double> r(static_cast<size_t>(C.n) * 2);
+  std::vector<double> r(static_cast<size_t>(C.n) * D);
   int st = tg_particles_download(ctx, TG_FIELD_R, r.data());
   if (st != TG_OK) return st;
   const double unit_radius = tg::kernel_unit_radius(C.P.kernel);
-  std::vector<double> seg, edges;
+  std::vector<double> coords, edges, cont_tri;
   std::vector<uint32_t> vert;
   std::vector<uint32_t> cell_count(static_cast<size_t>(C.total_cells) + 1, 0);
   std::vector<std::pair<uint32_t, uint32_t>> cell_pairs;  // (cell, face)
   std::vector<uint32_t> row_off(static_cast<size_t>(nt), 0), tank_edges(static_cast<size_t>(nt), 0);
+  std::vector<uint32_t> cont_start(static_cast<size_t>(nt) + 1, 0);
+  std::vector<int8_t> cell_state;
+  if (D == 3) cell_state.assign(static_cast<size_t>(C.total_cells), 1);
   uint32_t total_rows = 0;
   for (int32_t t = 0; t < nt; ++t) {
     row_off[t] = total_rows;
-    total_rows += static_cast<uint32_t>(C.tankdev[t].nc[1]);
+    if (D == 2) total_rows += static_cast<uint32_t>(C.tankdev[t].nc[1]);
   }
   std::vector<std::vector<uint32_t>> row_lists(total_rows);
   for (int32_t t = 0; t < nt; ++t) {
-    if (static_cast<size_t>(t) >= C.face_host.size()) break;
+    cont_start[t] = static_cast<uint32_t>(cont_tri.size() / 9);
+    if (static_cast<size_t>(t) >= C.face_host.size()) continue;
     const auto& F = C.face_host[t];
     if (F.face_verts.empty()) continue;
     const tg::TankDev& T = C.tankdev[t];
@@ -898,35 +937,111 @@ int build_faces(tg_context* ctx) {
       const double f = std::floor((x - T.lo[k]) * T.inv_cs);
       return static_cast<int>(std::min(std::max(f, 0.0), static_cast<double>(T.nc[k] - 1)));
     };
-    for (size_t f = 0; f < F.face_verts.size() / 2; ++f) {
-      const uint32_t u0 = C.wall_from[t] + static_cast<uint32_t>(F.face_verts[2 * f]);
-      const uint32_t u1 = C.wall_from[t] + static_cast<uint32_t>(F.face_verts[2 * f + 1]);
-      const double ax = r[2 * u0], ay = r[2 * u0 + 1], bx = r[2 * u1], by = r[2 * u1 + 1];
-      const uint32_t gf = static_cast<uint32_t>(vert.size() / 2);
-      seg.insert(seg.end(), {ax, ay, bx, by});
-      vert.insert(vert.end(), {u0, u1});
-      const int x0 = cell_index(std::min(ax, bx) - R, 0), x1 = cell_index(std::max(ax, bx) + R, 0);
-      const int y0 = cell_index(std::min(ay, by) - R, 1), y1 = cell_index(std::max(ay, by) + R, 1);
-      for (int y = y0; y <= y1; ++y) {
-        for (int x = x0; x <= x1; ++x) {
-          const uint32_t gc = T.cell_off + static_cast<uint32_t>(y) * T.nc[0] + x;
-          cell_pairs.emplace_back(gc, gf);
-          ++cell_count[gc];
+    auto gcell = [&](int x, int y, int z) {
+      return T.cell_off + (static_cast<uint32_t>(z) * T.nc[1] + static_cast<uint32_t>(y)) *
+                              static_cast<uint32_t>(T.nc[0]) + static_cast<uint32_t>(x);
+    };
+    for (size_t f = 0; f < F.face_verts.size() / D; ++f) {
+      const uint32_t gf = static_cast<uint32_t>(vert.size() / D);
+      double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {0.0, 0.0, 0.0};
+      for (int j = 0; j < D; ++j) {
+        const uint32_t u = C.wall_from[t] + static_cast<uint32_t>(F.face_verts[D * f + j]);
+        vert.push_back(u);
+        for (int k = 0; k < D; ++k) {
+          const double x = r[static_cast<size_t>(D) * u + k];
+          coords.push_back(x);
+          lo[k] = j == 0 ? x : std::min(lo[k], x);
+          hi[k] = j == 0 ? x : std::max(hi[k], x);
+        }
+      }
+      int c0[3] = {0, 0, 0}, c1[3] = {0, 0, 0};
+      for (int k = 0; k < D; ++k) {
+        c0[k] = cell_index(lo[k] - R, k);
+        c1[k] = cell_index(hi[k] + R, k);
+      }
+      for (int z = c0[2]; z <= c1[2]; ++z) {
+        for (int y = c0[1]; y <= c1[1]; ++y) {
+          for (int x = c0[0]; x <= c1[0]; ++x) {
+            const uint32_t gc = gcell(x, y, z);
+            cell_pairs.emplace_back(gc, gf);
+            ++cell_count[gc];
+          }
         }
       }
     }
-    const size_t np = F.poly.size() / 2;
-    for (size_t e = 0; e < np; ++e) {
-      const size_t e1 = (e + 1) % np;
-      const double x0 = F.poly[2 * e], y0 = F.poly[2 * e + 1];
-      const double x1 = F.poly[2 * e1], y1 = F.poly[2 * e1 + 1];
-      const uint32_t ge = static_cast<uint32_t>(edges.size() / 4);
-      edges.insert(edges.end(), {x0, y0, x1, y1});
-      const int r0 = cell_index(std::min(y0, y1), 1), r1 = cell_index(std::max(y0, y1), 1);
-      for (int y = r0; y <= r1; ++y) row_lists[row_off[t] + y].push_back(ge);
-      ++tank_edges[t];
+    if (D == 2) {
+      const size_t np = F.poly.size() / 2;
+      for (size_t e = 0; e < np; ++e) {
+        const size_t e1 = (e + 1) % np;
+        const double x0 = F.poly[2 * e], y0 = F.poly[2 * e + 1];
+        const double x1 = F.poly[2 * e1], y1 = F.poly[2 * e1 + 1];
+        const uint32_t ge = static_cast<uint32_t>(edges.size() / 4);
+        edges.insert(edges.end(), {x0, y0, x1, y1});
+        const int r0 = cell_index(std::min(y0, y1), 1), r1 = cell_index(std::max(y0, y1), 1);
+        for (int y = r0; y <= r1; ++y) row_lists[row_off[t] + y].push_back(ge);
+        ++tank_edges[t];
+      }
+      continue;
+    }
+    // 3D containment of this tank.
+    const size_t first = cont_tri.size() / 9;
+    const size_t ntri = F.poly.size() / 9;
+    cont_tri.insert(cont_tri.end(), F.poly.begin(), F.poly.end());
+    tank_edges[t] = static_cast<uint32_t>(ntri);
+    const double hair = 1e-9 * T.cs;
+    for (size_t i = 0; i < ntri; ++i) {
+      const double* tri = F.poly.data() + 9 * i;
+      int c0[3], c1[3];
+      for (int k = 0; k < 3; ++k) {
+        const double lo = std::min(std::min(tri[k], tri[3 + k]), tri[6 + k]);
+        const double hi = std::max(std::max(tri[k], tri[3 + k]), tri[6 + k]);
+        c0[k] = cell_index(lo - hair, k);
+        c1[k] = cell_index(hi + hair, k);
+      }
+      for (int z = c0[2]; z <= c1[2]; ++z) {
+        for (int y = c0[1]; y <= c1[1]; ++y) {
+          for (int x = c0[0]; x <= c1[0]; ++x) cell_state[gcell(x, y, z)] = -1;
+        }
+      }
+    }
+    // Components of the unmarked cells (face neighbours), one exact
+    // evaluation each.
+    const uint32_t ncell = static_cast<uint32_t>(T.nc[0]) * T.nc[1] * T.nc[2];
+    std::vector<uint8_t> seen(ncell, 0);
+    std::vector<uint32_t> stack;
+    for (uint32_t l = 0; l < ncell; ++l) {
+      if (seen[l] || cell_state[T.cell_off + l] < 0) continue;
+      const int lx = static_cast<int>(l % T.nc[0]);
+      const int ly = static_cast<int>((l / T.nc[0]) % T.nc[1]);
+      const int lz = static_cast<int>(l / (static_cast<uint32_t>(T.nc[0]) * T.nc[1]));
+      const double centre[3] = {T.lo[0] + (lx + 0.5) * T.cs, T.lo[1] + (ly + 0.5) * T.cs,
+                                T.lo[2] + (lz + 0.5) * T.cs};
+      const int8_t in = winding_number3(cont_tri, first, ntri, centre) > 0.5 ? 1 : 0;
+      stack.assign(1, l);
+      seen[l] = 1;
+      while (!stack.empty()) {
+        const uint32_t m = stack.back();
+        stack.pop_back();
+        cell_state[T.cell_off + m] = in;
+        const int mx = static_cast<int>(m % T.nc[0]);
+        const int my = static_cast<int>((m / T.nc[0]) % T.nc[1]);
+        const int mz = static_cast<int>(m / (static_cast<uint32_t>(T.nc[0]) * T.nc[1]));
+        const int nb[6][3] = {{mx - 1, my, mz}, {mx + 1, my, mz}, {mx, my - 1, mz},
+                              {mx, my + 1, mz}, {mx, my, mz - 1}, {mx, my, mz + 1}};
+        for (const auto& q : nb) {
+          if (q[0] < 0 || q[1] < 0 || q[2] < 0 || q[0] >= T.nc[0] || q[1] >= T.nc[1] ||
+              q[2] >= T.nc[2]) {
+            continue;
+          }
+          const uint32_t n2 = gcell(q[0], q[1], q[2]) - T.cell_off;
+          if (seen[n2] || cell_state[T.cell_off + n2] < 0) continue;
+          seen[n2] = 1;
+          stack.push_back(n2);
+        }
+      }
     }
   }
+  cont_start[nt] = static_cast<uint32_t>(cont_tri.size() / 9);
   // CSR of the per-cell face lists (faces ascending within each cell).
   std::vector<uint32_t> cell_start(static_cast<size_t>(C.total_cells) + 1, 0);
   for (uint32_t c = 0; c < C.total_cells; ++c) cell_start[c + 1] = cell_start[c] + cell_count[c];
@@ -942,6 +1057,8 @@ int build_faces(tg_context* ctx) {
   }
   if (row_edge.empty()) row_edge.push_back(0);
   if (edges.empty()) edges.assign(4, 0.0);
+  if (cont_tri.empty()) cont_tri.assign(9, 0.0);
+  if (cell_state.empty()) cell_state.assign(1, 1);
   tg::FaceArgs fa{};
   auto up = [&](auto*& dst, const auto& src) -> cudaError_t {
     using T = std::remove_const_t<std::remove_pointer_t<std::remove_reference_t<decltype(dst)>>>;
@@ -953,7 +1070,7 @@ int build_faces(tg_context* ctx) {
     dst = static_cast<T*>(p);
     return e;
   };
-  TG_CUDA(&C, up(fa.seg, seg));
+  TG_CUDA(&C, up(fa.coords, coords));
   TG_CUDA(&C, up(fa.vert, vert));
   TG_CUDA(&C, up(fa.cell_start, cell_start));
   TG_CUDA(&C, up(fa.cell_face, cell_face));
@@ -962,13 +1079,18 @@ int build_faces(tg_context* ctx) {
   TG_CUDA(&C, up(fa.row_edge, row_edge));
   TG_CUDA(&C, up(fa.row_off, row_off));
   TG_CUDA(&C, up(fa.tank_edges, tank_edges));
+  TG_CUDA(&C, up(fa.cell_state, cell_state));
+  TG_CUDA(&C, up(fa.cont_tri, cont_tri));
+  TG_CUDA(&C, up(fa.cont_start, cont_start));
   const int64_t nn = C.n > 0 ? C.n : 1;
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.slot_of), sizeof(uint32_t) * nn));
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.gamma), sizeof(double) * nn));
-  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.ggam), sizeof(double) * 2 * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.ggam), sizeof(double) * D * nn));
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_drho), sizeof(double) * nn));
-  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_dv), sizeof(double) * 2 * nn));
-  fa.weight = kernel_weight(C.P.kernel, 2);
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_dv), sizeof(double) * D * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.post_face),
+                      sizeof(double) * (2 * D + 2 * D * D) * nn));
+  fa.weight = kernel_weight(C.P.kernel, D);
   fa.on = 1;
   TG_CUDA(&C, cudaStreamSynchronize(C.stream));
   C.faces = fa;
@@ -987,31 +1109,34 @@ int tg_tank_faces(tg_context* ctx, int32_t tank, int32_t n_faces,
   if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
   Context& C = ctx->c;
   if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
-  if (C.P.dim != 2) {
-    return fail(&C, TG_ERR_INVALID_ARGUMENT, "boundary faces run in 2D");
-  }
+  const int D = C.P.dim;
   if (tank < 0 || tank >= C.ntanks || n_faces < 0) {
     return fail(&C, TG_ERR_INVALID_ARGUMENT, "bad tank or face count");
   }
-  if (n_faces > 0 && (face_verts == nullptr || n_poly < 3 || poly == nullptr)) {
+  const int32_t min_poly = D == 2 ? 3 : 4;
+  if (n_faces > 0 && (face_verts == nullptr || n_poly < min_poly || poly == nullptr)) {
     return fail(&C, TG_ERR_INVALID_ARGUMENT,
-                "faces need vertex pairs and a containment polygon");
+                D == 2 ? "faces need vertex pairs and a containment polygon"
+                       : "faces need vertex triples and a containment mesh");
   }
-  for (int32_t i = 0; i < 2 * n_faces; ++i) {
+  for (int32_t i = 0; i < D * n_faces; ++i) {
     if (face_verts[i] < 0 || face_verts[i] >= C.tanks[tank].n_wall) {
       return fail(&C, TG_ERR_INVALID_ARGUMENT,
                   "face vertex is not a fixed particle of the tank");
     }
   }
-  for (int32_t i = 0; i < 2 * n_poly; ++i) {
+  // The containment: 2D a loop of n_poly vertices, 3D n_poly triangles.
+  const size_t poly_doubles =
+      n_faces > 0 ? (D == 2 ? 2 : 9) * static_cast<size_t>(n_poly) : 0;
+  for (size_t i = 0; i < poly_doubles; ++i) {
     if (!std::isfinite(poly[i])) {
-      return fail(&C, TG_ERR_INVALID_ARGUMENT, "non-finite containment polygon");
+      return fail(&C, TG_ERR_INVALID_ARGUMENT, "non-finite containment surface");
     }
   }
   if (C.face_host.size() < static_cast<size_t>(C.ntanks)) C.face_host.resize(C.ntanks);
   auto& F = C.face_host[tank];
-  F.face_verts.assign(face_verts, face_verts + 2 * static_cast<size_t>(n_faces));
-  F.poly.assign(poly, poly + (n_faces > 0 ? 2 * static_cast<size_t>(n_poly) : 0));
+  F.face_verts.assign(face_verts, face_verts + D * static_cast<size_t>(n_faces));
+  F.poly.assign(poly, poly + poly_doubles);
   return build_faces(ctx);
 }
 

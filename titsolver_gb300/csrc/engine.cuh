@@ -96,8 +96,9 @@ struct Context {
   // Boundary faces (tg_tank_faces): host copies per tank and the device
   // view; faces.on = 0 with particle walls.
   struct TankFaces {
-    std::vector<int32_t> face_verts;  // 2 per face, tank-local fixed index
-    std::vector<double> poly;         // 2 per containment vertex
+    std::vector<int32_t> face_verts;  // dim per face, tank-local fixed index
+    std::vector<double> poly;         // 2D: 2 per containment vertex;
+                                      // 3D: 9 per containment triangle
   };
   std::vector<TankFaces> face_host;
   FaceArgs faces{};

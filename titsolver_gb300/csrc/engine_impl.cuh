@@ -266,7 +266,8 @@ class Engine final : public EngineBase {
     const int per_stage = 3 * passes + 2 + 2 + (C.n_wall > 0 ? 1 : 0);
     const int gam = C.faces.on ? 2 : 0;  // k_gamma, k_face_terms
     const int post = C.P.post_integrate == TG_POST_SHIFTING
-                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + (gam > 0 ? 1 : 0) : 0) + 5
+                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + (gam > 0 ? 1 : 0) : 0) + 5 +
+                               (gam > 0 ? 1 : 0)
                          : 0;
     return static_cast<int64_t>(stages) * (per_stage + gam) + post + 1;
   }
@@ -369,6 +370,10 @@ class Engine final : public EngineBase {
     p.k_fs = C.post_k_fs;
     p.shift = -C.P.cfl * 0.2;
     const unsigned grid = grid_for(C.n, 128);
+    if (C.faces.on) {
+      k_post_faces<D, F, K><<<grid, 128, 0, C.stream>>>(p);
+      C.launches += 1;
+    }
     k_post_sums<D, F, K><<<grid, 128, 0, C.stream>>>(p);
     k_post_phi<D, F><<<grid, 128, 0, C.stream>>>(p);
     k_post_near<D, F, K><<<grid, 128, 0, C.stream>>>(p);
@@ -383,11 +388,9 @@ class Engine final : public EngineBase {
   // Face boundaries: gamma and grad gamma of every particle at the positions
   // of this prepare (before the wall pass, which reads grad gamma).
   void enqueue_gamma(Context& C, const StageArgs<D, F>& a) {
-    if constexpr (D == 2) {
-      if (a.fc.on) {
-        k_gamma<K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
-        C.launches += 1;
-      }
+    if (a.fc.on) {
+      k_gamma<D, K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+      C.launches += 1;
     }
   }
 
@@ -424,18 +427,17 @@ class Engine final : public EngineBase {
       C.launches += 1;
       C.group_end(tok);
     }
-    if constexpr (D == 2) {
-      if (a.fc.on) {
-        k_face_terms<K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
-        C.launches += 1;
-      }
+    if (a.fc.on) {
+      k_face_terms<D, K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+      C.launches += 1;
     }
     tok = C.group_begin(kGroupForces);
     if constexpr (F == TG_FP32C) {
       const int phys = physics_preset(C.P);
       bool staged = false;
       if constexpr (D == 2) {
-        if (C.P.staging) {
+        // The staged kernel has no face terms.
+        if (C.P.staging && !a.fc.on) {
           k_forces_staged2<K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
           staged = true;
         }

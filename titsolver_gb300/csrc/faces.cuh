@@ -1,16 +1,18 @@
-// faces.cuh - semi-analytical face boundaries in 2D (FP64 form): the
+// faces.cuh - semi-analytical face boundaries (FP64 arithmetic): the
 // reference's wall mode with boundary faces and a containment function
 // (FluidEquations with a non-empty domain, fluid_equations.hpp:122-193,
-// 241-247, 278-291, 340-349, 491-511).
+// 241-247, 278-291, 340-349, 491-511); segments in 2D, triangles in 3D.
 //
 // The tank's fixed particles are the face vertices.  Per prepare, k_gamma
 // computes for every particle the kernel flux sum over its adjacent faces
-// (grad gamma), the containment (winding number > 1/2, by signed crossings
-// of the +x ray with the polygon edges of the particle's grid row), and
-// gamma = contains - sum of antigradient fluxes at r + (2 contains - 1)
-// n h^2 (fluid_equations.hpp:166-193).  The wall extrapolation, the force
-// pass and the post-integration passes then read gamma and grad gamma and
-// add the face terms.
+// (grad gamma), the containment (winding number > 1/2: in 2D by signed
+// crossings of the +x ray with the polygon edges of the particle's grid
+// row; in 3D from the particle's cell when the containment surface does not
+// reach that cell, else by the exact winding number of the surface's
+// triangles), and gamma = contains - sum of antigradient fluxes at
+// r + (2 contains - 1) n h^2 (fluid_equations.hpp:166-193).  The wall
+// extrapolation, the force pass and the post-integration passes then read
+// gamma and grad gamma and add the face terms.
 //
 // Kernel flux and antigradient flux of a segment (kernel.hpp:194-221,
 // 286-314) are sums over the kernel's support pieces w_i(q) = sum_p c_p q^p
@@ -32,23 +34,36 @@ namespace tg {
 // Device view of the boundary faces of a context (all tanks); on = 0 when
 // the tanks have particle walls.
 struct FaceArgs {
-  const double* seg;          // 4 per face: a.x, a.y, b.x, b.y
-  const uint32_t* vert;       // 2 per face: upload indices of the vertices
+  const double* coords;       // D * D per face: the vertices a, b (, c)
+  const uint32_t* vert;       // D per face: upload indices of the vertices
   const uint32_t* cell_start; // per global cell (+1): its face list
   const uint32_t* cell_face;  // faces within reach of each cell, ascending
+  // 2D containment: the polygon's edges by grid row.
   const double* poly_edge;    // 4 per containment edge: x0, y0, x1, y1
   const uint32_t* row_start;  // per global grid row (+1): its edge list
   const uint32_t* row_edge;   // containment edges overlapping each row
   const uint32_t* row_off;    // per tank: first global grid row
+  // 3D containment: per-cell answers and the surface's triangles.
+  const int8_t* cell_state;   // per global cell: 1 inside, 0 outside,
+                              // -1 reached by the surface (exact test)
+  const double* cont_tri;     // 9 per containment triangle
+  const uint32_t* cont_start; // per tank (+1): its containment triangles
   uint32_t* slot_of;          // upload index -> cell-order slot (walls)
   double* gamma;              // per particle, cell order
-  double* ggam;               // grad gamma, 2 per particle
+  double* ggam;               // grad gamma, D per particle
   double* face_drho;          // face terms of continuity, per particle
-  double* face_dv;            // face terms of momentum, 2 per particle
-  const uint32_t* tank_edges; // per tank: containment edges (0: all inside)
-  double weight;              // the kernel's 2D weight
+  double* face_dv;            // face terms of momentum, D per particle
+  double* post_face;          // face terms of the shifting sums per
+                              // particle: N, L, grad v, grad rho
+  const uint32_t* tank_edges; // per tank: containment edges or triangles
+                              // (0: particle walls, all inside)
+  double weight;              // the kernel's weight in D dimensions
   int on;
 };
+
+// Doubles per particle in FaceArgs::post_face.
+template<int D>
+constexpr int kPostFaceSums = 2 * D + 2 * D * D;
 
 struct FacePiece {
   double cutoff;
@@ -188,8 +203,8 @@ __device__ __forceinline__ double face_antigrad_flux(const double* ab,
 }
 
 // Segment::intersects(BSphere) (geom/segment.hpp:108-112).
-__device__ __forceinline__ bool face_in_sphere(const double* ab,
-                                               const double* c, double radius) {
+__device__ __forceinline__ bool segment_in_sphere(const double* ab,
+                                                  const double* c, double radius) {
   for (int k = 0; k < 2; ++k) {
     const double lo = fmin(ab[k], ab[2 + k]), hi = fmax(ab[k], ab[2 + k]);
     if (!(c[k] - radius <= hi && lo <= c[k] + radius)) return false;
@@ -211,9 +226,374 @@ __device__ __forceinline__ bool face_in_sphere(const double* ab,
   return d0 * d0 + d1 * d1 <= radius * radius;
 }
 
+// ---------------------------------------------------------------------------
+// Triangles (3D): kernel flux and antigradient flux (kernel.hpp:194-221,
+// 316-399; kernel.gen.cpp:321-466).  The triangle is projected into its
+// plane around x and scaled by 1/h; per support piece at wall distance
+// eta < cutoff the integral is a sum over the edges.  Edge p0 -> p1 with
+// unit tangent t: delta = det(p0, t), beta^2 = eta^2 + delta^2, z from
+// dot(p0, t) over the edge's length, split where the edge crosses the circle
+// of radius sqrt(cutoff^2 - eta^2); inside the circle a sub-interval adds
+// the line primitive's difference, outside the sector value times the arc
+// angle atan2(delta (z_hi - z_lo), z_lo z_hi + delta^2).  Line primitive:
+// rho^2 = z^2 + beta^2, A = atan2(delta z (rho - eta), delta^2 rho +
+// z^2 eta) (0 for tiny delta), L = asinh(z / beta) (0 for tiny beta),
+// J_0 = z, J_1 = (z rho + beta^2 L)/2, J_k = (z rho^k + k beta^2 J_{k-2}) /
+// (k + 1), K_0 = A, K_1 = delta L, K_k = delta J_{k-2} + eta^2 K_{k-2};
+//   flux line       = sum_p c_p/(p+2) K_{p+2} - K_0 sum_p c_p eta^{p+2}/(p+2)
+//   flux sector     = sum_p c_p (cutoff^{p+2} - eta^{p+2})/(p+2)
+//   antigrad line   = s_0 K_0 + sum_{p>=3} s_p (eta K_{p-1} - eta^p K_0)/(p-1)
+//   antigrad sector = s_0 (1 - eta/cutoff)
+//                     + sum_{p>=3} s_p (eta cutoff^{p-1} - eta^p)/(p-1)
+// with s_p the coefficients of the piece's 3D tail moment.
+
+struct FaceTail3 {
+  int deg;
+  double s[15];
+};
+
+// 3D tail moments cutoff^3 Q(cutoff) - q^3 Q(q), Q(q) = sum_p c_p q^p/(p+3),
+// of the pieces of c_face_pieces, in the same order.
+static __constant__ FaceTail3 c_face_tail3[6][3] = {
+  // cubic spline
+  {{6, {4.0 / 15.0, 0.0, 0.0, -2.0 / 3.0, 3.0 / 4.0, -3.0 / 10.0, 1.0 / 24.0}},
+   {6, {-1.0 / 60.0, 0.0, 0.0, 1.0 / 3.0, -3.0 / 4.0, 3.0 / 5.0, -1.0 / 6.0}}},
+  // quartic spline
+  {{7, {15625.0 / 2688.0, 0.0, 0.0, -625.0 / 48.0, 125.0 / 8.0, -15.0 / 2.0, 5.0 / 3.0, -1.0 / 7.0}},
+   {7, {-729.0 / 896.0, 0.0, 0.0, 135.0 / 16.0, -135.0 / 8.0, 27.0 / 2.0, -5.0, 5.0 / 7.0}},
+   {7, {1.0 / 1344.0, 0.0, 0.0, -5.0 / 24.0, 5.0 / 4.0, -3.0, 10.0 / 3.0, -10.0 / 7.0}}},
+  // quintic spline
+  {{8, {2187.0 / 56.0, 0.0, 0.0, -81.0, 405.0 / 4.0, -54.0, 15.0, -15.0 / 7.0, 1.0 / 8.0}},
+   {8, {-64.0 / 7.0, 0.0, 0.0, 64.0, -120.0, 96.0, -40.0, 60.0 / 7.0, -3.0 / 4.0}},
+   {8, {5.0 / 56.0, 0.0, 0.0, -5.0, 75.0 / 4.0, -30.0, 25.0, -75.0 / 7.0, 15.0 / 8.0}}},
+  // Wendland C2
+  {{8, {4.0 / 21.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 1.0 / 2.0, -5.0 / 12.0, 15.0 / 112.0, -1.0 / 64.0}}},
+  // Wendland C4
+  {{11, {64.0 / 495.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 7.0 / 15.0, 0.0, -5.0 / 8.0, 7.0 / 12.0, -35.0 / 144.0, 1.0 / 20.0, -35.0 / 8448.0}}},
+  // Wendland C6
+  {{14, {128.0 / 1365.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 11.0 / 20.0, 0.0, -33.0 / 56.0, 0.0, 77.0 / 96.0, -33.0 / 40.0, 105.0 / 256.0, -11.0 / 96.0, 231.0 / 13312.0, -1.0 / 896.0}}},
+};
+
+// Integer power by squaring in the order of core/math.hpp:92-104:
+// a^p = a (a^2)^(p/2) for odd p, (a^2)^(p/2) for even p.
+__device__ __forceinline__ double face_ipow(double a, int p) {
+  if (p == 0) return 1.0;
+  double odd[5];
+  int n = 0;
+  while (p > 1) {
+    if (p & 1) odd[n++] = a;
+    a = a * a;
+    p >>= 1;
+  }
+  for (int i = n - 1; i >= 0; --i) a = odd[i] * a;
+  return a;
+}
+
+__device__ __forceinline__ double face_edge_primitive(const FacePiece& kp,
+                                                      const FaceTail3& tp,
+                                                      bool antigrad, double eta,
+                                                      double delta, double beta2,
+                                                      double beta, double z) {
+  const double rho = sqrt(z * z + beta2);
+  const double A = fabs(delta) <= kTiny
+                       ? 0.0
+                       : atan2(delta * z * (rho - eta), delta * delta * rho + z * z * eta);
+  const double L = fabs(beta) <= kTiny
+                       ? 0.0
+                       : copysign(log1p((fabs(z) + z * z / (rho + beta)) / beta), z);
+  const int kmax = antigrad ? max(tp.deg - 1, 1) : kp.deg + 2;
+  double J[16], Kk[16];
+  J[0] = z;
+  J[1] = (z * rho + beta2 * L) / 2.0;
+  double rp = rho;
+  for (int k = 2; k <= kmax; ++k) {
+    rp *= rho;
+    J[k] = (z * rp + k * beta2 * J[k - 2]) / (k + 1);
+  }
+  Kk[0] = A;
+  Kk[1] = delta * L;
+  for (int k = 2; k <= kmax; ++k) Kk[k] = delta * J[k - 2] + eta * eta * Kk[k - 2];
+  double s = 0.0;
+  if (!antigrad) {
+    double c0 = 0.0;
+    for (int p = 0; p <= kp.deg; ++p) {
+      if (kp.c[p] == 0.0) continue;
+      s += kp.c[p] / (p + 2) * Kk[p + 2];
+      c0 -= kp.c[p] * face_ipow(eta, p + 2) / (p + 2);
+    }
+    return s + c0 * Kk[0];
+  }
+  for (int p = 0; p <= tp.deg; ++p) {
+    if (tp.s[p] == 0.0) continue;
+    if (p == 0) s += tp.s[0] * Kk[0];
+    else s += tp.s[p] * (eta * Kk[p - 1] - face_ipow(eta, p) * Kk[0]) / (p - 1);
+  }
+  return s;
+}
+
+__device__ __forceinline__ double face_sector(const FacePiece& kp,
+                                              const FaceTail3& tp,
+                                              bool antigrad, double eta) {
+  double s = 0.0;
+  if (!antigrad) {
+    for (int p = 0; p <= kp.deg; ++p) {
+      if (kp.c[p] == 0.0) continue;
+      s += kp.c[p] * (face_ipow(kp.cutoff, p + 2) - face_ipow(eta, p + 2)) / (p + 2);
+    }
+    return s;
+  }
+  for (int p = 0; p <= tp.deg; ++p) {
+    if (tp.s[p] == 0.0) continue;
+    if (p == 0) s += tp.s[0] * (1.0 - eta / kp.cutoff);
+    else s += tp.s[p] * (eta * face_ipow(kp.cutoff, p - 1) - face_ipow(eta, p)) / (p - 1);
+  }
+  return s;
+}
+
+// unit_triangle_integral (kernel.hpp:316-399) summed over the pieces; v =
+// the three projected vertices (2 doubles each).
+template<int K>
+__device__ __noinline__ double face_unit_triangle(bool antigrad, double eta,
+                                                  const double* v) {
+  const FacePieces& P = c_face_pieces[K];
+  double total = 0.0;
+  for (int i = 0; i < P.n; ++i) {
+    const FacePiece& kp = P.p[i];
+    const FaceTail3& tp = c_face_tail3[K][i];
+    if (eta >= kp.cutoff) continue;
+    const double radius2 = kp.cutoff * kp.cutoff - eta * eta;
+    const double sector = face_sector(kp, tp, antigrad, eta);
+    for (int e = 0; e < 3; ++e) {
+      const double* p0 = v + 2 * e;
+      const double* p1 = v + 2 * (e == 2 ? 0 : e + 1);
+      const double ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
+      const double len2 = ed[0] * ed[0] + ed[1] * ed[1];
+      if (len2 <= kTiny * kTiny) continue;
+      const double len = sqrt(len2);
+      const double t[2] = {ed[0] / len, ed[1] / len};
+      const double delta = p0[0] * t[1] - p0[1] * t[0];
+      const double delta2 = delta * delta;
+      const double beta2 = eta * eta + delta2;
+      const double beta = sqrt(beta2);
+      const double z0 = p0[0] * t[0] + p0[1] * t[1];
+      const double z1 = z0 + len;
+      double zs[4];
+      int nz = 0;
+      zs[nz++] = z0;
+      if (radius2 > delta2) {
+        const double zc = sqrt(radius2 - delta2);
+        if (z0 < -zc && -zc < z1) zs[nz++] = -zc;
+        if (z0 < zc && zc < z1) zs[nz++] = zc;
+      }
+      zs[nz++] = z1;
+      for (int j = 0; j + 1 < nz; ++j) {
+        const double lo = zs[j], hi = zs[j + 1];
+        if (fabs(hi - lo) <= kTiny) continue;
+        const double mid = (lo + hi) / 2.0;
+        if (mid * mid + delta2 < radius2) {
+          total += face_edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, hi) -
+                   face_edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, lo);
+        } else {
+          total += sector * atan2(delta * (hi - lo), lo * hi + delta2);
+        }
+      }
+    }
+  }
+  return total;
+}
+
+__device__ __forceinline__ void face_cross(const double* a, const double* b,
+                                           double* out) {
+  out[0] = a[1] * b[2] - a[2] * b[1];
+  out[1] = a[2] * b[0] - a[0] * b[2];
+  out[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// normalize() in 3D with the |a|^2 >= tiny^2 guard; sums left to right.
+__device__ __forceinline__ void normalize3(const double* a, double* out) {
+  const double n2 = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2];
+  const double s = n2 >= kTiny * kTiny ? 1.0 / sqrt(n2) : 0.0;
+  out[0] = a[0] * s;
+  out[1] = a[1] * s;
+  out[2] = a[2] * s;
+}
+
+template<int D>
+__device__ __forceinline__ void normalize_d(const double* a, double* out) {
+  if constexpr (D == 2) normalize2(a, out);
+  else normalize3(a, out);
+}
+
+template<int D>
+__device__ __forceinline__ double dot_d(const double* a, const double* b) {
+  double s = a[0] * b[0] + a[1] * b[1];
+  if constexpr (D == 3) s += a[2] * b[2];
+  return s;
+}
+
+// Triangle frame at x (geom/triangle.hpp): normal = normalize(cross(b - a,
+// c - a) / 2), signed distance d and the vertices projected on
+// e1 = normalize(b - a), e2 = normalize(cross(wnormal, e1)) (units of h).
+struct TriFrame {
+  double n[3], d, p[6];
+};
+__device__ __forceinline__ TriFrame tri_frame(const double* t, const double* x,
+                                              double hinv) {
+  const double ba[3] = {t[3] - t[0], t[4] - t[1], t[5] - t[2]};
+  const double ca[3] = {t[6] - t[0], t[7] - t[1], t[8] - t[2]};
+  double wn[3];
+  face_cross(ba, ca, wn);
+  wn[0] /= 2.0;
+  wn[1] /= 2.0;
+  wn[2] /= 2.0;
+  TriFrame F;
+  normalize3(wn, F.n);
+  double e1[3], e2[3], u[3];
+  normalize3(ba, e1);
+  face_cross(wn, e1, u);
+  normalize3(u, e2);
+  const double xa[3] = {x[0] - t[0], x[1] - t[1], x[2] - t[2]};
+  F.d = dot_d<3>(xa, F.n) * hinv;
+  for (int i = 0; i < 3; ++i) {
+    const double vx[3] = {t[3 * i] - x[0], t[3 * i + 1] - x[1], t[3 * i + 2] - x[2]};
+    F.p[2 * i] = dot_d<3>(vx, e1) * hinv;
+    F.p[2 * i + 1] = dot_d<3>(vx, e2) * hinv;
+  }
+  return F;
+}
+
+// Kernel::flux of face g (segment or triangle) at x; wd = the kernel's
+// weight in D dimensions.
+template<int K, int D>
+__device__ __forceinline__ void face_flux_d(const double* g, const double* x,
+                                            double h, double wd, double* out) {
+  if constexpr (D == 2) {
+    face_flux<K>(g, x, h, wd, out);
+  } else {
+    const double hinv = 1.0 / h;
+    const TriFrame F = tri_frame(g, x, hinv);
+    const double s = wd * hinv * face_unit_triangle<K>(false, fabs(F.d), F.p);
+    out[0] = F.n[0] * s;
+    out[1] = F.n[1] * s;
+    out[2] = F.n[2] * s;
+  }
+}
+
+// Kernel::antigrad_flux of face g at x.
+template<int K, int D>
+__device__ __forceinline__ double face_antigrad_flux_d(const double* g,
+                                                       const double* x, double h,
+                                                       double wd) {
+  if constexpr (D == 2) {
+    return face_antigrad_flux<K>(g, x, h, wd);
+  } else {
+    const TriFrame F = tri_frame(g, x, 1.0 / h);
+    return copysign(wd, F.d) * face_unit_triangle<K>(true, fabs(F.d), F.p);
+  }
+}
+
+// Closest point of a segment (Segment::clamp, geom/segment.hpp:91-106).
+__device__ __forceinline__ void segment_clamp3(const double* a, const double* b,
+                                               const double* x, double* q) {
+  const double ba[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+  const double xa[3] = {x[0] - a[0], x[1] - a[1], x[2] - a[2]};
+  q[0] = a[0];
+  q[1] = a[1];
+  q[2] = a[2];
+  const double len2 = dot_d<3>(ba, ba);
+  if (fabs(len2) <= kTiny) return;
+  const double t = dot_d<3>(xa, ba) / len2;
+  if (t > 1.0) {
+    q[0] = b[0];
+    q[1] = b[1];
+    q[2] = b[2];
+  } else if (!(t < 0.0)) {
+    q[0] = a[0] + t * ba[0];
+    q[1] = a[1] + t * ba[1];
+    q[2] = a[2] + t * ba[2];
+  }
+}
+
+// Closest point of a triangle (Triangle::clamp, geom/triangle.hpp): the
+// Voronoi-region walk of Ericson, Real-Time Collision Detection 5.1.5; a
+// degenerate triangle clamps to its longest edge.
+__device__ __forceinline__ void triangle_clamp(const double* t, const double* x,
+                                               double* q) {
+  const double* a = t;
+  const double* b = t + 3;
+  const double* c = t + 6;
+  const double ba[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+  const double ca[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+  const double cb[3] = {c[0] - b[0], c[1] - b[1], c[2] - b[2]};
+  double wn[3];
+  face_cross(ba, ca, wn);
+  wn[0] /= 2.0;
+  wn[1] /= 2.0;
+  wn[2] /= 2.0;
+  if (sqrt(dot_d<3>(wn, wn)) <= kTiny) {
+    const double l_ab = dot_d<3>(ba, ba), l_bc = dot_d<3>(cb, cb), l_ca = dot_d<3>(ca, ca);
+    if (l_ab >= l_bc && l_ab >= l_ca) return segment_clamp3(a, b, x, q);
+    if (l_bc >= l_ca) return segment_clamp3(b, c, x, q);
+    return segment_clamp3(a, c, x, q);
+  }
+  const double pa[3] = {x[0] - a[0], x[1] - a[1], x[2] - a[2]};
+  const double d1 = dot_d<3>(ba, pa), d2 = dot_d<3>(ca, pa);
+  const double* corner = nullptr;
+  if (d1 <= 0.0 && d2 <= 0.0) corner = a;
+  const double pb[3] = {x[0] - b[0], x[1] - b[1], x[2] - b[2]};
+  const double d3 = dot_d<3>(ba, pb), d4 = dot_d<3>(ca, pb);
+  if (corner == nullptr && d3 >= 0.0 && d4 <= d3) corner = b;
+  const double pc[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+  const double d5 = dot_d<3>(ba, pc), d6 = dot_d<3>(ca, pc);
+  if (corner == nullptr && d6 >= 0.0 && d5 <= d6) corner = c;
+  if (corner != nullptr) {
+    q[0] = corner[0];
+    q[1] = corner[1];
+    q[2] = corner[2];
+    return;
+  }
+  const double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+    const double s = d1 / (d1 - d3);
+    for (int k = 0; k < 3; ++k) q[k] = a[k] + s * ba[k];
+    return;
+  }
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+    const double s = d2 / (d2 - d6);
+    for (int k = 0; k < 3; ++k) q[k] = a[k] + s * ca[k];
+    return;
+  }
+  const double va = d3 * d6 - d5 * d4;
+  if (va <= 0.0 && d4 >= d3 && d5 >= d6) {
+    const double s = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    for (int k = 0; k < 3; ++k) q[k] = b[k] + s * cb[k];
+    return;
+  }
+  const double v = vb / (va + vb + vc);
+  const double w = vc / (va + vb + vc);
+  for (int k = 0; k < 3; ++k) q[k] = a[k] + v * ba[k] + w * ca[k];
+}
+
+// Triangle::intersects(BSphere): boxes overlap and the closest point of the
+// triangle is in the sphere.
+__device__ __forceinline__ bool triangle_in_sphere(const double* t,
+                                                   const double* x,
+                                                   double radius) {
+  for (int k = 0; k < 3; ++k) {
+    const double lo = fmin(fmin(t[k], t[3 + k]), t[6 + k]);
+    const double hi = fmax(fmax(t[k], t[3 + k]), t[6 + k]);
+    if (!(x[k] - radius <= hi && lo <= x[k] + radius)) return false;
+  }
+  double q[3];
+  triangle_clamp(t, x, q);
+  const double d[3] = {q[0] - x[0], q[1] - x[1], q[2] - x[2]};
+  return dot_d<3>(d, d) <= radius * radius;
+}
+
 // Faces within the support radius of x, in ascending face order (the
 // particle's cell list holds every face within reach of the cell).
-template<class Fn>
+template<int D, class Fn>
 __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
                                                    uint32_t gcell,
                                                    const double* x,
@@ -221,9 +601,39 @@ __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
   const uint32_t s = fc.cell_start[gcell], e = fc.cell_start[gcell + 1];
   for (uint32_t i = s; i < e; ++i) {
     const uint32_t f = fc.cell_face[i];
-    const double* ab = fc.seg + 4 * static_cast<size_t>(f);
-    if (face_in_sphere(ab, x, radius)) fn(f, ab);
+    const double* g = fc.coords + D * D * static_cast<size_t>(f);
+    bool in;
+    if constexpr (D == 2) in = segment_in_sphere(g, x, radius);
+    else in = triangle_in_sphere(g, x, radius);
+    if (in) fn(f, g);
   }
+}
+
+// 3D containment: the particle's cell answers unless the containment
+// surface reaches it; there the exact winding number of the surface
+// (Triangle::winding_number, geom/triangle.hpp: per triangle
+// atan2(det(a', b', c'), |a'||b'||c'| + (a'.b')|c'| + (b'.c')|a'| +
+// (c'.a')|b'|) / (2 pi), primes = vertex - x) decides, > 1/2.
+__device__ __forceinline__ bool face_contains3(const FaceArgs& fc, uint32_t tank,
+                                               uint32_t gcell, const double* x) {
+  const int st = fc.cell_state[gcell];
+  if (st >= 0) return st != 0;
+  double w = 0.0;
+  for (uint32_t i = fc.cont_start[tank]; i < fc.cont_start[tank + 1]; ++i) {
+    const double* t = fc.cont_tri + 9 * static_cast<size_t>(i);
+    const double ap[3] = {t[0] - x[0], t[1] - x[1], t[2] - x[2]};
+    const double bp[3] = {t[3] - x[0], t[4] - x[1], t[5] - x[2]};
+    const double cp[3] = {t[6] - x[0], t[7] - x[1], t[8] - x[2]};
+    const double na = sqrt(dot_d<3>(ap, ap));
+    const double nb = sqrt(dot_d<3>(bp, bp));
+    const double nc = sqrt(dot_d<3>(cp, cp));
+    const double den = na * nb * nc + dot_d<3>(ap, bp) * nc +
+                       dot_d<3>(bp, cp) * na + dot_d<3>(cp, ap) * nb;
+    double bc[3];
+    face_cross(bp, cp, bc);
+    w += atan2(dot_d<3>(ap, bc), den) / (2.0 * 3.141592653589793);
+  }
+  return w > 0.5;
 }
 
 // Winding number > 1/2 by signed crossings of the ray from x towards +x

@@ -734,9 +734,7 @@ __global__ void __launch_bounds__(128)
     // hydrostatic term g (r_be . n_e) n_e[1] (fluid_equations.hpp:146-160);
     // zero with particle walls.
     double ne[3] = {0.0, 0.0, 0.0};
-    if constexpr (D == 2) {
-      if (A.fc.on && valid) normalize2(A.fc.ggam + 2 * static_cast<size_t>(e), ne);
-    }
+    if (A.fc.on && valid) normalize_d<D>(A.fc.ggam + D * static_cast<size_t>(e), ne);
     if (valid && !A.walls_keep && !skip) {
       auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
         for (uint32_t j = s; j < en; ++j) {
@@ -748,9 +746,7 @@ __global__ void __launch_bounds__(128)
           const double W = w * KernelPoly<K>::value(sqrt(s2) * hinv);
           const double Vb = m * b.invrho;
           double Hb = potential_f64(A.phys, T, b.rho);
-          if constexpr (D == 2) {
-            if (A.fc.on) Hb += A.phys.g * (d[0] * ne[0] + d[1] * ne[1]) * ne[1];
-          }
+          if (A.fc.on) Hb += A.phys.g * dot_d<D>(d, ne) * ne[1];
           S += Vb * W;
           H += Vb * Hb * W;
         }
@@ -791,14 +787,12 @@ __global__ void __launch_bounds__(128)
     skip = __shfl_sync(0xffffffffu, skip, 0, kWallTeam);
     // Face boundaries: wall normal and hydrostatic term (see the FP64 path);
     // here r_be = -d.
-    float nef[2] = {0.f, 0.f};
-    if constexpr (D == 2) {
-      if (A.fc.on && valid) {
-        double ne[2];
-        normalize2(A.fc.ggam + 2 * static_cast<size_t>(e), ne);
-        nef[0] = static_cast<float>(ne[0]);
-        nef[1] = static_cast<float>(ne[1]);
-      }
+    float nef[3] = {0.f, 0.f, 0.f};
+    if (A.fc.on && valid) {
+      double ne[3];
+      normalize_d<D>(A.fc.ggam + D * static_cast<size_t>(e), ne);
+#pragma unroll
+      for (int k = 0; k < D; ++k) nef[k] = static_cast<float>(ne[k]);
     }
     if (valid && !A.walls_keep && !skip) {
       auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
@@ -815,8 +809,10 @@ __global__ void __launch_bounds__(128)
           const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
           const float Vb = m * b.invrho;
           float Hb = potential_f32(A.phys, T, b.drho);
-          if constexpr (D == 2) {
-            if (A.fc.on) Hb -= A.phys.g_f * (d[0] * nef[0] + d[1] * nef[1]) * nef[1];
+          if (A.fc.on) {
+            float dn = d[0] * nef[0] + d[1] * nef[1];
+            if constexpr (D == 3) dn += d[2] * nef[2];
+            Hb -= A.phys.g_f * dn * nef[1];
           }
           S.add(Vb * W);
           H.add(Vb * Hb * W);
@@ -842,7 +838,10 @@ __global__ void __launch_bounds__(128)
             const Dat32 bd = load_dat_coherent(A.datrec, j);
             const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
             const float Vb = m * bd.invrho;
-            const float Hb = potential_f32(A.phys, T, bd.drho);
+            float Hb = potential_f32(A.phys, T, bd.drho);
+            if (A.fc.on) {
+              Hb -= A.phys.g_f * (d[0] * nef[0] + d[1] * nef[1] + d[2] * nef[2]) * nef[1];
+            }
             S.add(Vb * W);
             H.add(Vb * Hb * W);
           }
@@ -1130,6 +1129,7 @@ __device__ __forceinline__ void target_fields(const Dat64& a, const TankDev&,
                                               double* v, double& rho, double& P) {
   v[0] = a.vx;
   v[1] = a.vy;
+  v[2] = a.vz;
   rho = a.rho;
   P = a.P;
 }
@@ -1137,68 +1137,98 @@ __device__ __forceinline__ void target_fields(const Dat32& a, const TankDev& T,
                                               double* v, double& rho, double& P) {
   v[0] = a.vx;
   v[1] = a.vy;
+  v[2] = a.vz;
   rho = T.rho0 + static_cast<double>(a.drho);
   P = a.P;
 }
 
-template<int K, int F>
-__global__ void __launch_bounds__(128) k_face_terms(StageArgs<2, F> A) {
+// Global cell of a particle's key.
+template<int D>
+__device__ __forceinline__ uint32_t global_cell(const TankDev& T, const int* c) {
+  uint32_t g = static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
+  if constexpr (D == 3) g += static_cast<uint32_t>(c[2]) * T.nc[1] * T.nc[0];
+  return T.cell_off + g;
+}
+
+// Face vertex average of a scalar: (a + b)/2 or (a + b + c)/3
+// (field.hpp:59-64, core/math.hpp:130).
+template<int D>
+__device__ __forceinline__ double face_avg(const double* x) {
+  if constexpr (D == 2) return (x[0] + x[1]) / 2.0;
+  else return (x[0] + x[1] + x[2]) / 3.0;
+}
+
+template<int D, int K, int F>
+__global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   const FaceArgs& fc = A.fc;
-  double drho = 0.0, dv[2] = {0.0, 0.0};
+  double drho = 0.0, dv[3] = {0.0, 0.0, 0.0};
   if (!(A.Y.id[i] & kWallBit)) {
     const uint32_t key = A.skey[i];
     const TankDev& T = A.tanks[tank_of_key(key, A.tank_off, A.ntanks)];
     int c[3] = {0, 0, 0};
-    cell_from_key<2>(T, key, c);
-    const uint32_t gcell = T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
-    const double pa[2] = {A.Y.pos[0][i], A.Y.pos[1][i]};
+    cell_from_key<D>(T, key, c);
+    const uint32_t gcell = global_cell<D>(T, c);
+    double pa[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) pa[k] = A.Y.pos[k][i];
     const double radius = KernelPoly<K>::unit_radius * T.h;
     const double gam = fc.gamma[i];
-    double va[2], rho_a, P_a;
+    double va[3], rho_a, P_a;
     target_fields(load_dat(A.datrec, static_cast<uint32_t>(i)), T, va, rho_a, P_a);
-    for_adjacent_faces(fc, gcell, pa, radius, [&](uint32_t f, const double* ab) {
-      double gg[2];
-      face_flux<K>(ab, pa, T.h, fc.weight, gg);
-      const double rho_v0 = vertex_rho(A.datrec, fc.slot_of[fc.vert[2 * f]], T);
-      const double rho_v1 = vertex_rho(A.datrec, fc.slot_of[fc.vert[2 * f + 1]], T);
-      const double rho_s = (rho_v0 + rho_v1) / 2.0;
-      double p0, p1, c0, c1;
-      tait_f64(A.phys, T, rho_v0, p0, c0);
-      tait_f64(A.phys, T, rho_v1, p1, c1);
-      const double p_s = (p0 + p1) / 2.0;
-      drho -= rho_s * (va[0] * gg[0] + va[1] * gg[1]) / gam;
+    for_adjacent_faces<D>(fc, gcell, pa, radius, [&](uint32_t f, const double* g) {
+      double gg[3];
+      face_flux_d<K, D>(g, pa, T.h, fc.weight, gg);
+      double rv[3], pv[3];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        double cj;
+        rv[j] = vertex_rho(A.datrec, fc.slot_of[fc.vert[D * f + j]], T);
+        tait_f64(A.phys, T, rv[j], pv[j], cj);
+      }
+      const double rho_s = face_avg<D>(rv);
+      const double p_s = face_avg<D>(pv);
+      // The face vertices' velocities are zero (no-slip walls), so
+      // v_as = v_a.
+      drho -= rho_s * dot_d<D>(va, gg) / gam;
       const double P_as = rho_s * (P_a + p_s / (rho_s * rho_s));
-      double n_s[2], t_as[2];
-      normalize2(gg, n_s);
-      const double vn = va[0] * n_s[0] + va[1] * n_s[1];
-      const double vt[2] = {va[0] - vn * n_s[0], va[1] - vn * n_s[1]};
-      normalize2(vt, t_as);
-      const double r_as[2] = {pa[0] - (ab[0] + ab[2]) / 2.0, pa[1] - (ab[1] + ab[3]) / 2.0};
-      const double dr_as = fmax(T.h / 2.0, r_as[0] * n_s[0] + r_as[1] * n_s[1]);
-      const double Pi_s =
-          2.0 * A.phys.mu / (rho_a * dr_as) * (va[0] * t_as[0] + va[1] * t_as[1]);
-      const double ng = sqrt(gg[0] * gg[0] + gg[1] * gg[1]);
-      dv[0] += (P_as * gg[0] - Pi_s * t_as[0] * ng) / gam;
-      dv[1] += (P_as * gg[1] - Pi_s * t_as[1] * ng) / gam;
+      double n_s[3], t_as[3], vt[3], r_as[3];
+      normalize_d<D>(gg, n_s);
+      const double vn = dot_d<D>(va, n_s);
+#pragma unroll
+      for (int k = 0; k < D; ++k) vt[k] = va[k] - vn * n_s[k];
+      normalize_d<D>(vt, t_as);
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        double xk[3];
+#pragma unroll
+        for (int j = 0; j < D; ++j) xk[j] = g[D * j + k];
+        r_as[k] = pa[k] - face_avg<D>(xk);
+      }
+      const double dr_as = fmax(T.h / 2.0, dot_d<D>(r_as, n_s));
+      const double Pi_s = 2.0 * A.phys.mu / (rho_a * dr_as) * dot_d<D>(va, t_as);
+      const double ng = sqrt(dot_d<D>(gg, gg));
+#pragma unroll
+      for (int k = 0; k < D; ++k) dv[k] += (P_as * gg[k] - Pi_s * t_as[k] * ng) / gam;
     });
   }
   fc.face_drho[i] = drho;
-  fc.face_dv[2 * i] = dv[0];
-  fc.face_dv[2 * i + 1] = dv[1];
+#pragma unroll
+  for (int k = 0; k < D; ++k) fc.face_dv[D * i + k] = dv[k];
 }
 
 // The force pass's share: pair sums over gamma, plus the stored face terms
 // and gravity.
-template<int F>
-__device__ __forceinline__ void apply_face_terms(const StageArgs<2, F>& A,
+template<int D, int F>
+__device__ __forceinline__ void apply_face_terms(const StageArgs<D, F>& A,
                                                  int64_t i, double& drho,
                                                  double* dv) {
   const double gam = A.fc.gamma[i];
   drho = drho / gam + A.fc.face_drho[i];
-  dv[0] = dv[0] / gam + A.fc.face_dv[2 * i];
-  dv[1] = dv[1] / gam + A.fc.face_dv[2 * i + 1] - A.phys.g;
+#pragma unroll
+  for (int k = 0; k < D; ++k) dv[k] = dv[k] / gam + A.fc.face_dv[D * i + k];
+  dv[1] -= A.phys.g;
 }
 
 // Team lanes share one target: each takes every Team-th cell of the block
@@ -1240,7 +1270,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     const double eps2 = T.visc_eps2, dk = T.diff_k;
     double drho = 0.0;
     // Face boundaries: gravity is added after the gamma division.
-    const bool faces = D == 2 && A.fc.on;
+    const bool faces = A.fc.on;
     double dv[3] = {0.0, (lane == 0 && !faces) ? -A.phys.g : 0.0, 0.0};
     auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
       for (uint32_t j = s; j < en; ++j) {
@@ -1294,9 +1324,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
       }
       if (lane != 0) return;
     }
-    if constexpr (D == 2) {
-      if (faces) apply_face_terms(A, i, drho, dv);
-    }
+    if (faces) apply_face_terms(A, i, drho, dv);
 #pragma unroll
     for (int k = 0; k < D; ++k) dv_out[k] = dv[k];
     drho_out = drho;
@@ -1304,7 +1332,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     PairF32<D, K, Phys> acc;
     acc.init(A.phys, T, load_dat(A.datrec, static_cast<uint32_t>(i)), A.kahan);
     // Gravity once per target; with face boundaries after the gamma division.
-    const bool faces = D == 2 && A.fc.on;
+    const bool faces = A.fc.on;
     if (lane != 0 || faces) acc.dv[1].s = 0.f;
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
@@ -1375,15 +1403,13 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     }
     rho_self = acc.a.drho;
     drho_out = acc.drho.value();
-    if constexpr (D == 2) {
-      if (faces) {
-        double drho = drho_out;
-        double dv[2] = {dv_out[0], dv_out[1]};
-        apply_face_terms(A, i, drho, dv);
-        drho_out = static_cast<float>(drho);
-        dv_out[0] = static_cast<float>(dv[0]);
-        dv_out[1] = static_cast<float>(dv[1]);
-      }
+    if (faces) {
+      double drho = drho_out;
+      double dv[3] = {dv_out[0], dv_out[1], dv_out[2]};
+      apply_face_terms(A, i, drho, dv);
+      drho_out = static_cast<float>(drho);
+#pragma unroll
+      for (int k = 0; k < D; ++k) dv_out[k] = static_cast<float>(dv[k]);
     }
   }
   forces_epilogue<D, F>(A, i, id, tk, T, c, va, rho_self, dv_out, drho_out);
@@ -1687,8 +1713,8 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
 // gamma and grad gamma of every particle (FluidEquations::compute_gamma,
 // fluid_equations.hpp:166-193); also records the cell-order slot of each
 // fixed particle for the face terms' vertex lookups.
-template<int K, int F>
-__global__ void __launch_bounds__(128) k_gamma(StageArgs<2, F> A) {
+template<int D, int K, int F>
+__global__ void __launch_bounds__(128) k_gamma(StageArgs<D, F> A) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   const FaceArgs& fc = A.fc;
@@ -1698,31 +1724,38 @@ __global__ void __launch_bounds__(128) k_gamma(StageArgs<2, F> A) {
   const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
   const TankDev& T = A.tanks[tk];
   int c[3] = {0, 0, 0};
-  cell_from_key<2>(T, key, c);
-  const uint32_t gcell = T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
-  const double x[2] = {A.Y.pos[0][i], A.Y.pos[1][i]};
+  cell_from_key<D>(T, key, c);
+  const uint32_t gcell = global_cell<D>(T, c);
+  double x[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < D; ++k) x[k] = A.Y.pos[k][i];
   const double radius = KernelPoly<K>::unit_radius * T.h;
   const double wd = fc.weight;
-  double g[2] = {0.0, 0.0};
-  for_adjacent_faces(fc, gcell, x, radius, [&](uint32_t, const double* ab) {
-    double fl[2];
-    face_flux<K>(ab, x, T.h, wd, fl);
-    g[0] += fl[0];
-    g[1] += fl[1];
+  double g[3] = {0.0, 0.0, 0.0};
+  for_adjacent_faces<D>(fc, gcell, x, radius, [&](uint32_t, const double* f) {
+    double fl[3];
+    face_flux_d<K, D>(f, x, T.h, wd, fl);
+#pragma unroll
+    for (int k = 0; k < D; ++k) g[k] += fl[k];
   });
-  double ga = face_contains(fc, tk, fc.row_off[tk] + c[1], x) ? 1.0 : 0.0;
-  const double ng = sqrt(g[0] * g[0] + g[1] * g[1]);
+  bool inside;
+  if constexpr (D == 2) inside = face_contains(fc, tk, fc.row_off[tk] + c[1], x);
+  else inside = fc.tank_edges[tk] == 0 || face_contains3(fc, tk, gcell, x);
+  double ga = inside ? 1.0 : 0.0;
+  const double ng = sqrt(dot_d<D>(g, g));
   if (!(ng <= kTiny)) {
     const double s = 2.0 * ga - 1.0;
     const double h2 = T.h * T.h;
-    const double xs[2] = {x[0] + s * (g[0] / ng) * h2, x[1] + s * (g[1] / ng) * h2};
-    for_adjacent_faces(fc, gcell, x, radius, [&](uint32_t, const double* ab) {
-      ga -= face_antigrad_flux<K>(ab, xs, T.h, wd);
+    double xs[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) xs[k] = x[k] + s * (g[k] / ng) * h2;
+    for_adjacent_faces<D>(fc, gcell, x, radius, [&](uint32_t, const double* f) {
+      ga -= face_antigrad_flux_d<K, D>(f, xs, T.h, wd);
     });
   }
   fc.gamma[i] = ga;
-  fc.ggam[2 * i] = g[0];
-  fc.ggam[2 * i + 1] = g[1];
+#pragma unroll
+  for (int k = 0; k < D; ++k) fc.ggam[D * i + k] = g[k];
 }
 
 // ---------------------------------------------------------------------------

@@ -145,6 +145,68 @@ __device__ __forceinline__ bool post_target(const PostArgs<D, F>& A, int64_t& i,
   return true;
 }
 
+// Face terms of the shifting sums of each fluid particle (N, L, grad v,
+// grad rho; fluid_equations.hpp:340-349), divided by gamma_a; k_post_sums
+// starts its pair sums from them.  A pass of its own keeps the face
+// integrals' registers out of the pair loop.
+template<int D, int F, int K>
+__global__ void __launch_bounds__(128) k_post_faces(PostArgs<D, F> A) {
+  int64_t i;
+  uint32_t id;
+  const TankDev* Tp;
+  int c[3] = {0, 0, 0};
+  if (!post_target(A, i, id, Tp, c)) return;
+  if (id & kWallBit) return;
+  const TankDev& T = *Tp;
+  double rho_a, va[3];
+  post_neighbour<D>(A.S.datrec, static_cast<uint32_t>(i), T, rho_a, va);
+  double pa[3];
+#pragma unroll
+  for (int k = 0; k < D; ++k) pa[k] = A.S.Y.pos[k][i];
+  double N[D] = {}, L[D * D] = {}, gv[D * D] = {}, gr[D] = {};
+  const double gam = A.S.fc.gamma[i];
+  const double radius = KernelPoly<K>::unit_radius * T.h;
+  for_adjacent_faces<D>(A.S.fc, global_cell<D>(T, c), pa, radius,
+                        [&](uint32_t f, const double* g) {
+    double gg[3], rv[3], r_sa[3];
+    face_flux_d<K, D>(g, pa, T.h, A.S.fc.weight, gg);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      rv[j] = vertex_rho(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[D * f + j]], T);
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      double xk[3];
+#pragma unroll
+      for (int j = 0; j < D; ++j) xk[j] = g[D * j + k];
+      r_sa[k] = face_avg<D>(xk) - pa[k];
+    }
+    // The face vertices' velocities are zero: v_sa = -v_a.
+    const double rho_sa = face_avg<D>(rv) - rho_a;
+#pragma unroll
+    for (int a2 = 0; a2 < D; ++a2) {
+      N[a2] -= gg[a2] / gam;
+#pragma unroll
+      for (int b2 = 0; b2 < D; ++b2) {
+        L[a2 * D + b2] -= r_sa[a2] * gg[b2] / gam;
+        gv[a2 * D + b2] -= -va[a2] * gg[b2] / gam;
+      }
+      gr[a2] -= rho_sa * gg[a2] / gam;
+    }
+  });
+  double* out = A.S.fc.post_face + kPostFaceSums<D> * static_cast<size_t>(i);
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    out[k] = N[k];
+    out[D + 2 * D * D + k] = gr[k];
+  }
+#pragma unroll
+  for (int k = 0; k < D * D; ++k) {
+    out[D + k] = L[k];
+    out[D + D * D + k] = gv[k];
+  }
+}
+
 template<int D, int F, int K>
 __global__ void __launch_bounds__(128) k_post_sums(PostArgs<D, F> A) {
   int64_t i;
@@ -168,30 +230,21 @@ __global__ void __launch_bounds__(128) k_post_sums(PostArgs<D, F> A) {
   const double tiny2 = 6.0554544523933395e-06 * 6.0554544523933395e-06;
   // Face boundaries (fluid_equations.hpp:335-349): face terms first, and
   // every sum divided by gamma_a.
+  // Face boundaries (fluid_equations.hpp:335-349): the face terms come
+  // first (k_post_faces), and every sum is divided by gamma_a.
   double gam = 1.0;
-  if constexpr (D == 2) {
-    if (A.S.fc.on) {
-      gam = A.S.fc.gamma[i];
-      const uint32_t gcell =
-          T.cell_off + static_cast<uint32_t>(c[1]) * T.nc[0] + c[0];
-      const double radius = KernelPoly<K>::unit_radius * T.h;
-      for_adjacent_faces(A.S.fc, gcell, pa, radius, [&](uint32_t f, const double* ab) {
-        double gg[2];
-        face_flux<K>(ab, pa, T.h, A.S.fc.weight, gg);
-        const double rho_v0 = vertex_rho(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f]], T);
-        const double rho_v1 = vertex_rho(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[2 * f + 1]], T);
-        const double r_sa[2] = {(ab[0] + ab[2]) / 2.0 - pa[0], (ab[1] + ab[3]) / 2.0 - pa[1]};
-        const double v_sa[2] = {-va[0], -va[1]};
-        const double rho_sa = (rho_v0 + rho_v1) / 2.0 - rho_a;
-        for (int a2 = 0; a2 < 2; ++a2) {
-          N[a2] -= gg[a2] / gam;
-          for (int b2 = 0; b2 < 2; ++b2) {
-            L[a2 * D + b2] -= r_sa[a2] * gg[b2] / gam;
-            gv[a2 * D + b2] -= v_sa[a2] * gg[b2] / gam;
-          }
-          gr[a2] -= rho_sa * gg[a2] / gam;
-        }
-      });
+  if (A.S.fc.on) {
+    gam = A.S.fc.gamma[i];
+    const double* f0 = A.S.fc.post_face + kPostFaceSums<D> * static_cast<size_t>(i);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      N[k] = f0[k];
+      gr[k] = f0[D + 2 * D * D + k];
+    }
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) {
+      L[k] = f0[D + k];
+      gv[k] = f0[D + D * D + k];
     }
   }
   for_cells<D, false>(T, c, A.S.k, A.S.cell_start,
