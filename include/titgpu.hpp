@@ -29,12 +29,12 @@
  * as TIT_ENSURE does (source/tit/core/exception.hpp:81).
  *
  * Walls: either fixed particles with an empty domain surface ("particle
- * walls": gamma = 1 and no face terms, fluid_equations.hpp:122-163), or,
- * in 2D, the reference's semi-analytical face walls: a
- * tessellated domain surface whose vertices are the fixed particles and a
- * winding-number containment (geom::MakeFastWinding), as titwcsph sets up
- * (wcsph.cpp:55-77, 109-112).  Every fluid particle must lie inside the
- * containment.
+ * walls": gamma = 1 and no face terms, fluid_equations.hpp:122-163), or
+ * the reference's semi-analytical face walls: a tessellated domain surface
+ * (segments in 2D, triangles in 3D) whose vertices are the fixed particles
+ * and a winding-number containment (geom::MakeFastWinding), as titwcsph
+ * sets up (wcsph.cpp:55-77, 109-112).  Every fluid particle must lie inside
+ * the containment.
  *
  * GPU-only choices (precision form, the textbook term set, CFL constants)
  * come in an optional trailing sph::GpuOptions argument of FluidEquations.
@@ -48,6 +48,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <functional>
+#include <map>
 #include <memory>
 #include <ranges>
 #include <span>
@@ -140,9 +141,9 @@ Vec(T, U...) -> Vec<std::common_type_t<T, U...>, 1 + sizeof...(U)>;
 namespace geom {
 
 /// Boundary surface (source/tit/geom/surface.hpp): vertices and faces
-/// (segments in 2D).  An empty surface means particle walls; a 2D surface
-/// with faces selects the semi-analytical wall mode, whose fixed particles
-/// are the surface's vertices in order (wcsph.cpp:109-112).
+/// (segments in 2D, triangles in 3D).  An empty surface means particle
+/// walls; a surface with faces selects the semi-analytical wall mode, whose
+/// fixed particles are the surface's vertices in order (wcsph.cpp:109-112).
 template<class V>
 class Surface {
 public:
@@ -169,6 +170,7 @@ private:
 /// original vertices first, then each face's new vertices in order
 /// (source/tit/geom/tessellation.hpp:30-60).
 template<class V>
+  requires (V::dim() == 2)
 auto tessellate(const Surface<V>& surf, double d_max) -> Surface<V> {
   if (!(d_max > 0.0)) throw Exception{"tessellate: d_max <= 0"};
   Surface<V> out;
@@ -194,38 +196,134 @@ auto tessellate(const Surface<V>& surf, double d_max) -> Surface<V> {
   return out;
 }
 
-/// Containment by the winding number of a closed polygon (> 1/2 inside),
-/// the role of the reference's FastWinding (fast_winding.hpp:80-95); the
-/// GPU receives the polygon itself.
+/// 3D: red refinement until no edge is longer than d_max.  Each round
+/// bisects every edge longer than d_max (one midpoint per edge, appended in
+/// the order the faces' edges ab, bc, ca are met), then splits each
+/// triangle into 2, 3 or 4 by its bisected edges, keeping its orientation
+/// (source/tit/geom/tessellation.hpp:66-186).
+template<class V>
+  requires (V::dim() == 3)
+auto tessellate(const Surface<V>& surf, double d_max) -> Surface<V> {
+  if (!(d_max > 0.0)) throw Exception{"tessellate: d_max <= 0"};
+  std::vector<V> verts;
+  for (std::size_t i = 0; i < surf.num_verts(); ++i) verts.push_back(surf.vert(i));
+  using Tri = std::array<std::size_t, 3>;
+  std::vector<Tri> tris, next;
+  for (std::size_t fi = 0; fi < surf.num_faces(); ++fi) tris.push_back(surf.face_verts(fi));
+  std::map<std::pair<std::size_t, std::size_t>, std::size_t> mid;
+  constexpr std::size_t none = static_cast<std::size_t>(-1);
+  for (;;) {
+    mid.clear();
+    const auto split = [&](std::size_t a, std::size_t b) {
+      const auto key = std::minmax(a, b);
+      if (mid.contains(key)) return;
+      const V e = verts[b] - verts[a];
+      if (static_cast<double>(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) <= d_max * d_max) {
+        return;
+      }
+      using Num = std::remove_cvref_t<decltype(verts[a][0])>;
+      verts.push_back((verts[a] + verts[b]) * Num{0.5});
+      mid.emplace(key, verts.size() - 1);
+    };
+    for (const auto& [a, b, c] : tris) {
+      split(a, b);
+      split(b, c);
+      split(c, a);
+    }
+    if (mid.empty()) break;
+    const auto at = [&](std::size_t a, std::size_t b) {
+      const auto it = mid.find(std::minmax(a, b));
+      return it == mid.end() ? none : it->second;
+    };
+    next.clear();
+    for (const auto& [a, b, c] : tris) {
+      const std::size_t ab = at(a, b), bc = at(b, c), ca = at(c, a);
+      const int n = (ab != none) + (bc != none) + (ca != none);
+      if (n == 3) {
+        next.insert(next.end(), {Tri{a, ab, ca}, Tri{ab, b, bc}, Tri{ca, bc, c}, Tri{ab, bc, ca}});
+      } else if (n == 2 && ca == none) {
+        next.insert(next.end(), {Tri{a, ab, c}, Tri{ab, bc, c}, Tri{ab, b, bc}});
+      } else if (n == 2 && ab == none) {
+        next.insert(next.end(), {Tri{b, bc, a}, Tri{bc, ca, a}, Tri{bc, c, ca}});
+      } else if (n == 2) {
+        next.insert(next.end(), {Tri{c, ca, b}, Tri{ca, ab, b}, Tri{ca, a, ab}});
+      } else if (ab != none) {
+        next.insert(next.end(), {Tri{a, ab, c}, Tri{ab, b, c}});
+      } else if (bc != none) {
+        next.insert(next.end(), {Tri{b, bc, a}, Tri{bc, c, a}});
+      } else if (ca != none) {
+        next.insert(next.end(), {Tri{c, ca, b}, Tri{ca, a, b}});
+      } else {
+        next.push_back(Tri{a, b, c});
+      }
+    }
+    tris.swap(next);
+  }
+  Surface<V> out;
+  for (const V& v : verts) out.append_vert(v);
+  for (const Tri& t : tris) out.append_face(t);
+  return out;
+}
+
+/// Containment by the winding number of a closed surface (> 1/2 inside),
+/// the role of the reference's FastWinding (fast_winding.hpp:80-95): in 2D
+/// a closed polygon (the faces' first vertices in order), in 3D a closed
+/// triangle mesh with outward normals.  The GPU receives the surface
+/// itself (surface_data: 2 doubles per polygon vertex or 9 per triangle).
 template<class V>
 class Winding {
 public:
   explicit Winding(const Surface<V>& surf) {
     for (std::size_t fi = 0; fi < surf.num_faces(); ++fi) {
-      loop_.push_back(surf.vert(surf.face_verts(fi)[0]));
+      if constexpr (V::dim() == 2) {
+        pts_.push_back(surf.vert(surf.face_verts(fi)[0]));
+      } else {
+        for (const auto v : surf.face_verts(fi)) pts_.push_back(surf.vert(v));
+      }
     }
   }
   auto operator()(const V& x) const -> double {
+    constexpr double two_pi = 2.0 * 3.14159265358979323846;
     double w = 0.0;
-    for (std::size_t i = 0; i < loop_.size(); ++i) {
-      const V a = loop_[i] - x, b = loop_[(i + 1) % loop_.size()] - x;
-      w += std::atan2(static_cast<double>(a[0] * b[1] - a[1] * b[0]),
-                      static_cast<double>(a[0] * b[0] + a[1] * b[1]));
+    if constexpr (V::dim() == 2) {
+      for (std::size_t i = 0; i < pts_.size(); ++i) {
+        const V a = pts_[i] - x, b = pts_[(i + 1) % pts_.size()] - x;
+        w += std::atan2(static_cast<double>(a[0] * b[1] - a[1] * b[0]),
+                        static_cast<double>(a[0] * b[0] + a[1] * b[1]));
+      }
+    } else {
+      // Solid angle of each triangle (Van Oosterom and Strackee), as
+      // Triangle::winding_number (geom/triangle.hpp).
+      const auto dot = [](const V& a, const V& b) {
+        return static_cast<double>(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+      };
+      for (std::size_t i = 0; i < pts_.size(); i += 3) {
+        const V a = pts_[i] - x, b = pts_[i + 1] - x, c = pts_[i + 2] - x;
+        const double na = std::sqrt(dot(a, a)), nb = std::sqrt(dot(b, b)),
+                     nc = std::sqrt(dot(c, c));
+        const double det =
+            static_cast<double>(a[0] * (b[1] * c[2] - b[2] * c[1]) +
+                                a[1] * (b[2] * c[0] - b[0] * c[2]) +
+                                a[2] * (b[0] * c[1] - b[1] * c[0]));
+        w += std::atan2(det, na * nb * nc + dot(a, b) * nc + dot(b, c) * na +
+                                 dot(c, a) * nb);
+      }
     }
-    return w / (2.0 * 3.14159265358979323846);
+    return w / two_pi;
   }
   auto contains(const V& x) const -> bool { return (*this)(x) > 0.5; }
-  auto polygon() const -> std::vector<double> {
+  auto surface_data() const -> std::vector<double> {
     std::vector<double> out;
-    for (const V& v : loop_) {
-      out.push_back(static_cast<double>(v[0]));
-      out.push_back(static_cast<double>(v[1]));
+    for (const V& v : pts_) {
+      for (std::size_t k = 0; k < V::dim(); ++k) out.push_back(static_cast<double>(v[k]));
     }
     return out;
   }
+  /// The 2D polygon's vertices (x, y), as surface_data.
+  auto polygon() const -> std::vector<double> { return surface_data(); }
 
 private:
-  std::vector<V> loop_;
+  std::vector<V> pts_;
 };
 
 /// Maker of winding-number containment functions (the reference's
@@ -398,8 +496,8 @@ public:
       : g_{g}, mu_{mu}, domain_{std::move(domain)},
         containment_{std::move(containment)}, eos_{eos}, options_{options} {
     if (domain_.num_faces() != 0) {
-      if constexpr (Dim != 2 || !has_polygon_) {
-        throw Exception{"FluidEquations: boundary faces need 2D and a "
+      if constexpr (!has_surface_) {
+        throw Exception{"FluidEquations: boundary faces need a "
                         "winding-number containment (geom::MakeFastWinding)"};
       }
     }
@@ -443,7 +541,7 @@ public:
                       static_cast<double>(eos_.cs_0()),
                       options_.graph,
                       options_.autotune && domain_.num_faces() == 0);
-    if constexpr (Dim == 2 && has_polygon_) {
+    if constexpr (has_surface_) {
       if (domain_.num_faces() != 0) attach_faces_(particles);
     }
   }
@@ -459,8 +557,8 @@ private:
     }
   }
 
-  static constexpr bool has_polygon_ =
-      requires(const Containment& c) { c.polygon(); };
+  static constexpr bool has_surface_ =
+      requires(const Containment& c) { c.surface_data(); };
 
   // The tank's fixed particles must be the domain's vertices, in order
   // (wcsph.cpp:109-112); the faces index them.
@@ -482,11 +580,12 @@ private:
         fv.push_back(static_cast<std::int32_t>(v));
       }
     }
-    const std::vector<double> poly = containment_.polygon();
+    const std::vector<double> surf = containment_.surface_data();
+    const std::size_t per = Dim == 2 ? 2 : 9;
     gpu_detail::ensure(
         tg_tank_faces(particles.context(), 0,
                       static_cast<std::int32_t>(domain_.num_faces()), fv.data(),
-                      static_cast<std::int32_t>(poly.size() / 2), poly.data()),
+                      static_cast<std::int32_t>(surf.size() / per), surf.data()),
         particles.context(), "tg_tank_faces");
     if (options_.autotune) {
       tg_tuning tuned{};

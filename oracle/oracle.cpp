@@ -252,14 +252,20 @@ constexpr KernelPieces kPieces[6] = {
 
 
 
+// 1/k, k = 0..17 (entry 0 unused): the recursions multiply by these.
+constexpr double kInv[18] = {
+    0.0, 1.0, 1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0, 1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0, 1.0 / 8.0,
+    1.0 / 9.0, 1.0 / 10.0, 1.0 / 11.0, 1.0 / 12.0, 1.0 / 13.0, 1.0 / 14.0, 1.0 / 15.0,
+    1.0 / 16.0, 1.0 / 17.0};
+
 void line_integrals(double eta, double z, double rho, double L, int pmax,
                     double* J) {
   J[0] = z;
-  if (pmax >= 1) J[1] = (z * rho + eta * eta * L) / 2.0;
+  if (pmax >= 1) J[1] = (z * rho + eta * eta * L) * 0.5;
   double rp = rho;
   for (int p = 2; p <= pmax; ++p) {
     rp *= rho;
-    J[p] = (z * rp + p * eta * eta * J[p - 2]) / (p + 1);
+    J[p] = (z * rp + p * eta * eta * J[p - 2]) * kInv[p + 1];
   }
 }
 
@@ -437,25 +443,47 @@ constexpr TailPiece3 kTail3[6][3] = {
   {{14, {128.0 / 1365.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 11.0 / 20.0, 0.0, -33.0 / 56.0, 0.0, 77.0 / 96.0, -33.0 / 40.0, 105.0 / 256.0, -11.0 / 96.0, 231.0 / 13312.0, -1.0 / 896.0}}},
 };
 
-// Edge primitives J_0..J_kmax and K_0..K_kmax at z.
-void edge_integrals(double eta, double delta, double beta2, double z,
-                    double rho, double A, double L, int kmax, double* J,
-                    double* K) {
-  J[0] = z;
-  J[1] = (z * rho + beta2 * L) / 2.0;
-  double rp = rho;
-  for (int k = 2; k <= kmax; ++k) {
-    rp *= rho;
-    J[k] = (z * rp + k * beta2 * J[k - 2]) / (k + 1);
+// The parts of the edge and sector values that depend on eta only: with
+// a_p = c_p/(p + 2) and b_p = s_p/(p - 1),
+//   flux:     lead = -sum_p a_p eta^{p+2}, sector = sum_p a_p cutoff^{p+2} + lead
+//   antigrad: lead = s_0 - sum_{p>=3} b_p eta^p,
+//             sector = lead + eta (sum_{p>=3} b_p cutoff^{p-1} - s_0/cutoff)
+// (the sector formulas above, regrouped); the line primitive is then
+// sum_p a_p K_{p+2} + lead K_0 or lead K_0 + eta sum_{p>=3} b_p K_{p-1}.
+struct EdgeCoef {
+  double lead, sector;
+};
+EdgeCoef edge_coef(const KernelPiece& kp, const TailPiece3& tp, bool antigrad,
+                   double eta) {
+  EdgeCoef e{0.0, 0.0};
+  if (!antigrad) {
+    double ep = eta * eta, cp = kp.cutoff * kp.cutoff, cut = 0.0;
+    for (int p = 0; p <= kp.deg; ++p) {
+      const double a = kp.c[p] * kInv[p + 2];
+      e.lead -= a * ep;
+      cut += a * cp;
+      ep *= eta;
+      cp *= kp.cutoff;
+    }
+    e.sector = cut + e.lead;
+    return e;
   }
-  K[0] = A;
-  K[1] = delta * L;
-  for (int k = 2; k <= kmax; ++k) K[k] = delta * J[k - 2] + eta * eta * K[k - 2];
+  double ep = eta * eta * eta, cp = kp.cutoff * kp.cutoff, cut = 0.0;
+  e.lead = tp.s[0];
+  for (int p = 3; p <= tp.deg; ++p) {
+    const double b = tp.s[p] * kInv[p - 1];
+    e.lead -= b * ep;
+    cut += b * cp;
+    ep *= eta;
+    cp *= kp.cutoff;
+  }
+  e.sector = e.lead + eta * (cut - tp.s[0] / kp.cutoff);
+  return e;
 }
 
 double edge_primitive(const KernelPiece& kp, const TailPiece3& tp,
-                      bool antigrad, double eta, double delta, double beta2,
-                      double beta, double z) {
+                      const EdgeCoef& ec, bool antigrad, double eta,
+                      double delta, double beta2, double beta, double z) {
   const double rho = std::sqrt(z * z + beta2);
   const double A =
       is_tiny(delta)
@@ -465,43 +493,25 @@ double edge_primitive(const KernelPiece& kp, const TailPiece3& tp,
       is_tiny(beta)
           ? 0.0
           : std::copysign(std::log1p((std::abs(z) + z * z / (rho + beta)) / beta), z);
+  const int kmax = antigrad ? std::max(tp.deg - 1, 1) : kp.deg + 2;
   double J[16], K[16];
+  J[0] = z;
+  J[1] = (z * rho + beta2 * L) * 0.5;
+  double rp = rho;
+  for (int k = 2; k <= kmax; ++k) {
+    rp *= rho;
+    J[k] = (z * rp + k * beta2 * J[k - 2]) * kInv[k + 1];
+  }
+  K[0] = A;
+  K[1] = delta * L;
+  for (int k = 2; k <= kmax; ++k) K[k] = delta * J[k - 2] + eta * eta * K[k - 2];
   double s = 0.0;
   if (!antigrad) {
-    edge_integrals(eta, delta, beta2, z, rho, A, L, kp.deg + 2, J, K);
-    double c0 = 0.0;
-    for (int p = 0; p <= kp.deg; ++p) {
-      if (kp.c[p] == 0.0) continue;
-      s += kp.c[p] / (p + 2) * K[p + 2];
-      c0 -= kp.c[p] * ipow(eta, p + 2) / (p + 2);
-    }
-    return s + c0 * K[0];
+    for (int p = 0; p <= kp.deg; ++p) s += kp.c[p] * kInv[p + 2] * K[p + 2];
+    return s + ec.lead * K[0];
   }
-  edge_integrals(eta, delta, beta2, z, rho, A, L, std::max(tp.deg - 1, 1), J, K);
-  for (int p = 0; p <= tp.deg; ++p) {
-    if (tp.s[p] == 0.0) continue;
-    if (p == 0) s += tp.s[0] * K[0];
-    else s += tp.s[p] * (eta * K[p - 1] - ipow(eta, p) * K[0]) / (p - 1);
-  }
-  return s;
-}
-
-double sector_value(const KernelPiece& kp, const TailPiece3& tp, bool antigrad,
-                    double eta) {
-  double s = 0.0;
-  if (!antigrad) {
-    for (int p = 0; p <= kp.deg; ++p) {
-      if (kp.c[p] == 0.0) continue;
-      s += kp.c[p] * (ipow(kp.cutoff, p + 2) - ipow(eta, p + 2)) / (p + 2);
-    }
-    return s;
-  }
-  for (int p = 0; p <= tp.deg; ++p) {
-    if (tp.s[p] == 0.0) continue;
-    if (p == 0) s += tp.s[0] * (1.0 - eta / kp.cutoff);
-    else s += tp.s[p] * (eta * ipow(kp.cutoff, p - 1) - ipow(eta, p)) / (p - 1);
-  }
-  return s;
+  for (int p = 3; p <= tp.deg; ++p) s += tp.s[p] * kInv[p - 1] * K[p - 1];
+  return ec.lead * K[0] + eta * s;
 }
 
 // unit_triangle_integral (kernel.hpp:316-399) for one piece; v = the three
@@ -510,7 +520,7 @@ double unit_triangle_piece(const KernelPiece& kp, const TailPiece3& tp,
                            bool antigrad, double eta, const double* v) {
   if (eta >= kp.cutoff) return 0.0;
   const double radius2 = kp.cutoff * kp.cutoff - eta * eta;
-  const double sector = sector_value(kp, tp, antigrad, eta);
+  const EdgeCoef ec = edge_coef(kp, tp, antigrad, eta);
   double total = 0.0;
   for (int e = 0; e < 3; ++e) {
     const double* p0 = v + 2 * e;
@@ -538,12 +548,12 @@ double unit_triangle_piece(const KernelPiece& kp, const TailPiece3& tp,
     for (int i = 0; i + 1 < nz; ++i) {
       const double lo = zs[i], hi = zs[i + 1];
       if (is_tiny(hi - lo)) continue;
-      const double mid = (lo + hi) / 2.0;
+      const double mid = (lo + hi) * 0.5;
       if (mid * mid + delta2 < radius2) {
-        total += edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, hi) -
-                 edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, lo);
+        total += edge_primitive(kp, tp, ec, antigrad, eta, delta, beta2, beta, hi) -
+                 edge_primitive(kp, tp, ec, antigrad, eta, delta, beta2, beta, lo);
       } else {
-        total += sector * std::atan2(delta * (hi - lo), lo * hi + delta2);
+        total += ec.sector * std::atan2(delta * (hi - lo), lo * hi + delta2);
       }
     }
   }

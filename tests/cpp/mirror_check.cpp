@@ -89,8 +89,8 @@ auto main(int argc, char** argv) -> int {
   }));
   CHECK(throws([] { TaitEquationOfState{-1.0, 1000.0}; }));
 
-  // Face walls: tessellation as the reference splits faces, winding-number
-  // containment, and the FP32 form refused with faces.
+  // Face walls: tessellation as the reference splits faces and the
+  // winding-number containment.
   {
     geom::Surface<Vec<double, 2>> pool;
     pool.append_vert({0.0, 1.0});
@@ -123,6 +123,46 @@ auto main(int argc, char** argv) -> int {
       FluidEquations bad{9.81, 0.001, t, geom::AllInside{},
                          TaitEquationOfState{20.0, 1000.0}, SixthOrderWendlandKernel{}};
     }));
+  }
+  // 3D face walls: red refinement of a box keeps it closed and oriented,
+  // with every edge at most d_max; the winding number of the outward box.
+  {
+    geom::Surface<Vec<double, 3>> box;
+    const double X = 2.0, Y = 1.0, Z = 0.5;
+    for (int i = 0; i < 8; ++i) {
+      box.append_vert({(i & 1) ? X : 0.0, (i & 2) ? Y : 0.0, (i & 4) ? Z : 0.0});
+    }
+    // Outward quads split into two triangles each.
+    const std::size_t quads[6][4] = {{0, 2, 3, 1}, {4, 5, 7, 6}, {0, 1, 5, 4},
+                                     {2, 6, 7, 3}, {1, 3, 7, 5}, {0, 4, 6, 2}};
+    for (const auto& q : quads) {
+      box.append_face({q[0], q[1], q[2]});
+      box.append_face({q[0], q[2], q[3]});
+    }
+    const geom::MakeFastWinding<double> make_winding;
+    const auto inside = make_winding(box);
+    CHECK(inside.contains(Vec{1.0, 0.5, 0.25}) && !inside.contains(Vec{2.5, 0.5, 0.25}));
+    CHECK(std::abs(inside(Vec{1.0, 0.5, 0.25}) - 1.0) < 1e-12);
+    CHECK(inside.surface_data().size() == 12 * 9);
+    const auto t = geom::tessellate(box, 0.3);
+    CHECK(t.num_verts() > 8 && t.num_faces() > 12);
+    std::map<std::pair<std::size_t, std::size_t>, int> edges;
+    double area = 0.0;
+    for (std::size_t fi = 0; fi < t.num_faces(); ++fi) {
+      const auto f = t.face_verts(fi);
+      for (int k = 0; k < 3; ++k) {
+        const auto d = t.vert(f[(k + 1) % 3]) - t.vert(f[k]);
+        CHECK(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] <= 0.3 * 0.3);
+        ++edges[{f[k], f[(k + 1) % 3]}];
+      }
+      const auto u = t.vert(f[1]) - t.vert(f[0]), v = t.vert(f[2]) - t.vert(f[0]);
+      const double cx = u[1] * v[2] - u[2] * v[1], cy = u[2] * v[0] - u[0] * v[2],
+                   cz = u[0] * v[1] - u[1] * v[0];
+      area += std::sqrt(cx * cx + cy * cy + cz * cz) / 2.0;
+    }
+    for (const auto& [e, n] : edges) CHECK(n == 1 && edges.count({e.second, e.first}) == 1);
+    CHECK(std::abs(area - 2.0 * (X * Y + X * Z + Y * Z)) < 1e-12);
+    CHECK(std::abs(make_winding(t)(Vec{1.0, 0.5, 0.25}) - 1.0) < 1e-12);
   }
   CHECK(throws([] { geom::GridSearch{0.0}; }));
 

@@ -254,6 +254,7 @@ int tg_context_create(const tg_params* params, tg_context** out) {
   Context& C = ctx->c;
   C.P = *params;
   cudaGetDevice(&C.device);
+  cudaDeviceGetAttribute(&C.sm_count, cudaDevAttrMultiProcessorCount, C.device);
   if (cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete ctx;
     return TG_ERR_CUDA;
@@ -1084,6 +1085,9 @@ int build_faces(tg_context* ctx) {
   TG_CUDA(&C, up(fa.cont_start, cont_start));
   const int64_t nn = C.n > 0 ? C.n : 1;
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.slot_of), sizeof(uint32_t) * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_list), sizeof(uint32_t) * nn));
+  TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_count), sizeof(uint32_t)));
+  TG_CUDA(&C, cudaMemsetAsync(fa.face_count, 0, sizeof(uint32_t), C.stream));
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.gamma), sizeof(double) * nn));
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.ggam), sizeof(double) * D * nn));
   TG_CUDA(&C, C.alloc(reinterpret_cast<void**>(&fa.face_drho), sizeof(double) * nn));

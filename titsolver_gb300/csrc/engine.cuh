@@ -76,6 +76,7 @@ struct Context {
   tg_params P{};
   PhysDev phys{};
   int device = 0;
+  int sm_count = 0;  // multiprocessors of the device
   cudaStream_t stream = nullptr;
 
   // Particles and tanks.

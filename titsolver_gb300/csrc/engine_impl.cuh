@@ -264,9 +264,9 @@ class Engine final : public EngineBase {
     const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
     const int stages = force_passes(C.P.integrator);
     const int per_stage = 3 * passes + 2 + 2 + (C.n_wall > 0 ? 1 : 0);
-    const int gam = C.faces.on ? 2 : 0;  // k_gamma, k_face_terms
+    const int gam = C.faces.on ? 3 : 0;  // k_gamma_init, k_gamma_faces, k_face_terms
     const int post = C.P.post_integrate == TG_POST_SHIFTING
-                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + (gam > 0 ? 1 : 0) : 0) + 5 +
+                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + (gam > 0 ? 2 : 0) : 0) + 5 +
                                (gam > 0 ? 1 : 0)
                          : 0;
     return static_cast<int64_t>(stages) * (per_stage + gam) + post + 1;
@@ -371,7 +371,7 @@ class Engine final : public EngineBase {
     p.shift = -C.P.cfl * 0.2;
     const unsigned grid = grid_for(C.n, 128);
     if (C.faces.on) {
-      k_post_faces<D, F, K><<<grid, 128, 0, C.stream>>>(p);
+      k_post_faces<D, F, K><<<face_grid(C), 128, 0, C.stream>>>(p);
       C.launches += 1;
     }
     k_post_sums<D, F, K><<<grid, 128, 0, C.stream>>>(p);
@@ -389,9 +389,18 @@ class Engine final : public EngineBase {
   // of this prepare (before the wall pass, which reads grad gamma).
   void enqueue_gamma(Context& C, const StageArgs<D, F>& a) {
     if (a.fc.on) {
-      k_gamma<D, K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
-      C.launches += 1;
+      cudaMemsetAsync(a.fc.face_count, 0, sizeof(uint32_t), C.stream);
+      k_gamma_init<D, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+      k_gamma_faces<D, K, F><<<face_grid(C), 128, 0, C.stream>>>(a);
+      C.launches += 2;
     }
+  }
+
+  // Grid of the warp-per-face-particle passes: they loop over the face
+  // list (its length is known on the device only), four warps per block.
+  static unsigned face_grid(const Context& C) {
+    const int64_t cap = 32 * static_cast<int64_t>(C.sm_count > 0 ? C.sm_count : 152);
+    return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((C.n + 3) / 4, cap)));
   }
 
   // One force pass of a step: its index (stage 0 copies the start state
@@ -428,7 +437,7 @@ class Engine final : public EngineBase {
       C.group_end(tok);
     }
     if (a.fc.on) {
-      k_face_terms<D, K, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
+      k_face_terms<D, K, F><<<face_grid(C), 128, 0, C.stream>>>(a);
       C.launches += 1;
     }
     tok = C.group_begin(kGroupForces);

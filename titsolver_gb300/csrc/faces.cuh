@@ -49,6 +49,8 @@ struct FaceArgs {
   const double* cont_tri;     // 9 per containment triangle
   const uint32_t* cont_start; // per tank (+1): its containment triangles
   uint32_t* slot_of;          // upload index -> cell-order slot (walls)
+  uint32_t* face_list;        // particles (cell order) whose cell lists faces
+  uint32_t* face_count;       // entries of face_list (this prepare)
   double* gamma;              // per particle, cell order
   double* ggam;               // grad gamma, D per particle
   double* face_drho;          // face terms of continuity, per particle
@@ -78,7 +80,9 @@ struct FacePieces {
 };
 
 // Support pieces of the six kernels (kernel.gen.cpp:520-553), expanded.
-static __constant__ FacePieces c_face_pieces[6] = {
+// Read at compile time only: the face integrals are unrolled per kernel and
+// piece, with the coefficients as immediates.
+inline constexpr FacePieces kFacePieces[6] = {
   // cubic spline
   {2, {{2.0, 3, {2.0, -3.0, 3.0 / 2.0, -1.0 / 4.0}, 5, {2.0 / 5.0, 0.0, -1.0, 1.0, -3.0 / 8.0, 1.0 / 20.0}},
    {1.0, 3, {-1.0, 3.0, -3.0, 1.0}, 5, {-1.0 / 20.0, 0.0, 1.0 / 2.0, -1.0, 3.0 / 4.0, -1.0 / 5.0}}}},
@@ -100,56 +104,80 @@ static __constant__ FacePieces c_face_pieces[6] = {
 
 constexpr double kTiny = 6.0554544523933395e-06;
 
-__device__ __forceinline__ void face_line_integrals(double eta, double z,
-                                                    double rho, double L,
-                                                    int pmax, double* J) {
-  J[0] = z;
-  if (pmax >= 1) J[1] = (z * rho + eta * eta * L) / 2.0;
-  double rp = rho;
-  for (int p = 2; p <= pmax; ++p) {
-    rp *= rho;
-    J[p] = (z * rp + p * eta * eta * J[p - 2]) / (p + 1);
+// 1/k for k = 0..17 (entry 0 unused): the recursions multiply by these
+// instead of dividing (FP64 division is a long instruction sequence).
+inline constexpr double kFaceInv[18] = {
+    0.0, 1.0, 1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0, 1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0, 1.0 / 8.0,
+    1.0 / 9.0, 1.0 / 10.0, 1.0 / 11.0, 1.0 / 12.0, 1.0 / 13.0, 1.0 / 14.0, 1.0 / 15.0,
+    1.0 / 16.0, 1.0 / 17.0};
+
+// x^n at compile time (n >= 0).
+constexpr double constexpr_pow(double x, int n) {
+  double r = 1.0;
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+// Compile-time loop: f.template operator()<B>() ... <E - 1>().
+template<int B, int E, class Fn>
+__device__ __forceinline__ void static_for(Fn&& f) {
+  if constexpr (B < E) {
+    f.template operator()<B>();
+    static_for<B + 1, E>(f);
   }
 }
 
-__device__ __forceinline__ double face_primitive(const FacePiece& kp,
-                                                 bool antigrad, double eta,
-                                                 double z) {
+// Segment line primitive of piece I of kernel K at z (units of h), with the
+// J_p recursion and the coefficients unrolled.
+template<int K, int I, bool Anti>
+__device__ __forceinline__ double face_primitive(double eta, double z) {
+  constexpr FacePiece kp = kFacePieces[K].p[I];
+  constexpr int pmax = Anti ? (kp.tdeg - 2 > 0 ? kp.tdeg - 2 : 0) : kp.deg;
   const double rho = sqrt(z * z + eta * eta);
-  const double A = atan2(z, eta);
   const double L = fabs(eta) <= kTiny
                        ? 0.0
                        : copysign(log1p((fabs(z) + z * z / (rho + eta)) / eta), z);
-  double J[14];
+  double J[pmax + 1];
+  J[0] = z;
+  if constexpr (pmax >= 1) J[1] = (z * rho + eta * eta * L) * 0.5;
+  double rp = rho;
+  static_for<2, pmax + 1>([&]<int P>() {
+    constexpr double inv = kFaceInv[P + 1];
+    rp *= rho;
+    J[P] = (z * rp + P * eta * eta * J[P - 2]) * inv;
+  });
   double s = 0.0;
-  if (!antigrad) {
-    face_line_integrals(eta, z, rho, L, kp.deg, J);
-    for (int p = 0; p <= kp.deg; ++p) s += kp.c[p] * J[p];
-    return s;
-  }
-  face_line_integrals(eta, z, rho, L, max(kp.tdeg - 2, 0), J);
-  for (int p = 0; p <= kp.tdeg; ++p) {
-    if (p == 0) s += kp.t[0] * A;
-    else if (p == 1) s += kp.t[1] * eta * L;
-    else s += kp.t[p] * eta * J[p - 2];
+  if constexpr (!Anti) {
+    static_for<0, kp.deg + 1>([&]<int P>() {
+      constexpr double c = kp.c[P];
+      if constexpr (c != 0.0) s += c * J[P];
+    });
+  } else {
+    const double A = atan2(z, eta);
+    static_for<0, kp.tdeg + 1>([&]<int P>() {
+      constexpr double t = kp.t[P];
+      if constexpr (t != 0.0) {
+        if constexpr (P == 0) s += t * A;
+        else if constexpr (P == 1) s += t * eta * L;
+        else s += t * eta * J[P - 2];
+      }
+    });
   }
   return s;
 }
 
-template<int K>
-__device__ __forceinline__ double face_unit_segment(bool antigrad, double eta,
-                                                    double zmin, double zmax) {
-  const FacePieces& P = c_face_pieces[K];
+template<int K, bool Anti>
+__device__ __forceinline__ double face_unit_segment(double eta, double zmin,
+                                                    double zmax) {
   double total = 0.0;
-  for (int i = 0; i < P.n; ++i) {
-    const FacePiece& kp = P.p[i];
-    if (eta >= kp.cutoff) continue;
-    const double zc = sqrt(kp.cutoff * kp.cutoff - eta * eta);
+  static_for<0, kFacePieces[K].n>([&]<int I>() {
+    constexpr double cutoff = kFacePieces[K].p[I].cutoff;
+    if (eta >= cutoff) return;
+    const double zc = sqrt(cutoff * cutoff - eta * eta);
     const double lo = fmax(zmin, -zc), hi = fmin(zmax, zc);
-    if (lo >= hi) continue;
-    total += face_primitive(kp, antigrad, eta, hi) -
-             face_primitive(kp, antigrad, eta, lo);
-  }
+    if (lo >= hi) return;
+    total += face_primitive<K, I, Anti>(eta, hi) - face_primitive<K, I, Anti>(eta, lo);
+  });
   return total;
 }
 
@@ -188,7 +216,7 @@ __device__ __forceinline__ void face_flux(const double* ab, const double* x,
                                           double h, double wd, double* out) {
   const double hinv = 1.0 / h;
   const FaceFrame F = face_frame(ab, x, hinv);
-  const double s = wd * hinv * face_unit_segment<K>(false, fabs(F.d), F.za, F.zb);
+  const double s = wd * hinv * face_unit_segment<K, false>(fabs(F.d), F.za, F.zb);
   out[0] = F.n[0] * s;
   out[1] = F.n[1] * s;
 }
@@ -199,7 +227,7 @@ __device__ __forceinline__ double face_antigrad_flux(const double* ab,
                                                      const double* x, double h,
                                                      double wd) {
   const FaceFrame F = face_frame(ab, x, 1.0 / h);
-  return copysign(wd, F.d) * face_unit_segment<K>(true, fabs(F.d), F.za, F.zb);
+  return copysign(wd, F.d) * face_unit_segment<K, true>(fabs(F.d), F.za, F.zb);
 }
 
 // Segment::intersects(BSphere) (geom/segment.hpp:108-112).
@@ -253,8 +281,8 @@ struct FaceTail3 {
 };
 
 // 3D tail moments cutoff^3 Q(cutoff) - q^3 Q(q), Q(q) = sum_p c_p q^p/(p+3),
-// of the pieces of c_face_pieces, in the same order.
-static __constant__ FaceTail3 c_face_tail3[6][3] = {
+// of the pieces of kFacePieces, in the same order (compile time only).
+inline constexpr FaceTail3 kFaceTail3[6][3] = {
   // cubic spline
   {{6, {4.0 / 15.0, 0.0, 0.0, -2.0 / 3.0, 3.0 / 4.0, -3.0 / 10.0, 1.0 / 24.0}},
    {6, {-1.0 / 60.0, 0.0, 0.0, 1.0 / 3.0, -3.0 / 4.0, 3.0 / 5.0, -1.0 / 6.0}}},
@@ -274,26 +302,58 @@ static __constant__ FaceTail3 c_face_tail3[6][3] = {
   {{14, {128.0 / 1365.0, 0.0, 0.0, -1.0 / 3.0, 0.0, 11.0 / 20.0, 0.0, -33.0 / 56.0, 0.0, 77.0 / 96.0, -33.0 / 40.0, 105.0 / 256.0, -11.0 / 96.0, 231.0 / 13312.0, -1.0 / 896.0}}},
 };
 
-// Integer power by squaring in the order of core/math.hpp:92-104:
-// a^p = a (a^2)^(p/2) for odd p, (a^2)^(p/2) for even p.
-__device__ __forceinline__ double face_ipow(double a, int p) {
-  if (p == 0) return 1.0;
-  double odd[5];
-  int n = 0;
-  while (p > 1) {
-    if (p & 1) odd[n++] = a;
-    a = a * a;
-    p >>= 1;
+// Per support piece and wall distance eta, the parts of the edge and sector
+// values that do not depend on z: with a_p = c_p/(p + 2) and, for the
+// antigradient, b_p = s_p/(p - 1),
+//   flux:     lead = -sum_p a_p eta^{p+2},
+//             sector = sum_p a_p cutoff^{p+2} + lead
+//   antigrad: lead = s_0 - sum_{p>=3} b_p eta^p,
+//             sector = lead + eta (sum_{p>=3} b_p cutoff^{p-1} - s_0/cutoff)
+// so that the line primitive is sum_p a_p K_{p+2} + lead K_0 (flux) or
+// lead K_0 + eta sum_{p>=3} b_p K_{p-1} (antigradient).
+struct EdgeCoef {
+  double lead, sector;
+};
+template<int K, int I, bool Anti>
+__device__ __forceinline__ EdgeCoef face_edge_coef(double eta) {
+  constexpr FacePiece kp = kFacePieces[K].p[I];
+  constexpr FaceTail3 tp = kFaceTail3[K][I];
+  EdgeCoef e{0.0, 0.0};
+  double cut = 0.0;
+  if constexpr (!Anti) {
+    double ep = eta * eta;
+    static_for<0, kp.deg + 1>([&]<int P>() {
+      constexpr double a = kp.c[P] * kFaceInv[P + 2];
+      constexpr double ac = a * constexpr_pow(kp.cutoff, P + 2);
+      e.lead -= a * ep;
+      cut += ac;
+      ep *= eta;
+    });
+    e.sector = cut + e.lead;
+  } else {
+    double ep = eta * eta * eta;
+    e.lead = tp.s[0];
+    static_for<3, tp.deg + 1>([&]<int P>() {
+      constexpr double b = tp.s[P] * kFaceInv[P - 1];
+      constexpr double bc = b * constexpr_pow(kp.cutoff, P - 1);
+      e.lead -= b * ep;
+      cut += bc;
+      ep *= eta;
+    });
+    constexpr double s0c = tp.s[0] / kp.cutoff;
+    e.sector = e.lead + eta * (cut - s0c);
   }
-  for (int i = n - 1; i >= 0; --i) a = odd[i] * a;
-  return a;
+  return e;
 }
 
-__device__ __forceinline__ double face_edge_primitive(const FacePiece& kp,
-                                                      const FaceTail3& tp,
-                                                      bool antigrad, double eta,
-                                                      double delta, double beta2,
-                                                      double beta, double z) {
+template<int K, int I, bool Anti>
+__device__ __forceinline__ double face_edge_primitive(const EdgeCoef& ec,
+                                                      double eta, double delta,
+                                                      double beta2, double beta,
+                                                      double z) {
+  constexpr FacePiece kp = kFacePieces[K].p[I];
+  constexpr FaceTail3 tp = kFaceTail3[K][I];
+  constexpr int kmax = Anti ? (tp.deg - 1 > 1 ? tp.deg - 1 : 1) : kp.deg + 2;
   const double rho = sqrt(z * z + beta2);
   const double A = fabs(delta) <= kTiny
                        ? 0.0
@@ -301,104 +361,89 @@ __device__ __forceinline__ double face_edge_primitive(const FacePiece& kp,
   const double L = fabs(beta) <= kTiny
                        ? 0.0
                        : copysign(log1p((fabs(z) + z * z / (rho + beta)) / beta), z);
-  const int kmax = antigrad ? max(tp.deg - 1, 1) : kp.deg + 2;
-  double J[16], Kk[16];
+  double J[kmax + 1], Kk[kmax + 1];
   J[0] = z;
-  J[1] = (z * rho + beta2 * L) / 2.0;
+  J[1] = (z * rho + beta2 * L) * 0.5;
   double rp = rho;
-  for (int k = 2; k <= kmax; ++k) {
+  static_for<2, kmax + 1>([&]<int P>() {
+    constexpr double inv = kFaceInv[P + 1];
     rp *= rho;
-    J[k] = (z * rp + k * beta2 * J[k - 2]) / (k + 1);
-  }
+    J[P] = (z * rp + P * beta2 * J[P - 2]) * inv;
+  });
   Kk[0] = A;
   Kk[1] = delta * L;
-  for (int k = 2; k <= kmax; ++k) Kk[k] = delta * J[k - 2] + eta * eta * Kk[k - 2];
+  const double eta2 = eta * eta;
+  static_for<2, kmax + 1>([&]<int P>() { Kk[P] = delta * J[P - 2] + eta2 * Kk[P - 2]; });
   double s = 0.0;
-  if (!antigrad) {
-    double c0 = 0.0;
-    for (int p = 0; p <= kp.deg; ++p) {
-      if (kp.c[p] == 0.0) continue;
-      s += kp.c[p] / (p + 2) * Kk[p + 2];
-      c0 -= kp.c[p] * face_ipow(eta, p + 2) / (p + 2);
-    }
-    return s + c0 * Kk[0];
+  if constexpr (!Anti) {
+    static_for<0, kp.deg + 1>([&]<int P>() {
+      constexpr double a = kp.c[P] * kFaceInv[P + 2];
+      if constexpr (a != 0.0) s += a * Kk[P + 2];
+    });
+    return s + ec.lead * Kk[0];
+  } else {
+    static_for<3, tp.deg + 1>([&]<int P>() {
+      constexpr double b = tp.s[P] * kFaceInv[P - 1];
+      if constexpr (b != 0.0) s += b * Kk[P - 1];
+    });
+    return ec.lead * Kk[0] + eta * s;
   }
-  for (int p = 0; p <= tp.deg; ++p) {
-    if (tp.s[p] == 0.0) continue;
-    if (p == 0) s += tp.s[0] * Kk[0];
-    else s += tp.s[p] * (eta * Kk[p - 1] - face_ipow(eta, p) * Kk[0]) / (p - 1);
-  }
-  return s;
 }
 
-__device__ __forceinline__ double face_sector(const FacePiece& kp,
-                                              const FaceTail3& tp,
-                                              bool antigrad, double eta) {
-  double s = 0.0;
-  if (!antigrad) {
-    for (int p = 0; p <= kp.deg; ++p) {
-      if (kp.c[p] == 0.0) continue;
-      s += kp.c[p] * (face_ipow(kp.cutoff, p + 2) - face_ipow(eta, p + 2)) / (p + 2);
-    }
-    return s;
-  }
-  for (int p = 0; p <= tp.deg; ++p) {
-    if (tp.s[p] == 0.0) continue;
-    if (p == 0) s += tp.s[0] * (1.0 - eta / kp.cutoff);
-    else s += tp.s[p] * (eta * face_ipow(kp.cutoff, p - 1) - face_ipow(eta, p)) / (p - 1);
-  }
-  return s;
-}
-
-// unit_triangle_integral (kernel.hpp:316-399) summed over the pieces; v =
-// the three projected vertices (2 doubles each).
-template<int K>
-__device__ __noinline__ double face_unit_triangle(bool antigrad, double eta,
-                                                  const double* v) {
-  const FacePieces& P = c_face_pieces[K];
+// unit_triangle_integral (kernel.hpp:316-399) of piece I; v = the three
+// projected vertices (2 doubles each).
+template<int K, int I, bool Anti>
+__device__ __forceinline__ double face_triangle_piece(double eta, const double* v) {
+  constexpr double cutoff = kFacePieces[K].p[I].cutoff;
+  if (eta >= cutoff) return 0.0;
+  const double radius2 = cutoff * cutoff - eta * eta;
+  const EdgeCoef ec = face_edge_coef<K, I, Anti>(eta);
   double total = 0.0;
-  for (int i = 0; i < P.n; ++i) {
-    const FacePiece& kp = P.p[i];
-    const FaceTail3& tp = c_face_tail3[K][i];
-    if (eta >= kp.cutoff) continue;
-    const double radius2 = kp.cutoff * kp.cutoff - eta * eta;
-    const double sector = face_sector(kp, tp, antigrad, eta);
-    for (int e = 0; e < 3; ++e) {
-      const double* p0 = v + 2 * e;
-      const double* p1 = v + 2 * (e == 2 ? 0 : e + 1);
-      const double ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
-      const double len2 = ed[0] * ed[0] + ed[1] * ed[1];
-      if (len2 <= kTiny * kTiny) continue;
-      const double len = sqrt(len2);
-      const double t[2] = {ed[0] / len, ed[1] / len};
-      const double delta = p0[0] * t[1] - p0[1] * t[0];
-      const double delta2 = delta * delta;
-      const double beta2 = eta * eta + delta2;
-      const double beta = sqrt(beta2);
-      const double z0 = p0[0] * t[0] + p0[1] * t[1];
-      const double z1 = z0 + len;
-      double zs[4];
-      int nz = 0;
-      zs[nz++] = z0;
-      if (radius2 > delta2) {
-        const double zc = sqrt(radius2 - delta2);
-        if (z0 < -zc && -zc < z1) zs[nz++] = -zc;
-        if (z0 < zc && zc < z1) zs[nz++] = zc;
-      }
-      zs[nz++] = z1;
-      for (int j = 0; j + 1 < nz; ++j) {
-        const double lo = zs[j], hi = zs[j + 1];
-        if (fabs(hi - lo) <= kTiny) continue;
-        const double mid = (lo + hi) / 2.0;
-        if (mid * mid + delta2 < radius2) {
-          total += face_edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, hi) -
-                   face_edge_primitive(kp, tp, antigrad, eta, delta, beta2, beta, lo);
-        } else {
-          total += sector * atan2(delta * (hi - lo), lo * hi + delta2);
-        }
+  for (int e = 0; e < 3; ++e) {
+    const double* p0 = v + 2 * e;
+    const double* p1 = v + 2 * (e == 2 ? 0 : e + 1);
+    const double ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
+    const double len2 = ed[0] * ed[0] + ed[1] * ed[1];
+    if (len2 <= kTiny * kTiny) continue;
+    const double len = sqrt(len2);
+    const double t[2] = {ed[0] / len, ed[1] / len};
+    const double delta = p0[0] * t[1] - p0[1] * t[0];
+    const double delta2 = delta * delta;
+    const double beta2 = eta * eta + delta2;
+    const double beta = sqrt(beta2);
+    const double z0 = p0[0] * t[0] + p0[1] * t[1];
+    const double z1 = z0 + len;
+    double zs[4];
+    int nz = 0;
+    zs[nz++] = z0;
+    if (radius2 > delta2) {
+      const double zc = sqrt(radius2 - delta2);
+      if (z0 < -zc && -zc < z1) zs[nz++] = -zc;
+      if (z0 < zc && zc < z1) zs[nz++] = zc;
+    }
+    zs[nz++] = z1;
+    for (int j = 0; j + 1 < nz; ++j) {
+      const double lo = zs[j], hi = zs[j + 1];
+      if (fabs(hi - lo) <= kTiny) continue;
+      const double mid = (lo + hi) * 0.5;
+      if (mid * mid + delta2 < radius2) {
+        total += face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, hi) -
+                 face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, lo);
+      } else {
+        total += ec.sector * atan2(delta * (hi - lo), lo * hi + delta2);
       }
     }
   }
+  return total;
+}
+
+// The triangle integral summed over the kernel's pieces.
+template<int K, bool Anti>
+__device__ __noinline__ double face_unit_triangle(double eta, const double* v) {
+  double total = 0.0;
+  static_for<0, kFacePieces[K].n>([&]<int I>() {
+    total += face_triangle_piece<K, I, Anti>(eta, v);
+  });
   return total;
 }
 
@@ -472,7 +517,7 @@ __device__ __forceinline__ void face_flux_d(const double* g, const double* x,
   } else {
     const double hinv = 1.0 / h;
     const TriFrame F = tri_frame(g, x, hinv);
-    const double s = wd * hinv * face_unit_triangle<K>(false, fabs(F.d), F.p);
+    const double s = wd * hinv * face_unit_triangle<K, false>(fabs(F.d), F.p);
     out[0] = F.n[0] * s;
     out[1] = F.n[1] * s;
     out[2] = F.n[2] * s;
@@ -488,7 +533,7 @@ __device__ __forceinline__ double face_antigrad_flux_d(const double* g,
     return face_antigrad_flux<K>(g, x, h, wd);
   } else {
     const TriFrame F = tri_frame(g, x, 1.0 / h);
-    return copysign(wd, F.d) * face_unit_triangle<K>(true, fabs(F.d), F.p);
+    return copysign(wd, F.d) * face_unit_triangle<K, true>(fabs(F.d), F.p);
   }
 }
 
@@ -591,15 +636,17 @@ __device__ __forceinline__ bool triangle_in_sphere(const double* t,
   return dot_d<3>(d, d) <= radius * radius;
 }
 
-// Faces within the support radius of x, in ascending face order (the
-// particle's cell list holds every face within reach of the cell).
+// Faces within the support radius of x (the particle's cell list holds
+// every face within reach of the cell); lane l of a warp takes list entries
+// l, l + 32, ... so that the warp shares one particle's faces.
 template<int D, class Fn>
 __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
                                                    uint32_t gcell,
                                                    const double* x,
-                                                   double radius, Fn&& fn) {
+                                                   double radius, int lane,
+                                                   Fn&& fn) {
   const uint32_t s = fc.cell_start[gcell], e = fc.cell_start[gcell + 1];
-  for (uint32_t i = s; i < e; ++i) {
+  for (uint32_t i = s + lane; i < e; i += 32) {
     const uint32_t f = fc.cell_face[i];
     const double* g = fc.coords + D * D * static_cast<size_t>(f);
     bool in;
@@ -609,17 +656,27 @@ __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
   }
 }
 
+// Sum over the lanes of a warp (all lanes active), butterfly order.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // 3D containment: the particle's cell answers unless the containment
 // surface reaches it; there the exact winding number of the surface
 // (Triangle::winding_number, geom/triangle.hpp: per triangle
 // atan2(det(a', b', c'), |a'||b'||c'| + (a'.b')|c'| + (b'.c')|a'| +
 // (c'.a')|b'|) / (2 pi), primes = vertex - x) decides, > 1/2.
+// With lanes = 32 the warp splits the triangles (lane l takes l, l + 32,
+// ...) and every lane gets the answer; with lanes = 1 one thread sums them.
 __device__ __forceinline__ bool face_contains3(const FaceArgs& fc, uint32_t tank,
-                                               uint32_t gcell, const double* x) {
+                                               uint32_t gcell, const double* x,
+                                               int lane, int lanes) {
   const int st = fc.cell_state[gcell];
   if (st >= 0) return st != 0;
   double w = 0.0;
-  for (uint32_t i = fc.cont_start[tank]; i < fc.cont_start[tank + 1]; ++i) {
+  for (uint32_t i = fc.cont_start[tank] + lane; i < fc.cont_start[tank + 1]; i += lanes) {
     const double* t = fc.cont_tri + 9 * static_cast<size_t>(i);
     const double ap[3] = {t[0] - x[0], t[1] - x[1], t[2] - x[2]};
     const double bp[3] = {t[3] - x[0], t[4] - x[1], t[5] - x[2]};
@@ -633,6 +690,7 @@ __device__ __forceinline__ bool face_contains3(const FaceArgs& fc, uint32_t tank
     face_cross(bp, cp, bc);
     w += atan2(dot_d<3>(ap, bc), den) / (2.0 * 3.141592653589793);
   }
+  if (lanes == 32) w = warp_sum(w);
   return w > 0.5;
 }
 

@@ -1158,13 +1158,18 @@ __device__ __forceinline__ double face_avg(const double* x) {
   else return (x[0] + x[1] + x[2]) / 3.0;
 }
 
+// Face terms of continuity and momentum (fluid_equations.hpp:241-247,
+// 278-291) of the face particles, one warp per particle with the lanes
+// splitting its faces; k_gamma_init zeroed the other particles' terms.
 template<int D, int K, int F>
 __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
-  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= A.n) return;
   const FaceArgs& fc = A.fc;
-  double drho = 0.0, dv[3] = {0.0, 0.0, 0.0};
-  if (!(A.Y.id[i] & kWallBit)) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  const uint32_t count = *fc.face_count;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += nwarps) {
+    const uint32_t i = fc.face_list[w];
+    if (A.Y.id[i] & kWallBit) continue;
     const uint32_t key = A.skey[i];
     const TankDev& T = A.tanks[tank_of_key(key, A.tank_off, A.ntanks)];
     int c[3] = {0, 0, 0};
@@ -1176,8 +1181,9 @@ __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
     const double radius = KernelPoly<K>::unit_radius * T.h;
     const double gam = fc.gamma[i];
     double va[3], rho_a, P_a;
-    target_fields(load_dat(A.datrec, static_cast<uint32_t>(i)), T, va, rho_a, P_a);
-    for_adjacent_faces<D>(fc, gcell, pa, radius, [&](uint32_t f, const double* g) {
+    target_fields(load_dat(A.datrec, i), T, va, rho_a, P_a);
+    double drho = 0.0, dv[3] = {0.0, 0.0, 0.0};
+    for_adjacent_faces<D>(fc, gcell, pa, radius, lane, [&](uint32_t f, const double* g) {
       double gg[3];
       face_flux_d<K, D>(g, pa, T.h, fc.weight, gg);
       double rv[3], pv[3];
@@ -1212,10 +1218,15 @@ __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
 #pragma unroll
       for (int k = 0; k < D; ++k) dv[k] += (P_as * gg[k] - Pi_s * t_as[k] * ng) / gam;
     });
-  }
-  fc.face_drho[i] = drho;
+    drho = warp_sum(drho);
 #pragma unroll
-  for (int k = 0; k < D; ++k) fc.face_dv[D * i + k] = dv[k];
+    for (int k = 0; k < D; ++k) dv[k] = warp_sum(dv[k]);
+    if (lane == 0) {
+      fc.face_drho[i] = drho;
+#pragma unroll
+      for (int k = 0; k < D; ++k) fc.face_dv[D * i + k] = dv[k];
+    }
+  }
 }
 
 // The force pass's share: pair sums over gamma, plus the stored face terms
@@ -1711,51 +1722,107 @@ __global__ void __launch_bounds__(128) k_sumdens(CloudArgs<D> A) {
 
 // ---------------------------------------------------------------------------
 // gamma and grad gamma of every particle (FluidEquations::compute_gamma,
-// fluid_equations.hpp:166-193); also records the cell-order slot of each
-// fixed particle for the face terms' vertex lookups.
-template<int D, int K, int F>
-__global__ void __launch_bounds__(128) k_gamma(StageArgs<D, F> A) {
+// fluid_equations.hpp:166-193) in two passes.  k_gamma_init, per particle:
+// records the cell-order slot of each fixed particle (for the face terms'
+// vertex lookups) and lists the face particles, those whose cell lists
+// faces; the others have grad gamma = 0, gamma = the containment answer,
+// and zero face terms.  k_gamma_faces, one warp per face particle with the
+// lanes splitting its faces: grad gamma = the sum of kernel fluxes, then
+// gamma = contains - the sum of antigradient fluxes at r + (2 contains - 1)
+// n h^2.  A fixed particle's gamma is never read (its grad gamma gives the
+// wall normal), so it is set to 1 without the containment and antigradient
+// sums.
+template<int D, int F>
+__global__ void __launch_bounds__(128) k_gamma_init(StageArgs<D, F> A) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   const FaceArgs& fc = A.fc;
   const uint32_t id = A.Y.id[i];
-  if (id & kWallBit) fc.slot_of[id & kIdMask] = static_cast<uint32_t>(i);
+  const bool wall = (id & kWallBit) != 0;
+  if (wall) fc.slot_of[id & kIdMask] = static_cast<uint32_t>(i);
   const uint32_t key = A.skey[i];
   const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
   const TankDev& T = A.tanks[tk];
   int c[3] = {0, 0, 0};
   cell_from_key<D>(T, key, c);
   const uint32_t gcell = global_cell<D>(T, c);
-  double x[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-  for (int k = 0; k < D; ++k) x[k] = A.Y.pos[k][i];
-  const double radius = KernelPoly<K>::unit_radius * T.h;
-  const double wd = fc.weight;
-  double g[3] = {0.0, 0.0, 0.0};
-  for_adjacent_faces<D>(fc, gcell, x, radius, [&](uint32_t, const double* f) {
-    double fl[3];
-    face_flux_d<K, D>(f, x, T.h, wd, fl);
-#pragma unroll
-    for (int k = 0; k < D; ++k) g[k] += fl[k];
-  });
-  bool inside;
-  if constexpr (D == 2) inside = face_contains(fc, tk, fc.row_off[tk] + c[1], x);
-  else inside = fc.tank_edges[tk] == 0 || face_contains3(fc, tk, gcell, x);
-  double ga = inside ? 1.0 : 0.0;
-  const double ng = sqrt(dot_d<D>(g, g));
-  if (!(ng <= kTiny)) {
-    const double s = 2.0 * ga - 1.0;
-    const double h2 = T.h * T.h;
-    double xs[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-    for (int k = 0; k < D; ++k) xs[k] = x[k] + s * (g[k] / ng) * h2;
-    for_adjacent_faces<D>(fc, gcell, x, radius, [&](uint32_t, const double* f) {
-      ga -= face_antigrad_flux_d<K, D>(f, xs, T.h, wd);
-    });
+  if (fc.cell_start[gcell + 1] > fc.cell_start[gcell]) {
+    fc.face_list[atomicAdd(fc.face_count, 1u)] = static_cast<uint32_t>(i);
+    return;
   }
-  fc.gamma[i] = ga;
+  bool inside = true;
+  if (!wall) {
+    double x[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-  for (int k = 0; k < D; ++k) fc.ggam[D * i + k] = g[k];
+    for (int k = 0; k < D; ++k) x[k] = A.Y.pos[k][i];
+    if constexpr (D == 2) inside = face_contains(fc, tk, fc.row_off[tk] + c[1], x);
+    else inside = fc.tank_edges[tk] == 0 || face_contains3(fc, tk, gcell, x, 0, 1);
+  }
+  fc.gamma[i] = inside ? 1.0 : 0.0;
+  fc.face_drho[i] = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    fc.ggam[D * i + k] = 0.0;
+    fc.face_dv[D * i + k] = 0.0;
+  }
+}
+
+template<int D, int K, int F>
+__global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
+  const FaceArgs& fc = A.fc;
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  const uint32_t count = *fc.face_count;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += nwarps) {
+    const uint32_t i = fc.face_list[w];
+    const bool wall = (A.Y.id[i] & kWallBit) != 0;
+    const uint32_t key = A.skey[i];
+    const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
+    const TankDev& T = A.tanks[tk];
+    int c[3] = {0, 0, 0};
+    cell_from_key<D>(T, key, c);
+    const uint32_t gcell = global_cell<D>(T, c);
+    double x[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) x[k] = A.Y.pos[k][i];
+    const double radius = KernelPoly<K>::unit_radius * T.h;
+    const double wd = fc.weight;
+    double g[3] = {0.0, 0.0, 0.0};
+    for_adjacent_faces<D>(fc, gcell, x, radius, lane, [&](uint32_t, const double* f) {
+      double fl[3];
+      face_flux_d<K, D>(f, x, T.h, wd, fl);
+#pragma unroll
+      for (int k = 0; k < D; ++k) g[k] += fl[k];
+    });
+#pragma unroll
+    for (int k = 0; k < D; ++k) g[k] = warp_sum(g[k]);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < D; ++k) fc.ggam[D * i + k] = g[k];
+    }
+    if (wall) {
+      if (lane == 0) fc.gamma[i] = 1.0;
+      continue;
+    }
+    bool inside;
+    if constexpr (D == 2) inside = face_contains(fc, tk, fc.row_off[tk] + c[1], x);
+    else inside = fc.tank_edges[tk] == 0 || face_contains3(fc, tk, gcell, x, lane, 32);
+    double ga = inside ? 1.0 : 0.0;
+    const double ng = sqrt(dot_d<D>(g, g));
+    if (!(ng <= kTiny)) {
+      const double s = 2.0 * ga - 1.0;
+      const double h2 = T.h * T.h;
+      double xs[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+      for (int k = 0; k < D; ++k) xs[k] = x[k] + s * (g[k] / ng) * h2;
+      double ag = 0.0;
+      for_adjacent_faces<D>(fc, gcell, x, radius, lane, [&](uint32_t, const double* f) {
+        ag += face_antigrad_flux_d<K, D>(f, xs, T.h, wd);
+      });
+      ga -= warp_sum(ag);
+    }
+    if (lane == 0) fc.gamma[i] = ga;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -145,65 +145,69 @@ __device__ __forceinline__ bool post_target(const PostArgs<D, F>& A, int64_t& i,
   return true;
 }
 
-// Face terms of the shifting sums of each fluid particle (N, L, grad v,
-// grad rho; fluid_equations.hpp:340-349), divided by gamma_a; k_post_sums
-// starts its pair sums from them.  A pass of its own keeps the face
-// integrals' registers out of the pair loop.
+// Face terms of the shifting sums of the fluid face particles (N, L,
+// grad v, grad rho; fluid_equations.hpp:340-349), divided by gamma_a, one
+// warp per particle with the lanes splitting its faces; k_post_sums starts
+// its pair sums from them (zero for particles whose cell lists no faces).
+// A pass of its own keeps the face integrals' registers out of the pair
+// loop.
 template<int D, int F, int K>
 __global__ void __launch_bounds__(128) k_post_faces(PostArgs<D, F> A) {
-  int64_t i;
-  uint32_t id;
-  const TankDev* Tp;
-  int c[3] = {0, 0, 0};
-  if (!post_target(A, i, id, Tp, c)) return;
-  if (id & kWallBit) return;
-  const TankDev& T = *Tp;
-  double rho_a, va[3];
-  post_neighbour<D>(A.S.datrec, static_cast<uint32_t>(i), T, rho_a, va);
-  double pa[3];
+  const FaceArgs& fc = A.S.fc;
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  const uint32_t count = *fc.face_count;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += nwarps) {
+    const uint32_t i = fc.face_list[w];
+    if (A.S.Y.id[i] & kWallBit) continue;
+    const uint32_t key = A.S.skey[i];
+    const TankDev& T = A.S.tanks[tank_of_key(key, A.S.tank_off, A.S.ntanks)];
+    int c[3] = {0, 0, 0};
+    cell_from_key<D>(T, key, c);
+    double rho_a, va[3];
+    post_neighbour<D>(A.S.datrec, i, T, rho_a, va);
+    double pa[3];
 #pragma unroll
-  for (int k = 0; k < D; ++k) pa[k] = A.S.Y.pos[k][i];
-  double N[D] = {}, L[D * D] = {}, gv[D * D] = {}, gr[D] = {};
-  const double gam = A.S.fc.gamma[i];
-  const double radius = KernelPoly<K>::unit_radius * T.h;
-  for_adjacent_faces<D>(A.S.fc, global_cell<D>(T, c), pa, radius,
-                        [&](uint32_t f, const double* g) {
-    double gg[3], rv[3], r_sa[3];
-    face_flux_d<K, D>(g, pa, T.h, A.S.fc.weight, gg);
+    for (int k = 0; k < D; ++k) pa[k] = A.S.Y.pos[k][i];
+    double sums[kPostFaceSums<D>] = {};
+    double* N = sums;
+    double* L = sums + D;
+    double* gv = sums + D + D * D;
+    double* gr = sums + D + 2 * D * D;
+    const double gam = fc.gamma[i];
+    const double radius = KernelPoly<K>::unit_radius * T.h;
+    for_adjacent_faces<D>(fc, global_cell<D>(T, c), pa, radius, lane,
+                          [&](uint32_t f, const double* g) {
+      double gg[3], rv[3], r_sa[3];
+      face_flux_d<K, D>(g, pa, T.h, fc.weight, gg);
 #pragma unroll
-    for (int j = 0; j < D; ++j) {
-      rv[j] = vertex_rho(A.S.datrec, A.S.fc.slot_of[A.S.fc.vert[D * f + j]], T);
-    }
+      for (int j = 0; j < D; ++j) rv[j] = vertex_rho(A.S.datrec, fc.slot_of[fc.vert[D * f + j]], T);
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-      double xk[3];
+      for (int k = 0; k < D; ++k) {
+        double xk[3];
 #pragma unroll
-      for (int j = 0; j < D; ++j) xk[j] = g[D * j + k];
-      r_sa[k] = face_avg<D>(xk) - pa[k];
-    }
-    // The face vertices' velocities are zero: v_sa = -v_a.
-    const double rho_sa = face_avg<D>(rv) - rho_a;
-#pragma unroll
-    for (int a2 = 0; a2 < D; ++a2) {
-      N[a2] -= gg[a2] / gam;
-#pragma unroll
-      for (int b2 = 0; b2 < D; ++b2) {
-        L[a2 * D + b2] -= r_sa[a2] * gg[b2] / gam;
-        gv[a2 * D + b2] -= -va[a2] * gg[b2] / gam;
+        for (int j = 0; j < D; ++j) xk[j] = g[D * j + k];
+        r_sa[k] = face_avg<D>(xk) - pa[k];
       }
-      gr[a2] -= rho_sa * gg[a2] / gam;
+      // The face vertices' velocities are zero: v_sa = -v_a.
+      const double rho_sa = face_avg<D>(rv) - rho_a;
+#pragma unroll
+      for (int a2 = 0; a2 < D; ++a2) {
+        N[a2] -= gg[a2] / gam;
+#pragma unroll
+        for (int b2 = 0; b2 < D; ++b2) {
+          L[a2 * D + b2] -= r_sa[a2] * gg[b2] / gam;
+          gv[a2 * D + b2] -= -va[a2] * gg[b2] / gam;
+        }
+        gr[a2] -= rho_sa * gg[a2] / gam;
+      }
+    });
+    double* out = fc.post_face + kPostFaceSums<D> * static_cast<size_t>(i);
+#pragma unroll
+    for (int k = 0; k < kPostFaceSums<D>; ++k) {
+      const double v = warp_sum(sums[k]);
+      if (lane == 0) out[k] = v;
     }
-  });
-  double* out = A.S.fc.post_face + kPostFaceSums<D> * static_cast<size_t>(i);
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    out[k] = N[k];
-    out[D + 2 * D * D + k] = gr[k];
-  }
-#pragma unroll
-  for (int k = 0; k < D * D; ++k) {
-    out[D + k] = L[k];
-    out[D + D * D + k] = gv[k];
   }
 }
 
@@ -233,8 +237,9 @@ __global__ void __launch_bounds__(128) k_post_sums(PostArgs<D, F> A) {
   // Face boundaries (fluid_equations.hpp:335-349): the face terms come
   // first (k_post_faces), and every sum is divided by gamma_a.
   double gam = 1.0;
-  if (A.S.fc.on) {
-    gam = A.S.fc.gamma[i];
+  const uint32_t gcell = A.S.fc.on ? global_cell<D>(T, c) : 0u;
+  if (A.S.fc.on) gam = A.S.fc.gamma[i];
+  if (A.S.fc.on && A.S.fc.cell_start[gcell + 1] > A.S.fc.cell_start[gcell]) {
     const double* f0 = A.S.fc.post_face + kPostFaceSums<D> * static_cast<size_t>(i);
 #pragma unroll
     for (int k = 0; k < D; ++k) {
