@@ -329,10 +329,8 @@ def run_gpu(args, ranks) -> dict | None:
     def e2e_step():
         ctx32.update(pin["r"].array, pin["v"].array, pin["rho"].array, pin["dv"].array)
         ctx32.step(1)
-        ctx32.download(_abi.TG_FIELD_R, pin["r"].array)
-        ctx32.download(_abi.TG_FIELD_V, pin["v"].array)
-        ctx32.download(_abi.TG_FIELD_RHO, pin["rho"].array)
-        ctx32.download(_abi.TG_FIELD_DV_DT, pin["dv"].array)
+        ctx32.download_state(r=pin["r"].array, v=pin["v"].array, rho=pin["rho"].array,
+                             dv_dt=pin["dv"].array)
 
     for _ in range(2):
         e2e_step()

@@ -209,6 +209,14 @@ int tg_time(tg_context* ctx, double* time_out);
 /* Copy a field into out, in upload order. */
 int tg_particles_download(tg_context* ctx, int32_t field, double* out);
 
+/* Copy the state fields r, v (n x dim), rho, drho/dt (n) and dv/dt
+ * (n x dim) in upload order, each skipped when NULL: one pass over the
+ * device state, the copies issued back to back, one wait.  Replaces the
+ * per-field reads of ParticleArray after a step (particle_array.hpp:165-172,
+ * field.hpp:172-218) in a host loop that reads the whole state. */
+int tg_particles_download_state(tg_context* ctx, double* r, double* v,
+                                double* rho, double* drho_dt, double* dv_dt);
+
 /* Neighbour count and order-independent hash (sum of splitmix64(id + 1))
  * of every particle's neighbour set at the current positions: all particles
  * of its tank within 2h, inclusive, self included.  In upload order. */

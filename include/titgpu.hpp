@@ -860,31 +860,23 @@ public:
     storage.write_frame_async(series.id(), time, std::move(arrays));
   }
 
-  /// Bring the host copy up to date (downloads after GPU steps).
+  /// Bring the host copy up to date (one state download after GPU steps).
   void sync() const {
     if (state_ != State::device_ahead) return;
-    std::vector<double> buf(size() * Dim);
-    const auto get = [&](std::int32_t field, auto& dst) {
-      using T = typename std::decay_t<decltype(dst)>::value_type;
-      const std::size_t width = std::is_same_v<T, Real> ? 1 : Dim;
-      buf.resize(size() * width);
-      gpu_detail::ensure(tg_particles_download(ctx_, field, buf.data()), ctx_,
-                         "tg_particles_download");
-      for (std::size_t i = 0; i < size(); ++i) {
-        if constexpr (std::is_same_v<T, Real>) {
-          dst[i] = static_cast<Real>(buf[i]);
-        } else {
-          for (std::size_t d = 0; d < Dim; ++d) {
-            dst[i][d] = static_cast<Real>(buf[i * Dim + d]);
-          }
-        }
+    const std::size_t n = size();
+    std::vector<double> r(n * Dim), v(n * Dim), dv(n * Dim), rho(n), drho(n);
+    gpu_detail::ensure(tg_particles_download_state(ctx_, r.data(), v.data(), rho.data(),
+                                                   drho.data(), dv.data()),
+                       ctx_, "tg_particles_download_state");
+    for (std::size_t i = 0; i < n; ++i) {
+      for (std::size_t d = 0; d < Dim; ++d) {
+        r_[i][d] = static_cast<Real>(r[i * Dim + d]);
+        v_[i][d] = static_cast<Real>(v[i * Dim + d]);
+        dv_dt_[i][d] = static_cast<Real>(dv[i * Dim + d]);
       }
-    };
-    get(TG_FIELD_R, r_);
-    get(TG_FIELD_V, v_);
-    get(TG_FIELD_DV_DT, dv_dt_);
-    get(TG_FIELD_RHO, rho_);
-    get(TG_FIELD_DRHO_DT, drho_dt_);
+      rho_[i] = static_cast<Real>(rho[i]);
+      drho_dt_[i] = static_cast<Real>(drho[i]);
+    }
     state_ = State::synced;
   }
 

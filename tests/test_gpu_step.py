@@ -130,6 +130,28 @@ def test_graph_and_direct_launches_bit_identical(gpu_lib):
         np.testing.assert_array_equal(out[0][k], out[2][k])
 
 
+@pytest.mark.parametrize("dim,precision", ((2, _abi.TG_FP64), (2, _abi.TG_FP32C),
+                                           (3, _abi.TG_FP32C)))
+def test_download_state_matches_field_downloads(gpu_lib, dim, precision):
+    scn = scenarios.dam_break_2d(nx_per_H=20) if dim == 2 else scenarios.dam_break_3d(nx_per_H=8)
+    P = physics.baseline_params(dim, precision=precision)
+    with gpu_context(scn, P) as ctx:
+        ctx.step(3)
+        n = scn["r"].shape[0]
+        r, v, dv = (np.full((n, dim), np.nan) for _ in range(3))
+        rho, drho = np.full(n, np.nan), np.full(n, np.nan)
+        ctx.download_state(r=r, v=v, rho=rho, drho_dt=drho, dv_dt=dv)
+        g = gpu_state(ctx)
+        only_r = np.full((n, dim), np.nan)
+        ctx.download_state(r=only_r)
+    np.testing.assert_array_equal(r, g["r"])
+    np.testing.assert_array_equal(v, g["v"])
+    np.testing.assert_array_equal(rho, g["rho"])
+    np.testing.assert_array_equal(drho, g["drho_dt"])
+    np.testing.assert_array_equal(dv, g["dv_dt"])
+    np.testing.assert_array_equal(only_r, g["r"])
+
+
 def test_update_round_trip_continues_the_run(gpu_lib):
     scn = scenarios.dam_break_2d(nx_per_H=20)
     P = physics.baseline_params(2)

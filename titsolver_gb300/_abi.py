@@ -121,6 +121,7 @@ SIGNATURES = [
     ("tg_step", ctypes.c_int, [_P, ctypes.c_int32, _D]),
     ("tg_time", ctypes.c_int, [_P, _D]),
     ("tg_particles_download", ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    ("tg_particles_download_state", ctypes.c_int, [_P, _D, _D, _D, _D, _D]),
     ("tg_neighbour_counts", ctypes.c_int, [_P, _I32, _U64]),
     ("tg_neighbour_lists", ctypes.c_int, [_P, _I64, _I32, ctypes.c_int64]),
     ("tg_summation_density", ctypes.c_int, [_P, ctypes.c_int32, _D, _I32, _U64]),
@@ -289,6 +290,15 @@ class Context:
                                                    _ptr(out, ctypes.c_double)),
                     "tg_particles_download")
         return out
+
+    def download_state(self, r=None, v=None, rho=None, drho_dt=None, dv_dt=None):
+        """tg_particles_download_state into the given arrays (None: skipped)."""
+        for a in (r, v, rho, drho_dt, dv_dt):
+            assert a is None or (a.dtype == np.float64 and a.flags.c_contiguous)
+        self._check(self.lib.tg_particles_download_state(
+            self.handle, _ptr(r, ctypes.c_double), _ptr(v, ctypes.c_double),
+            _ptr(rho, ctypes.c_double), _ptr(drho_dt, ctypes.c_double),
+            _ptr(dv_dt, ctypes.c_double)), "tg_particles_download_state")
 
     def neighbour_counts(self):
         c = np.zeros(self.n, dtype=np.int32)

@@ -682,6 +682,38 @@ int tg_particles_download(tg_context* ctx, int32_t field, double* out) {
   return TG_OK;
 }
 
+int tg_particles_download_state(tg_context* ctx, double* r, double* v,
+                                double* rho, double* drho_dt, double* dv_dt) {
+  if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
+  Context& C = ctx->c;
+  if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
+  if (C.n == 0) return TG_OK;
+  if (rho != nullptr && !C.walls_fresh && C.n_wall > 0) {
+    TG_CUDA(&C, C.engine->enqueue_prepare(C));
+    C.walls_fresh = true;
+  }
+  const size_t n = static_cast<size_t>(C.n), dim = static_cast<size_t>(C.P.dim);
+  double* d_rho = C.d_stage3;
+  double* d_drho = C.d_stage3 + n;
+  TG_CUDA(&C, C.engine->enqueue_pack_state(C, r ? C.d_stage : nullptr,
+                                           v ? C.d_stage2 : nullptr,
+                                           rho ? d_rho : nullptr,
+                                           drho_dt ? d_drho : nullptr,
+                                           dv_dt ? C.d_stage4 : nullptr));
+  const auto get = [&](double* dst, const double* src, size_t count) -> cudaError_t {
+    if (dst == nullptr) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                           C.stream);
+  };
+  TG_CUDA(&C, get(r, C.d_stage, n * dim));
+  TG_CUDA(&C, get(v, C.d_stage2, n * dim));
+  TG_CUDA(&C, get(rho, d_rho, n));
+  TG_CUDA(&C, get(drho_dt, d_drho, n));
+  TG_CUDA(&C, get(dv_dt, C.d_stage4, n * dim));
+  TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  return TG_OK;
+}
+
 int tg_neighbour_counts(tg_context* ctx, int32_t* counts, uint64_t* hashes) {
   if (ctx == nullptr) return TG_ERR_INVALID_ARGUMENT;
   Context& C = ctx->c;

@@ -47,6 +47,10 @@ struct EngineBase {
   // Enqueue a pack of one field into the device staging buffer (upload
   // order).
   virtual cudaError_t enqueue_pack(Context& C, int field) = 0;
+  // The state fields into device buffers in upload order (nulls skipped).
+  virtual cudaError_t enqueue_pack_state(Context& C, double* r, double* v,
+                                         double* rho, double* drho,
+                                         double* dv) = 0;
   // Enqueue the neighbour export (counts/hashes by id; indices at offsets).
   virtual cudaError_t enqueue_neighbours(Context& C, int32_t* counts,
                                          uint64_t* hashes,

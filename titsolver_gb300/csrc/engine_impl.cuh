@@ -205,6 +205,15 @@ class Engine final : public EngineBase {
     return cudaGetLastError();
   }
 
+  cudaError_t enqueue_pack_state(Context& C, double* r, double* v, double* rho,
+                                 double* drho, double* dv) override {
+    if (C.n == 0) return cudaSuccess;
+    k_pack_state<D, R><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
+        X_, C.d_tank_of, C.d_tanks, r, v, rho, drho, dv, C.n);
+    C.launches += 1;
+    return cudaGetLastError();
+  }
+
   cudaError_t enqueue_neighbours(Context& C, int32_t* counts,
                                  uint64_t* hashes, const int64_t* offsets,
                                  int32_t* indices) override {

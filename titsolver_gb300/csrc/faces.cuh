@@ -637,23 +637,49 @@ __device__ __forceinline__ bool triangle_in_sphere(const double* t,
 }
 
 // Faces within the support radius of x (the particle's cell list holds
-// every face within reach of the cell); lane l of a warp takes list entries
-// l, l + 32, ... so that the warp shares one particle's faces.
+// every face within reach of the cell), shared by the lanes of a warp: the
+// lanes test 32 list entries at a time and queue the faces that pass in a
+// per-warp shared buffer, and every full batch of 32 queued faces is
+// integrated with one face per lane (the rest at the end), so the costly
+// integrals run on full warps.  Blocks of kFaceBlock threads.
+constexpr int kFaceBlock = 128;
+
 template<int D, class Fn>
 __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
                                                    uint32_t gcell,
                                                    const double* x,
                                                    double radius, int lane,
                                                    Fn&& fn) {
+  __shared__ uint32_t queue[kFaceBlock / 32][64];
+  uint32_t* q = queue[threadIdx.x >> 5];
   const uint32_t s = fc.cell_start[gcell], e = fc.cell_start[gcell + 1];
-  for (uint32_t i = s + lane; i < e; i += 32) {
-    const uint32_t f = fc.cell_face[i];
-    const double* g = fc.coords + D * D * static_cast<size_t>(f);
-    bool in;
-    if constexpr (D == 2) in = segment_in_sphere(g, x, radius);
-    else in = triangle_in_sphere(g, x, radius);
-    if (in) fn(f, g);
+  int pending = 0;
+  for (uint32_t base = s; base < e; base += 32) {
+    const uint32_t i = base + static_cast<uint32_t>(lane);
+    bool in = false;
+    uint32_t f = 0;
+    if (i < e) {
+      f = fc.cell_face[i];
+      const double* g = fc.coords + D * D * static_cast<size_t>(f);
+      if constexpr (D == 2) in = segment_in_sphere(g, x, radius);
+      else in = triangle_in_sphere(g, x, radius);
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, in);
+    if (in) q[pending + __popc(mask & ((1u << lane) - 1u))] = f;
+    pending += __popc(mask);
+    __syncwarp();
+    if (pending >= 32) {
+      pending -= 32;
+      const uint32_t g = q[pending + lane];
+      __syncwarp();
+      fn(g, fc.coords + D * D * static_cast<size_t>(g));
+    }
   }
+  if (lane < pending) {
+    const uint32_t g = q[lane];
+    fn(g, fc.coords + D * D * static_cast<size_t>(g));
+  }
+  __syncwarp();
 }
 
 // Sum over the lanes of a warp (all lanes active), butterfly order.

@@ -1922,6 +1922,34 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Download of the whole state in one pass: r, v, dv/dt (AoS), rho and
+// drho/dt into upload order; a null output is skipped.
+template<int D, class R>
+__global__ void __launch_bounds__(256)
+    k_pack_state(StateBuf<R> X, const uint32_t* __restrict__ tank_of,
+                 const TankDev* tanks, double* __restrict__ r,
+                 double* __restrict__ v, double* __restrict__ rho,
+                 double* __restrict__ drho, double* __restrict__ dv, int64_t n) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t id = X.id[i] & kIdMask;
+  const int64_t o = static_cast<int64_t>(id) * D;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    if (r != nullptr) r[o + k] = X.pos[k][i];
+    if (v != nullptr) v[o + k] = X.vel[k][i];
+    if (dv != nullptr) dv[o + k] = X.dv[k][i];
+  }
+  if (rho != nullptr) {
+    if constexpr (sizeof(R) == 8) {
+      rho[id] = X.rho[i];
+    } else {
+      rho[id] = tanks[tank_of[id]].rho0 + static_cast<double>(X.rho[i]);
+    }
+  }
+  if (drho != nullptr) drho[id] = X.drho[i];
+}
+
 // End of step: advance per-tank time, keep dt, reset the dt reduction.
 static __global__ void k_step_end(double* dt, double* dt_last, double* time,
                                   uint32_t* err, int ntanks) {
