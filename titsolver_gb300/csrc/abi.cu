@@ -311,6 +311,11 @@ int tg_context_destroy(tg_context* ctx) {
   }
   C.release_all();
   C.engine.reset();
+  if (C.copy_stream != nullptr) {
+    cudaStreamSynchronize(C.copy_stream);
+    cudaStreamDestroy(C.copy_stream);
+  }
+  if (C.copy_ready != nullptr) cudaEventDestroy(C.copy_ready);
   cudaStreamDestroy(C.stream);
   delete ctx;
   return TG_OK;
@@ -688,29 +693,53 @@ int tg_particles_download_state(tg_context* ctx, double* r, double* v,
   Context& C = ctx->c;
   if (!C.uploaded) return fail(&C, TG_ERR_NOT_READY, "no particles uploaded");
   if (C.n == 0) return TG_OK;
-  if (rho != nullptr && !C.walls_fresh && C.n_wall > 0) {
-    TG_CUDA(&C, C.engine->enqueue_prepare(C));
-    C.walls_fresh = true;
-  }
   const size_t n = static_cast<size_t>(C.n), dim = static_cast<size_t>(C.P.dim);
   double* d_rho = C.d_stage3;
   double* d_drho = C.d_stage3 + n;
-  TG_CUDA(&C, C.engine->enqueue_pack_state(C, r ? C.d_stage : nullptr,
-                                           v ? C.d_stage2 : nullptr,
-                                           rho ? d_rho : nullptr,
-                                           drho_dt ? d_drho : nullptr,
-                                           dv_dt ? C.d_stage4 : nullptr));
-  const auto get = [&](double* dst, const double* src, size_t count) -> cudaError_t {
+  const auto get = [&](double* dst, const double* src, size_t count,
+                       cudaStream_t s) -> cudaError_t {
     if (dst == nullptr) return cudaSuccess;
-    return cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyDeviceToHost,
-                           C.stream);
+    return cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyDeviceToHost, s);
   };
-  TG_CUDA(&C, get(r, C.d_stage, n * dim));
-  TG_CUDA(&C, get(v, C.d_stage2, n * dim));
-  TG_CUDA(&C, get(rho, d_rho, n));
-  TG_CUDA(&C, get(drho_dt, d_drho, n));
-  TG_CUDA(&C, get(dv_dt, C.d_stage4, n * dim));
+  const bool prepare = rho != nullptr && !C.walls_fresh && C.n_wall > 0;
+  if (!prepare) {
+    TG_CUDA(&C, C.engine->enqueue_pack_state(C, r ? C.d_stage : nullptr,
+                                             v ? C.d_stage2 : nullptr,
+                                             rho ? d_rho : nullptr,
+                                             drho_dt ? d_drho : nullptr,
+                                             dv_dt ? C.d_stage4 : nullptr));
+    TG_CUDA(&C, get(r, C.d_stage, n * dim, C.stream));
+    TG_CUDA(&C, get(v, C.d_stage2, n * dim, C.stream));
+    TG_CUDA(&C, get(rho, d_rho, n, C.stream));
+    TG_CUDA(&C, get(drho_dt, d_drho, n, C.stream));
+    TG_CUDA(&C, get(dv_dt, C.d_stage4, n * dim, C.stream));
+    TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+    return TG_OK;
+  }
+  // The densities need the closing prepare (the wall extrapolation at the
+  // current positions); r, v and dv/dt do not change in it (it only puts
+  // the home state in the new cell order), so they are packed first and
+  // copied on a second stream while the prepare runs.
+  if (C.copy_stream == nullptr) {
+    TG_CUDA(&C, cudaStreamCreateWithFlags(&C.copy_stream, cudaStreamNonBlocking));
+    TG_CUDA(&C, cudaEventCreateWithFlags(&C.copy_ready, cudaEventDisableTiming));
+  }
+  TG_CUDA(&C, C.engine->enqueue_pack_state(C, r ? C.d_stage : nullptr,
+                                           v ? C.d_stage2 : nullptr, nullptr, nullptr,
+                                           dv_dt ? C.d_stage4 : nullptr));
+  TG_CUDA(&C, cudaEventRecord(C.copy_ready, C.stream));
+  TG_CUDA(&C, cudaStreamWaitEvent(C.copy_stream, C.copy_ready, 0));
+  TG_CUDA(&C, get(r, C.d_stage, n * dim, C.copy_stream));
+  TG_CUDA(&C, get(v, C.d_stage2, n * dim, C.copy_stream));
+  TG_CUDA(&C, get(dv_dt, C.d_stage4, n * dim, C.copy_stream));
+  TG_CUDA(&C, C.engine->enqueue_prepare(C));
+  C.walls_fresh = true;
+  TG_CUDA(&C, C.engine->enqueue_pack_state(C, nullptr, nullptr, d_rho,
+                                           drho_dt ? d_drho : nullptr, nullptr));
+  TG_CUDA(&C, get(rho, d_rho, n, C.stream));
+  TG_CUDA(&C, get(drho_dt, d_drho, n, C.stream));
   TG_CUDA(&C, cudaStreamSynchronize(C.stream));
+  TG_CUDA(&C, cudaStreamSynchronize(C.copy_stream));
   return TG_OK;
 }
 

@@ -82,6 +82,10 @@ struct Context {
   int device = 0;
   int sm_count = 0;  // multiprocessors of the device
   cudaStream_t stream = nullptr;
+  // Device-to-host copies that overlap kernels of `stream` (state download
+  // with a closing prepare); created on first use.
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ready = nullptr;
 
   // Particles and tanks.
   int64_t n = 0, n_fluid = 0, n_wall = 0;
