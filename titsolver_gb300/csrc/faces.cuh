@@ -63,6 +63,10 @@ struct FaceArgs {
   int on;
 };
 
+// Block size of the warp-per-face-particle passes (their shared queues are
+// sized by it).
+constexpr int kFaceBlock = 128;
+
 // Doubles per particle in FaceArgs::post_face.
 template<int D>
 constexpr int kPostFaceSums = 2 * D + 2 * D * D;
@@ -390,59 +394,114 @@ __device__ __forceinline__ double face_edge_primitive(const EdgeCoef& ec,
   }
 }
 
-// unit_triangle_integral (kernel.hpp:316-399) of piece I; v = the three
-// projected vertices (2 doubles each).
+// unit_triangle_integral (kernel.hpp:316-399) for the triangles of a warp,
+// one per lane (inactive lanes pass active = false and get 0); all 32 lanes
+// call it together.  Per support piece every lane walks its triangle's
+// edges: a sub-interval outside the support circle adds the sector value
+// times its arc angle at once, the (at most one) inside sub-interval of an
+// edge becomes a task in a per-warp queue; the warp then evaluates the
+// queued tasks (each P(z_hi) - P(z_lo) of the line primitive) 32 at a time,
+// one per lane, so that the costly primitives run on full warps whatever
+// mix of clipped and unclipped edges the lanes hold, and every lane adds up
+// its own tasks.  v = the lane's three projected vertices (units of h).
+struct EdgeTask {
+  double zlo, zhi, delta, eta, lead;
+};
+constexpr int kTasksPerLane = 3;  // one inside sub-interval per edge
+
 template<int K, int I, bool Anti>
-__device__ __forceinline__ double face_triangle_piece(double eta, const double* v) {
+__device__ __forceinline__ double warp_triangle_piece(bool active, double eta,
+                                                      const double* v,
+                                                      EdgeTask* tq, double* tv,
+                                                      uint8_t* ti, int lane) {
   constexpr double cutoff = kFacePieces[K].p[I].cutoff;
-  if (eta >= cutoff) return 0.0;
-  const double radius2 = cutoff * cutoff - eta * eta;
-  const EdgeCoef ec = face_edge_coef<K, I, Anti>(eta);
-  double total = 0.0;
-  for (int e = 0; e < 3; ++e) {
-    const double* p0 = v + 2 * e;
-    const double* p1 = v + 2 * (e == 2 ? 0 : e + 1);
-    const double ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
-    const double len2 = ed[0] * ed[0] + ed[1] * ed[1];
-    if (len2 <= kTiny * kTiny) continue;
-    const double len = sqrt(len2);
-    const double t[2] = {ed[0] / len, ed[1] / len};
-    const double delta = p0[0] * t[1] - p0[1] * t[0];
-    const double delta2 = delta * delta;
-    const double beta2 = eta * eta + delta2;
-    const double beta = sqrt(beta2);
-    const double z0 = p0[0] * t[0] + p0[1] * t[1];
-    const double z1 = z0 + len;
-    double zs[4];
-    int nz = 0;
-    zs[nz++] = z0;
-    if (radius2 > delta2) {
-      const double zc = sqrt(radius2 - delta2);
-      if (z0 < -zc && -zc < z1) zs[nz++] = -zc;
-      if (z0 < zc && zc < z1) zs[nz++] = zc;
-    }
-    zs[nz++] = z1;
-    for (int j = 0; j + 1 < nz; ++j) {
-      const double lo = zs[j], hi = zs[j + 1];
-      if (fabs(hi - lo) <= kTiny) continue;
-      const double mid = (lo + hi) * 0.5;
-      if (mid * mid + delta2 < radius2) {
-        total += face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, hi) -
-                 face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, lo);
-      } else {
-        total += ec.sector * atan2(delta * (hi - lo), lo * hi + delta2);
+  double sector_sum = 0.0;
+  int nt = 0;
+  if (active && eta < cutoff) {
+    const double radius2 = cutoff * cutoff - eta * eta;
+    const EdgeCoef ec = face_edge_coef<K, I, Anti>(eta);
+    for (int e = 0; e < 3; ++e) {
+      const double* p0 = v + 2 * e;
+      const double* p1 = v + 2 * (e == 2 ? 0 : e + 1);
+      const double ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
+      const double len2 = ed[0] * ed[0] + ed[1] * ed[1];
+      if (len2 <= kTiny * kTiny) continue;
+      const double len = sqrt(len2);
+      const double t[2] = {ed[0] / len, ed[1] / len};
+      const double delta = p0[0] * t[1] - p0[1] * t[0];
+      const double delta2 = delta * delta;
+      const double z0 = p0[0] * t[0] + p0[1] * t[1];
+      const double z1 = z0 + len;
+      double zs[4];
+      int nz = 0;
+      zs[nz++] = z0;
+      if (radius2 > delta2) {
+        const double zc = sqrt(radius2 - delta2);
+        if (z0 < -zc && -zc < z1) zs[nz++] = -zc;
+        if (z0 < zc && zc < z1) zs[nz++] = zc;
+      }
+      zs[nz++] = z1;
+      for (int j = 0; j + 1 < nz; ++j) {
+        const double lo = zs[j], hi = zs[j + 1];
+        if (fabs(hi - lo) <= kTiny) continue;
+        const double mid = (lo + hi) * 0.5;
+        if (mid * mid + delta2 < radius2) {
+          if (nt < kTasksPerLane) {
+            tq[lane * kTasksPerLane + nt] = EdgeTask{lo, hi, delta, eta, ec.lead};
+            ++nt;
+          } else {
+            // Not reached (an edge has one inside sub-interval); evaluated
+            // in place should rounding ever split one.
+            const double beta2 = eta * eta + delta2;
+            const double beta = sqrt(beta2);
+            sector_sum += face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, hi) -
+                          face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, lo);
+          }
+        } else {
+          sector_sum += ec.sector * atan2(delta * (hi - lo), lo * hi + delta2);
+        }
       }
     }
   }
-  return total;
+  // Dense list of the warp's tasks (inclusive scan of the counts).
+  int off = nt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, off, o);
+    if (lane >= o) off += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, off, 31);
+  off -= nt;
+  for (int k = 0; k < nt; ++k) ti[off + k] = static_cast<uint8_t>(lane * kTasksPerLane + k);
+  __syncwarp();
+  for (int t = lane; t < total; t += 32) {
+    const int slot = ti[t];
+    const EdgeTask q = tq[slot];
+    const double beta2 = q.eta * q.eta + q.delta * q.delta;
+    const double beta = sqrt(beta2);
+    const EdgeCoef ec{q.lead, 0.0};
+    tv[slot] = face_edge_primitive<K, I, Anti>(ec, q.eta, q.delta, beta2, beta, q.zhi) -
+               face_edge_primitive<K, I, Anti>(ec, q.eta, q.delta, beta2, beta, q.zlo);
+  }
+  __syncwarp();
+  double s = sector_sum;
+  for (int k = 0; k < nt; ++k) s += tv[lane * kTasksPerLane + k];
+  __syncwarp();
+  return s;
 }
 
-// The triangle integral summed over the kernel's pieces.
+// The triangle integral summed over the kernel's pieces (all lanes call).
 template<int K, bool Anti>
-__device__ __noinline__ double face_unit_triangle(double eta, const double* v) {
+__device__ __forceinline__ double warp_unit_triangle(bool active, double eta,
+                                                     const double* v) {
+  __shared__ EdgeTask tq_all[kFaceBlock / 32][32 * kTasksPerLane];
+  __shared__ double tv_all[kFaceBlock / 32][32 * kTasksPerLane];
+  __shared__ uint8_t ti_all[kFaceBlock / 32][32 * kTasksPerLane];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double total = 0.0;
   static_for<0, kFacePieces[K].n>([&]<int I>() {
-    total += face_triangle_piece<K, I, Anti>(eta, v);
+    total += warp_triangle_piece<K, I, Anti>(active, eta, v, tq_all[w], tv_all[w],
+                                             ti_all[w], lane);
   });
   return total;
 }
@@ -508,32 +567,35 @@ __device__ __forceinline__ TriFrame tri_frame(const double* t, const double* x,
 }
 
 // Kernel::flux of face g (segment or triangle) at x; wd = the kernel's
-// weight in D dimensions.
+// weight in D dimensions.  Called by all lanes of a warp together (the 3D
+// integral is warp-cooperative); inactive lanes get zero.
 template<int K, int D>
-__device__ __forceinline__ void face_flux_d(const double* g, const double* x,
-                                            double h, double wd, double* out) {
+__device__ __forceinline__ void face_flux_d(bool active, const double* g,
+                                            const double* x, double h, double wd,
+                                            double* out) {
   if constexpr (D == 2) {
-    face_flux<K>(g, x, h, wd, out);
+    out[0] = out[1] = 0.0;
+    if (active) face_flux<K>(g, x, h, wd, out);
   } else {
     const double hinv = 1.0 / h;
     const TriFrame F = tri_frame(g, x, hinv);
-    const double s = wd * hinv * face_unit_triangle<K, false>(fabs(F.d), F.p);
+    const double s = wd * hinv * warp_unit_triangle<K, false>(active, fabs(F.d), F.p);
     out[0] = F.n[0] * s;
     out[1] = F.n[1] * s;
     out[2] = F.n[2] * s;
   }
 }
 
-// Kernel::antigrad_flux of face g at x.
+// Kernel::antigrad_flux of face g at x (all lanes together, as above).
 template<int K, int D>
-__device__ __forceinline__ double face_antigrad_flux_d(const double* g,
+__device__ __forceinline__ double face_antigrad_flux_d(bool active, const double* g,
                                                        const double* x, double h,
                                                        double wd) {
   if constexpr (D == 2) {
-    return face_antigrad_flux<K>(g, x, h, wd);
+    return active ? face_antigrad_flux<K>(g, x, h, wd) : 0.0;
   } else {
     const TriFrame F = tri_frame(g, x, 1.0 / h);
-    return copysign(wd, F.d) * face_unit_triangle<K, true>(fabs(F.d), F.p);
+    return copysign(wd, F.d) * warp_unit_triangle<K, true>(active, fabs(F.d), F.p);
   }
 }
 
@@ -640,9 +702,10 @@ __device__ __forceinline__ bool triangle_in_sphere(const double* t,
 // every face within reach of the cell), shared by the lanes of a warp: the
 // lanes test 32 list entries at a time and queue the faces that pass in a
 // per-warp shared buffer, and every full batch of 32 queued faces is
-// integrated with one face per lane (the rest at the end), so the costly
-// integrals run on full warps.  Blocks of kFaceBlock threads.
-constexpr int kFaceBlock = 128;
+// integrated with one face per lane (the rest at the end, with the idle
+// lanes inactive), so the costly integrals run on full warps.  fn(active,
+// f, coords) is called by all 32 lanes together.  Blocks of kFaceBlock
+// threads.
 
 template<int D, class Fn>
 __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
@@ -672,12 +735,13 @@ __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
       pending -= 32;
       const uint32_t g = q[pending + lane];
       __syncwarp();
-      fn(g, fc.coords + D * D * static_cast<size_t>(g));
+      fn(true, g, fc.coords + D * D * static_cast<size_t>(g));
     }
   }
-  if (lane < pending) {
-    const uint32_t g = q[lane];
-    fn(g, fc.coords + D * D * static_cast<size_t>(g));
+  if (pending > 0) {
+    const bool active = lane < pending;
+    const uint32_t g = q[active ? lane : 0];
+    fn(active, g, fc.coords + D * D * static_cast<size_t>(g));
   }
   __syncwarp();
 }

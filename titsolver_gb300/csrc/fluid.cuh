@@ -1183,9 +1183,11 @@ __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
     double va[3], rho_a, P_a;
     target_fields(load_dat(A.datrec, i), T, va, rho_a, P_a);
     double drho = 0.0, dv[3] = {0.0, 0.0, 0.0};
-    for_adjacent_faces<D>(fc, gcell, pa, radius, lane, [&](uint32_t f, const double* g) {
+    for_adjacent_faces<D>(fc, gcell, pa, radius, lane,
+                          [&](bool active, uint32_t f, const double* g) {
       double gg[3];
-      face_flux_d<K, D>(g, pa, T.h, fc.weight, gg);
+      face_flux_d<K, D>(active, g, pa, T.h, fc.weight, gg);
+      if (!active) return;
       double rv[3], pv[3];
 #pragma unroll
       for (int j = 0; j < D; ++j) {
@@ -1788,9 +1790,11 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
     const double radius = KernelPoly<K>::unit_radius * T.h;
     const double wd = fc.weight;
     double g[3] = {0.0, 0.0, 0.0};
-    for_adjacent_faces<D>(fc, gcell, x, radius, lane, [&](uint32_t, const double* f) {
+    for_adjacent_faces<D>(fc, gcell, x, radius, lane,
+                          [&](bool active, uint32_t, const double* f) {
       double fl[3];
-      face_flux_d<K, D>(f, x, T.h, wd, fl);
+      face_flux_d<K, D>(active, f, x, T.h, wd, fl);
+      if (!active) return;
 #pragma unroll
       for (int k = 0; k < D; ++k) g[k] += fl[k];
     });
@@ -1816,8 +1820,10 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
 #pragma unroll
       for (int k = 0; k < D; ++k) xs[k] = x[k] + s * (g[k] / ng) * h2;
       double ag = 0.0;
-      for_adjacent_faces<D>(fc, gcell, x, radius, lane, [&](uint32_t, const double* f) {
-        ag += face_antigrad_flux_d<K, D>(f, xs, T.h, wd);
+      for_adjacent_faces<D>(fc, gcell, x, radius, lane,
+                            [&](bool active, uint32_t, const double* f) {
+        const double a = face_antigrad_flux_d<K, D>(active, f, xs, T.h, wd);
+        if (active) ag += a;
       });
       ga -= warp_sum(ag);
     }

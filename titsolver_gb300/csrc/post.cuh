@@ -177,9 +177,10 @@ __global__ void __launch_bounds__(128) k_post_faces(PostArgs<D, F> A) {
     const double gam = fc.gamma[i];
     const double radius = KernelPoly<K>::unit_radius * T.h;
     for_adjacent_faces<D>(fc, global_cell<D>(T, c), pa, radius, lane,
-                          [&](uint32_t f, const double* g) {
+                          [&](bool active, uint32_t f, const double* g) {
       double gg[3], rv[3], r_sa[3];
-      face_flux_d<K, D>(g, pa, T.h, fc.weight, gg);
+      face_flux_d<K, D>(active, g, pa, T.h, fc.weight, gg);
+      if (!active) return;
 #pragma unroll
       for (int j = 0; j < D; ++j) rv[j] = vertex_rho(A.S.datrec, fc.slot_of[fc.vert[D * f + j]], T);
 #pragma unroll
