@@ -16,12 +16,18 @@ one full SSPRK3 step (three neighbour rebuilds, three fused force passes).
   the same number of steps from the same start.
 * ``e2e``: the same metric through the C ABI with host buffers: every step
   uploads r, v, rho, dv/dt from pinned host memory, steps, and downloads
-  them again (tg_particles_update / tg_step / tg_particles_download).
+  them again (tg_particles_update / tg_step / tg_particles_download_state).
 * ``roofline``: the fused force kernel (k_forces): algorithmic bytes per
   launch = fluid particles x 3S (S = state bytes per particle) over its mean
   launch time from a profiled pass with CUDA events on the same stream.
 * ``cpu_baseline``: the oracle (the C++ restatement of the reference's CPU
   path) on the host cores, on a bounded sample of the same workload.
+
+Other workloads (``--config``): c0, c3, c4, c4q, c4half, c5 (2D / 3D /
+batched dam breaks, the same report), c2 (point-cloud search + summation
+density), f2 and f3 (the reference's face-wall mode: the titwcsph pool in
+2D, a triangulated 3D pool; reference physics with shifting; device time
+per step of each form).
 
 ``--impl reference`` times that CPU path alone (the reference itself needs
 C++26 / GCC 16 and cannot be built here).  ``--gpus N`` under
@@ -99,6 +105,17 @@ def make_config(name: str):
         return ("64 independent 3D dam breaks, column height N~U{12..40} particles, "
                 "length and depth U[0.5,2] N, dx=1/100, Wendland C2 h=1.3dx, same physics"), \
             lambda: scenarios.batched_tanks_3d(64)
+    if name == "f2":
+        return ("titwcsph 2D pool with the reference's face walls: H=0.6, column 2HxH at "
+                "dx=H/80 (12,800 fluid), pool 5.366Hx4H tessellated at dx (one fixed "
+                "particle per vertex), Wendland C4 h=2dx, cs0=20sqrt(gH), Ferrari + Morris "
+                "mu=0.001, SSPRK3 CFL 0.4, shifting"), \
+            lambda: scenarios.dam_break_2d_faces(nx_per_H=80)
+    if name == "f3":
+        return ("3D pool with triangle face walls: column 2HxHxH at dx=H/20 (16,000 fluid), "
+                "pool 3Hx1.5Hx(H+dx) triangulated at dx (7,382 vertices, 14,760 triangles), "
+                "box containment, Wendland C4 h=1.3dx, reference physics, shifting"), \
+            lambda: scenarios.dam_break_3d_faces(nx_per_H=20, tank=(3.0, 1.5))
     if name == "c4half":
         return ("3D dam break 2Hx1HxH/2, dx=H/200 (8,000,000 fluid + 3-layer walls), "
                 "Wendland C2 h=1.3dx, same physics"), \
@@ -238,6 +255,9 @@ def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks,
 
     ctx = _abi.Context(params)
     ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+    for t, fc in enumerate(scn.get("faces") or []):
+        if fc is not None:
+            ctx.set_faces(t, fc["face_verts"], fc["poly"])
     if autotune:
         # Untimed setup: the autotuner times a few steps per launch shape and
         # leaves the context at the fastest, with the uploaded state.
@@ -461,6 +481,35 @@ def run_cloud(args, ranks) -> dict | None:
     return out
 
 
+def run_faces(args, ranks) -> dict | None:
+    """The reference's face-wall mode (configs f2, f3): reference physics
+    with shifting, both forms (or --only one), device time per step."""
+    from titsolver_gb300 import _abi, physics, scenarios
+
+    workload, make = make_config(args.config)
+    scn = make()
+    nf = scenarios.n_fluid(scn)
+    forms = [args.only] if args.only else ["fp32c", "fp64"]
+    res, launches = {}, 0
+    for form in forms:
+        P = physics.reference_params(
+            scn["dim"], precision=_abi.TG_FP32C if form == "fp32c" else _abi.TG_FP64)
+        P.post_integrate = _abi.TG_POST_SHIFTING
+        P.device = ranks.local_rank
+        ctx, ms, n_launch, _ = gpu_leg(scn, P, args.warmup, args.steps, 0, ranks, False)
+        ctx.close()
+        res[form] = {"value": nf * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps}
+        launches += n_launch
+    if ranks.rank != 0:
+        return None
+    head = res[forms[0]]
+    return {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+            "higher_is_better": True, "forms": res,
+            "faces": int(sum(fc["face_verts"].shape[0] for fc in scn["faces"] if fc)),
+            "config": {"workload": workload}, "gpu_launches": launches}
+
+
 def run_single_form(args, ranks) -> dict | None:
     """One form on the configured workload (used under ncu)."""
     from titsolver_gb300 import _abi, physics, scenarios
@@ -526,6 +575,8 @@ def main() -> int:
         ranks.barrier()
         if args.config == "c2":
             out = run_cloud(args, ranks)
+        elif args.config in ("f2", "f3"):
+            out = run_faces(args, ranks)
         elif args.only is not None:
             out = run_single_form(args, ranks)
         else:
