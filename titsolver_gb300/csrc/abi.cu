@@ -5,11 +5,13 @@
 // status code with a message in tg_last_error), the per-tank cell grids,
 // device allocation, CUDA-graph capture of one step, and profiling.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
 #include <new>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -1104,6 +1106,53 @@ int build_faces(tg_context* ctx) {
     }
   }
   cont_start[nt] = static_cast<uint32_t>(cont_tri.size() / 9);
+  // 3D: coplanar neighbours across each edge (see face_skip_edges): the
+  // edge shared by exactly two faces that traverse it in opposite
+  // directions, with equal unit normals and the same plane.
+  const size_t nfaces = vert.size() / static_cast<size_t>(D);
+  std::vector<int32_t> edge_nbr(D == 3 ? 3 * nfaces : 1, -1);
+  if (D == 3) {
+    std::vector<std::array<double, 4>> plane(nfaces);  // unit normal, offset
+    double scale = 0.0;
+    for (size_t f = 0; f < nfaces; ++f) {
+      const double* a = coords.data() + 9 * f;
+      const double u[3] = {a[3] - a[0], a[4] - a[1], a[5] - a[2]};
+      const double w[3] = {a[6] - a[0], a[7] - a[1], a[8] - a[2]};
+      double n[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2],
+                     u[0] * w[1] - u[1] * w[0]};
+      const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      if (len > 0.0) {
+        for (double& c : n) c /= len;
+      }
+      plane[f] = {n[0], n[1], n[2], n[0] * a[0] + n[1] * a[1] + n[2] * a[2]};
+      for (int k = 0; k < 9; ++k) scale = std::max(scale, std::fabs(a[k]));
+    }
+    std::map<std::pair<uint32_t, uint32_t>, std::vector<std::pair<uint32_t, int>>> edges_of;
+    for (size_t f = 0; f < nfaces; ++f) {
+      for (int e = 0; e < 3; ++e) {
+        const uint32_t p0 = vert[3 * f + e], p1 = vert[3 * f + (e + 1) % 3];
+        edges_of[{std::min(p0, p1), std::max(p0, p1)}].emplace_back(
+            static_cast<uint32_t>(f), e);
+      }
+    }
+    const double tol_n = 1e-12, tol_d = 1e-12 * std::max(scale, 1.0);
+    for (const auto& [key, list] : edges_of) {
+      if (list.size() != 2) continue;
+      const auto [f0, e0] = list[0];
+      const auto [f1, e1] = list[1];
+      // Opposite traversal: f0 runs p -> q where f1 runs q -> p.
+      if (vert[3 * f0 + e0] != vert[3 * f1 + (e1 + 1) % 3]) continue;
+      const auto& P = plane[f0];
+      const auto& Q = plane[f1];
+      if (std::fabs(P[0] - Q[0]) > tol_n || std::fabs(P[1] - Q[1]) > tol_n ||
+          std::fabs(P[2] - Q[2]) > tol_n || std::fabs(P[3] - Q[3]) > tol_d ||
+          P[0] * P[0] + P[1] * P[1] + P[2] * P[2] < 0.5) {
+        continue;
+      }
+      edge_nbr[3 * f0 + e0] = static_cast<int32_t>(f1);
+      edge_nbr[3 * f1 + e1] = static_cast<int32_t>(f0);
+    }
+  }
   // CSR of the per-cell face lists (faces ascending within each cell).
   std::vector<uint32_t> cell_start(static_cast<size_t>(C.total_cells) + 1, 0);
   for (uint32_t c = 0; c < C.total_cells; ++c) cell_start[c + 1] = cell_start[c] + cell_count[c];
@@ -1133,6 +1182,7 @@ int build_faces(tg_context* ctx) {
     return e;
   };
   TG_CUDA(&C, up(fa.coords, coords));
+  TG_CUDA(&C, up(fa.edge_nbr, edge_nbr));
   TG_CUDA(&C, up(fa.vert, vert));
   TG_CUDA(&C, up(fa.cell_start, cell_start));
   TG_CUDA(&C, up(fa.cell_face, cell_face));

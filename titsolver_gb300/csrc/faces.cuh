@@ -35,6 +35,10 @@ namespace tg {
 // the tanks have particle walls.
 struct FaceArgs {
   const double* coords;       // D * D per face: the vertices a, b (, c)
+  // 3D: per face and edge (ab, bc, ca) the coplanar neighbour across it
+  // (shares the edge, traversed the other way, same plane and normal), or
+  // -1.  An edge whose neighbour is also within reach cancels against it.
+  const int32_t* edge_nbr;
   const uint32_t* vert;       // D per face: upload indices of the vertices
   const uint32_t* cell_start; // per global cell (+1): its face list
   const uint32_t* cell_face;  // faces within reach of each cell, ascending
@@ -411,7 +415,7 @@ constexpr int kTasksPerLane = 3;  // one inside sub-interval per edge
 
 template<int K, int I, bool Anti>
 __device__ __forceinline__ double warp_triangle_piece(bool active, double eta,
-                                                      const double* v,
+                                                      const double* v, unsigned skip,
                                                       EdgeTask* tq, double* tv,
                                                       uint8_t* ti, int lane) {
   constexpr double cutoff = kFacePieces[K].p[I].cutoff;
@@ -421,6 +425,7 @@ __device__ __forceinline__ double warp_triangle_piece(bool active, double eta,
     const double radius2 = cutoff * cutoff - eta * eta;
     const EdgeCoef ec = face_edge_coef<K, I, Anti>(eta);
     for (int e = 0; e < 3; ++e) {
+      if (skip & (1u << e)) continue;
       const double* p0 = v + 2 * e;
       const double* p1 = v + 2 * (e == 2 ? 0 : e + 1);
       const double ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
@@ -490,17 +495,18 @@ __device__ __forceinline__ double warp_triangle_piece(bool active, double eta,
   return s;
 }
 
-// The triangle integral summed over the kernel's pieces (all lanes call).
+// The triangle integral summed over the kernel's pieces (all lanes call);
+// edges in `skip` (bit e: edge e) are left out.
 template<int K, bool Anti>
 __device__ __forceinline__ double warp_unit_triangle(bool active, double eta,
-                                                     const double* v) {
+                                                     const double* v, unsigned skip) {
   __shared__ EdgeTask tq_all[kFaceBlock / 32][32 * kTasksPerLane];
   __shared__ double tv_all[kFaceBlock / 32][32 * kTasksPerLane];
   __shared__ uint8_t ti_all[kFaceBlock / 32][32 * kTasksPerLane];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double total = 0.0;
   static_for<0, kFacePieces[K].n>([&]<int I>() {
-    total += warp_triangle_piece<K, I, Anti>(active, eta, v, tq_all[w], tv_all[w],
+    total += warp_triangle_piece<K, I, Anti>(active, eta, v, skip, tq_all[w], tv_all[w],
                                              ti_all[w], lane);
   });
   return total;
@@ -568,18 +574,20 @@ __device__ __forceinline__ TriFrame tri_frame(const double* t, const double* x,
 
 // Kernel::flux of face g (segment or triangle) at x; wd = the kernel's
 // weight in D dimensions.  Called by all lanes of a warp together (the 3D
-// integral is warp-cooperative); inactive lanes get zero.
+// integral is warp-cooperative); inactive lanes get zero.  skip: the
+// triangle's edges that cancel against in-range coplanar neighbours
+// (face_skip_edges).
 template<int K, int D>
 __device__ __forceinline__ void face_flux_d(bool active, const double* g,
                                             const double* x, double h, double wd,
-                                            double* out) {
+                                            double* out, unsigned skip = 0) {
   if constexpr (D == 2) {
     out[0] = out[1] = 0.0;
     if (active) face_flux<K>(g, x, h, wd, out);
   } else {
     const double hinv = 1.0 / h;
     const TriFrame F = tri_frame(g, x, hinv);
-    const double s = wd * hinv * warp_unit_triangle<K, false>(active, fabs(F.d), F.p);
+    const double s = wd * hinv * warp_unit_triangle<K, false>(active, fabs(F.d), F.p, skip);
     out[0] = F.n[0] * s;
     out[1] = F.n[1] * s;
     out[2] = F.n[2] * s;
@@ -590,12 +598,12 @@ __device__ __forceinline__ void face_flux_d(bool active, const double* g,
 template<int K, int D>
 __device__ __forceinline__ double face_antigrad_flux_d(bool active, const double* g,
                                                        const double* x, double h,
-                                                       double wd) {
+                                                       double wd, unsigned skip = 0) {
   if constexpr (D == 2) {
     return active ? face_antigrad_flux<K>(g, x, h, wd) : 0.0;
   } else {
     const TriFrame F = tri_frame(g, x, 1.0 / h);
-    return copysign(wd, F.d) * warp_unit_triangle<K, true>(active, fabs(F.d), F.p);
+    return copysign(wd, F.d) * warp_unit_triangle<K, true>(active, fabs(F.d), F.p, skip);
   }
 }
 
@@ -696,6 +704,27 @@ __device__ __forceinline__ bool triangle_in_sphere(const double* t,
   triangle_clamp(t, x, q);
   const double d[3] = {q[0] - x[0], q[1] - x[1], q[2] - x[2]};
   return dot_d<3>(d, d) <= radius * radius;
+}
+
+// Edges of triangle f whose coplanar neighbour across them is also within
+// the support radius of x (a face adjacent to the particle): the two
+// triangles traverse the shared edge in opposite directions in the same
+// plane (their frames differ by a rotation in it), so its edge integrals
+// (line primitive differences and sector arcs, both odd under reversing
+// the edge) cancel, and plain sums of the particle's face fluxes (grad
+// gamma, the antigradient sum of gamma) are the same without them.  Sums
+// that weight each face differently (the face terms) keep every edge.
+__device__ __forceinline__ unsigned face_skip_edges(const FaceArgs& fc, uint32_t f,
+                                                    const double* x, double radius) {
+  unsigned skip = 0;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    const int32_t nb = fc.edge_nbr[3 * static_cast<size_t>(f) + e];
+    if (nb >= 0 && triangle_in_sphere(fc.coords + 9 * static_cast<size_t>(nb), x, radius)) {
+      skip |= 1u << e;
+    }
+  }
+  return skip;
 }
 
 // Faces within the support radius of x (the particle's cell list holds

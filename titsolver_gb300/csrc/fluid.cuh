@@ -1185,6 +1185,8 @@ __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
     double drho = 0.0, dv[3] = {0.0, 0.0, 0.0};
     for_adjacent_faces<D>(fc, gcell, pa, radius, lane,
                           [&](bool active, uint32_t f, const double* g) {
+      // Each face's flux is weighted by its own vertex densities and
+      // pressures, so no edges cancel here.
       double gg[3];
       face_flux_d<K, D>(active, g, pa, T.h, fc.weight, gg);
       if (!active) return;
@@ -1791,9 +1793,11 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
     const double wd = fc.weight;
     double g[3] = {0.0, 0.0, 0.0};
     for_adjacent_faces<D>(fc, gcell, x, radius, lane,
-                          [&](bool active, uint32_t, const double* f) {
+                          [&](bool active, uint32_t fi, const double* f) {
       double fl[3];
-      face_flux_d<K, D>(active, f, x, T.h, wd, fl);
+      unsigned skip = 0;
+      if constexpr (D == 3) skip = active ? face_skip_edges(fc, fi, x, radius) : 0u;
+      face_flux_d<K, D>(active, f, x, T.h, wd, fl, skip);
       if (!active) return;
 #pragma unroll
       for (int k = 0; k < D; ++k) g[k] += fl[k];
@@ -1821,8 +1825,11 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
       for (int k = 0; k < D; ++k) xs[k] = x[k] + s * (g[k] / ng) * h2;
       double ag = 0.0;
       for_adjacent_faces<D>(fc, gcell, x, radius, lane,
-                            [&](bool active, uint32_t, const double* f) {
-        const double a = face_antigrad_flux_d<K, D>(active, f, xs, T.h, wd);
+                            [&](bool active, uint32_t fi, const double* f) {
+        // The adjacency is that of x (the face set does not move with xs).
+        unsigned skip = 0;
+        if constexpr (D == 3) skip = active ? face_skip_edges(fc, fi, x, radius) : 0u;
+        const double a = face_antigrad_flux_d<K, D>(active, f, xs, T.h, wd, skip);
         if (active) ag += a;
       });
       ga -= warp_sum(ag);

@@ -178,6 +178,7 @@ __global__ void __launch_bounds__(128) k_post_faces(PostArgs<D, F> A) {
     const double radius = KernelPoly<K>::unit_radius * T.h;
     for_adjacent_faces<D>(fc, global_cell<D>(T, c), pa, radius, lane,
                           [&](bool active, uint32_t f, const double* g) {
+      // Per-face weights (vertex density, face centre): no edges cancel.
       double gg[3], rv[3], r_sa[3];
       face_flux_d<K, D>(active, g, pa, T.h, fc.weight, gg);
       if (!active) return;
