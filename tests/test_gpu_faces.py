@@ -120,6 +120,30 @@ def test_3d_faces_other_kernels_and_term_sets(gpu_lib, kernel):
     _compare(scn, physics.baseline_params(3, kernel=kernel), 2, 1e-10)
 
 
+@pytest.mark.parametrize("integrator", (_abi.TG_EULER, _abi.TG_VERLET, _abi.TG_SSPRK2))
+def test_3d_faces_other_integrators(gpu_lib, integrator):
+    scn = _scn3()
+    P = physics.reference_params(3)
+    P.integrator = integrator
+    _compare(scn, P, 3, 1e-10)
+
+
+def test_3d_faces_survive_autotune(gpu_lib):
+    scn = _scn3()
+    P = physics.reference_params(3)
+    P.post_integrate = _abi.TG_POST_SHIFTING
+    f = fluid_mask(scn)
+    with gpu_context(scn, P) as ctx, gpu_context(scn, P) as ref:
+        ctx.step(1)
+        ref.step(1)
+        ctx.autotune(2)
+        ctx.step(2)
+        ref.step(2)
+        a, b = gpu_state(ctx), gpu_state(ref)
+    assert rel_l2(a["rho"][f], b["rho"][f]) <= 1e-11
+    assert rel_l2(a["r"][f], b["r"][f]) <= 1e-11
+
+
 def test_3d_faces_batched_with_a_particle_wall_tank(gpu_lib):
     a = _scn3()
     b = scenarios.dam_break_3d(nx_per_H=6)
