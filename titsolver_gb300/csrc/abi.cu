@@ -1106,11 +1106,46 @@ int build_faces(tg_context* ctx) {
     }
   }
   cont_start[nt] = static_cast<uint32_t>(cont_tri.size() / 9);
-  // 3D: coplanar neighbours across each edge (see face_skip_edges): the
-  // edge shared by exactly two faces that traverse it in opposite
-  // directions, with equal unit normals and the same plane.
+  // Coplanar neighbours across each edge (3D) or collinear neighbours
+  // across each end (2D), see face_skip_edges: 3D, the edge shared by
+  // exactly two faces that traverse it in opposite directions, with equal
+  // unit normals and the same plane; 2D, the only segment ending at a
+  // vertex and the only one starting there, on the same line with the same
+  // direction.
   const size_t nfaces = vert.size() / static_cast<size_t>(D);
-  std::vector<int32_t> edge_nbr(D == 3 ? 3 * nfaces : 1, -1);
+  std::vector<int32_t> edge_nbr(std::max<size_t>(1, static_cast<size_t>(D) * nfaces), -1);
+  if (D == 2) {
+    std::map<uint32_t, std::pair<std::vector<uint32_t>, std::vector<uint32_t>>> at;  // in, out
+    double scale = 0.0;
+    for (size_t f = 0; f < nfaces; ++f) {
+      at[vert[2 * f + 1]].first.push_back(static_cast<uint32_t>(f));
+      at[vert[2 * f]].second.push_back(static_cast<uint32_t>(f));
+      for (int k = 0; k < 4; ++k) scale = std::max(scale, std::fabs(coords[4 * f + k]));
+    }
+    const auto line = [&](size_t f) {
+      const double* a = coords.data() + 4 * f;
+      double e[2] = {a[2] - a[0], a[3] - a[1]};
+      const double len = std::sqrt(e[0] * e[0] + e[1] * e[1]);
+      if (len > 0.0) {
+        e[0] /= len;
+        e[1] /= len;
+      }
+      return std::array<double, 3>{e[0], e[1], e[1] * a[0] - e[0] * a[1]};
+    };
+    const double tol_n = 1e-12, tol_d = 1e-12 * std::max(scale, 1.0);
+    for (const auto& [u, io] : at) {
+      if (io.first.size() != 1 || io.second.size() != 1) continue;
+      const uint32_t fi = io.first[0], fo = io.second[0];
+      if (fi == fo) continue;
+      const auto P = line(fi), Q = line(fo);
+      if (std::fabs(P[0] - Q[0]) > tol_n || std::fabs(P[1] - Q[1]) > tol_n ||
+          std::fabs(P[2] - Q[2]) > tol_d || P[0] * P[0] + P[1] * P[1] < 0.5) {
+        continue;
+      }
+      edge_nbr[2 * fi + 1] = static_cast<int32_t>(fo);  // across fi's end b
+      edge_nbr[2 * fo] = static_cast<int32_t>(fi);      // across fo's end a
+    }
+  }
   if (D == 3) {
     std::vector<std::array<double, 4>> plane(nfaces);  // unit normal, offset
     double scale = 0.0;

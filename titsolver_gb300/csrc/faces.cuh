@@ -35,9 +35,11 @@ namespace tg {
 // the tanks have particle walls.
 struct FaceArgs {
   const double* coords;       // D * D per face: the vertices a, b (, c)
-  // 3D: per face and edge (ab, bc, ca) the coplanar neighbour across it
-  // (shares the edge, traversed the other way, same plane and normal), or
-  // -1.  An edge whose neighbour is also within reach cancels against it.
+  // Per face the coplanar neighbour across each edge (3D: ab, bc, ca;
+  // shares the edge, traversed the other way, same plane and normal) or the
+  // collinear neighbour across each end (2D: a, b; the segment ending at a
+  // / starting at b on the same line, same direction), or -1.  An edge or
+  // end whose neighbour is also within reach cancels against it.
   const int32_t* edge_nbr;
   const uint32_t* vert;       // D per face: upload indices of the vertices
   const uint32_t* cell_start; // per global cell (+1): its face list
@@ -174,17 +176,29 @@ __device__ __forceinline__ double face_primitive(double eta, double z) {
   return s;
 }
 
+// unit_segment_integral (kernel.hpp:286-314) summed over the pieces: per
+// piece P(clip(z_max)) - P(clip(z_min)), clip to |z| <= sqrt(cutoff^2 -
+// eta^2).  skip bit 0 / 1 leaves out the z_min / z_max end (an end shared
+// with an in-range collinear neighbour, whose opposite term cancels it;
+// face_skip_edges).
 template<int K, bool Anti>
 __device__ __forceinline__ double face_unit_segment(double eta, double zmin,
-                                                    double zmax) {
+                                                    double zmax, unsigned skip) {
   double total = 0.0;
   static_for<0, kFacePieces[K].n>([&]<int I>() {
     constexpr double cutoff = kFacePieces[K].p[I].cutoff;
     if (eta >= cutoff) return;
     const double zc = sqrt(cutoff * cutoff - eta * eta);
-    const double lo = fmax(zmin, -zc), hi = fmin(zmax, zc);
-    if (lo >= hi) return;
-    total += face_primitive<K, I, Anti>(eta, hi) - face_primitive<K, I, Anti>(eta, lo);
+    if (skip == 0) {
+      const double lo = fmax(zmin, -zc), hi = fmin(zmax, zc);
+      if (lo >= hi) return;
+      total += face_primitive<K, I, Anti>(eta, hi) - face_primitive<K, I, Anti>(eta, lo);
+      return;
+    }
+    // The clipped ends (a segment outside the circle gives P(+-zc) twice,
+    // i.e. zero, as the early return above does).
+    if (!(skip & 2u)) total += face_primitive<K, I, Anti>(eta, fmin(fmax(zmax, -zc), zc));
+    if (!(skip & 1u)) total -= face_primitive<K, I, Anti>(eta, fmin(fmax(zmin, -zc), zc));
   });
   return total;
 }
@@ -221,10 +235,11 @@ __device__ __forceinline__ FaceFrame face_frame(const double* ab,
 // wd = the kernel's 2D weight.
 template<int K>
 __device__ __forceinline__ void face_flux(const double* ab, const double* x,
-                                          double h, double wd, double* out) {
+                                          double h, double wd, double* out,
+                                          unsigned skip = 0) {
   const double hinv = 1.0 / h;
   const FaceFrame F = face_frame(ab, x, hinv);
-  const double s = wd * hinv * face_unit_segment<K, false>(fabs(F.d), F.za, F.zb);
+  const double s = wd * hinv * face_unit_segment<K, false>(fabs(F.d), F.za, F.zb, skip);
   out[0] = F.n[0] * s;
   out[1] = F.n[1] * s;
 }
@@ -233,9 +248,9 @@ __device__ __forceinline__ void face_flux(const double* ab, const double* x,
 template<int K>
 __device__ __forceinline__ double face_antigrad_flux(const double* ab,
                                                      const double* x, double h,
-                                                     double wd) {
+                                                     double wd, unsigned skip = 0) {
   const FaceFrame F = face_frame(ab, x, 1.0 / h);
-  return copysign(wd, F.d) * face_unit_segment<K, true>(fabs(F.d), F.za, F.zb);
+  return copysign(wd, F.d) * face_unit_segment<K, true>(fabs(F.d), F.za, F.zb, skip);
 }
 
 // Segment::intersects(BSphere) (geom/segment.hpp:108-112).
@@ -583,7 +598,7 @@ __device__ __forceinline__ void face_flux_d(bool active, const double* g,
                                             double* out, unsigned skip = 0) {
   if constexpr (D == 2) {
     out[0] = out[1] = 0.0;
-    if (active) face_flux<K>(g, x, h, wd, out);
+    if (active) face_flux<K>(g, x, h, wd, out, skip);
   } else {
     const double hinv = 1.0 / h;
     const TriFrame F = tri_frame(g, x, hinv);
@@ -600,7 +615,7 @@ __device__ __forceinline__ double face_antigrad_flux_d(bool active, const double
                                                        const double* x, double h,
                                                        double wd, unsigned skip = 0) {
   if constexpr (D == 2) {
-    return active ? face_antigrad_flux<K>(g, x, h, wd) : 0.0;
+    return active ? face_antigrad_flux<K>(g, x, h, wd, skip) : 0.0;
   } else {
     const TriFrame F = tri_frame(g, x, 1.0 / h);
     return copysign(wd, F.d) * warp_unit_triangle<K, true>(active, fabs(F.d), F.p, skip);
@@ -706,23 +721,30 @@ __device__ __forceinline__ bool triangle_in_sphere(const double* t,
   return dot_d<3>(d, d) <= radius * radius;
 }
 
-// Edges of triangle f whose coplanar neighbour across them is also within
-// the support radius of x (a face adjacent to the particle): the two
-// triangles traverse the shared edge in opposite directions in the same
-// plane (their frames differ by a rotation in it), so its edge integrals
-// (line primitive differences and sector arcs, both odd under reversing
-// the edge) cancel, and plain sums of the particle's face fluxes (grad
-// gamma, the antigradient sum of gamma) are the same without them.  Sums
-// that weight each face differently (the face terms) keep every edge.
+// Edges (3D) or ends (2D) of face f whose coplanar (collinear) neighbour
+// across them is also within the support radius of x (a face adjacent to
+// the particle).  3D: the two triangles traverse the shared edge in
+// opposite directions in the same plane (their frames differ by a rotation
+// in it), so its edge integrals (line primitive differences and sector
+// arcs, both odd under reversing the edge) cancel.  2D: the shared end is
+// the upper end of one segment and the lower end of the other on the same
+// line, so its two clipped primitive terms cancel.  Plain sums of the
+// particle's face fluxes (grad gamma, the antigradient sum of gamma) are
+// the same without them; sums that weight each face differently (the face
+// terms) keep every edge.
+template<int D>
 __device__ __forceinline__ unsigned face_skip_edges(const FaceArgs& fc, uint32_t f,
                                                     const double* x, double radius) {
   unsigned skip = 0;
 #pragma unroll
-  for (int e = 0; e < 3; ++e) {
-    const int32_t nb = fc.edge_nbr[3 * static_cast<size_t>(f) + e];
-    if (nb >= 0 && triangle_in_sphere(fc.coords + 9 * static_cast<size_t>(nb), x, radius)) {
-      skip |= 1u << e;
-    }
+  for (int e = 0; e < (D == 2 ? 2 : 3); ++e) {
+    const int32_t nb = fc.edge_nbr[(D == 2 ? 2 : 3) * static_cast<size_t>(f) + e];
+    if (nb < 0) continue;
+    const double* g = fc.coords + D * D * static_cast<size_t>(nb);
+    bool in;
+    if constexpr (D == 2) in = segment_in_sphere(g, x, radius);
+    else in = triangle_in_sphere(g, x, radius);
+    if (in) skip |= 1u << e;
   }
   return skip;
 }

@@ -1796,7 +1796,7 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
                           [&](bool active, uint32_t fi, const double* f) {
       double fl[3];
       unsigned skip = 0;
-      if constexpr (D == 3) skip = active ? face_skip_edges(fc, fi, x, radius) : 0u;
+      if (active) skip = face_skip_edges<D>(fc, fi, x, radius);
       face_flux_d<K, D>(active, f, x, T.h, wd, fl, skip);
       if (!active) return;
 #pragma unroll
@@ -1828,7 +1828,7 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
                             [&](bool active, uint32_t fi, const double* f) {
         // The adjacency is that of x (the face set does not move with xs).
         unsigned skip = 0;
-        if constexpr (D == 3) skip = active ? face_skip_edges(fc, fi, x, radius) : 0u;
+        if (active) skip = face_skip_edges<D>(fc, fi, x, radius);
         const double a = face_antigrad_flux_d<K, D>(active, f, xs, T.h, wd, skip);
         if (active) ag += a;
       });
