@@ -922,6 +922,25 @@ struct PairF32 {
   int visc, diff;
   bool kahan;
   Kahan drho, dv[3];
+  // Plain partial sums of the current cell or row range; the compensated
+  // accumulators take one add per range (close) instead of one per pair.
+  float pd, pv[3];
+
+  __device__ __forceinline__ void open() {
+    pd = 0.f;
+    pv[0] = pv[1] = pv[2] = 0.f;
+  }
+  __device__ __forceinline__ void close() {
+    if (Phys != kPhysGeneric || kahan) {
+      drho.add(pd);
+#pragma unroll
+      for (int k = 0; k < D; ++k) dv[k].add(pv[k]);
+    } else {
+      drho.s += pd;
+#pragma unroll
+      for (int k = 0; k < D; ++k) dv[k].s += pv[k];
+    }
+  }
 
   __device__ __forceinline__ void init(const PhysDev& P, const TankDev& T,
                                        const Dat32& own, int kahan_on) {
@@ -977,15 +996,9 @@ struct PairF32 {
                     : 0.f;
     }
     const float coef = m * (Pi - (a.P + b.P)) * Fk;
-    if (Phys != kPhysGeneric || kahan) {
-      drho.add(dr);
+    pd += dr;
 #pragma unroll
-      for (int k = 0; k < D; ++k) dv[k].add(coef * d[k]);
-    } else {
-      drho.s += dr;
-#pragma unroll
-      for (int k = 0; k < D; ++k) dv[k].s += coef * d[k];
-    }
+    for (int k = 0; k < D; ++k) pv[k] += coef * d[k];
   }
 };
 
@@ -1357,6 +1370,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
       oas[2] = D == 3 ? oa[2] - dz * csz : 0.f;
+      acc.open();
       for (uint32_t j = s; j < en; ++j) {
         if (j == static_cast<uint32_t>(i)) continue;
         float ob[3], d[3];
@@ -1368,6 +1382,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
         if (s2 > acc.R2) continue;
         acc.add(d, s2, load_dat(A.datrec, j));
       }
+      acc.close();
     };
     // 3D: one range per row of cells; each candidate's x offset is moved
     // to the target's cell by its cell's x index (record word w).  Same
@@ -1376,6 +1391,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
       if constexpr (D == 3) {
         const float oay = oa[1] - dy * csz;
         const float oaz = oa[2] - dz * csz;
+        acc.open();
         for (uint32_t j = s; j < en; ++j) {
           if (j == static_cast<uint32_t>(i)) continue;
           const Pos32_3 b = A.posrec[j];
@@ -1388,6 +1404,7 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
           if (s2 > acc.R2) continue;
           acc.add(d, s2, load_dat(A.datrec, j));
         }
+        acc.close();
       }
     };
     if constexpr (Team == 1 && D == 3) {
@@ -1523,6 +1540,7 @@ __global__ void __launch_bounds__(128, 7)
       for (int x = xlo; x <= xhi; ++x) {
         const uint32_t ge = __ldg(A.cell_start + 2 * (row + x + 1));
         oas[0] = oa[0] - (x - c[0]) * csz;
+        acc.open();
         for (uint32_t j = gs; j < ge; ++j) {
           if (j == static_cast<uint32_t>(i)) continue;
           const int sj = static_cast<int>(j) + shift;
@@ -1533,6 +1551,7 @@ __global__ void __launch_bounds__(128, 7)
           const float4 b0 = s_dat[2 * sj], b1 = s_dat[2 * sj + 1];
           acc.add(d, s2, Dat32{b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w});
         }
+        acc.close();
         gs = ge;
       }
     }
@@ -1542,6 +1561,7 @@ __global__ void __launch_bounds__(128, 7)
       float oas[3];
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
+      acc.open();
       for (uint32_t j = s; j < en; ++j) {
         if (j == static_cast<uint32_t>(i)) continue;
         float ob[3], d[3];
@@ -1553,6 +1573,7 @@ __global__ void __launch_bounds__(128, 7)
         if (s2 > acc.R2) continue;
         acc.add(d, s2, load_dat(A.datrec, j));
       }
+      acc.close();
     });
   }
   float va[3], dv_out[3];
