@@ -3,16 +3,17 @@
 // (FluidEquations with a non-empty domain, fluid_equations.hpp:122-193,
 // 241-247, 278-291, 340-349, 491-511); segments in 2D, triangles in 3D.
 //
-// The tank's fixed particles are the face vertices.  Per prepare, k_gamma
-// computes for every particle the kernel flux sum over its adjacent faces
-// (grad gamma), the containment (winding number > 1/2: in 2D by signed
-// crossings of the +x ray with the polygon edges of the particle's grid
-// row; in 3D from the particle's cell when the containment surface does not
-// reach that cell, else by the exact winding number of the surface's
-// triangles), and gamma = contains - sum of antigradient fluxes at
-// r + (2 contains - 1) n h^2 (fluid_equations.hpp:166-193).  The wall
-// extrapolation, the force pass and the post-integration passes then read
-// gamma and grad gamma and add the face terms.
+// The tank's fixed particles are the face vertices.  Per prepare,
+// k_gamma_init / k_gamma_faces compute for every particle the kernel flux
+// sum over its adjacent faces (grad gamma), the containment (winding
+// number > 1/2: in 2D by signed crossings of the +x ray with the polygon
+// edges of the particle's grid row; in 3D from the particle's cell when the
+// containment surface does not reach that cell, else by the exact winding
+// number of the surface's triangles), and gamma = contains - sum of
+// antigradient fluxes at r + (2 contains - 1) n h^2
+// (fluid_equations.hpp:166-193).  The wall extrapolation, the force pass
+// and the post-integration passes then read gamma and grad gamma and add
+// the face terms.
 //
 // Kernel flux and antigradient flux of a segment (kernel.hpp:194-221,
 // 286-314) are sums over the kernel's support pieces w_i(q) = sum_p c_p q^p
