@@ -108,3 +108,27 @@ def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting, f
         (frames[0][0],)).fetchone()[0]), "<f8").reshape(-1, 2)
     np.testing.assert_array_equal(r_first, r0)
     con.close()
+
+
+def test_titwcsph_full_run_to_the_reference_end_time(gpu_lib, tmp_path):
+    # The reference's integration test runs titwcsph to t* = 10
+    # (tests/titwcsph/test.cmake:10-16) and compares a platform-specific
+    # checksum; here the same run (face walls, dr = H/80, compensated form)
+    # must end cleanly with the physics of a collapsed column: every fluid
+    # particle finite and inside the pool, the mean height about halved,
+    # densities within 2% of rho_0.
+    exe = gpu_build.build_host()["titwcsph_gpu"]
+    dump = tmp_path / "state.bin"
+    cmd = [str(exe), "--faces", "--fp32c", "--nx", "80", "--end-time", "10", "--dump", str(dump)]
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr
+    tank, (r0, v0, rho0), (r1, v1, rho1), t, steps, fc = read_dump(dump)
+    nf = tank["n_fluid"]
+    assert t * np.sqrt(9.81 / 0.6) >= 10.0
+    assert np.all(np.isfinite(r1)) and np.all(np.isfinite(v1)) and np.all(np.isfinite(rho1))
+    poly = fc[0]["poly"]
+    assert np.all((r1[:nf] > poly.min(axis=0)) & (r1[:nf] < poly.max(axis=0)))
+    assert 0.4 < r1[:nf, 1].mean() / r0[:nf, 1].mean() < 0.6
+    assert r1[:nf, 0].max() > 0.95 * poly[:, 0].max()
+    assert np.all(np.abs(rho1[:nf] / 1000.0 - 1.0) < 0.02)
+    np.testing.assert_array_equal(r1[nf:], r0[nf:])
