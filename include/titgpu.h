@@ -190,7 +190,9 @@ int tg_particles_upload(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
  * new host values: r, v (Dim doubles per particle), rho, and optionally
  * dv_dt (NULL resets it to zero; it feeds the force time step).  The cell
  * grids of the tanks are kept.  This is the per-step host->device sync of a
- * driver that keeps its ParticleArray on the host. */
+ * driver that keeps its ParticleArray on the host.  Page-locked arrays
+ * (tg_host_alloc, cudaHostAlloc, registered) are read by the device
+ * directly, others are staged; the arrays may be reused when it returns. */
 int tg_particles_update(tg_context* ctx, const double* r, const double* v,
                         const double* rho, const double* dv_dt);
 

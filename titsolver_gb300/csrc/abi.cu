@@ -184,6 +184,18 @@ double kernel_weight(int k, int dim) {
   return 1.0 / (tg::kernel_zero_moment(k, dim) * area);
 }
 
+// The device view of a page-locked (cudaMallocHost / cudaHostAlloc /
+// registered) host array, or nullptr for other memory.
+const double* mapped_host(const double* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+  return static_cast<const double*>(a.devicePointer);
+}
+
 int key_bits_for(uint32_t total_cells) {
   int bits = 1;
   while (bits < 32 && (static_cast<uint64_t>(1) << bits) < total_cells) ++bits;
@@ -548,7 +560,7 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
                                 cudaMemcpyHostToDevice, s));
     TG_CUDA(&C, cudaMemcpyAsync(C.d_stage3, rho, sizeof(double) * n,
                                 cudaMemcpyHostToDevice, s));
-    TG_CUDA(&C, C.engine->upload_state(C, false));
+    TG_CUDA(&C, C.engine->upload_state(C, C.d_stage, C.d_stage2, C.d_stage3, nullptr));
   }
   TG_CUDA(&C, cudaStreamSynchronize(s));
   C.uploaded = true;
@@ -571,17 +583,31 @@ int tg_particles_update(tg_context* ctx, const double* r, const double* v,
   }
   const int dim = C.P.dim;
   cudaStream_t s = C.stream;
-  TG_CUDA(&C, cudaMemcpyAsync(C.d_stage, r, sizeof(double) * C.n * dim,
-                              cudaMemcpyHostToDevice, s));
-  TG_CUDA(&C, cudaMemcpyAsync(C.d_stage2, v, sizeof(double) * C.n * dim,
-                              cudaMemcpyHostToDevice, s));
-  TG_CUDA(&C, cudaMemcpyAsync(C.d_stage3, rho, sizeof(double) * C.n,
-                              cudaMemcpyHostToDevice, s));
-  if (dv_dt != nullptr) {
-    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage4, dv_dt, sizeof(double) * C.n * dim,
+  // Page-locked host arrays are read by the unpack kernel itself over the
+  // host link; other host memory goes through the staging buffers.
+  const double* dr = mapped_host(r);
+  const double* dv = mapped_host(v);
+  const double* drho = mapped_host(rho);
+  const double* ddv = dv_dt != nullptr ? mapped_host(dv_dt) : nullptr;
+  if (dr != nullptr && dv != nullptr && drho != nullptr &&
+      (dv_dt == nullptr || ddv != nullptr)) {
+    TG_CUDA(&C, C.engine->upload_state(C, dr, dv, drho, ddv));
+  } else {
+    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage, r, sizeof(double) * C.n * dim,
                                 cudaMemcpyHostToDevice, s));
+    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage2, v, sizeof(double) * C.n * dim,
+                                cudaMemcpyHostToDevice, s));
+    TG_CUDA(&C, cudaMemcpyAsync(C.d_stage3, rho, sizeof(double) * C.n,
+                                cudaMemcpyHostToDevice, s));
+    if (dv_dt != nullptr) {
+      TG_CUDA(&C, cudaMemcpyAsync(C.d_stage4, dv_dt, sizeof(double) * C.n * dim,
+                                  cudaMemcpyHostToDevice, s));
+    }
+    TG_CUDA(&C, C.engine->upload_state(C, C.d_stage, C.d_stage2, C.d_stage3,
+                                       dv_dt != nullptr ? C.d_stage4 : nullptr));
   }
-  TG_CUDA(&C, C.engine->upload_state(C, dv_dt != nullptr));
+  // The host arrays may be reused as soon as this returns.
+  TG_CUDA(&C, cudaStreamSynchronize(s));
   C.walls_fresh = false;
   return TG_OK;
 }

@@ -36,7 +36,8 @@ struct EngineBase {
   // Unpack the staged host arrays (upload order: r, v, rho in d_stage,
   // d_stage2, d_stage3; dv/dt in d_stage4 when with_dv) into the home state,
   // then compute the cell keys.
-  virtual cudaError_t upload_state(Context& C, bool with_dv) = 0;
+  virtual cudaError_t upload_state(Context& C, const double* r, const double* v,
+                                   const double* rho, const double* dv) = 0;
   // Recompute the home cell keys from the positions if they are stale.
   virtual cudaError_t ensure_keys(Context& C) = 0;
   // Enqueue one full integrator step on C.stream.

@@ -90,11 +90,11 @@ class Engine final : public EngineBase {
     return e;
   }
 
-  cudaError_t upload_state(Context& C, bool with_dv) override {
+  cudaError_t upload_state(Context& C, const double* r, const double* v,
+                           const double* rho, const double* dv) override {
     if (C.n == 0) return cudaSuccess;
     k_unpack<D, R><<<grid_for(C.n, 256), 256, 0, C.stream>>>(
-        X_, C.d_stage, C.d_stage2, C.d_stage3, with_dv ? C.d_stage4 : nullptr,
-        C.d_tank_of, C.d_tanks, C.d_wall_from, C.n);
+        X_, r, v, rho, dv, C.d_tank_of, C.d_tanks, C.d_wall_from, C.n);
     C.launches += 1;
     C.keys_valid = false;
     return ensure_keys(C);
