@@ -8,6 +8,7 @@
 // Usage: titwcsph_gpu [--nx N] [--steps S] [--end-time T] [--fp32c]
 //                     [--integrator ssprk3|ssprk2|euler|verlet]
 //                     [--no-shifting] [--faces] [--ttdb FILE] [--dump FILE]
+//                     [--log]
 //   --nx       particles per column height H (default 80, as wcsph.cpp:42)
 //   --steps    stop after S steps (default: run to scaled time T)
 //   --end-time scaled end time t sqrt(g/H) (default 10, as wcsph.cpp:183)
@@ -18,6 +19,9 @@
 //   --faces    the reference's face walls
 //   --ttdb     write frames every 100 steps to this .ttdb file
 //   --dump     write the initial and final state as raw binary (see below)
+//   --log      print the reference's per-step line: step, scaled time, wall
+//              seconds of the previous step and of the previous write
+//              (wcsph.cpp:172-176)
 //
 // Dump layout (little-endian): int64 n, n_fluid, steps; float64 h, m, rho_0,
 // cs_0, time; then r (n x 2), v (n x 2), rho (n) of the initial state and
@@ -25,6 +29,7 @@
 // pairs of int32 fixed-particle indices, int64 n_poly and n_poly (x, y)
 // float64 containment vertices.
 
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -51,6 +56,7 @@ struct Options {
   bool faces = false;
   std::string ttdb;
   std::string dump;
+  bool log = false;
 };
 
 auto parse(int argc, char** argv) -> Options {
@@ -70,6 +76,7 @@ auto parse(int argc, char** argv) -> Options {
     else if (a == "--faces") o.faces = true;
     else if (a == "--ttdb") o.ttdb = next();
     else if (a == "--dump") o.dump = next();
+    else if (a == "--log") o.log = true;
     else throw Exception{"unknown option " + a};
   }
   if (o.nx < 4) throw Exception{"--nx must be at least 4"};
@@ -317,13 +324,23 @@ auto simulate(const Options& opt, const Equations& equations,
   // Run the simulation.
   Real time{};
   std::size_t step = 1;
+  double exec_s = 0.0, print_s = 0.0;
+  using clock = std::chrono::steady_clock;
   for (;; ++step) {
     const auto scaled_time = time * std::sqrt(g / H);
+    if (opt.log) {
+      std::printf("%15zu\t\t%10.5f\t\t%10.5f\t\t%10.5f\n", step,
+                  static_cast<double>(scaled_time), exec_s, print_s);
+    }
+    const auto t0 = clock::now();
     const Real dt = time_integrator.step(mesh, particles);
+    exec_s = std::chrono::duration<double>(clock::now() - t0).count();
     const bool end = opt.steps >= 0 ? static_cast<long>(step) >= opt.steps
                                     : scaled_time >= opt.end_time;
     if (series && ((step % 100 == 0) || end)) {
+      const auto t1 = clock::now();
       particles.write(scaled_time + dt * std::sqrt(g / H), *series);
+      print_s = std::chrono::duration<double>(clock::now() - t1).count();
     }
     time += dt;
     if (end) break;
