@@ -132,3 +132,17 @@ def test_titwcsph_full_run_to_the_reference_end_time(gpu_lib, tmp_path):
     assert r1[:nf, 0].max() > 0.95 * poly[:, 0].max()
     assert np.all(np.abs(rho1[:nf] / 1000.0 - 1.0) < 0.02)
     np.testing.assert_array_equal(r1[nf:], r0[nf:])
+
+
+def test_driver_log_lines(gpu_lib):
+    # --log prints the reference's per-step line (wcsph.cpp:172-176): step,
+    # scaled time, and the wall seconds of the previous step and write.
+    exe = gpu_build.build_host()["titwcsph_gpu"]
+    res = subprocess.run([str(exe), "--nx", "10", "--steps", "3", "--log"],
+                         capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    rows = [line.split() for line in res.stdout.splitlines() if line.startswith(" ")]
+    assert [int(r[0]) for r in rows] == [1, 2, 3]
+    times = [float(r[1]) for r in rows]
+    assert times[0] == 0.0 and times[0] < times[1] < times[2]
+    assert all(len(r) == 4 for r in rows)
