@@ -208,8 +208,13 @@ def cpu_sample(budget_s: float, steps: int, threads: int, fill: bool = False) ->
     st = oracle.State(scn)
     nf = scn["tanks"][0]["n_fluid"]
     if fill:
-        # At the largest sample size, more steps fill the time budget.
-        steps = max(steps, min(50, int(budget_s * rate / max(nf, 1))))
+        # At the largest sample size, more steps fill the time budget: one
+        # untimed step at this size gives the rate (the small calibration
+        # case underestimates it: thread start-up dominates there).
+        t0 = time.perf_counter()
+        oracle.step(P, st, 1, nthreads=threads)
+        one = max(time.perf_counter() - t0, 1e-6)
+        steps = max(steps, min(50, int(budget_s / one)))
     t0 = time.perf_counter()
     oracle.step(P, st, steps, nthreads=threads)
     sec = time.perf_counter() - t0
