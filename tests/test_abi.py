@@ -75,3 +75,18 @@ def test_context_without_device_fails_cleanly(gpu_lib):
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _abi.load(tmp_path / "libtitgpu.so")
+
+
+def test_null_context_rejected_by_every_entry(gpu_lib):
+    # Every entry point that takes a context returns TG_ERR_INVALID_ARGUMENT
+    # for a null one, before touching a device.
+    null = None
+    d = ctypes.POINTER(ctypes.c_double)()
+    bad = _abi.TG_ERR_INVALID_ARGUMENT
+    assert gpu_lib.tg_particles_download_state(null, d, d, d, d, d) == bad
+    assert gpu_lib.tg_particles_download(null, 0, d) == bad
+    assert gpu_lib.tg_particles_update(null, d, d, d, d) == bad
+    assert gpu_lib.tg_step(null, 1, d) == bad
+    assert gpu_lib.tg_prepare(null) == bad
+    assert gpu_lib.tg_tank_faces(null, 0, 0, ctypes.POINTER(ctypes.c_int32)(), 0, d) == bad
+    assert gpu_lib.tg_time(null, d) == bad
