@@ -115,6 +115,14 @@ enum {
   TG_FIELD_CS = 6       /* 1, sound speed of the downloaded rho */
 };
 
+/* Equation of state (the closed set of equation_of_state.hpp:127-129). */
+enum {
+  TG_EOS_TAIT = 0,       /* TaitEquationOfState (equation_of_state.hpp:19-72):
+                            p = rho0 cs0^2/xi ((rho/rho0)^xi - 1) */
+  TG_EOS_LINEAR_TAIT = 1 /* LinearTaitEquationOfState (:78-122):
+                            p = cs0^2 (rho - rho0), c = cs0; xi unused */
+};
+
 /* ---- parameter blocks -------------------------------------------------- */
 /* Global physics and numerics.  tg_params_default() fills the reference's
  * values: SixthOrderWendlandKernel (wcsph.cpp:89), xi = 7
@@ -137,7 +145,7 @@ typedef struct tg_params {
   int32_t staging;          /* 2D FP32C: read neighbour windows from
                                shared memory (1) or through L1 (0, default;
                                measured faster on GB300) */
-  int32_t reserved1;
+  int32_t eos;              /* TG_EOS_TAIT (default) | TG_EOS_LINEAR_TAIT */
   double xi;      /* Tait polytropic index */
   double g;       /* gravity, acting along -axis 1 */
   double mu;      /* Morris dynamic viscosity */

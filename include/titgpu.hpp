@@ -14,6 +14,7 @@
  *                                                   field.hpp:172-218
  *   particles.all() / fluid() / fixed()             particle_array.hpp:203-228
  *   TaitEquationOfState{cs_0, rho_0[, xi]}          equation_of_state.hpp:19-72
+ *   LinearTaitEquationOfState{cs_0, rho_0}          equation_of_state.hpp:78-122
  *   FluidEquations{g, mu, domain, containment, eos, kernel}
  *                                                   fluid_equations.hpp:61-69
  *   SSPRKIntegrator{equations, SSPRKOrder::three}   time_integrator.hpp:153-156
@@ -427,11 +428,43 @@ public:
   constexpr auto rho_0() const noexcept -> Num { return rho_0_; }
   constexpr auto xi() const noexcept -> Num { return xi_; }
 
+  static constexpr std::int32_t gpu_id = TG_EOS_TAIT;
+
 private:
   Num cs_0_;
   Num rho_0_;
   Num xi_;
 };
+
+/// Linear Tait equation of state (source/tit/sph/equation_of_state.hpp
+/// :78-122): p = cs_0^2 (rho - rho_0), constant sound speed cs_0.
+template<class Num>
+class LinearTaitEquationOfState {
+public:
+  constexpr LinearTaitEquationOfState(Num cs_0, Num rho_0)
+      : cs_0_{cs_0}, rho_0_{rho_0} {
+    if (!(cs_0 > Num{0}) || !(rho_0 > Num{0})) {
+      throw Exception{"LinearTaitEquationOfState: need cs_0 > 0, rho_0 > 0"};
+    }
+  }
+  auto pressure_from_density(Num rho) const -> Num {
+    return pow2(cs_0_) * (rho - rho_0_);
+  }
+  auto density_from_pressure(Num p) const -> Num {
+    return rho_0_ + p / pow2(cs_0_);
+  }
+  auto sound_speed_from_density(Num /*rho*/) const -> Num { return cs_0_; }
+  constexpr auto cs_0() const noexcept -> Num { return cs_0_; }
+  constexpr auto rho_0() const noexcept -> Num { return rho_0_; }
+  static constexpr std::int32_t gpu_id = TG_EOS_LINEAR_TAIT;
+
+private:
+  Num cs_0_;
+  Num rho_0_;
+};
+
+template<class Num>
+LinearTaitEquationOfState(Num, Num) -> LinearTaitEquationOfState<Num>;
 
 /// Arithmetic form of the GPU pair sums.
 enum class Precision : std::int32_t {
@@ -481,16 +514,20 @@ private:
   double spacing_;
 };
 
-/// Fluid equations (source/tit/sph/fluid_equations.hpp:61-69), particle
-/// walls only.
-template<class Real, std::size_t Dim, class Containment, class Kernel>
+/// Fluid equations (source/tit/sph/fluid_equations.hpp:61-69) with either
+/// equation of state of the reference's closed set.
+template<class Real, std::size_t Dim, class Containment, class EOS, class Kernel>
 class FluidEquations {
+  static_assert(std::is_same_v<EOS, TaitEquationOfState<Real>> ||
+                    std::is_same_v<EOS, LinearTaitEquationOfState<Real>>,
+                "equation_of_state: TaitEquationOfState or LinearTaitEquationOfState");
+
 public:
   FluidEquations(Real g,
                  Real mu,
                  geom::Surface<Vec<Real, Dim>> domain,
                  Containment containment,
-                 TaitEquationOfState<Real> eos,
+                 EOS eos,
                  Kernel /*kernel*/,
                  GpuOptions options = {})
       : g_{g}, mu_{mu}, domain_{std::move(domain)},
@@ -524,7 +561,8 @@ public:
     P.diffusion = options_.diffusion;
     P.kahan = options_.kahan ? 1 : 0;
     P.device = options_.device;
-    P.xi = static_cast<double>(eos_.xi());
+    P.eos = EOS::gpu_id;
+    if constexpr (requires { eos_.xi(); }) P.xi = static_cast<double>(eos_.xi());
     P.g = static_cast<double>(g_);
     P.mu = static_cast<double>(mu_);
     P.alpha = options_.alpha;
@@ -546,7 +584,7 @@ public:
     }
   }
 
-  auto eos() const noexcept -> const TaitEquationOfState<Real>& { return eos_; }
+  auto eos() const noexcept -> const EOS& { return eos_; }
 
 private:
   auto contains_(const Vec<Real, Dim>& x) const -> bool {
@@ -598,19 +636,19 @@ private:
   Real mu_;
   geom::Surface<Vec<Real, Dim>> domain_;
   Containment containment_;
-  TaitEquationOfState<Real> eos_;
+  EOS eos_;
   GpuOptions options_;
 };
 
-template<class Real, std::size_t Dim, class Containment, class Kernel>
+template<class Real, std::size_t Dim, class Containment, class EOS, class Kernel>
 FluidEquations(Real,
                Real,
                geom::Surface<Vec<Real, Dim>>,
                Containment,
-               TaitEquationOfState<Real>,
+               EOS,
                Kernel,
                GpuOptions = {})
-    -> FluidEquations<Real, Dim, Containment, Kernel>;
+    -> FluidEquations<Real, Dim, Containment, EOS, Kernel>;
 
 namespace integrator_detail {
 // One GPU step of a ParticleArray bound to a context.

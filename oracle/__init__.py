@@ -29,7 +29,7 @@ class _Params(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "dim", "precision", "kernel", "integrator", "viscosity", "diffusion",
         "post_integrate", "cells_per_radius", "kahan", "device", "staging",
-        "reserved1")] + [
+        "eos")] + [
         (n, ctypes.c_double) for n in (
             "xi", "g", "mu", "alpha", "delta", "cfl", "c_force", "c_visc")]
 
@@ -57,6 +57,7 @@ def lib():
             "or_kernel_unit_value": (ctypes.c_double, [ctypes.c_int32, ctypes.c_double]),
             "or_kernel_unit_deriv": (ctypes.c_double, [ctypes.c_int32, ctypes.c_double]),
             "or_tait": (None, [ctypes.c_double] * 4 + [_D, _D, _D]),
+            "or_eos": (None, [ctypes.c_int32] + [ctypes.c_double] * 4 + [_D, _D, _D, _D]),
             "or_tait_density_from_potential": (ctypes.c_double, [ctypes.c_double] * 4),
             "or_splitmix64": (ctypes.c_uint64, [ctypes.c_uint64]),
             "or_grid_search": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int64, _D, ctypes.c_double,
@@ -157,6 +158,13 @@ def tait(rho, rho0, cs0, xi=7.0):
     p, c, H = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     lib().or_tait(rho, rho0, cs0, xi, ctypes.byref(p), ctypes.byref(c), ctypes.byref(H))
     return p.value, c.value, H.value
+
+
+def eos(kind: int, rho, rho0, cs0, xi=7.0):
+    """(p, c, H(rho), rho(H(rho))) of TG_EOS_TAIT (0) or TG_EOS_LINEAR_TAIT (1)."""
+    out = [ctypes.c_double() for _ in range(4)]
+    lib().or_eos(kind, rho, rho0, cs0, xi, *(ctypes.byref(o) for o in out))
+    return tuple(o.value for o in out)
 
 
 def density_from_potential(H, rho0, cs0, xi=7.0):

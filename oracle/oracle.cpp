@@ -762,18 +762,25 @@ struct Kern {
 
 struct Tait {
   double rho0, cs0, xi;
+  // LinearTaitEquationOfState (equation_of_state.hpp:78-122): p = cs0^2
+  // (rho - rho0), c = cs0, H = cs0^2 log(rho / rho0).
+  bool linear = false;
   double pressure(double rho) const {
+    if (linear) return pow2(cs0) * (rho - rho0);
     const double B = rho0 * pow2(cs0) / xi;
     return B * (std::pow(rho / rho0, xi) - 1.0);
   }
   double sound_speed(double rho) const {
+    if (linear) return cs0;
     return cs0 * std::pow(rho / rho0, (xi - 1.0) / 2.0);
   }
   double potential(double rho) const {
+    if (linear) return pow2(cs0) * std::log(rho / rho0);
     const double xi_1 = xi - 1.0;
     return pow2(cs0) * (std::pow(rho / rho0, xi_1) - 1.0) / xi_1;
   }
   double density_from_potential(double H) const {
+    if (linear) return rho0 * std::exp(H / pow2(cs0));
     const double xi_1 = xi - 1.0;
     return rho0 * std::pow(1.0 + xi_1 * H / pow2(cs0), 1.0 / xi_1);
   }
@@ -1583,6 +1590,7 @@ bool valid_params(const tg_params* P) {
   if (P->dim != 2 && P->dim != 3) return false;
   if (P->kernel < 0 || P->kernel > 5) return false;
   if (P->integrator < 0 || P->integrator > 3) return false;
+  if (P->eos != TG_EOS_TAIT && P->eos != TG_EOS_LINEAR_TAIT) return false;
   return true;
 }
 
@@ -1612,6 +1620,16 @@ double or_kernel_unit_value(int32_t kernel, double q) {
 
 double or_kernel_unit_deriv(int32_t kernel, double q) {
   return unit_deriv<double>(kernel, q);
+}
+
+void or_eos(int32_t eos, double rho, double rho0, double cs0, double xi,
+            double* p, double* cs, double* potential, double* rho_back) {
+  const Tait E{rho0, cs0, xi, eos == TG_EOS_LINEAR_TAIT};
+  const double H = E.potential(rho);
+  if (p) *p = E.pressure(rho);
+  if (cs) *cs = E.sound_speed(rho);
+  if (potential) *potential = H;
+  if (rho_back) *rho_back = E.density_from_potential(H);
 }
 
 void or_tait(double rho, double rho0, double cs0, double xi, double* p,
@@ -1761,7 +1779,7 @@ int32_t or_wcsph_step_faces(const tg_params* params, int32_t n_tanks,
     T.n = T.nf + T.nw;
     T.h = tanks[t].h;
     T.m = tanks[t].m;
-    T.eos = Tait{tanks[t].rho0, tanks[t].cs0, params->xi};
+    T.eos = Tait{tanks[t].rho0, tanks[t].cs0, params->xi, params->eos == TG_EOS_LINEAR_TAIT};
     T.r = r + base * dim;
     T.v = v + base * dim;
     T.rho = rho + base;

@@ -38,6 +38,10 @@ double or_kernel_unit_value(int32_t kernel, double q);
 double or_kernel_unit_deriv(int32_t kernel, double q);
 
 /* Tait EOS (equation_of_state.hpp:37-64). */
+/* Pressure, sound speed, potential H(rho) and rho(H(rho)) of equation of
+ * state eos (TG_EOS_TAIT or TG_EOS_LINEAR_TAIT). */
+void or_eos(int32_t eos, double rho, double rho0, double cs0, double xi,
+            double* p, double* cs, double* potential, double* rho_back);
 void or_tait(double rho, double rho0, double cs0, double xi, double* p,
              double* cs, double* potential);
 double or_tait_density_from_potential(double H, double rho0, double cs0,

@@ -88,6 +88,17 @@ auto main(int argc, char** argv) -> int {
                        QuarticWendlandKernel{}};
   }));
   CHECK(throws([] { TaitEquationOfState{-1.0, 1000.0}; }));
+  {
+    // The reference's other equation of state (equation_of_state.hpp:78-122).
+    const LinearTaitEquationOfState lin{20.0, 1000.0};
+    CHECK(lin.pressure_from_density(1001.0) == 400.0 * 1.0);
+    CHECK(lin.sound_speed_from_density(1100.0) == 20.0);
+    CHECK(lin.density_from_pressure(400.0) == 1001.0);
+    const FluidEquations linear{9.81, 0.001, domain, geom::AllInside{}, lin,
+                                QuarticWendlandKernel{}};
+    CHECK(linear.eos().cs_0() == 20.0);
+    CHECK(throws([] { LinearTaitEquationOfState{20.0, -1.0}; }));
+  }
 
   // Face walls: tessellation as the reference splits faces and the
   // winding-number containment.

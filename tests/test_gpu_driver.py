@@ -110,6 +110,25 @@ def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting, f
     con.close()
 
 
+def test_driver_linear_tait_matches_oracle(gpu_lib, tmp_path):
+    # titwcsph with LinearTaitEquationOfState{cs_0, rho_0} and face walls.
+    exe = gpu_build.build_host()["titwcsph_gpu"]
+    dump = tmp_path / "state.bin"
+    cmd = [str(exe), "--nx", "20", "--steps", "10", "--faces", "--eos", "linear",
+           "--dump", str(dump)]
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    tank, (r0, v0, rho0), (r1, v1, rho1), t, steps, fc = read_dump(dump)
+    scn = dict(dim=2, tanks=[tank], r=r0.copy(), v=v0.copy(), rho=rho0.copy(), faces=fc)
+    P = physics.reference_params(2)
+    P.eos = _abi.TG_EOS_LINEAR_TAIT
+    P.post_integrate = _abi.TG_POST_SHIFTING
+    o = oracle_run(scn, P, steps)
+    f = np.arange(r0.shape[0]) < tank["n_fluid"]
+    assert rel_l2(r1[f], o.r[f]) <= 1e-9
+    assert rel_l2(rho1[f], o.rho[f]) <= 1e-7
+
+
 def test_titwcsph_full_run_to_the_reference_end_time(gpu_lib, tmp_path):
     # The reference's integration test runs titwcsph to t* = 10
     # (tests/titwcsph/test.cmake:10-16) and compares a platform-specific

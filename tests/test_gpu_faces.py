@@ -51,6 +51,15 @@ def test_faces_other_kernels_and_term_sets(gpu_lib, kernel):
     _compare(scn, physics.baseline_params(2, kernel=kernel), 2, 1e-10)
 
 
+def test_faces_linear_tait(gpu_lib):
+    scn = scenarios.dam_break_2d_faces(nx_per_H=16)
+    P = physics.reference_params(2)
+    P.eos = _abi.TG_EOS_LINEAR_TAIT
+    P.post_integrate = _abi.TG_POST_SHIFTING
+    _compare(scn, P, 1, 1e-11, 1e-9)
+    _compare(scn, P, 3, 1e-10)
+
+
 @pytest.mark.parametrize("integrator", (_abi.TG_EULER, _abi.TG_VERLET, _abi.TG_SSPRK2))
 def test_faces_other_integrators(gpu_lib, integrator):
     scn = scenarios.dam_break_2d_faces(nx_per_H=16)

@@ -152,6 +152,36 @@ def test_download_state_matches_field_downloads(gpu_lib, dim, precision):
     np.testing.assert_array_equal(only_r, g["r"])
 
 
+@pytest.mark.parametrize("dim", (2, 3))
+def test_linear_tait_equation_of_state(gpu_lib, dim):
+    # LinearTaitEquationOfState (equation_of_state.hpp:78-122) in both forms:
+    # the plain form against the oracle at the one-step tolerances, the
+    # compensated form after 30 steps.
+    scn = scenarios.dam_break_2d(nx_per_H=20) if dim == 2 else scenarios.dam_break_3d(nx_per_H=6)
+    P = physics.reference_params(dim)
+    P.eos = _abi.TG_EOS_LINEAR_TAIT
+    _compare(scn, P, 1, 1e-12, 1e-9)
+    _compare(scn, P, 5, 1e-10)
+    if dim == 2:
+        P32 = physics.reference_params(dim, precision=_abi.TG_FP32C)
+        P32.eos = _abi.TG_EOS_LINEAR_TAIT
+        o = oracle_run(scn, P, 30)
+        f = fluid_mask(scn)
+        with gpu_context(scn, P32) as ctx:
+            ctx.step(30)
+            g = gpu_state(ctx)
+        assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5
+        assert rel_l2(g["r"][f], o.r[f]) <= 1e-6
+        # The pressure download follows the linear law.
+        with gpu_context(scn, P) as ctx:
+            rho = ctx.download(_abi.TG_FIELD_RHO)
+            p = ctx.download(_abi.TG_FIELD_P)
+            c = ctx.download(_abi.TG_FIELD_CS)
+        cs0 = scn["tanks"][0]["cs0"]
+        np.testing.assert_allclose(p, cs0 ** 2 * (rho - 1000.0), rtol=1e-12, atol=1e-9)
+        np.testing.assert_array_equal(c, np.full_like(c, cs0))
+
+
 def test_update_round_trip_continues_the_run(gpu_lib):
     scn = scenarios.dam_break_2d(nx_per_H=20)
     P = physics.baseline_params(2)

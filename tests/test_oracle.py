@@ -127,6 +127,20 @@ def test_tait_round_trip():
         assert oracle.density_from_potential(H, rho0, cs0, 7.0) == pytest.approx(rho, rel=1e-13)
 
 
+def test_linear_tait_equation_of_state():
+    # LinearTaitEquationOfState (equation_of_state.hpp:91-115): p = cs0^2
+    # (rho - rho0), c = cs0, H = cs0^2 log(rho / rho0), rho(H) = rho0 e^(H/cs0^2).
+    rho0, cs0 = 1000.0, 31.32
+    for rho in (990.0, 1000.0, 1003.7, 1020.0):
+        p, c, H, back = oracle.eos(1, rho, rho0, cs0)
+        assert p == pytest.approx(cs0 ** 2 * (rho - rho0), rel=1e-14, abs=1e-12)
+        assert c == cs0
+        assert H == pytest.approx(cs0 ** 2 * math.log(rho / rho0), rel=1e-13, abs=1e-12)
+        assert back == pytest.approx(rho, rel=1e-14)
+        # The Tait form through the same entry.
+        assert oracle.eos(0, rho, rho0, cs0)[:3] == oracle.tait(rho, rho0, cs0, 7.0)
+
+
 def _rows(off, idx):
     return [list(idx[off[i]:off[i + 1]]) for i in range(len(off) - 1)]
 

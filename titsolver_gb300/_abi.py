@@ -39,6 +39,7 @@ TG_SSPRK3, TG_SSPRK2, TG_EULER, TG_VERLET = range(4)
 TG_VISC_MORRIS, TG_VISC_MONAGHAN = 0, 1
 TG_DIFF_FERRARI, TG_DIFF_MOLTENI, TG_DIFF_NONE = 0, 1, 2
 TG_POST_PREPARE, TG_POST_SHIFTING = 0, 1
+TG_EOS_TAIT, TG_EOS_LINEAR_TAIT = 0, 1
 (TG_FIELD_R, TG_FIELD_V, TG_FIELD_RHO, TG_FIELD_DRHO_DT, TG_FIELD_DV_DT,
  TG_FIELD_P, TG_FIELD_CS) = range(7)
 
@@ -58,7 +59,7 @@ class TgParams(ctypes.Structure):
         ("kahan", ctypes.c_int32),
         ("device", ctypes.c_int32),
         ("staging", ctypes.c_int32),
-        ("reserved1", ctypes.c_int32),
+        ("eos", ctypes.c_int32),
         ("xi", ctypes.c_double),
         ("g", ctypes.c_double),
         ("mu", ctypes.c_double),

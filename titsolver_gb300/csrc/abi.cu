@@ -160,6 +160,10 @@ bool valid_params(const tg_params* P, std::string* why) {
     *why = "unknown diffusion model";
     return false;
   }
+  if (P->eos != TG_EOS_TAIT && P->eos != TG_EOS_LINEAR_TAIT) {
+    *why = "unknown equation of state";
+    return false;
+  }
   if (P->post_integrate != TG_POST_PREPARE &&
       P->post_integrate != TG_POST_SHIFTING) {
     *why = "unknown post_integrate mode";
@@ -281,6 +285,7 @@ int tg_context_create(const tg_params* params, tg_context** out) {
   C.phys.c_force = params->c_force;
   C.phys.c_visc = params->c_visc;
   C.phys.xi_is_7 = params->xi == 7.0 ? 1 : 0;
+  C.phys.eos = params->eos;
   C.phys.viscosity = params->viscosity;
   C.phys.diffusion = params->diffusion;
   C.phys.kernel = params->kernel;

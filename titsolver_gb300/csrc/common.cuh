@@ -67,6 +67,7 @@ struct PhysDev {
   double alpha;
   double cfl, c_force, c_visc;
   int32_t xi_is_7;
+  int32_t eos;  // TG_EOS_*
   int32_t viscosity;
   int32_t diffusion;
   int32_t kernel;
@@ -327,6 +328,12 @@ struct EosOut {
 
 __device__ __forceinline__ void tait_f64(const PhysDev& P, const TankDev& T,
                                          double rho, double& p, double& c) {
+  if (P.eos == TG_EOS_LINEAR_TAIT) {
+    // LinearTaitEquationOfState (equation_of_state.hpp:91-105).
+    p = T.cs0 * T.cs0 * (rho - T.rho0);
+    c = T.cs0;
+    return;
+  }
   const double x = rho / T.rho0;
   if (P.xi_is_7) {
     const double x2 = x * x;
@@ -341,6 +348,7 @@ __device__ __forceinline__ void tait_f64(const PhysDev& P, const TankDev& T,
 
 __device__ __forceinline__ double potential_f64(const PhysDev& P,
                                                 const TankDev& T, double rho) {
+  if (P.eos == TG_EOS_LINEAR_TAIT) return T.cs0 * T.cs0 * log(rho / T.rho0);
   const double x = rho / T.rho0;
   if (P.xi_is_7) {
     const double x2 = x * x;
@@ -352,6 +360,7 @@ __device__ __forceinline__ double potential_f64(const PhysDev& P,
 
 __device__ __forceinline__ double density_from_potential_f64(
     const PhysDev& P, const TankDev& T, double H) {
+  if (P.eos == TG_EOS_LINEAR_TAIT) return T.rho0 * exp(H / (T.cs0 * T.cs0));
   const double xi_1 = P.xi - 1.0;
   return T.rho0 * pow(1.0 + xi_1 * H / (T.cs0 * T.cs0), 1.0 / xi_1);
 }
@@ -359,6 +368,11 @@ __device__ __forceinline__ double density_from_potential_f64(
 // Compensated form: d = drho / rho0 in FP32.
 __device__ __forceinline__ void tait_f32(const PhysDev& P, const TankDev& T,
                                          float drho, float& p, float& c) {
+  if (P.eos == TG_EOS_LINEAR_TAIT) {
+    p = T.c02_f * drho;
+    c = T.cs0_f;
+    return;
+  }
   const float d = __fdividef(drho, T.rho0_f);
   const float B = T.B_f;
   const float c0 = T.cs0_f;
@@ -379,6 +393,7 @@ __device__ __forceinline__ float potential_f32(const PhysDev& P,
                                                const TankDev& T, float drho) {
   const float d = __fdividef(drho, T.rho0_f);
   const float c02 = T.c02_f;
+  if (P.eos == TG_EOS_LINEAR_TAIT) return c02 * log1pf(d);
   if (P.xi_is_7) {
     const float poly =
         6.f + d * (15.f + d * (20.f + d * (15.f + d * (6.f + d))));
@@ -391,6 +406,7 @@ __device__ __forceinline__ float potential_f32(const PhysDev& P,
 // Returns the density deviation rho - rho0.
 __device__ __forceinline__ float deviation_from_potential_f32(
     const PhysDev& P, const TankDev& T, float H) {
+  if (P.eos == TG_EOS_LINEAR_TAIT) return T.rho0_f * expm1f(H / T.c02_f);
   const float xi_1 = P.xi_f - 1.f;
   const float u = xi_1 * H / T.c02_f;
   return T.rho0_f * expm1f(log1pf(u) / xi_1);

@@ -8,7 +8,7 @@
 // Usage: titwcsph_gpu [--nx N] [--steps S] [--end-time T] [--fp32c]
 //                     [--integrator ssprk3|ssprk2|euler|verlet]
 //                     [--no-shifting] [--faces] [--ttdb FILE] [--dump FILE]
-//                     [--log]
+//                     [--log] [--eos tait|linear]
 //   --nx       particles per column height H (default 80, as wcsph.cpp:42)
 //   --steps    stop after S steps (default: run to scaled time T)
 //   --end-time scaled end time t sqrt(g/H) (default 10, as wcsph.cpp:183)
@@ -19,6 +19,8 @@
 //   --faces    the reference's face walls
 //   --ttdb     write frames every 100 steps to this .ttdb file
 //   --dump     write the initial and final state as raw binary (see below)
+//   --eos      equation of state: TaitEquationOfState (default, as
+//              wcsph.cpp:83) or LinearTaitEquationOfState
 //   --log      print the reference's per-step line: step, scaled time, wall
 //              seconds of the previous step and of the previous write
 //              (wcsph.cpp:172-176)
@@ -57,6 +59,7 @@ struct Options {
   std::string ttdb;
   std::string dump;
   bool log = false;
+  std::string eos = "tait";
 };
 
 auto parse(int argc, char** argv) -> Options {
@@ -77,9 +80,11 @@ auto parse(int argc, char** argv) -> Options {
     else if (a == "--ttdb") o.ttdb = next();
     else if (a == "--dump") o.dump = next();
     else if (a == "--log") o.log = true;
+    else if (a == "--eos") o.eos = next();
     else throw Exception{"unknown option " + a};
   }
   if (o.nx < 4) throw Exception{"--nx must be at least 4"};
+  if (o.eos != "tait" && o.eos != "linear") throw Exception{"unknown --eos " + o.eos};
   if (o.integrator != "ssprk3" && o.integrator != "ssprk2" &&
       o.integrator != "euler" && o.integrator != "verlet") {
     throw Exception{"unknown integrator " + o.integrator};
@@ -112,15 +117,11 @@ template<class Real, class Equations>
 auto run_integrator(const Options& opt, const Equations& equations,
                     const geom::Surface<Vec<Real, 2>>* domain) -> int;
 
-template<class Real>
-auto sph_main(int argc, char** argv) -> int {
-  const Options opt = parse(argc, argv);
-
+template<class Real, class EOS>
+auto sph_main_eos(const Options& opt, const EOS& eos) -> int {
   constexpr Real H = 0.6; // Water column height.
 
   constexpr Real g = 9.81;
-  constexpr Real rho_0 = 1000.0;
-  const Real cs_0 = 20 * std::sqrt(g * H);
   constexpr Real mu = 0.001;
 
   GpuOptions gpu;
@@ -154,8 +155,7 @@ auto sph_main(int argc, char** argv) -> int {
     const geom::MakeFastWinding<Real> make_winding;
     const auto containment = make_winding(domain2);
     const FluidEquations equations{
-        g, mu, domain, containment, TaitEquationOfState{cs_0, rho_0},
-        SixthOrderWendlandKernel{}, gpu,
+        g, mu, domain, containment, eos, SixthOrderWendlandKernel{}, gpu,
     };
     return run_integrator<Real>(opt, equations, &domain);
   }
@@ -170,12 +170,25 @@ auto sph_main(int argc, char** argv) -> int {
       domain,
       geom::AllInside{},
       // Weakly compressible equation of state.
-      TaitEquationOfState{cs_0, rho_0},
+      eos,
       // C4 Wendland's spline kernel.
       SixthOrderWendlandKernel{},
       gpu,
   };
   return run_integrator<Real>(opt, equations, nullptr);
+}
+
+template<class Real>
+auto sph_main(int argc, char** argv) -> int {
+  const Options opt = parse(argc, argv);
+  constexpr Real H = 0.6;
+  constexpr Real g = 9.81;
+  constexpr Real rho_0 = 1000.0;
+  const Real cs_0 = 20 * std::sqrt(g * H);
+  if (opt.eos == "linear") {
+    return sph_main_eos<Real>(opt, LinearTaitEquationOfState{cs_0, rho_0});
+  }
+  return sph_main_eos<Real>(opt, TaitEquationOfState{cs_0, rho_0});
 }
 
 template<class Real, class Equations>
