@@ -347,6 +347,13 @@ struct GridSearch {
   }
 };
 
+/// K-dimensional tree search (source/tit/geom/search/kd_tree_search.hpp
+/// :151-165).  The neighbour sets are those of the inclusive sphere
+/// predicate whatever the index, so on the GPU it selects the grid search
+/// with the library's default cells per support radius.
+struct KDTreeSearch {};
+inline constexpr KDTreeSearch kd_tree_indexing{};
+
 /// Face search and partitioners of the reference mesh.  The GPU path has no
 /// faces and sums in gather form, so these only record the driver's choice.
 struct GridFaceSearch {
@@ -508,6 +515,10 @@ public:
   template<class... Rest>
   explicit ParticleMesh(geom::GridSearch search, Rest&&... /*rest*/) noexcept
       : spacing_{search.spacing} {}
+  template<class... Rest>
+  explicit ParticleMesh(geom::KDTreeSearch /*search*/, Rest&&... /*rest*/) noexcept
+      : spacing_{0.0} {}
+  /// Grid search spacing (0: the library's default grid, as for a k-d tree).
   auto spacing() const noexcept -> double { return spacing_; }
 
 private:
@@ -570,10 +581,13 @@ public:
     P.cfl = options_.cfl;
     P.c_force = options_.c_force;
     P.c_visc = options_.c_visc;
-    // Cells of the grid search's spacing across the support radius.
-    const double radius = Kernel::unit_radius * particles.uniform_h();
-    const long k = std::lround(radius / mesh.spacing());
-    P.cells_per_radius = static_cast<std::int32_t>(k < 1 ? 1 : (k > 3 ? 3 : k));
+    // Cells of the grid search's spacing across the support radius (the
+    // default grid for a k-d tree search).
+    if (mesh.spacing() > 0.0) {
+      const double radius = Kernel::unit_radius * particles.uniform_h();
+      const long k = std::lround(radius / mesh.spacing());
+      P.cells_per_radius = static_cast<std::int32_t>(k < 1 ? 1 : (k > 3 ? 3 : k));
+    }
     particles.attach_(P,
                       static_cast<double>(eos_.rho_0()),
                       static_cast<double>(eos_.cs_0()),

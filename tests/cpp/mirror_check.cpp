@@ -176,6 +176,12 @@ auto main(int argc, char** argv) -> int {
     CHECK(std::abs(make_winding(t)(Vec{1.0, 0.5, 0.25}) - 1.0) < 1e-12);
   }
   CHECK(throws([] { geom::GridSearch{0.0}; }));
+  // A k-d tree search selects the default GPU grid (same neighbour sets).
+  CHECK(ParticleMesh{geom::kd_tree_indexing}.spacing() == 0.0);
+  {
+    const ParticleMesh kd_mesh{geom::KDTreeSearch{}, geom::GridFaceSearch{0.1}};
+    CHECK(kd_mesh.spacing() == 0.0);
+  }
 
   // A fluid particle outside the containment is refused before any device
   // call; mixed masses too.
