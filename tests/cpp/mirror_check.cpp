@@ -2,6 +2,8 @@
 // (titgpu_data.hpp); no kernel runs.  Writes a storage to argv[1] for the
 // Python side to read back.  Prints "ok" and exits 0 when every check holds.
 
+#include <array>
+#include <cmath>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -135,6 +137,80 @@ auto main(int argc, char** argv) -> int {
                          TaitEquationOfState{20.0, 1000.0}, SixthOrderWendlandKernel{}};
     }));
   }
+  // geom::tessellate against the reference's known answers
+  // (geom/tessellation.test.cpp): a 3-4-5 triangle outline at d_max = 1, and
+  // red refinement of a tetrahedron at d_max = 2, uniform and with the z edge
+  // twice as long (vertex order and face order included).
+  {
+    const auto same_verts = [](const auto& surf, const auto& want) {
+      if (surf.num_verts() != want.size()) return false;
+      for (std::size_t i = 0; i < want.size(); ++i) {
+        for (std::size_t k = 0; k < want[i].size(); ++k) {
+          if (std::abs(surf.vert(i)[k] - want[i][k]) > 1e-12) return false;
+        }
+      }
+      return true;
+    };
+    const auto same_faces = [](const auto& surf, const auto& want) {
+      if (surf.num_faces() != want.size()) return false;
+      for (std::size_t i = 0; i < want.size(); ++i) {
+        const auto f = surf.face_verts(i);
+        for (std::size_t k = 0; k < want[i].size(); ++k) {
+          if (f[k] != want[i][k]) return false;
+        }
+      }
+      return true;
+    };
+    geom::Surface<Vec<double, 2>> tri;
+    tri.append_vert({0.0, 0.0});
+    tri.append_vert({3.0, 0.0});
+    tri.append_vert({0.0, 4.0});
+    tri.append_face({0, 1});
+    tri.append_face({1, 2});
+    tri.append_face({2, 0});
+    const auto t2 = geom::tessellate(tri, 1.0);
+    const std::vector<std::array<double, 2>> v2 = {
+        {0.0, 0.0}, {3.0, 0.0}, {0.0, 4.0}, {1.0, 0.0}, {2.0, 0.0}, {2.4, 0.8},
+        {1.8, 1.6}, {1.2, 2.4}, {0.6, 3.2}, {0.0, 3.0}, {0.0, 2.0}, {0.0, 1.0}};
+    const std::vector<std::array<std::size_t, 2>> f2 = {
+        {0, 3}, {3, 4}, {4, 1}, {1, 5}, {5, 6}, {6, 7},
+        {7, 8}, {8, 2}, {2, 9}, {9, 10}, {10, 11}, {11, 0}};
+    CHECK(same_verts(t2, v2) && same_faces(t2, f2));
+    const auto tetra = [](double z) {
+      geom::Surface<Vec<double, 3>> t;
+      t.append_vert({0.0, 0.0, 0.0});
+      t.append_vert({2.0, 0.0, 0.0});
+      t.append_vert({0.0, 2.0, 0.0});
+      t.append_vert({0.0, 0.0, z});
+      t.append_face({0, 2, 1});
+      t.append_face({0, 1, 3});
+      t.append_face({0, 3, 2});
+      t.append_face({1, 2, 3});
+      return t;
+    };
+    const auto u = geom::tessellate(tetra(2.0), 2.0);
+    const std::vector<std::array<double, 3>> uv = {
+        {0.0, 0.0, 0.0}, {2.0, 0.0, 0.0}, {0.0, 2.0, 0.0}, {0.0, 0.0, 2.0},
+        {1.0, 1.0, 0.0}, {1.0, 0.0, 1.0}, {0.0, 1.0, 1.0}};
+    const std::vector<std::array<std::size_t, 3>> uf = {
+        {2, 4, 0}, {4, 1, 0}, {1, 5, 0}, {5, 3, 0}, {3, 6, 0},
+        {6, 2, 0}, {1, 4, 5}, {4, 2, 6}, {5, 6, 3}, {4, 6, 5}};
+    CHECK(same_verts(u, uv) && same_faces(u, uf));
+    const auto zl = geom::tessellate(tetra(4.0), 2.0);
+    const std::vector<std::array<double, 3>> zv = {
+        {0.0, 0.0, 0.0}, {2.0, 0.0, 0.0}, {0.0, 2.0, 0.0}, {0.0, 0.0, 4.0},
+        {1.0, 1.0, 0.0}, {1.0, 0.0, 2.0}, {0.0, 0.0, 2.0}, {0.0, 1.0, 2.0},
+        {1.5, 0.0, 1.0}, {0.5, 0.0, 1.0}, {0.5, 0.0, 3.0}, {0.0, 1.0, 1.0},
+        {0.0, 1.5, 1.0}, {0.0, 0.5, 3.0}, {1.0, 0.5, 1.0}, {0.5, 1.0, 1.0}};
+    const std::vector<std::array<std::size_t, 3>> zf = {
+        {2, 4, 0},   {4, 1, 0},   {1, 8, 0},   {8, 9, 0},   {8, 5, 9},   {0, 9, 6},
+        {9, 5, 6},   {5, 10, 6},  {10, 3, 6},  {6, 11, 0},  {11, 2, 0},  {7, 12, 6},
+        {12, 11, 6}, {12, 2, 11}, {3, 13, 6},  {13, 7, 6},  {4, 14, 1},  {14, 8, 1},
+        {14, 5, 8},  {2, 12, 4},  {12, 15, 4}, {12, 7, 15}, {7, 13, 5},  {13, 10, 5},
+        {13, 3, 10}, {5, 14, 7},  {14, 15, 7}, {14, 4, 15}};
+    CHECK(same_verts(zl, zv) && same_faces(zl, zf));
+  }
+
   // 3D face walls: red refinement of a box keeps it closed and oriented,
   // with every edge at most d_max; the winding number of the outward box.
   {
