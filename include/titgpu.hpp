@@ -267,19 +267,41 @@ auto tessellate(const Surface<V>& surf, double d_max) -> Surface<V> {
 }
 
 /// Containment by the winding number of a closed surface (> 1/2 inside),
-/// the role of the reference's FastWinding (fast_winding.hpp:80-95): in 2D
-/// a closed polygon (the faces' first vertices in order), in 3D a closed
-/// triangle mesh with outward normals.  The GPU receives the surface
-/// itself (surface_data: 2 doubles per polygon vertex or 9 per triangle).
+/// the role of the reference's FastWinding (fast_winding.hpp:80-95): the
+/// exact generalized winding number, summed per face (Segment / Triangle
+/// ::winding_number), so the faces may come in any order.  The GPU receives
+/// the surface itself (surface_data: in 2D the vertices of the closed loop
+/// the segments chain into, in 3D 9 doubles per triangle).
 template<class V>
 class Winding {
 public:
   explicit Winding(const Surface<V>& surf) {
     for (std::size_t fi = 0; fi < surf.num_faces(); ++fi) {
-      if constexpr (V::dim() == 2) {
-        pts_.push_back(surf.vert(surf.face_verts(fi)[0]));
-      } else {
-        for (const auto v : surf.face_verts(fi)) pts_.push_back(surf.vert(v));
+      for (const auto v : surf.face_verts(fi)) pts_.push_back(surf.vert(v));
+    }
+    if constexpr (V::dim() == 2) {
+      // Chain the segments into one closed loop for the GPU.
+      if (surf.num_faces() == 0) return;
+      std::vector<std::size_t> next(surf.num_verts(), static_cast<std::size_t>(-1));
+      for (std::size_t fi = 0; fi < surf.num_faces(); ++fi) {
+        const auto [a, b] = surf.face_verts(fi);
+        if (next[a] != static_cast<std::size_t>(-1)) {
+          throw Exception{"Winding: a 2D containment vertex starts two segments"};
+        }
+        next[a] = b;
+      }
+      const std::size_t start = surf.face_verts(0)[0];
+      std::size_t v = start;
+      for (std::size_t k = 0; k < surf.num_faces(); ++k) {
+        loop_.push_back(surf.vert(v));
+        v = next[v];
+        if (v == static_cast<std::size_t>(-1)) {
+          throw Exception{"Winding: the 2D containment segments do not close"};
+        }
+        if (v == start) break;
+      }
+      if (v != start || loop_.size() != surf.num_faces()) {
+        throw Exception{"Winding: the 2D containment must be one closed loop"};
       }
     }
   }
@@ -287,8 +309,8 @@ public:
     constexpr double two_pi = 2.0 * 3.14159265358979323846;
     double w = 0.0;
     if constexpr (V::dim() == 2) {
-      for (std::size_t i = 0; i < pts_.size(); ++i) {
-        const V a = pts_[i] - x, b = pts_[(i + 1) % pts_.size()] - x;
+      for (std::size_t i = 0; i < pts_.size(); i += 2) {
+        const V a = pts_[i] - x, b = pts_[i + 1] - x;
         w += std::atan2(static_cast<double>(a[0] * b[1] - a[1] * b[0]),
                         static_cast<double>(a[0] * b[0] + a[1] * b[1]));
       }
@@ -315,16 +337,17 @@ public:
   auto contains(const V& x) const -> bool { return (*this)(x) > 0.5; }
   auto surface_data() const -> std::vector<double> {
     std::vector<double> out;
-    for (const V& v : pts_) {
+    for (const V& v : V::dim() == 2 ? loop_ : pts_) {
       for (std::size_t k = 0; k < V::dim(); ++k) out.push_back(static_cast<double>(v[k]));
     }
     return out;
   }
-  /// The 2D polygon's vertices (x, y), as surface_data.
+  /// The 2D loop's vertices (x, y), as surface_data.
   auto polygon() const -> std::vector<double> { return surface_data(); }
 
 private:
-  std::vector<V> pts_;
+  std::vector<V> pts_;   // the faces' vertices, dim per face
+  std::vector<V> loop_;  // 2D: the chained loop
 };
 
 /// Maker of winding-number containment functions (the reference's

@@ -211,6 +211,81 @@ auto main(int argc, char** argv) -> int {
     CHECK(same_verts(zl, zv) && same_faces(zl, zf));
   }
 
+  // Winding containment against the reference's known answers
+  // (geom/winding.test.cpp): the unit square with its faces listed forwards
+  // and backwards (the same counter-clockwise loop), the outward tetrahedron
+  // and its reversal, coarse and tessellated at 0.05; a degenerate pair of
+  // faces winds 0.
+  {
+    const geom::MakeFastWinding<double> make_winding;
+    const auto square = [](bool reverse) {
+      geom::Surface<Vec<double, 2>> s;
+      s.append_vert({0.0, 0.0});
+      s.append_vert({1.0, 0.0});
+      s.append_vert({1.0, 1.0});
+      s.append_vert({0.0, 1.0});
+      if (reverse) {
+        s.append_face({3, 0});
+        s.append_face({2, 3});
+        s.append_face({1, 2});
+        s.append_face({0, 1});
+      } else {
+        s.append_face({0, 1});
+        s.append_face({1, 2});
+        s.append_face({2, 3});
+        s.append_face({3, 0});
+      }
+      return s;
+    };
+    const auto tetra = [](bool reverse) {
+      geom::Surface<Vec<double, 3>> s;
+      s.append_vert({0.0, 0.0, 0.0});
+      s.append_vert({1.0, 0.0, 0.0});
+      s.append_vert({0.0, 1.0, 0.0});
+      s.append_vert({0.0, 0.0, 1.0});
+      if (reverse) {
+        s.append_face({0, 1, 2});
+        s.append_face({0, 3, 1});
+        s.append_face({0, 2, 3});
+        s.append_face({1, 3, 2});
+      } else {
+        s.append_face({0, 2, 1});
+        s.append_face({0, 1, 3});
+        s.append_face({0, 3, 2});
+        s.append_face({1, 2, 3});
+      }
+      return s;
+    };
+    for (const bool reverse : {false, true}) {
+      const double sign = reverse ? -1.0 : 1.0;
+      for (const auto& sq : {square(reverse), geom::tessellate(square(reverse), 0.05)}) {
+        const auto w = make_winding(sq);
+        CHECK(std::abs(w(Vec{0.5, 0.5}) - 1.0) < 1e-12);
+        CHECK(std::abs(w(Vec{0.1, 0.1}) - 1.0) < 1e-12);
+        CHECK(std::abs(w(Vec{1.5, 0.5})) < 1e-12 && std::abs(w(Vec{100.0, 100.0})) < 1e-12);
+        CHECK(w.contains(Vec{0.9, 0.75}));
+        CHECK(w.surface_data().size() == 2 * sq.num_faces());
+      }
+      for (const auto& te : {tetra(reverse), geom::tessellate(tetra(reverse), 0.05)}) {
+        const auto w = make_winding(te);
+        CHECK(std::abs(w(Vec{0.25, 0.25, 0.25}) - sign) < 1e-12);
+        CHECK(std::abs(w(Vec{0.1, 0.1, 0.1}) - sign) < 1e-12);
+        CHECK(std::abs(w(Vec{1.0, 1.0, 1.0})) < 1e-12);
+        CHECK(std::abs(w(Vec{3.0, 2.0, 1.0})) < 1e-12);
+        CHECK(w.contains(Vec{0.25, 0.25, 0.25}) == !reverse);
+        CHECK(!w.contains(Vec{100.0, 100.0, 100.0}));
+      }
+    }
+    geom::Surface<Vec<double, 3>> flat;
+    flat.append_vert({0.0, 0.0, 0.0});
+    flat.append_vert({1.0, 0.0, 0.0});
+    flat.append_vert({2.0, 0.0, 0.0});
+    flat.append_face({0, 1, 2});
+    flat.append_face({2, 1, 0});
+    CHECK(std::abs(make_winding(flat)(Vec{0.0, 1.0, 0.0})) < 1e-12);
+    CHECK(std::abs(make_winding(geom::Surface<Vec<double, 2>>{})(Vec{0.0, 0.0})) < 1e-12);
+  }
+
   // 3D face walls: red refinement of a box keeps it closed and oriented,
   // with every edge at most d_max; the winding number of the outward box.
   {
