@@ -89,6 +89,8 @@ def lib():
                                                            ctypes.c_double]),
             "or_winding_number3": (ctypes.c_double, [ctypes.c_int32, _D, _D]),
             "or_triangle_in_sphere": (ctypes.c_int32, [_D, _D, _D, _D, ctypes.c_double]),
+            "or_triangle_clamp": (None, [_D, _D, _D, _D, _D]),
+            "or_triangle_project": (None, [_D, _D, _D, _D, _D]),
             "or_tank_neighbour_counts": (ctypes.c_int32, [ctypes.POINTER(_Params), ctypes.c_int32,
                                                           ctypes.POINTER(_Tank), _D, _I32, _U64,
                                                           ctypes.c_int32]),
@@ -331,6 +333,24 @@ def triangle_in_sphere(a, b, c, x, radius: float) -> bool:
     return bool(lib().or_triangle_in_sphere(_p(A, ctypes.c_double), _p(B, ctypes.c_double),
                                             _p(C, ctypes.c_double), _p(X, ctypes.c_double),
                                             radius))
+
+
+def triangle_clamp(a, b, c, x) -> np.ndarray:
+    out = np.zeros(3)
+    A, B, C, X = (np.ascontiguousarray(u, dtype=np.float64) for u in (a, b, c, x))
+    lib().or_triangle_clamp(_p(A, ctypes.c_double), _p(B, ctypes.c_double),
+                            _p(C, ctypes.c_double), _p(X, ctypes.c_double),
+                            _p(out, ctypes.c_double))
+    return out
+
+
+def triangle_project(a, b, c, origin) -> np.ndarray:
+    out = np.zeros(6)
+    A, B, C, O = (np.ascontiguousarray(u, dtype=np.float64) for u in (a, b, c, origin))
+    lib().or_triangle_project(_p(A, ctypes.c_double), _p(B, ctypes.c_double),
+                              _p(C, ctypes.c_double), _p(O, ctypes.c_double),
+                              _p(out, ctypes.c_double))
+    return out.reshape(3, 2)
 
 
 def tank_neighbour_counts(params, tanks, r: np.ndarray, nthreads: int = 0):

@@ -1837,6 +1837,17 @@ int32_t or_triangle_in_sphere(const double* a, const double* b, const double* c,
   return tri_in_sphere(a, b, c, x, radius) ? 1 : 0;
 }
 
+void or_triangle_clamp(const double* a, const double* b, const double* c,
+                       const double* x, double* out) {
+  tri_clamp(a, b, c, x, out);
+}
+
+void or_triangle_project(const double* a, const double* b, const double* c,
+                         const double* origin, double* out) {
+  const TriFrame F = tri_frame(a, b, c, origin, 1.0);
+  for (int i = 0; i < 6; ++i) out[i] = F.p[i];
+}
+
 int32_t or_tank_neighbour_counts(const tg_params* params, int32_t n_tanks,
                                  const tg_tank* tanks, const double* r,
                                  int32_t* counts, uint64_t* hashes,

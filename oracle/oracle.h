@@ -128,6 +128,12 @@ double or_kernel_antigrad_flux3(int32_t kernel, const double* a,
 double or_winding_number3(int32_t n_tris, const double* tris, const double* x);
 int32_t or_triangle_in_sphere(const double* a, const double* b, const double* c,
                               const double* x, double radius);
+/* Triangle::clamp (closest point, 3 doubles) and Triangle::project (the
+ * vertices in the plane frame around origin, 6 doubles). */
+void or_triangle_clamp(const double* a, const double* b, const double* c,
+                       const double* x, double* out);
+void or_triangle_project(const double* a, const double* b, const double* c,
+                         const double* origin, double* out);
 
 /* Neighbour counts and hashes of every particle in its tank (tank-local ids),
  * via or_grid_search with radius = unit_radius * h. */

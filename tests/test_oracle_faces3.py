@@ -214,3 +214,44 @@ def test_3d_face_scenario_steps():
     assert all(oracle.winding_number3(poly, x) > 0.5 for x in st.r[:nf])
     assert st.r[:nf, 0].max() > scn["r"][:nf, 0].max()
     np.testing.assert_array_equal(st.r[nf:], scn["r"][nf:])
+
+
+def test_triangle_geometry_known_answers():
+    # geom/triangle.test.cpp: winding number of the unit-simplex face seen
+    # from the origin (1/8 of the sphere), its flip, translation and scale;
+    # the projection around the face centre; the closest points.
+    a, b, c = np.eye(3)
+    o = np.zeros(3)
+    assert abs(oracle.winding_number3(np.array([[a, b, c]]), o) - 0.125) < 1e-14
+    assert abs(oracle.winding_number3(np.array([[c, b, a]]), o) + 0.125) < 1e-14
+    off = np.array([3.0, 4.0, 5.0])
+    assert abs(oracle.winding_number3(np.array([[a + off, b + off, c + off]]), off) - 0.125) < 1e-14
+    assert abs(oracle.winding_number3(np.array([[2 * a, 2 * b, 2 * c]]), o) - 0.125) < 1e-14
+    s2, s3 = math.sqrt(2.0), math.sqrt(3.0)
+    p = oracle.triangle_project(a, b, c, (a + b + c) / 3.0)
+    np.testing.assert_allclose(p, [[-1 / s2, -1 / (s2 * s3)], [1 / s2, -1 / (s2 * s3)],
+                                   [0.0, s2 / s3]], atol=1e-14)
+    A, B, C = np.array([0.0, 0, 0]), np.array([2.0, 0, 0]), np.array([0.0, 2, 0])
+    cases = [((-1, -1, 0), (0, 0, 0)), ((-0.5, -0.5, 5), (0, 0, 0)),
+             ((3, -1, 0), (2, 0, 0)), ((2.5, -0.5, -3), (2, 0, 0)),
+             ((-1, 3, 0), (0, 2, 0)), ((-0.5, 2.5, 2), (0, 2, 0)),
+             ((1, -1, 0), (1, 0, 0)), ((0.5, -2, -1), (0.5, 0, 0)),
+             ((-1, 1, 0), (0, 1, 0)), ((-2, 1.5, 4), (0, 1.5, 0)),
+             ((2, 2, 0), (1, 1, 0)), ((1.5, 1.5, -2), (1, 1, 0)),
+             ((0, 0, 0), (0, 0, 0)), ((2, 0, 0), (2, 0, 0)), ((0, 2, 0), (0, 2, 0)),
+             ((0.5, 0.5, 0), (0.5, 0.5, 0)), ((1, 1, 1), (1, 1, 0)), ((1, 1, -1), (1, 1, 0))]
+    for x, want in cases:
+        np.testing.assert_allclose(oracle.triangle_clamp(A, B, C, np.array(x, float)), want,
+                                   atol=1e-14)
+    # Degenerate triangles clamp to their longest edge, or their one point.
+    z, t = np.zeros(3), np.array([2.0, 2.0, 0.0])
+    for tri in ((z, z, t), (z, t, t), (z, t, z), (z, np.array([1.0, 1.0, 0.0]), t)):
+        for x, want in (((0, 0, 0), (0, 0, 0)), ((-1, -1, 0), (0, 0, 0)),
+                        ((-1, -1, -1), (0, 0, 0)), ((2, 2, 0), (2, 2, 0)),
+                        ((3, 3, 0), (2, 2, 0)), ((2, 2, 1), (2, 2, 0)),
+                        ((1, 1, 0), (1, 1, 0)), ((0.9, 1.1, 0), (1, 1, 0)),
+                        ((1.1, 0.9, 0), (1, 1, 0)), ((1.1, 0.9, 1), (1, 1, 0))):
+            np.testing.assert_allclose(oracle.triangle_clamp(*tri, np.array(x, float)), want,
+                                       atol=1e-14)
+    for x in ((0, 0, 0), (1, 1, 1), (-1, -1, -1)):
+        np.testing.assert_allclose(oracle.triangle_clamp(z, z, z, np.array(x, float)), z)
