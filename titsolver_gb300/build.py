@@ -2,7 +2,10 @@
 
 Every ``csrc/*.cu`` translation unit is compiled for sm_103a in parallel and
 linked into one shared library with the C ABI of ``include/titgpu.h``.
-Nothing is installed outside the package directory.
+``csrc/engine_inst.cu`` is compiled once per engine instance (dimension,
+precision form, smoothing kernel: 24 objects), the 3D FP64 instances first,
+so that no single object dominates the build time.  Nothing is installed
+outside the package directory.
 """
 
 from __future__ import annotations
@@ -46,23 +49,40 @@ def nvcc() -> str:
     return exe
 
 
+INSTANCE_SRC = CSRC / "engine_inst.cu"
+DIMS = (3, 2)
+FORMS = (0, 1)  # TG_FP64, TG_FP32C
+KERNELS = range(6)  # TG_KERNEL_*
+
+
 def _sources() -> list[pathlib.Path]:
     return sorted(CSRC.glob("*.cu"))
+
+
+def _jobs() -> list[tuple[pathlib.Path, str, list[str]]]:
+    """(source, object stem, extra nvcc defines) of every object, the
+    slowest first."""
+    jobs = [(INSTANCE_SRC, f"engine_{d}d_{'f64' if f == 0 else 'f32'}_k{k}",
+             [f"-DTG_INST_DIM={d}", f"-DTG_INST_FORM={f}", f"-DTG_INST_KERNEL={k}"])
+            for d in DIMS for f in FORMS for k in KERNELS]
+    jobs += [(src, src.stem, []) for src in _sources() if src != INSTANCE_SRC]
+    return jobs
 
 
 def _deps() -> list[pathlib.Path]:
     return sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "titgpu.h"]
 
 
-def _compile(src: pathlib.Path, verbose: bool) -> pathlib.Path:
-    obj = OBJ_DIR / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-I", str(ROOT / "include"), "-c",
+def _compile(job: tuple[pathlib.Path, str, list[str]], verbose: bool) -> pathlib.Path:
+    src, stem, defines = job
+    obj = OBJ_DIR / (stem + ".o")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *defines, "-I", str(ROOT / "include"), "-c",
            str(src), "-o", str(obj)]
     if verbose:
         cmd.insert(-4, "-Xptxas=-v")
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError(f"nvcc failed on {src.name}:\n{res.stdout}\n{res.stderr}")
+        raise RuntimeError(f"nvcc failed on {stem}:\n{res.stdout}\n{res.stderr}")
     if verbose and res.stderr:
         sys.stderr.write(res.stderr)
     return obj
@@ -81,10 +101,12 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         return LIB
     OUT_DIR.mkdir(exist_ok=True)
     OBJ_DIR.mkdir(exist_ok=True)
-    srcs = _sources()
-    jobs = jobs or min(len(srcs), max(1, os.cpu_count() or 1))
+    work = _jobs()
+    jobs = jobs or min(len(work), max(1, os.cpu_count() or 1))
+    for stale in OBJ_DIR.glob("*.o"):
+        stale.unlink()
     with concurrent.futures.ThreadPoolExecutor(max_workers=jobs) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+        objs = list(ex.map(lambda j: _compile(j, verbose), work))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)

@@ -106,6 +106,43 @@ void Context::drain_profile() {
   pending.clear();
 }
 
+namespace {
+
+template <int D, int F>
+std::unique_ptr<EngineBase> engine_for_kernel(int kernel) {
+  switch (kernel) {
+    case TG_KERNEL_CUBIC_SPLINE:
+      return make_engine_instance<D, F, TG_KERNEL_CUBIC_SPLINE>();
+    case TG_KERNEL_QUARTIC_SPLINE:
+      return make_engine_instance<D, F, TG_KERNEL_QUARTIC_SPLINE>();
+    case TG_KERNEL_QUINTIC_SPLINE:
+      return make_engine_instance<D, F, TG_KERNEL_QUINTIC_SPLINE>();
+    case TG_KERNEL_WENDLAND_C2:
+      return make_engine_instance<D, F, TG_KERNEL_WENDLAND_C2>();
+    case TG_KERNEL_WENDLAND_C4:
+      return make_engine_instance<D, F, TG_KERNEL_WENDLAND_C4>();
+    case TG_KERNEL_WENDLAND_C6:
+      return make_engine_instance<D, F, TG_KERNEL_WENDLAND_C6>();
+    default: return nullptr;
+  }
+}
+
+}  // namespace
+
+std::unique_ptr<EngineBase> make_engine(int dim, int form, int kernel) {
+  if (form != TG_FP64 && form != TG_FP32C) return nullptr;
+  const bool f64 = form == TG_FP64;
+  if (dim == 2) {
+    return f64 ? engine_for_kernel<2, TG_FP64>(kernel)
+               : engine_for_kernel<2, TG_FP32C>(kernel);
+  }
+  if (dim == 3) {
+    return f64 ? engine_for_kernel<3, TG_FP64>(kernel)
+               : engine_for_kernel<3, TG_FP32C>(kernel);
+  }
+  return nullptr;
+}
+
 }  // namespace tg
 
 namespace {
@@ -302,14 +339,7 @@ int tg_context_create(const tg_params* params, tg_context** out) {
     C.post_cos2_fov = cos_fov * cos_fov;
     C.post_k_fs = -std::log(0.05) / (0.01 * 0.01);
   }
-  const bool f64 = params->precision == TG_FP64;
-  if (params->dim == 2) {
-    C.engine = f64 ? tg::make_engine_2d_f64(params->kernel)
-                   : tg::make_engine_2d_f32(params->kernel);
-  } else {
-    C.engine = f64 ? tg::make_engine_3d_f64(params->kernel)
-                   : tg::make_engine_3d_f32(params->kernel);
-  }
+  C.engine = tg::make_engine(params->dim, params->precision, params->kernel);
   if (!C.engine) {
     cudaStreamDestroy(C.stream);
     delete ctx;

@@ -67,10 +67,15 @@ struct EngineBase {
   virtual bool supports_team(int team) const = 0;
 };
 
-std::unique_ptr<EngineBase> make_engine_2d_f64(int kernel);
-std::unique_ptr<EngineBase> make_engine_2d_f32(int kernel);
-std::unique_ptr<EngineBase> make_engine_3d_f64(int kernel);
-std::unique_ptr<EngineBase> make_engine_3d_f32(int kernel);
+// One engine template instance (dimension D, form F, smoothing kernel K).
+// Defined in engine_impl.cuh and explicitly instantiated once per instance by
+// engine_inst.cu, which the build compiles as separate objects in parallel.
+template <int D, int F, int K>
+std::unique_ptr<EngineBase> make_engine_instance();
+
+// The engine of a dimension, precision form and smoothing kernel; null for an
+// unknown combination.
+std::unique_ptr<EngineBase> make_engine(int dim, int form, int kernel);
 
 struct PendingEvent {
   int group;

@@ -504,23 +504,9 @@ class Engine final : public EngineBase {
   DatRec* datrec_ = nullptr;
 };
 
-template<int D, int F>
-std::unique_ptr<EngineBase> make_engine(int kernel) {
-  switch (kernel) {
-    case TG_KERNEL_CUBIC_SPLINE:
-      return std::make_unique<Engine<D, F, TG_KERNEL_CUBIC_SPLINE>>();
-    case TG_KERNEL_QUARTIC_SPLINE:
-      return std::make_unique<Engine<D, F, TG_KERNEL_QUARTIC_SPLINE>>();
-    case TG_KERNEL_QUINTIC_SPLINE:
-      return std::make_unique<Engine<D, F, TG_KERNEL_QUINTIC_SPLINE>>();
-    case TG_KERNEL_WENDLAND_C2:
-      return std::make_unique<Engine<D, F, TG_KERNEL_WENDLAND_C2>>();
-    case TG_KERNEL_WENDLAND_C4:
-      return std::make_unique<Engine<D, F, TG_KERNEL_WENDLAND_C4>>();
-    case TG_KERNEL_WENDLAND_C6:
-      return std::make_unique<Engine<D, F, TG_KERNEL_WENDLAND_C6>>();
-    default: return nullptr;
-  }
+template <int D, int F, int K>
+std::unique_ptr<EngineBase> make_engine_instance() {
+  return std::make_unique<Engine<D, F, K>>();
 }
 
 }  // namespace tg
