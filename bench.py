@@ -12,7 +12,8 @@ one full SSPRK3 step (three neighbour rebuilds, three fused force passes).
   steps / device time, state resident in HBM (working set > L2), CUDA-graph
   replay, timed with CUDA events on the library's stream.
 * ``forms.fp64``: the plain FP64 form on the same workload.
-* ``l2_error_vs_fp64``: relative L2 error of rho and r, FP32C vs FP64, after
+* ``l2_error_vs_fp64``: relative L2 error of rho, r and v, and the drift of
+  total momentum (|sum m v32 - sum m v64| / sum m |v64|), FP32C vs FP64, after
   the same number of steps from the same start.
 * ``e2e``: the same metric through the C ABI with host buffers: every step
   uploads r, v, rho, dv/dt from pinned host memory, steps, and downloads
@@ -331,10 +332,18 @@ def run_gpu(args, ranks) -> dict | None:
                             for t in scn["tanks"]])
         r32, r64 = ctx32.download(_abi.TG_FIELD_R)[f], ctx64.download(_abi.TG_FIELD_R)[f]
         d32, d64 = ctx32.download(_abi.TG_FIELD_RHO)[f], ctx64.download(_abi.TG_FIELD_RHO)[f]
+        v32, v64 = ctx32.download(_abi.TG_FIELD_V)[f], ctx64.download(_abi.TG_FIELD_V)[f]
         r0 = scn["r"][f]
+        # Equal masses within a tank: total momentum is m * sum(v) per tank.
+        m = np.concatenate([np.full(t["n_fluid"], t["m"]) for t in scn["tanks"]])[:, None]
+        p32, p64 = (m * v32).sum(axis=0), (m * v64).sum(axis=0)
         err = {"steps": total32,
                "rho": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
                "r": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
+               "v": float(np.linalg.norm(v32 - v64) / max(np.linalg.norm(v64), 1e-300)),
+               "momentum_drift": float(np.linalg.norm(p32 - p64) /
+                                       max(float((m * np.linalg.norm(v64, axis=1)[:, None]).sum()),
+                                           1e-300)),
                "r_vs_displacement": float(np.linalg.norm(r32 - r64) /
                                           max(np.linalg.norm(r64 - r0), 1e-300)),
                "rho_vs_deviation": float(np.linalg.norm(d32 - d64) /
