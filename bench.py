@@ -28,7 +28,8 @@ Other workloads (``--config``): c0, c3, c4, c4q, c4half, c5 (2D / 3D /
 batched dam breaks, the same report), c2 (point-cloud search + summation
 density), f2 and f3 (the reference's face-wall mode: the titwcsph pool in
 2D, a triangulated 3D pool; reference physics with shifting; device time
-per step of each form).
+per step of each form: fp32c with FP64 face integrals, fp32c_face32 with
+tg_params.face_fp32, fp64; and each compensated form's drift from fp64).
 
 ``--impl reference`` times that CPU path alone (the reference itself needs
 C++26 / GCC 16 and cannot be built here).  ``--gpus N`` under
@@ -503,23 +504,39 @@ def run_faces(args, ranks) -> dict | None:
     workload, make = make_config(args.config)
     scn = make()
     nf = scenarios.n_fluid(scn)
-    forms = [args.only] if args.only else ["fp32c", "fp64"]
-    res, launches = {}, 0
+    # fp32c: FP64 face integrals (the default); fp32c_face32: tg_params.face_fp32.
+    forms = [args.only] if args.only else ["fp32c", "fp32c_face32", "fp64"]
+    res, launches, state = {}, 0, {}
+    f = np.concatenate([np.r_[np.ones(t["n_fluid"], bool), np.zeros(t["n_wall"], bool)]
+                        for t in scn["tanks"]])
     for form in forms:
         P = physics.reference_params(
-            scn["dim"], precision=_abi.TG_FP32C if form == "fp32c" else _abi.TG_FP64)
+            scn["dim"], precision=_abi.TG_FP64 if form == "fp64" else _abi.TG_FP32C)
+        P.face_fp32 = 1 if form == "fp32c_face32" else 0
         P.post_integrate = _abi.TG_POST_SHIFTING
         P.device = ranks.local_rank
         ctx, ms, n_launch, _ = gpu_leg(scn, P, args.warmup, args.steps, 0, ranks, False)
+        state[form] = {k: ctx.download(fld)[f] for k, fld in
+                       (("r", _abi.TG_FIELD_R), ("v", _abi.TG_FIELD_V),
+                        ("rho", _abi.TG_FIELD_RHO))}
         ctx.close()
         res[form] = {"value": nf * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps}
         launches += n_launch
     if ranks.rank != 0:
         return None
+    err = None
+    if "fp64" in state and len(state) > 1:
+        b = state["fp64"]
+        err = {"steps": args.warmup + args.steps}
+        for form, a in state.items():
+            if form != "fp64":
+                err[form] = {k: float(np.linalg.norm(a[k] - b[k]) /
+                                      max(np.linalg.norm(b[k]), 1e-300))
+                             for k in ("rho", "r", "v")}
     head = res[forms[0]]
     return {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
-            "higher_is_better": True, "forms": res,
+            "higher_is_better": True, "forms": res, "l2_error_vs_fp64": err,
             "faces": int(sum(fc["face_verts"].shape[0] for fc in scn["faces"] if fc)),
             "config": {"workload": workload}, "gpu_launches": launches}
 
@@ -531,8 +548,9 @@ def run_single_form(args, ranks) -> dict | None:
     workload, make = make_config(args.config)
     scn = make()
     nf = scenarios.n_fluid(scn)
-    form = _abi.TG_FP32C if args.only == "fp32c" else _abi.TG_FP64
+    form = _abi.TG_FP64 if args.only == "fp64" else _abi.TG_FP32C
     P = physics.baseline_params(scn["dim"], precision=form)
+    P.face_fp32 = 1 if args.only == "fp32c_face32" else 0
     P.device = ranks.local_rank
     tune(P, args)
     auto = args.cells_per_radius is None and args.autotune == 1
@@ -568,8 +586,9 @@ def main() -> int:
                     help="pick the launch shape with tg_autotune before warm-up "
                          "(skipped when --cells-per-radius is given)")
     ap.add_argument("--staging", type=int, choices=(0, 1), default=0)
-    ap.add_argument("--only", choices=("fp32c", "fp64"), default=None,
-                    help="time one form only (profiling runs); prints its value")
+    ap.add_argument("--only", choices=("fp32c", "fp64", "fp32c_face32"), default=None,
+                    help="time one form only (profiling runs); prints its value; "
+                         "fp32c_face32 = fp32c with FP32 face integrals")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

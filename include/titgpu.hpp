@@ -516,6 +516,9 @@ struct GpuOptions {
   double c_force = 0.25;
   double c_visc = 0.125;
   bool kahan = true;
+  /// Face walls in the compensated form: closed-form face integrals in FP32
+  /// (faster, larger drift from the FP64 form) instead of FP64.
+  bool face_fp32 = false;
   std::int32_t device = -1; ///< CUDA ordinal; -1 = the current device
   bool graph = true;        ///< replay each step as a CUDA graph
   bool autotune = false;    ///< pick launch shapes with tg_autotune
@@ -594,6 +597,7 @@ public:
     P.viscosity = options_.viscosity;
     P.diffusion = options_.diffusion;
     P.kahan = options_.kahan ? 1 : 0;
+    P.face_fp32 = options_.face_fp32 ? 1 : 0;
     P.device = options_.device;
     P.eos = EOS::gpu_id;
     if constexpr (requires { eos_.xi(); }) P.xi = static_cast<double>(eos_.xi());

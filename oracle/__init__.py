@@ -29,7 +29,7 @@ class _Params(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "dim", "precision", "kernel", "integrator", "viscosity", "diffusion",
         "post_integrate", "cells_per_radius", "kahan", "device", "staging",
-        "eos")] + [
+        "eos", "face_fp32")] + [
         (n, ctypes.c_double) for n in (
             "xi", "g", "mu", "alpha", "delta", "cfl", "c_force", "c_visc")]
 

@@ -31,7 +31,9 @@ def test_library_exports_every_declared_symbol(gpu_lib):
 
 
 def test_struct_layouts_match_header():
-    assert ctypes.sizeof(_abi.TgParams) == 12 * 4 + 8 * 8
+    # 13 int32 fields, 4 bytes of padding, 8 doubles.
+    assert ctypes.sizeof(_abi.TgParams) == 13 * 4 + 4 + 8 * 8
+    assert _abi.TgParams.xi.offset == 56
     assert ctypes.sizeof(_abi.TgTank) == 2 * 8 + 4 * 8
     assert ctypes.sizeof(_abi.TgProfile) == 5 * 8 + 3 * 8
 
@@ -43,6 +45,7 @@ def test_params_default_are_reference_values(gpu_lib):
                                                            _abi.TG_SSPRK3)
     assert (p.viscosity, p.diffusion) == (_abi.TG_VISC_MORRIS, _abi.TG_DIFF_FERRARI)
     assert (p.cfl, p.c_force, p.c_visc, p.xi, p.g, p.mu) == (0.4, 0.25, 0.125, 7.0, 9.81, 0.001)
+    assert (p.eos, p.face_fp32) == (_abi.TG_EOS_TAIT, 0)
 
 
 def test_status_strings(gpu_lib):
@@ -58,6 +61,13 @@ def test_invalid_params_rejected_before_device(gpu_lib):
     assert gpu_lib.tg_context_create(ctypes.byref(p), ctypes.byref(h)) == _abi.TG_ERR_INVALID_ARGUMENT
     p = _abi.default_params()
     p.cells_per_radius = 9
+    assert gpu_lib.tg_context_create(ctypes.byref(p), ctypes.byref(h)) == _abi.TG_ERR_INVALID_ARGUMENT
+    # FP32 face integrals belong to the compensated form only.
+    p = _abi.default_params()
+    p.face_fp32 = 1
+    assert gpu_lib.tg_context_create(ctypes.byref(p), ctypes.byref(h)) == _abi.TG_ERR_INVALID_ARGUMENT
+    p.precision = _abi.TG_FP32C
+    p.face_fp32 = 2
     assert gpu_lib.tg_context_create(ctypes.byref(p), ctypes.byref(h)) == _abi.TG_ERR_INVALID_ARGUMENT
     assert gpu_lib.tg_context_destroy(None) == _abi.TG_OK
 

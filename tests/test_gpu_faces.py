@@ -177,8 +177,9 @@ def test_3d_faces_fp32_compensated_vs_fp64_oracle(gpu_lib):
 
 @pytest.mark.parametrize("shifting", (False, True))
 def test_faces_fp32_compensated_vs_fp64_oracle(gpu_lib, shifting):
-    # The compensated form with face walls: face integrals in FP64, pair sums
-    # in FP32 with Kahan sums, against the FP64 oracle after 30 steps.
+    # The compensated form with face walls: face integrals in FP64 (the
+    # default, face_fp32 = 0), pair sums in FP32 with Kahan sums, against the
+    # FP64 oracle after 30 steps.
     scn = scenarios.dam_break_2d_faces(nx_per_H=20)
     P64 = physics.reference_params(2)
     P32 = physics.reference_params(2, precision=_abi.TG_FP32C)
@@ -191,3 +192,49 @@ def test_faces_fp32_compensated_vs_fp64_oracle(gpu_lib, shifting):
         g = gpu_state(ctx)
     assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5
     assert rel_l2(g["r"][f], o.r[f]) <= 1e-6
+
+
+def _fp32_faces_params(dim, shifting, face_fp32, kernel=_abi.TG_KERNEL_WENDLAND_C4):
+    P = physics.reference_params(dim, precision=_abi.TG_FP32C, kernel=kernel)
+    P.post_integrate = _abi.TG_POST_SHIFTING if shifting else _abi.TG_POST_PREPARE
+    P.face_fp32 = face_fp32
+    return P
+
+
+@pytest.mark.parametrize("dim,shifting", ((2, False), (2, True), (3, False), (3, True)))
+def test_faces_fp32_integrals_vs_fp64_oracle(gpu_lib, dim, shifting):
+    # tg_params.face_fp32: the compensated form with the closed-form face
+    # integrals in FP32 too (face selection, frames and the sums over faces
+    # stay FP64).  Against the FP64 oracle after 30 (2D) / 20 (3D) steps:
+    # rho <= 1e-5 and r <= 5e-6 relative L2 over the fluid.
+    scn = scenarios.dam_break_2d_faces(nx_per_H=20) if dim == 2 else _scn3()
+    steps = 30 if dim == 2 else 20
+    P64 = physics.reference_params(dim)
+    P64.post_integrate = _abi.TG_POST_SHIFTING if shifting else _abi.TG_POST_PREPARE
+    o = oracle_run(scn, P64, steps)
+    f = fluid_mask(scn)
+    with gpu_context(scn, _fp32_faces_params(dim, shifting, 1)) as ctx:
+        ctx.step(steps)
+        g = gpu_state(ctx)
+    assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-5
+    assert rel_l2(g["r"][f], o.r[f]) <= 5e-6
+    # The switch is live: the FP64-integral run of the same form differs.
+    with gpu_context(scn, _fp32_faces_params(dim, shifting, 0)) as ctx:
+        ctx.step(steps)
+        h = gpu_state(ctx)
+    assert rel_l2(g["r"][f], h["r"][f]) > 0.0
+
+
+@pytest.mark.parametrize("kernel", range(6))
+def test_faces_fp32_integrals_every_kernel(gpu_lib, kernel):
+    # Every kernel's FP32 face integrals (2D segments and 3D triangles)
+    # against the FP64 oracle after 4 steps: rho and r <= 1e-6.
+    for dim, scn in ((2, scenarios.dam_break_2d_faces(nx_per_H=20)), (3, _scn3())):
+        P64 = physics.reference_params(dim, kernel=kernel)
+        o = oracle_run(scn, P64, 4)
+        f = fluid_mask(scn)
+        with gpu_context(scn, _fp32_faces_params(dim, False, 1, kernel)) as ctx:
+            ctx.step(4)
+            g = gpu_state(ctx)
+        assert rel_l2(g["rho"][f], o.rho[f]) <= 1e-6
+        assert rel_l2(g["r"][f], o.r[f]) <= 1e-6

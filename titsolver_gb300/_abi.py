@@ -60,6 +60,7 @@ class TgParams(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("staging", ctypes.c_int32),
         ("eos", ctypes.c_int32),
+        ("face_fp32", ctypes.c_int32),
         ("xi", ctypes.c_double),
         ("g", ctypes.c_double),
         ("mu", ctypes.c_double),

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -17,6 +18,11 @@
 
 #include "engine.cuh"
 #include "sort.cuh"
+
+// The layout the Python and C++ bindings mirror: 13 int32 fields, padding,
+// then the doubles.
+static_assert(offsetof(tg_params, xi) == 56 && sizeof(tg_params) == 120,
+              "tg_params layout changed: update the bindings");
 
 struct tg_context {
   tg::Context c;
@@ -199,6 +205,10 @@ bool valid_params(const tg_params* P, std::string* why) {
   }
   if (P->eos != TG_EOS_TAIT && P->eos != TG_EOS_LINEAR_TAIT) {
     *why = "unknown equation of state";
+    return false;
+  }
+  if (P->face_fp32 != 0 && !(P->face_fp32 == 1 && P->precision == TG_FP32C)) {
+    *why = "face_fp32 must be 0, or 1 with the FP32C form";
     return false;
   }
   if (P->post_integrate != TG_POST_PREPARE &&

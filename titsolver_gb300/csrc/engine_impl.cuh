@@ -380,7 +380,9 @@ class Engine final : public EngineBase {
     p.shift = -C.P.cfl * 0.2;
     const unsigned grid = grid_for(C.n, 128);
     if (C.faces.on) {
-      k_post_faces<D, F, K><<<face_grid(C), 128, 0, C.stream>>>(p);
+      with_face_real(C, [&](auto real) {
+        k_post_faces<D, F, K, decltype(real)><<<face_grid(C), 128, 0, C.stream>>>(p);
+      });
       C.launches += 1;
     }
     k_post_sums<D, F, K><<<grid, 128, 0, C.stream>>>(p);
@@ -400,9 +402,25 @@ class Engine final : public EngineBase {
     if (a.fc.on) {
       cudaMemsetAsync(a.fc.face_count, 0, sizeof(uint32_t), C.stream);
       k_gamma_init<D, F><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
-      k_gamma_faces<D, K, F><<<face_grid(C), 128, 0, C.stream>>>(a);
+      with_face_real(C, [&](auto real) {
+        k_gamma_faces<D, K, F, decltype(real)><<<face_grid(C), 128, 0, C.stream>>>(a);
+      });
       C.launches += 2;
     }
+  }
+
+  // Calls fn(float{}) when the face passes evaluate their closed-form
+  // integrals in FP32 (tg_params.face_fp32, compensated form only), else
+  // fn(double{}); the plain form never instantiates the FP32 passes.
+  template<class Fn>
+  static void with_face_real(const Context& C, Fn&& fn) {
+    if constexpr (F == TG_FP32C) {
+      if (C.P.face_fp32 != 0) {
+        fn(0.0f);
+        return;
+      }
+    }
+    fn(0.0);
   }
 
   // Grid of the warp-per-face-particle passes: they loop over the face
@@ -446,7 +464,9 @@ class Engine final : public EngineBase {
       C.group_end(tok);
     }
     if (a.fc.on) {
-      k_face_terms<D, K, F><<<face_grid(C), 128, 0, C.stream>>>(a);
+      with_face_real(C, [&](auto real) {
+        k_face_terms<D, K, F, decltype(real)><<<face_grid(C), 128, 0, C.stream>>>(a);
+      });
       C.launches += 1;
     }
     tok = C.group_begin(kGroupForces);

@@ -1,5 +1,4 @@
-// faces.cuh - semi-analytical face boundaries (FP64 arithmetic): the
-// reference's wall mode with boundary faces and a containment function
+// faces.cuh - semi-analytical face boundaries: the reference's wall mode with boundary faces and a containment function
 // (FluidEquations with a non-empty domain, fluid_equations.hpp:122-193,
 // 241-247, 278-291, 340-349, 491-511); segments in 2D, triangles in 3D.
 //
@@ -24,9 +23,17 @@
 // copysign(log1p((|z| + z^2/(rho + eta))/eta), z)), J_0 = z,
 // J_1 = (z rho + eta^2 L)/2, J_p = (z rho^p + p eta^2 J_{p-2})/(p + 1), and
 // t_p the coefficients of the piece's 2D tail moment.
+//
+// Arithmetic: face selection, containment, the face frames and the sums over
+// faces are FP64 in both forms.  The closed-form integrals of one face run
+// in the type T of their template: FP64 in the plain form and FP32 in the
+// compensated form, on the face's vertices already projected into its frame
+// around the particle and scaled by 1/h (O(1) values, so FP32 keeps ~1e-7
+// relative to h); GB300's FP64 rate is a small fraction of its FP32 rate.
 #pragma once
 
 #include <cstddef>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -138,39 +145,69 @@ __device__ __forceinline__ void static_for(Fn&& f) {
   }
 }
 
+// Scalar maths of the face integrals in their type: the float functions
+// for T = float (no silent promotion to FP64), the double ones otherwise.
+template<class T>
+struct FaceMath;
+template<>
+struct FaceMath<double> {
+  static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+  static __device__ __forceinline__ double abs(double x) { return ::fabs(x); }
+  static __device__ __forceinline__ double min(double a, double b) { return ::fmin(a, b); }
+  static __device__ __forceinline__ double max(double a, double b) { return ::fmax(a, b); }
+  static __device__ __forceinline__ double atan2(double y, double x) { return ::atan2(y, x); }
+  static __device__ __forceinline__ double log1p(double x) { return ::log1p(x); }
+  static __device__ __forceinline__ double copysign(double a, double b) {
+    return ::copysign(a, b);
+  }
+};
+template<>
+struct FaceMath<float> {
+  static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
+  static __device__ __forceinline__ float abs(float x) { return ::fabsf(x); }
+  static __device__ __forceinline__ float min(float a, float b) { return ::fminf(a, b); }
+  static __device__ __forceinline__ float max(float a, float b) { return ::fmaxf(a, b); }
+  static __device__ __forceinline__ float atan2(float y, float x) { return ::atan2f(y, x); }
+  static __device__ __forceinline__ float log1p(float x) { return ::log1pf(x); }
+  static __device__ __forceinline__ float copysign(float a, float b) {
+    return ::copysignf(a, b);
+  }
+};
+
 // Segment line primitive of piece I of kernel K at z (units of h), with the
 // J_p recursion and the coefficients unrolled.
-template<int K, int I, bool Anti>
-__device__ __forceinline__ double face_primitive(double eta, double z) {
+template<int K, int I, bool Anti, class T>
+__device__ __forceinline__ T face_primitive(T eta, T z) {
+  using M = FaceMath<T>;
   constexpr FacePiece kp = kFacePieces[K].p[I];
   constexpr int pmax = Anti ? (kp.tdeg - 2 > 0 ? kp.tdeg - 2 : 0) : kp.deg;
-  const double rho = sqrt(z * z + eta * eta);
-  const double L = fabs(eta) <= kTiny
-                       ? 0.0
-                       : copysign(log1p((fabs(z) + z * z / (rho + eta)) / eta), z);
-  double J[pmax + 1];
+  const T rho = M::sqrt(z * z + eta * eta);
+  const T L = M::abs(eta) <= T(kTiny)
+                  ? T(0)
+                  : M::copysign(M::log1p((M::abs(z) + z * z / (rho + eta)) / eta), z);
+  T J[pmax + 1];
   J[0] = z;
-  if constexpr (pmax >= 1) J[1] = (z * rho + eta * eta * L) * 0.5;
-  double rp = rho;
+  if constexpr (pmax >= 1) J[1] = (z * rho + eta * eta * L) * T(0.5);
+  T rp = rho;
   static_for<2, pmax + 1>([&]<int P>() {
-    constexpr double inv = kFaceInv[P + 1];
+    constexpr T inv = T(kFaceInv[P + 1]);
     rp *= rho;
-    J[P] = (z * rp + P * eta * eta * J[P - 2]) * inv;
+    J[P] = (z * rp + T(P) * eta * eta * J[P - 2]) * inv;
   });
-  double s = 0.0;
+  T s = T(0);
   if constexpr (!Anti) {
     static_for<0, kp.deg + 1>([&]<int P>() {
       constexpr double c = kp.c[P];
-      if constexpr (c != 0.0) s += c * J[P];
+      if constexpr (c != 0.0) s += T(c) * J[P];
     });
   } else {
-    const double A = atan2(z, eta);
+    const T A = M::atan2(z, eta);
     static_for<0, kp.tdeg + 1>([&]<int P>() {
       constexpr double t = kp.t[P];
       if constexpr (t != 0.0) {
-        if constexpr (P == 0) s += t * A;
-        else if constexpr (P == 1) s += t * eta * L;
-        else s += t * eta * J[P - 2];
+        if constexpr (P == 0) s += T(t) * A;
+        else if constexpr (P == 1) s += T(t) * eta * L;
+        else s += T(t) * eta * J[P - 2];
       }
     });
   }
@@ -182,24 +219,24 @@ __device__ __forceinline__ double face_primitive(double eta, double z) {
 // eta^2).  skip bit 0 / 1 leaves out the z_min / z_max end (an end shared
 // with an in-range collinear neighbour, whose opposite term cancels it;
 // face_skip_edges).
-template<int K, bool Anti>
-__device__ __forceinline__ double face_unit_segment(double eta, double zmin,
-                                                    double zmax, unsigned skip) {
-  double total = 0.0;
+template<int K, bool Anti, class T>
+__device__ __forceinline__ T face_unit_segment(T eta, T zmin, T zmax, unsigned skip) {
+  using M = FaceMath<T>;
+  T total = T(0);
   static_for<0, kFacePieces[K].n>([&]<int I>() {
-    constexpr double cutoff = kFacePieces[K].p[I].cutoff;
+    constexpr T cutoff = T(kFacePieces[K].p[I].cutoff);
     if (eta >= cutoff) return;
-    const double zc = sqrt(cutoff * cutoff - eta * eta);
+    const T zc = M::sqrt(cutoff * cutoff - eta * eta);
     if (skip == 0) {
-      const double lo = fmax(zmin, -zc), hi = fmin(zmax, zc);
+      const T lo = M::max(zmin, -zc), hi = M::min(zmax, zc);
       if (lo >= hi) return;
-      total += face_primitive<K, I, Anti>(eta, hi) - face_primitive<K, I, Anti>(eta, lo);
+      total += face_primitive<K, I, Anti, T>(eta, hi) - face_primitive<K, I, Anti, T>(eta, lo);
       return;
     }
     // The clipped ends (a segment outside the circle gives P(+-zc) twice,
     // i.e. zero, as the early return above does).
-    if (!(skip & 2u)) total += face_primitive<K, I, Anti>(eta, fmin(fmax(zmax, -zc), zc));
-    if (!(skip & 1u)) total -= face_primitive<K, I, Anti>(eta, fmin(fmax(zmin, -zc), zc));
+    if (!(skip & 2u)) total += face_primitive<K, I, Anti, T>(eta, M::min(M::max(zmax, -zc), zc));
+    if (!(skip & 1u)) total -= face_primitive<K, I, Anti, T>(eta, M::min(M::max(zmin, -zc), zc));
   });
   return total;
 }
@@ -233,25 +270,29 @@ __device__ __forceinline__ FaceFrame face_frame(const double* ab,
 }
 
 // Kernel::flux (kernel.hpp:194-206): n w h^-1 unit_flux(|d|, z_a, z_b);
-// wd = the kernel's 2D weight.
-template<int K>
+// wd = the kernel's 2D weight; the integral in type T.
+template<int K, class T = double>
 __device__ __forceinline__ void face_flux(const double* ab, const double* x,
                                           double h, double wd, double* out,
                                           unsigned skip = 0) {
   const double hinv = 1.0 / h;
   const FaceFrame F = face_frame(ab, x, hinv);
-  const double s = wd * hinv * face_unit_segment<K, false>(fabs(F.d), F.za, F.zb, skip);
+  const double u = static_cast<double>(face_unit_segment<K, false, T>(
+      static_cast<T>(fabs(F.d)), static_cast<T>(F.za), static_cast<T>(F.zb), skip));
+  const double s = wd * hinv * u;
   out[0] = F.n[0] * s;
   out[1] = F.n[1] * s;
 }
 
 // Kernel::antigrad_flux (kernel.hpp:209-221).
-template<int K>
+template<int K, class T = double>
 __device__ __forceinline__ double face_antigrad_flux(const double* ab,
                                                      const double* x, double h,
                                                      double wd, unsigned skip = 0) {
   const FaceFrame F = face_frame(ab, x, 1.0 / h);
-  return copysign(wd, F.d) * face_unit_segment<K, true>(fabs(F.d), F.za, F.zb, skip);
+  const double u = static_cast<double>(face_unit_segment<K, true, T>(
+      static_cast<T>(fabs(F.d)), static_cast<T>(F.za), static_cast<T>(F.zb), skip));
+  return copysign(wd, F.d) * u;
 }
 
 // Segment::intersects(BSphere) (geom/segment.hpp:108-112).
@@ -335,80 +376,80 @@ inline constexpr FaceTail3 kFaceTail3[6][3] = {
 //             sector = lead + eta (sum_{p>=3} b_p cutoff^{p-1} - s_0/cutoff)
 // so that the line primitive is sum_p a_p K_{p+2} + lead K_0 (flux) or
 // lead K_0 + eta sum_{p>=3} b_p K_{p-1} (antigradient).
+template<class T>
 struct EdgeCoef {
-  double lead, sector;
+  T lead, sector;
 };
-template<int K, int I, bool Anti>
-__device__ __forceinline__ EdgeCoef face_edge_coef(double eta) {
+template<int K, int I, bool Anti, class T>
+__device__ __forceinline__ EdgeCoef<T> face_edge_coef(T eta) {
   constexpr FacePiece kp = kFacePieces[K].p[I];
   constexpr FaceTail3 tp = kFaceTail3[K][I];
-  EdgeCoef e{0.0, 0.0};
-  double cut = 0.0;
+  EdgeCoef<T> e{T(0), T(0)};
+  T cut = T(0);
   if constexpr (!Anti) {
-    double ep = eta * eta;
+    T ep = eta * eta;
     static_for<0, kp.deg + 1>([&]<int P>() {
       constexpr double a = kp.c[P] * kFaceInv[P + 2];
       constexpr double ac = a * constexpr_pow(kp.cutoff, P + 2);
-      e.lead -= a * ep;
-      cut += ac;
+      e.lead -= T(a) * ep;
+      cut += T(ac);
       ep *= eta;
     });
     e.sector = cut + e.lead;
   } else {
-    double ep = eta * eta * eta;
-    e.lead = tp.s[0];
+    T ep = eta * eta * eta;
+    e.lead = T(tp.s[0]);
     static_for<3, tp.deg + 1>([&]<int P>() {
       constexpr double b = tp.s[P] * kFaceInv[P - 1];
       constexpr double bc = b * constexpr_pow(kp.cutoff, P - 1);
-      e.lead -= b * ep;
-      cut += bc;
+      e.lead -= T(b) * ep;
+      cut += T(bc);
       ep *= eta;
     });
     constexpr double s0c = tp.s[0] / kp.cutoff;
-    e.sector = e.lead + eta * (cut - s0c);
+    e.sector = e.lead + eta * (cut - T(s0c));
   }
   return e;
 }
 
-template<int K, int I, bool Anti>
-__device__ __forceinline__ double face_edge_primitive(const EdgeCoef& ec,
-                                                      double eta, double delta,
-                                                      double beta2, double beta,
-                                                      double z) {
+template<int K, int I, bool Anti, class T>
+__device__ __forceinline__ T face_edge_primitive(const EdgeCoef<T>& ec, T eta, T delta,
+                                                 T beta2, T beta, T z) {
+  using M = FaceMath<T>;
   constexpr FacePiece kp = kFacePieces[K].p[I];
   constexpr FaceTail3 tp = kFaceTail3[K][I];
   constexpr int kmax = Anti ? (tp.deg - 1 > 1 ? tp.deg - 1 : 1) : kp.deg + 2;
-  const double rho = sqrt(z * z + beta2);
-  const double A = fabs(delta) <= kTiny
-                       ? 0.0
-                       : atan2(delta * z * (rho - eta), delta * delta * rho + z * z * eta);
-  const double L = fabs(beta) <= kTiny
-                       ? 0.0
-                       : copysign(log1p((fabs(z) + z * z / (rho + beta)) / beta), z);
-  double J[kmax + 1], Kk[kmax + 1];
+  const T rho = M::sqrt(z * z + beta2);
+  const T A = M::abs(delta) <= T(kTiny)
+                  ? T(0)
+                  : M::atan2(delta * z * (rho - eta), delta * delta * rho + z * z * eta);
+  const T L = M::abs(beta) <= T(kTiny)
+                  ? T(0)
+                  : M::copysign(M::log1p((M::abs(z) + z * z / (rho + beta)) / beta), z);
+  T J[kmax + 1], Kk[kmax + 1];
   J[0] = z;
-  J[1] = (z * rho + beta2 * L) * 0.5;
-  double rp = rho;
+  J[1] = (z * rho + beta2 * L) * T(0.5);
+  T rp = rho;
   static_for<2, kmax + 1>([&]<int P>() {
-    constexpr double inv = kFaceInv[P + 1];
+    constexpr T inv = T(kFaceInv[P + 1]);
     rp *= rho;
-    J[P] = (z * rp + P * beta2 * J[P - 2]) * inv;
+    J[P] = (z * rp + T(P) * beta2 * J[P - 2]) * inv;
   });
   Kk[0] = A;
   Kk[1] = delta * L;
-  const double eta2 = eta * eta;
+  const T eta2 = eta * eta;
   static_for<2, kmax + 1>([&]<int P>() { Kk[P] = delta * J[P - 2] + eta2 * Kk[P - 2]; });
-  double s = 0.0;
+  T s = T(0);
   if constexpr (!Anti) {
     static_for<0, kp.deg + 1>([&]<int P>() {
       constexpr double a = kp.c[P] * kFaceInv[P + 2];
-      if constexpr (a != 0.0) s += a * Kk[P + 2];
+      if constexpr (a != 0.0) s += T(a) * Kk[P + 2];
     });
     return s + ec.lead * Kk[0];
   } else {
     static_for<3, tp.deg + 1>([&]<int P>() {
       constexpr double b = tp.s[P] * kFaceInv[P - 1];
-      if constexpr (b != 0.0) s += b * Kk[P - 1];
+      if constexpr (b != 0.0) s += T(b) * Kk[P - 1];
     });
     return ec.lead * Kk[0] + eta * s;
   }
@@ -424,62 +465,63 @@ __device__ __forceinline__ double face_edge_primitive(const EdgeCoef& ec,
 // one per lane, so that the costly primitives run on full warps whatever
 // mix of clipped and unclipped edges the lanes hold, and every lane adds up
 // its own tasks.  v = the lane's three projected vertices (units of h).
+template<class T>
 struct EdgeTask {
-  double zlo, zhi, delta, eta, lead;
+  T zlo, zhi, delta, eta, lead;
 };
 constexpr int kTasksPerLane = 3;  // one inside sub-interval per edge
 
-template<int K, int I, bool Anti>
-__device__ __forceinline__ double warp_triangle_piece(bool active, double eta,
-                                                      const double* v, unsigned skip,
-                                                      EdgeTask* tq, double* tv,
-                                                      uint8_t* ti, int lane) {
-  constexpr double cutoff = kFacePieces[K].p[I].cutoff;
-  double sector_sum = 0.0;
+template<int K, int I, bool Anti, class T>
+__device__ __forceinline__ T warp_triangle_piece(bool active, T eta, const T* v,
+                                                 unsigned skip, EdgeTask<T>* tq, T* tv,
+                                                 uint8_t* ti, int lane) {
+  using M = FaceMath<T>;
+  constexpr T cutoff = T(kFacePieces[K].p[I].cutoff);
+  T sector_sum = T(0);
   int nt = 0;
   if (active && eta < cutoff) {
-    const double radius2 = cutoff * cutoff - eta * eta;
-    const EdgeCoef ec = face_edge_coef<K, I, Anti>(eta);
+    const T radius2 = cutoff * cutoff - eta * eta;
+    const EdgeCoef<T> ec = face_edge_coef<K, I, Anti, T>(eta);
     for (int e = 0; e < 3; ++e) {
       if (skip & (1u << e)) continue;
-      const double* p0 = v + 2 * e;
-      const double* p1 = v + 2 * (e == 2 ? 0 : e + 1);
-      const double ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
-      const double len2 = ed[0] * ed[0] + ed[1] * ed[1];
-      if (len2 <= kTiny * kTiny) continue;
-      const double len = sqrt(len2);
-      const double t[2] = {ed[0] / len, ed[1] / len};
-      const double delta = p0[0] * t[1] - p0[1] * t[0];
-      const double delta2 = delta * delta;
-      const double z0 = p0[0] * t[0] + p0[1] * t[1];
-      const double z1 = z0 + len;
-      double zs[4];
+      const T* p0 = v + 2 * e;
+      const T* p1 = v + 2 * (e == 2 ? 0 : e + 1);
+      const T ed[2] = {p1[0] - p0[0], p1[1] - p0[1]};
+      const T len2 = ed[0] * ed[0] + ed[1] * ed[1];
+      if (len2 <= T(kTiny * kTiny)) continue;
+      const T len = M::sqrt(len2);
+      const T t[2] = {ed[0] / len, ed[1] / len};
+      const T delta = p0[0] * t[1] - p0[1] * t[0];
+      const T delta2 = delta * delta;
+      const T z0 = p0[0] * t[0] + p0[1] * t[1];
+      const T z1 = z0 + len;
+      T zs[4];
       int nz = 0;
       zs[nz++] = z0;
       if (radius2 > delta2) {
-        const double zc = sqrt(radius2 - delta2);
+        const T zc = M::sqrt(radius2 - delta2);
         if (z0 < -zc && -zc < z1) zs[nz++] = -zc;
         if (z0 < zc && zc < z1) zs[nz++] = zc;
       }
       zs[nz++] = z1;
       for (int j = 0; j + 1 < nz; ++j) {
-        const double lo = zs[j], hi = zs[j + 1];
-        if (fabs(hi - lo) <= kTiny) continue;
-        const double mid = (lo + hi) * 0.5;
+        const T lo = zs[j], hi = zs[j + 1];
+        if (M::abs(hi - lo) <= T(kTiny)) continue;
+        const T mid = (lo + hi) * T(0.5);
         if (mid * mid + delta2 < radius2) {
           if (nt < kTasksPerLane) {
-            tq[lane * kTasksPerLane + nt] = EdgeTask{lo, hi, delta, eta, ec.lead};
+            tq[lane * kTasksPerLane + nt] = EdgeTask<T>{lo, hi, delta, eta, ec.lead};
             ++nt;
           } else {
             // Not reached (an edge has one inside sub-interval); evaluated
             // in place should rounding ever split one.
-            const double beta2 = eta * eta + delta2;
-            const double beta = sqrt(beta2);
-            sector_sum += face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, hi) -
-                          face_edge_primitive<K, I, Anti>(ec, eta, delta, beta2, beta, lo);
+            const T beta2 = eta * eta + delta2;
+            const T beta = M::sqrt(beta2);
+            sector_sum += face_edge_primitive<K, I, Anti, T>(ec, eta, delta, beta2, beta, hi) -
+                          face_edge_primitive<K, I, Anti, T>(ec, eta, delta, beta2, beta, lo);
           }
         } else {
-          sector_sum += ec.sector * atan2(delta * (hi - lo), lo * hi + delta2);
+          sector_sum += ec.sector * M::atan2(delta * (hi - lo), lo * hi + delta2);
         }
       }
     }
@@ -497,15 +539,15 @@ __device__ __forceinline__ double warp_triangle_piece(bool active, double eta,
   __syncwarp();
   for (int t = lane; t < total; t += 32) {
     const int slot = ti[t];
-    const EdgeTask q = tq[slot];
-    const double beta2 = q.eta * q.eta + q.delta * q.delta;
-    const double beta = sqrt(beta2);
-    const EdgeCoef ec{q.lead, 0.0};
-    tv[slot] = face_edge_primitive<K, I, Anti>(ec, q.eta, q.delta, beta2, beta, q.zhi) -
-               face_edge_primitive<K, I, Anti>(ec, q.eta, q.delta, beta2, beta, q.zlo);
+    const EdgeTask<T> q = tq[slot];
+    const T beta2 = q.eta * q.eta + q.delta * q.delta;
+    const T beta = FaceMath<T>::sqrt(beta2);
+    const EdgeCoef<T> ec{q.lead, T(0)};
+    tv[slot] = face_edge_primitive<K, I, Anti, T>(ec, q.eta, q.delta, beta2, beta, q.zhi) -
+               face_edge_primitive<K, I, Anti, T>(ec, q.eta, q.delta, beta2, beta, q.zlo);
   }
   __syncwarp();
-  double s = sector_sum;
+  T s = sector_sum;
   for (int k = 0; k < nt; ++k) s += tv[lane * kTasksPerLane + k];
   __syncwarp();
   return s;
@@ -513,17 +555,17 @@ __device__ __forceinline__ double warp_triangle_piece(bool active, double eta,
 
 // The triangle integral summed over the kernel's pieces (all lanes call);
 // edges in `skip` (bit e: edge e) are left out.
-template<int K, bool Anti>
-__device__ __forceinline__ double warp_unit_triangle(bool active, double eta,
-                                                     const double* v, unsigned skip) {
-  __shared__ EdgeTask tq_all[kFaceBlock / 32][32 * kTasksPerLane];
-  __shared__ double tv_all[kFaceBlock / 32][32 * kTasksPerLane];
+template<int K, bool Anti, class T>
+__device__ __forceinline__ T warp_unit_triangle(bool active, T eta, const T* v,
+                                                unsigned skip) {
+  __shared__ EdgeTask<T> tq_all[kFaceBlock / 32][32 * kTasksPerLane];
+  __shared__ T tv_all[kFaceBlock / 32][32 * kTasksPerLane];
   __shared__ uint8_t ti_all[kFaceBlock / 32][32 * kTasksPerLane];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double total = 0.0;
+  T total = T(0);
   static_for<0, kFacePieces[K].n>([&]<int I>() {
-    total += warp_triangle_piece<K, I, Anti>(active, eta, v, skip, tq_all[w], tv_all[w],
-                                             ti_all[w], lane);
+    total += warp_triangle_piece<K, I, Anti, T>(active, eta, v, skip, tq_all[w], tv_all[w],
+                                                ti_all[w], lane);
   });
   return total;
 }
@@ -593,17 +635,24 @@ __device__ __forceinline__ TriFrame tri_frame(const double* t, const double* x,
 // integral is warp-cooperative); inactive lanes get zero.  skip: the
 // triangle's edges that cancel against in-range coplanar neighbours
 // (face_skip_edges).
-template<int K, int D>
+// The integral runs in type T (FaceReal of the form); frame, weights and
+// the result are FP64.
+template<int K, int D, class T = double>
 __device__ __forceinline__ void face_flux_d(bool active, const double* g,
                                             const double* x, double h, double wd,
                                             double* out, unsigned skip = 0) {
   if constexpr (D == 2) {
     out[0] = out[1] = 0.0;
-    if (active) face_flux<K>(g, x, h, wd, out, skip);
+    if (active) face_flux<K, T>(g, x, h, wd, out, skip);
   } else {
     const double hinv = 1.0 / h;
     const TriFrame F = tri_frame(g, x, hinv);
-    const double s = wd * hinv * warp_unit_triangle<K, false>(active, fabs(F.d), F.p, skip);
+    T p[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) p[k] = static_cast<T>(F.p[k]);
+    const double u = static_cast<double>(
+        warp_unit_triangle<K, false, T>(active, static_cast<T>(fabs(F.d)), p, skip));
+    const double s = wd * hinv * u;
     out[0] = F.n[0] * s;
     out[1] = F.n[1] * s;
     out[2] = F.n[2] * s;
@@ -611,15 +660,19 @@ __device__ __forceinline__ void face_flux_d(bool active, const double* g,
 }
 
 // Kernel::antigrad_flux of face g at x (all lanes together, as above).
-template<int K, int D>
+template<int K, int D, class T = double>
 __device__ __forceinline__ double face_antigrad_flux_d(bool active, const double* g,
                                                        const double* x, double h,
                                                        double wd, unsigned skip = 0) {
   if constexpr (D == 2) {
-    return active ? face_antigrad_flux<K>(g, x, h, wd, skip) : 0.0;
+    return active ? face_antigrad_flux<K, T>(g, x, h, wd, skip) : 0.0;
   } else {
     const TriFrame F = tri_frame(g, x, 1.0 / h);
-    return copysign(wd, F.d) * warp_unit_triangle<K, true>(active, fabs(F.d), F.p, skip);
+    T p[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) p[k] = static_cast<T>(F.p[k]);
+    return copysign(wd, F.d) * static_cast<double>(warp_unit_triangle<K, true, T>(
+                                   active, static_cast<T>(fabs(F.d)), p, skip));
   }
 }
 

@@ -1174,7 +1174,7 @@ __device__ __forceinline__ double face_avg(const double* x) {
 // Face terms of continuity and momentum (fluid_equations.hpp:241-247,
 // 278-291) of the face particles, one warp per particle with the lanes
 // splitting its faces; k_gamma_init zeroed the other particles' terms.
-template<int D, int K, int F>
+template<int D, int K, int F, class FT>
 __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
   const FaceArgs& fc = A.fc;
   const int lane = threadIdx.x & 31;
@@ -1201,7 +1201,7 @@ __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
       // Each face's flux is weighted by its own vertex densities and
       // pressures, so no edges cancel here.
       double gg[3];
-      face_flux_d<K, D>(active, g, pa, T.h, fc.weight, gg);
+      face_flux_d<K, D, FT>(active, g, pa, T.h, fc.weight, gg);
       if (!active) return;
       double rv[3], pv[3];
 #pragma unroll
@@ -1792,7 +1792,7 @@ __global__ void __launch_bounds__(128) k_gamma_init(StageArgs<D, F> A) {
   }
 }
 
-template<int D, int K, int F>
+template<int D, int K, int F, class FT>
 __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
   const FaceArgs& fc = A.fc;
   const int lane = threadIdx.x & 31;
@@ -1818,7 +1818,7 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
       double fl[3];
       unsigned skip = 0;
       if (active) skip = face_skip_edges<D>(fc, fi, x, radius);
-      face_flux_d<K, D>(active, f, x, T.h, wd, fl, skip);
+      face_flux_d<K, D, FT>(active, f, x, T.h, wd, fl, skip);
       if (!active) return;
 #pragma unroll
       for (int k = 0; k < D; ++k) g[k] += fl[k];
@@ -1850,7 +1850,7 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
         // The adjacency is that of x (the face set does not move with xs).
         unsigned skip = 0;
         if (active) skip = face_skip_edges<D>(fc, fi, x, radius);
-        const double a = face_antigrad_flux_d<K, D>(active, f, xs, T.h, wd, skip);
+        const double a = face_antigrad_flux_d<K, D, FT>(active, f, xs, T.h, wd, skip);
         if (active) ag += a;
       });
       ga -= warp_sum(ag);

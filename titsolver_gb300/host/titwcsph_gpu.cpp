@@ -8,11 +8,12 @@
 // Usage: titwcsph_gpu [--nx N] [--steps S] [--end-time T] [--fp32c]
 //                     [--integrator ssprk3|ssprk2|euler|verlet]
 //                     [--no-shifting] [--faces] [--ttdb FILE] [--dump FILE]
-//                     [--log] [--eos tait|linear]
+//                     [--log] [--eos tait|linear] [--face-fp32]
 //   --nx       particles per column height H (default 80, as wcsph.cpp:42)
 //   --steps    stop after S steps (default: run to scaled time T)
 //   --end-time scaled end time t sqrt(g/H) (default 10, as wcsph.cpp:183)
 //   --fp32c    FP32-compensated pair sums instead of plain FP64
+//   --face-fp32   with --fp32c --faces: face integrals in FP32
 //   --integrator  time integrator (default ssprk3, as wcsph.cpp:92)
 //   --no-shifting skip the post-step shifting and free-surface correction
 //                 (the reference always runs them)
@@ -60,6 +61,7 @@ struct Options {
   std::string dump;
   bool log = false;
   std::string eos = "tait";
+  bool face_fp32 = false;
 };
 
 auto parse(int argc, char** argv) -> Options {
@@ -81,10 +83,12 @@ auto parse(int argc, char** argv) -> Options {
     else if (a == "--dump") o.dump = next();
     else if (a == "--log") o.log = true;
     else if (a == "--eos") o.eos = next();
+    else if (a == "--face-fp32") o.face_fp32 = true;
     else throw Exception{"unknown option " + a};
   }
   if (o.nx < 4) throw Exception{"--nx must be at least 4"};
   if (o.eos != "tait" && o.eos != "linear") throw Exception{"unknown --eos " + o.eos};
+  if (o.face_fp32 && !o.fp32c) throw Exception{"--face-fp32 needs --fp32c"};
   if (o.integrator != "ssprk3" && o.integrator != "ssprk2" &&
       o.integrator != "euler" && o.integrator != "verlet") {
     throw Exception{"unknown integrator " + o.integrator};
@@ -127,6 +131,7 @@ auto sph_main_eos(const Options& opt, const EOS& eos) -> int {
   GpuOptions gpu;
   gpu.precision = opt.fp32c ? Precision::fp32_compensated : Precision::fp64;
   gpu.shifting = opt.shifting;
+  gpu.face_fp32 = opt.face_fp32;
   if (opt.faces) {
     // The reference's walls (wcsph.cpp:55-77): the pool surface tessellated
     // at dr, and a winding-number containment of the pool.
