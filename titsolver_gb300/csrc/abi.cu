@@ -1288,6 +1288,23 @@ int build_faces(tg_context* ctx) {
     return e;
   };
   TG_CUDA(&C, up(fa.coords, coords));
+  {
+    // The frame of every face, once (the faces are fixed).
+    const uint32_t nfaces = static_cast<uint32_t>(coords.size() / (D * D));
+    const size_t per = D == 2 ? tg::kFrameDoubles<2> : tg::kFrameDoubles<3>;
+    void* fr = nullptr;
+    TG_CUDA(&C, C.alloc(&fr, sizeof(double) * per * std::max<uint32_t>(nfaces, 1)));
+    fa.frame = static_cast<const double*>(fr);
+    if (nfaces > 0) {
+      const unsigned grid = (nfaces + 127) / 128;
+      if (D == 2) {
+        tg::k_face_frames<2><<<grid, 128, 0, C.stream>>>(fa.coords, static_cast<double*>(fr), nfaces);
+      } else {
+        tg::k_face_frames<3><<<grid, 128, 0, C.stream>>>(fa.coords, static_cast<double*>(fr), nfaces);
+      }
+      TG_CUDA(&C, cudaGetLastError());
+    }
+  }
   TG_CUDA(&C, up(fa.edge_nbr, edge_nbr));
   TG_CUDA(&C, up(fa.vert, vert));
   TG_CUDA(&C, up(fa.cell_start, cell_start));

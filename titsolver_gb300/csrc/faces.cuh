@@ -43,6 +43,9 @@ namespace tg {
 // the tanks have particle walls.
 struct FaceArgs {
   const double* coords;       // D * D per face: the vertices a, b (, c)
+  // Per face its frame (k_face_frames): 2D the unit normal and tangent (4);
+  // 3D the unit normal n and the in-plane axes e1, e2 (9).
+  const double* frame;
   // Per face the coplanar neighbour across each edge (3D: ab, bc, ca;
   // shares the edge, traversed the other way, same plane and normal) or the
   // collinear neighbour across each end (2D: a, b; the segment ending at a
@@ -253,16 +256,23 @@ struct FaceFrame {
   double n[2], d, za, zb;
 };
 
-// Segment frame at x: unit normal cross(b - a) = (y, -x) normalised, signed
-// distance d and projections of the endpoints (units of h).
-__device__ __forceinline__ FaceFrame face_frame(const double* ab,
-                                                const double* x, double hinv) {
+// Unit normal cross(b - a) = (y, -x) normalised and unit tangent of a
+// segment: its frame (4 doubles), stored once per face.
+__device__ __forceinline__ void segment_axes(const double* ab, double* fr) {
   const double ba[2] = {ab[2] - ab[0], ab[3] - ab[1]};
   const double cr[2] = {ba[1], -ba[0]};
+  normalize2(cr, fr);
+  normalize2(ba, fr + 2);
+}
+
+// Segment frame at x from the stored axes fr: signed distance d and
+// projections of the endpoints (units of h).
+__device__ __forceinline__ FaceFrame face_frame(const double* ab, const double* fr,
+                                                const double* x, double hinv) {
   FaceFrame F;
-  normalize2(cr, F.n);
-  double e[2];
-  normalize2(ba, e);
+  F.n[0] = fr[0];
+  F.n[1] = fr[1];
+  const double* e = fr + 2;
   F.d = ((x[0] - ab[0]) * F.n[0] + (x[1] - ab[1]) * F.n[1]) * hinv;
   F.za = ((ab[0] - x[0]) * e[0] + (ab[1] - x[1]) * e[1]) * hinv;
   F.zb = ((ab[2] - x[0]) * e[0] + (ab[3] - x[1]) * e[1]) * hinv;
@@ -272,11 +282,11 @@ __device__ __forceinline__ FaceFrame face_frame(const double* ab,
 // Kernel::flux (kernel.hpp:194-206): n w h^-1 unit_flux(|d|, z_a, z_b);
 // wd = the kernel's 2D weight; the integral in type T.
 template<int K, class T = double>
-__device__ __forceinline__ void face_flux(const double* ab, const double* x,
-                                          double h, double wd, double* out,
-                                          unsigned skip = 0) {
+__device__ __forceinline__ void face_flux(const double* ab, const double* fr,
+                                          const double* x, double h, double wd,
+                                          double* out, unsigned skip = 0) {
   const double hinv = 1.0 / h;
-  const FaceFrame F = face_frame(ab, x, hinv);
+  const FaceFrame F = face_frame(ab, fr, x, hinv);
   const double u = static_cast<double>(face_unit_segment<K, false, T>(
       static_cast<T>(fabs(F.d)), static_cast<T>(F.za), static_cast<T>(F.zb), skip));
   const double s = wd * hinv * u;
@@ -286,10 +296,10 @@ __device__ __forceinline__ void face_flux(const double* ab, const double* x,
 
 // Kernel::antigrad_flux (kernel.hpp:209-221).
 template<int K, class T = double>
-__device__ __forceinline__ double face_antigrad_flux(const double* ab,
+__device__ __forceinline__ double face_antigrad_flux(const double* ab, const double* fr,
                                                      const double* x, double h,
                                                      double wd, unsigned skip = 0) {
-  const FaceFrame F = face_frame(ab, x, 1.0 / h);
+  const FaceFrame F = face_frame(ab, fr, x, 1.0 / h);
   const double u = static_cast<double>(face_unit_segment<K, true, T>(
       static_cast<T>(fabs(F.d)), static_cast<T>(F.za), static_cast<T>(F.zb), skip));
   return copysign(wd, F.d) * u;
@@ -605,8 +615,8 @@ __device__ __forceinline__ double dot_d(const double* a, const double* b) {
 struct TriFrame {
   double n[3], d, p[6];
 };
-__device__ __forceinline__ TriFrame tri_frame(const double* t, const double* x,
-                                              double hinv) {
+// The axes n, e1, e2 of a triangle (9 doubles), stored once per face.
+__device__ __forceinline__ void triangle_axes(const double* t, double* fr) {
   const double ba[3] = {t[3] - t[0], t[4] - t[1], t[5] - t[2]};
   const double ca[3] = {t[6] - t[0], t[7] - t[1], t[8] - t[2]};
   double wn[3];
@@ -614,12 +624,21 @@ __device__ __forceinline__ TriFrame tri_frame(const double* t, const double* x,
   wn[0] /= 2.0;
   wn[1] /= 2.0;
   wn[2] /= 2.0;
+  normalize3(wn, fr);
+  double u[3];
+  normalize3(ba, fr + 3);
+  face_cross(wn, fr + 3, u);
+  normalize3(u, fr + 6);
+}
+// Triangle frame at x from the stored axes fr.
+__device__ __forceinline__ TriFrame tri_frame(const double* t, const double* fr,
+                                              const double* x, double hinv) {
   TriFrame F;
-  normalize3(wn, F.n);
-  double e1[3], e2[3], u[3];
-  normalize3(ba, e1);
-  face_cross(wn, e1, u);
-  normalize3(u, e2);
+  F.n[0] = fr[0];
+  F.n[1] = fr[1];
+  F.n[2] = fr[2];
+  const double* e1 = fr + 3;
+  const double* e2 = fr + 6;
   const double xa[3] = {x[0] - t[0], x[1] - t[1], x[2] - t[2]};
   F.d = dot_d<3>(xa, F.n) * hinv;
   for (int i = 0; i < 3; ++i) {
@@ -630,23 +649,43 @@ __device__ __forceinline__ TriFrame tri_frame(const double* t, const double* x,
   return F;
 }
 
+// Doubles per face in FaceArgs::frame.
+template<int D>
+constexpr int kFrameDoubles = D == 2 ? 4 : 9;
+
+template<int D>
+__device__ __forceinline__ const double* face_axes(const FaceArgs& fc, uint32_t f) {
+  return fc.frame + kFrameDoubles<D> * static_cast<size_t>(f);
+}
+
+// The frames of all faces (one thread per face), written once when the
+// faces are set.
+template<int D>
+__global__ void k_face_frames(const double* coords, double* frame, uint32_t nfaces) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nfaces) return;
+  const size_t i = f;
+  if constexpr (D == 2) segment_axes(coords + 4 * i, frame + 4 * i);
+  else triangle_axes(coords + 9 * i, frame + 9 * i);
+}
+
 // Kernel::flux of face g (segment or triangle) at x; wd = the kernel's
 // weight in D dimensions.  Called by all lanes of a warp together (the 3D
 // integral is warp-cooperative); inactive lanes get zero.  skip: the
 // triangle's edges that cancel against in-range coplanar neighbours
 // (face_skip_edges).
-// The integral runs in type T (FaceReal of the form); frame, weights and
-// the result are FP64.
+// fr = the face's stored axes (face_axes).  The integral runs in type T
+// (float with tg_params.face_fp32); frame, weights and the result are FP64.
 template<int K, int D, class T = double>
-__device__ __forceinline__ void face_flux_d(bool active, const double* g,
+__device__ __forceinline__ void face_flux_d(bool active, const double* g, const double* fr,
                                             const double* x, double h, double wd,
                                             double* out, unsigned skip = 0) {
   if constexpr (D == 2) {
     out[0] = out[1] = 0.0;
-    if (active) face_flux<K, T>(g, x, h, wd, out, skip);
+    if (active) face_flux<K, T>(g, fr, x, h, wd, out, skip);
   } else {
     const double hinv = 1.0 / h;
-    const TriFrame F = tri_frame(g, x, hinv);
+    const TriFrame F = tri_frame(g, fr, x, hinv);
     T p[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) p[k] = static_cast<T>(F.p[k]);
@@ -662,12 +701,13 @@ __device__ __forceinline__ void face_flux_d(bool active, const double* g,
 // Kernel::antigrad_flux of face g at x (all lanes together, as above).
 template<int K, int D, class T = double>
 __device__ __forceinline__ double face_antigrad_flux_d(bool active, const double* g,
-                                                       const double* x, double h,
-                                                       double wd, unsigned skip = 0) {
+                                                       const double* fr, const double* x,
+                                                       double h, double wd,
+                                                       unsigned skip = 0) {
   if constexpr (D == 2) {
-    return active ? face_antigrad_flux<K, T>(g, x, h, wd, skip) : 0.0;
+    return active ? face_antigrad_flux<K, T>(g, fr, x, h, wd, skip) : 0.0;
   } else {
-    const TriFrame F = tri_frame(g, x, 1.0 / h);
+    const TriFrame F = tri_frame(g, fr, x, 1.0 / h);
     T p[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) p[k] = static_cast<T>(F.p[k]);
@@ -849,6 +889,68 @@ __device__ __forceinline__ void for_adjacent_faces(const FaceArgs& fc,
     fn(active, g, fc.coords + D * D * static_cast<size_t>(g));
   }
   __syncwarp();
+}
+
+// Capacity of the per-warp list of a face particle's in-range faces
+// (collect_adjacent_faces); a particle with more takes the list-free path.
+constexpr int kFaceListCap = 256;
+
+// The faces of the particle's cell list within the support radius of x
+// (the for_adjacent_faces predicate), ascending, into the warp's list; all
+// lanes call and get the count.  A count above cap means the list holds
+// only the first cap faces.
+template<int D>
+__device__ __forceinline__ int collect_adjacent_faces(const FaceArgs& fc, uint32_t gcell,
+                                                      const double* x, double radius,
+                                                      int lane, uint32_t* list, int cap) {
+  __syncwarp();  // the previous particle's readers are done with the list
+  const uint32_t s = fc.cell_start[gcell], e = fc.cell_start[gcell + 1];
+  int count = 0;
+  for (uint32_t base = s; base < e; base += 32) {
+    const uint32_t i = base + static_cast<uint32_t>(lane);
+    bool in = false;
+    uint32_t f = 0;
+    if (i < e) {
+      f = fc.cell_face[i];
+      const double* g = fc.coords + D * D * static_cast<size_t>(f);
+      if constexpr (D == 2) in = segment_in_sphere(g, x, radius);
+      else in = triangle_in_sphere(g, x, radius);
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, in);
+    const int slot = count + __popc(mask & ((1u << lane) - 1u));
+    if (in && slot < cap) list[slot] = f;
+    count += __popc(mask);
+  }
+  __syncwarp();
+  return count;
+}
+
+// Whether face f is in the ascending list of n faces.
+__device__ __forceinline__ bool face_listed(const uint32_t* list, int n, uint32_t f) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (list[mid] < f) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < n && list[lo] == f;
+}
+
+// face_skip_edges with the in-range test of the neighbours answered by the
+// particle's complete list of in-range faces: a neighbour within the
+// support radius is in the particle's cell list (which holds every face
+// within reach of the cell), so it is listed exactly when the sphere test
+// passes.
+template<int D>
+__device__ __forceinline__ unsigned face_skip_edges_listed(const FaceArgs& fc, uint32_t f,
+                                                           const uint32_t* list, int n) {
+  unsigned skip = 0;
+#pragma unroll
+  for (int e = 0; e < (D == 2 ? 2 : 3); ++e) {
+    const int32_t nb = fc.edge_nbr[(D == 2 ? 2 : 3) * static_cast<size_t>(f) + e];
+    if (nb >= 0 && face_listed(list, n, static_cast<uint32_t>(nb))) skip |= 1u << e;
+  }
+  return skip;
 }
 
 // Sum over the lanes of a warp (all lanes active), butterfly order.

@@ -1201,7 +1201,7 @@ __global__ void __launch_bounds__(128) k_face_terms(StageArgs<D, F> A) {
       // Each face's flux is weighted by its own vertex densities and
       // pressures, so no edges cancel here.
       double gg[3];
-      face_flux_d<K, D, FT>(active, g, pa, T.h, fc.weight, gg);
+      face_flux_d<K, D, FT>(active, g, face_axes<D>(fc, f), pa, T.h, fc.weight, gg);
       if (!active) return;
       double rv[3], pv[3];
 #pragma unroll
@@ -1794,8 +1794,10 @@ __global__ void __launch_bounds__(128) k_gamma_init(StageArgs<D, F> A) {
 
 template<int D, int K, int F, class FT>
 __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
+  __shared__ uint32_t flist_all[kFaceBlock / 32][kFaceListCap];
   const FaceArgs& fc = A.fc;
   const int lane = threadIdx.x & 31;
+  uint32_t* flist = flist_all[threadIdx.x >> 5];
   const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
   const uint32_t count = *fc.face_count;
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += nwarps) {
@@ -1812,13 +1814,31 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
     for (int k = 0; k < D; ++k) x[k] = A.Y.pos[k][i];
     const double radius = KernelPoly<K>::unit_radius * T.h;
     const double wd = fc.weight;
+    // The in-range faces of x, found once for both sweeps (the antigradient
+    // sweep at xs keeps the adjacency of x); the skip masks come from the
+    // same list.  Past the list's capacity both sweeps test the cell list
+    // again, as for_adjacent_faces does.
+    const int nf = collect_adjacent_faces<D>(fc, gcell, x, radius, lane, flist, kFaceListCap);
+    auto sweep = [&](auto&& fn) {
+      if (nf <= kFaceListCap) {
+        for (int base = 0; base < nf; base += 32) {
+          const bool active = base + lane < nf;
+          const uint32_t fi = flist[active ? base + lane : base];
+          const unsigned skip = active ? face_skip_edges_listed<D>(fc, fi, flist, nf) : 0u;
+          fn(active, fi, fc.coords + D * D * static_cast<size_t>(fi), skip);
+        }
+      } else {
+        for_adjacent_faces<D>(fc, gcell, x, radius, lane,
+                              [&](bool active, uint32_t fi, const double* f) {
+          const unsigned skip = active ? face_skip_edges<D>(fc, fi, x, radius) : 0u;
+          fn(active, fi, f, skip);
+        });
+      }
+    };
     double g[3] = {0.0, 0.0, 0.0};
-    for_adjacent_faces<D>(fc, gcell, x, radius, lane,
-                          [&](bool active, uint32_t fi, const double* f) {
+    sweep([&](bool active, uint32_t fi, const double* f, unsigned skip) {
       double fl[3];
-      unsigned skip = 0;
-      if (active) skip = face_skip_edges<D>(fc, fi, x, radius);
-      face_flux_d<K, D, FT>(active, f, x, T.h, wd, fl, skip);
+      face_flux_d<K, D, FT>(active, f, face_axes<D>(fc, fi), x, T.h, wd, fl, skip);
       if (!active) return;
 #pragma unroll
       for (int k = 0; k < D; ++k) g[k] += fl[k];
@@ -1845,12 +1865,9 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
 #pragma unroll
       for (int k = 0; k < D; ++k) xs[k] = x[k] + s * (g[k] / ng) * h2;
       double ag = 0.0;
-      for_adjacent_faces<D>(fc, gcell, x, radius, lane,
-                            [&](bool active, uint32_t fi, const double* f) {
-        // The adjacency is that of x (the face set does not move with xs).
-        unsigned skip = 0;
-        if (active) skip = face_skip_edges<D>(fc, fi, x, radius);
-        const double a = face_antigrad_flux_d<K, D, FT>(active, f, xs, T.h, wd, skip);
+      sweep([&](bool active, uint32_t fi, const double* f, unsigned skip) {
+        const double a =
+            face_antigrad_flux_d<K, D, FT>(active, f, face_axes<D>(fc, fi), xs, T.h, wd, skip);
         if (active) ag += a;
       });
       ga -= warp_sum(ag);

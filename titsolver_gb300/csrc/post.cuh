@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(128) k_post_faces(PostArgs<D, F> A) {
                           [&](bool active, uint32_t f, const double* g) {
       // Per-face weights (vertex density, face centre): no edges cancel.
       double gg[3], rv[3], r_sa[3];
-      face_flux_d<K, D, FT>(active, g, pa, T.h, fc.weight, gg);
+      face_flux_d<K, D, FT>(active, g, face_axes<D>(fc, f), pa, T.h, fc.weight, gg);
       if (!active) return;
 #pragma unroll
       for (int j = 0; j < D; ++j) rv[j] = vertex_rho(A.S.datrec, fc.slot_of[fc.vert[D * f + j]], T);
