@@ -62,14 +62,19 @@ INTEGRATORS = {"ssprk3": _abi.TG_SSPRK3, "ssprk2": _abi.TG_SSPRK2,
     (False, "ssprk3", True, False), (True, "ssprk3", True, False),
     (False, "ssprk3", False, False), (False, "ssprk2", True, False),
     (False, "euler", True, False), (False, "verlet", False, False),
-    (False, "ssprk3", True, True), (False, "verlet", True, True), (True, "ssprk3", True, True)])
+    (False, "ssprk3", True, True), (False, "verlet", True, True), (True, "ssprk3", True, True),
+    ("face32", "ssprk3", True, True)])
 def test_driver_matches_oracle(gpu_lib, tmp_path, fp32c, integrator, shifting, faces):
+    # fp32c = "face32": the compensated form with --face-fp32 (FP32 face
+    # integrals), held to the compensated form's tolerances.
     exe = gpu_build.build_host()["titwcsph_gpu"]
     dump, ttdb = tmp_path / "state.bin", tmp_path / "particles.ttdb"
     cmd = [str(exe), "--nx", "20", "--steps", "20", "--dump", str(dump), "--ttdb", str(ttdb),
            "--integrator", integrator]
     if fp32c:
         cmd.append("--fp32c")
+    if fp32c == "face32":
+        cmd.append("--face-fp32")
     if not shifting:
         cmd.append("--no-shifting")
     if faces:

@@ -194,6 +194,23 @@ def test_faces_fp32_compensated_vs_fp64_oracle(gpu_lib, shifting):
     assert rel_l2(g["r"][f], o.r[f]) <= 1e-6
 
 
+def test_3d_faces_past_the_warp_face_list(gpu_lib):
+    # Walls tessellated at dr/3: a particle next to a wall has more faces
+    # within its support radius than the per-warp list of k_gamma_faces
+    # holds (256), so it takes the list-free path while particles further
+    # from the walls take the listed one; both against the oracle.
+    scn = scenarios.dam_break_3d_faces(nx_per_H=6, tank=(3.0, 1.5), face_refine=3)
+    t = scn["tanks"][0]
+    radius = 2.0 * t["h"]
+    cent = scn["r"][t["n_fluid"]:][scn["faces"][0]["face_verts"]].mean(axis=1)
+    fl = scn["r"][:t["n_fluid"]]
+    # A face whose centroid lies within the radius is within reach.
+    within = (((fl[:, None, :] - cent[None, :, :]) ** 2).sum(-1) <= radius ** 2).sum(1)
+    assert within.max() > 256
+    assert within.min() <= 256
+    _compare(scn, physics.reference_params(3), 2, 1e-10)
+
+
 def _fp32_faces_params(dim, shifting, face_fp32, kernel=_abi.TG_KERNEL_WENDLAND_C4):
     P = physics.reference_params(dim, precision=_abi.TG_FP32C, kernel=kernel)
     P.post_integrate = _abi.TG_POST_SHIFTING if shifting else _abi.TG_POST_PREPARE

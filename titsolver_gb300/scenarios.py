@@ -214,12 +214,13 @@ def box_faces(width: float, height: float, depth: float, dx: float):
 
 def dam_break_3d_faces(nx_per_H: int = 80, H: float = 0.6, column=(2.0, 1.0, 1.0),
                        tank=(5.366, 4.0), h_factor: float = 1.3, g: float = G,
-                       rho0: float = RHO0) -> dict:
+                       rho0: float = RHO0, face_refine: int = 1) -> dict:
     """The titwcsph scenario extruded to 3D with triangle faces: column
     column * H at dr (i + 1, j + 1, k + 1), pool tank[0] H x tank[1] H x
-    (K + 1) dr whose triangulated sides (box_faces) carry one fixed particle
-    per vertex, cs0 = 20 sqrt(gH), h = h_factor dr, m = rho0 dr^3,
-    hydrostatic density; the containment is the pool box (box_mesh)."""
+    (K + 1) dr whose triangulated sides (box_faces at dr / face_refine) carry
+    one fixed particle per vertex, cs0 = 20 sqrt(gH), h = h_factor dr,
+    m = rho0 dr^3, hydrostatic density; the containment is the pool box
+    (box_mesh)."""
     dx = H / nx_per_H
     L = column[0] * H
     M = int(round(L / dx))
@@ -229,7 +230,7 @@ def dam_break_3d_faces(nx_per_H: int = 80, H: float = 0.6, column=(2.0, 1.0, 1.0
     fluid = np.stack([dx * (i.ravel() + 1.0), dx * (j.ravel() + 1.0),
                       dx * (k.ravel() + 1.0)], axis=1)
     W, Ht, D = tank[0] * H, tank[1] * H, (K + 1) * dx
-    walls, faces = box_faces(W, Ht, D, dx)
+    walls, faces = box_faces(W, Ht, D, dx / face_refine)
     cs0 = 20.0 * math.sqrt(g * H)
     p = hydrostatic_pressure(fluid[:, 0], fluid[:, 1], H, L, g, rho0)
     rho_f = rho0 + p / (cs0 * cs0)
