@@ -191,10 +191,13 @@ def forces_traffic(dim: int, form: str, n_fluid: int):
     return float(d[key]["dram_bytes_per_fluid_particle"]) * n_fluid
 
 
-def cpu_sample(budget_s: float, steps: int, threads: int, fill: bool = False) -> dict:
+def cpu_sample(budget_s: float, steps: int, threads: int, fill: bool = False,
+               workload: dict | None = None) -> dict:
     """Time the oracle (CPU restatement of the reference path) on a dam break
     sized so that `steps` steps take about budget_s seconds (with fill, more
-    steps when the largest sample size is reached first)."""
+    steps when the largest sample size is reached first).  A 2D one-tank
+    workload smaller than that size is timed itself, with as many steps as
+    fill the budget (nx_per_H = 0 in the result)."""
     import oracle
     from titsolver_gb300 import physics, scenarios
 
@@ -207,6 +210,10 @@ def cpu_sample(budget_s: float, steps: int, threads: int, fill: bool = False) ->
     want = rate * budget_s / max(steps, 1)
     nx = int(max(40, min(800, math.sqrt(want / 2.0))))
     scn = scenarios.dam_break_2d(nx_per_H=nx)
+    if (workload is not None and workload["dim"] == 2 and len(workload["tanks"]) == 1
+            and not any(workload.get("faces") or [])
+            and workload["tanks"][0]["n_fluid"] < scn["tanks"][0]["n_fluid"]):
+        scn, nx = workload, 0
     st = oracle.State(scn)
     nf = scn["tanks"][0]["n_fluid"]
     if fill:
@@ -216,7 +223,7 @@ def cpu_sample(budget_s: float, steps: int, threads: int, fill: bool = False) ->
         t0 = time.perf_counter()
         oracle.step(P, st, 1, nthreads=threads)
         one = max(time.perf_counter() - t0, 1e-6)
-        steps = max(steps, min(50, int(budget_s / one)))
+        steps = max(steps, min(50 if nx else 200, int(budget_s / one)))
     t0 = time.perf_counter()
     oracle.step(P, st, steps, nthreads=threads)
     sec = time.perf_counter() - t0
@@ -230,10 +237,14 @@ def run_reference(args, ranks) -> dict:
     threads = oracle.default_threads()
     # Each timed step is one SSPRK3 step of a dam break sized so the whole
     # run takes about two minutes of host time.
-    res = cpu_sample(120.0, args.steps, threads)
-    workload, _ = make_config(args.config)
-    sample = (f"2D dam break dx=H/{res['nx_per_H']} ({res['fluid']} fluid), same physics, "
-              f"{res['steps']} SSPRK3 steps per timed run ({res['seconds']:.1f} s)")
+    workload, make = make_config(args.config)
+    # c0 is the one 2D single-tank workload smaller than the sample size.
+    res = cpu_sample(120.0, args.steps, threads,
+                     workload=make() if args.config == "c0" else None)
+    what = (f"the workload itself ({res['fluid']} fluid)" if res["nx_per_H"] == 0 else
+            f"2D dam break dx=H/{res['nx_per_H']} ({res['fluid']} fluid)")
+    sample = (f"{what}, same physics, {res['steps']} SSPRK3 steps per timed run "
+              f"({res['seconds']:.1f} s)")
     return {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
@@ -402,11 +413,12 @@ def run_gpu(args, ranks) -> dict | None:
         if ranks.world_size == 1 and not args.no_cpu:
             import oracle
             threads = oracle.default_threads()
-            c = cpu_sample(args.cpu_budget, 2, threads, fill=True)
+            c = cpu_sample(args.cpu_budget, 2, threads, fill=True, workload=scn)
+            what = (f"the workload itself ({c['fluid']} fluid)" if c["nx_per_H"] == 0 else
+                    f"2D dam break dx=H/{c['nx_per_H']} ({c['fluid']} fluid)")
             cpu = {"value": c["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": (f"2D dam break dx=H/{c['nx_per_H']} ({c['fluid']} fluid), "
-                              f"same physics, {c['steps']} SSPRK3 steps, {c['seconds']:.1f} s, "
-                              "oracle built g++ -O3 -ffp-contract=off")}
+                   "sample": (f"{what}, same physics, {c['steps']} SSPRK3 steps, "
+                              f"{c['seconds']:.1f} s, oracle built g++ -O3 -ffp-contract=off")}
         ws = scn["r"].shape[0] * 260
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
