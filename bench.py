@@ -21,6 +21,9 @@ one full SSPRK3 step (three neighbour rebuilds, three fused force passes).
 * ``roofline``: the fused force kernel (k_forces): algorithmic bytes per
   launch = fluid particles x 3S (S = state bytes per particle) over its mean
   launch time from a profiled pass with CUDA events on the same stream.
+  The kernel is not HBM-bound; ``ncu_working_ceiling`` carries, from its
+  recorded ncu capture under ``profiles/``, the unit that bounds it and how
+  busy that unit was.
 * ``cpu_baseline``: the oracle (the C++ restatement of the reference's CPU
   path) on the host cores, on a bounded sample of the same workload.
 
@@ -180,15 +183,26 @@ class ClockSampler:
                 "samples": len(rows), "reasons": reasons}
 
 
-def forces_traffic(dim: int, form: str, n_fluid: int):
+def _forces_profile(dim: int, form: str) -> dict | None:
     p = ROOT / "profiles" / "forces_traffic.json"
     if not p.exists():
         return None
-    d = json.loads(p.read_text())
-    key = f"{form}_{dim}d"
-    if key not in d:
+    return json.loads(p.read_text()).get(f"{form}_{dim}d")
+
+
+def forces_traffic(dim: int, form: str, n_fluid: int):
+    d = _forces_profile(dim, form)
+    return None if d is None else float(d["dram_bytes_per_fluid_particle"]) * n_fluid
+
+
+def forces_ceiling(dim: int, form: str) -> dict | None:
+    """The unit that bounds k_forces in its ncu capture (issue slots for the
+    compensated form, the FP64 pipe for the plain one) and how busy it was:
+    a recorded capture, beside the live HBM fraction."""
+    d = _forces_profile(dim, form)
+    if d is None or "working_ceiling" not in d:
         return None
-    return float(d[key]["dram_bytes_per_fluid_particle"]) * n_fluid
+    return {**d["working_ceiling"], "source": d["source"]}
 
 
 def cpu_sample(budget_s: float, steps: int, threads: int, fill: bool = False,
@@ -401,7 +415,8 @@ def run_gpu(args, ranks) -> dict | None:
                 "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": f"{peaks['source']} hbm_gbs",
-                "alg_bytes_per_launch": alg, "avg_launch_ms": forces_avg_ms}
+                "alg_bytes_per_launch": alg, "avg_launch_ms": forces_avg_ms,
+                "ncu_working_ceiling": forces_ceiling(dim, "fp32c")}
 
     def shares(p):
         tot = p["sort_ms"] + p["reorder_ms"] + p["walls_ms"] + p["forces_ms"]
