@@ -3,7 +3,10 @@ the host cores): the 2D dam break at dx = H/800 (1,280,000 fluid, config C1)
 and the 3D dam break at dx = H/100 (2,000,000 fluid).
 
 * neighbour sets: counts and order-independent hashes of every particle
-  equal to the oracle's grid search (bit-exact predicate);
+  equal to the oracle's grid search (bit-exact predicate), in the plain
+  FP64 form and in the FP32-compensated form (whose FP32 test of
+  cell-relative offsets defers pairs near the support radius to the FP64
+  predicate), at the lattice start and after 20 steps of motion;
 * one plain FP64 step: r, v, rho within 1e-12 relative L2 of the oracle and
   the same dt; wall densities within 1e-12;
 * the FP32-compensated step against the FP64 oracle within the compensated
@@ -38,6 +41,25 @@ def test_full_size_neighbour_sets(gpu_lib, case):
     with gpu_context(scn, P) as ctx:
         cnt, hs = ctx.neighbour_counts()
     ocnt, ohs = oracle.tank_neighbour_counts(P, scn["tanks"], scn["r"])
+    np.testing.assert_array_equal(cnt, ocnt, err_msg=name)
+    np.testing.assert_array_equal(hs, ohs, err_msg=name)
+
+
+def test_full_size_neighbour_sets_fp32c(gpu_lib, case):
+    name, scn, _, _ = case
+    P32 = physics.baseline_params(scn["dim"], precision=_abi.TG_FP32C)
+    with gpu_context(scn, P32) as ctx:
+        cnt, hs = ctx.neighbour_counts()
+        ocnt, ohs = oracle.tank_neighbour_counts(P32, scn["tanks"], scn["r"])
+        np.testing.assert_array_equal(cnt, ocnt, err_msg=name)
+        np.testing.assert_array_equal(hs, ohs, err_msg=name)
+        # Moved particles: generic distances, the FP32 test decides almost
+        # every pair.
+        ctx.step(20)
+        r = ctx.download(_abi.TG_FIELD_R)
+        cnt, hs = ctx.neighbour_counts()
+    assert not np.array_equal(r, scn["r"])
+    ocnt, ohs = oracle.tank_neighbour_counts(P32, scn["tanks"], r)
     np.testing.assert_array_equal(cnt, ocnt, err_msg=name)
     np.testing.assert_array_equal(hs, ohs, err_msg=name)
 

@@ -67,6 +67,65 @@ def test_neighbour_sets_cloud_3d_fp64(gpu_lib, cells_per_radius):
     np.testing.assert_array_equal(hs, ohs)
 
 
+def _fp32c_sets_match(scn, P32, steps=0):
+    """Counts, hashes and (small cases) full lists of the compensated form's
+    neighbour sets against the oracle's FP64 grid search, on the context's
+    positions after `steps` steps."""
+    with gpu_context(scn, P32) as ctx:
+        if steps:
+            ctx.step(steps)
+        r = ctx.download(_abi.TG_FIELD_R)
+        cnt, hs = ctx.neighbour_counts()
+        lists = ctx.neighbour_lists() if r.shape[0] <= 20_000 else None
+    ocnt, ohs = oracle.tank_neighbour_counts(P32, scn["tanks"], r)
+    np.testing.assert_array_equal(cnt, ocnt)
+    np.testing.assert_array_equal(hs, ohs)
+    if lists is not None and len(scn["tanks"]) == 1:
+        t = scn["tanks"][0]
+        unit = 2.0  # support radius / h of the Wendland kernels used here
+        ooff, oidx = oracle.grid_search(r, unit * t["h"], t["h"])
+        assert _rows(*lists) == _rows(ooff, oidx)
+
+
+@pytest.mark.parametrize("nx", (10, 80))
+@pytest.mark.parametrize("steps", (0, 30))
+def test_neighbour_sets_fp32c_dam_break_2d(gpu_lib, nx, steps):
+    # At the lattice start, axis neighbours at exactly 2h fall in the band
+    # around the support radius and are decided by the FP64 predicate.
+    scn = scenarios.dam_break_2d(nx_per_H=nx)
+    _fp32c_sets_match(scn, physics.baseline_params(2, precision=_abi.TG_FP32C), steps)
+
+
+@pytest.mark.parametrize("steps", (0, 20))
+def test_neighbour_sets_fp32c_dam_break_3d(gpu_lib, steps):
+    scn = scenarios.dam_break_3d(nx_per_H=10)
+    _fp32c_sets_match(scn, physics.baseline_params(3, precision=_abi.TG_FP32C), steps)
+
+
+@pytest.mark.parametrize("cells_per_radius", (1, 2, 3))
+def test_neighbour_sets_fp32c_cloud_3d(gpu_lib, cells_per_radius):
+    scn = scenarios.cloud_3d(n_total=30_000, seed=9)
+    P = physics.baseline_params(3, precision=_abi.TG_FP32C)
+    P.cells_per_radius = cells_per_radius
+    _fp32c_sets_match(scn, P)
+
+
+@pytest.mark.parametrize("dim", (2, 3))
+def test_neighbour_sets_fp32c_mt19937_match_naive(gpu_lib, dim):
+    pts = oracle.mt19937_uniform_points(123, 200, dim)
+    for radius in (0.01, 0.1, 0.5, 1.0):
+        scn = _points_scenario(pts, radius / 2)
+        with gpu_context(scn, physics.baseline_params(dim, precision=_abi.TG_FP32C)) as ctx:
+            off, idx = ctx.neighbour_lists()
+        naive = _rows(*oracle.naive_search(pts, radius, inclusive=False))
+        assert _rows(off, idx) == naive, radius
+
+
+def test_neighbour_sets_fp32c_batched_tanks(gpu_lib):
+    scn = scenarios.batched_tanks(n_tanks=6, n_range=(8, 16), seed=4)
+    _fp32c_sets_match(scn, physics.baseline_params(2, precision=_abi.TG_FP32C), 10)
+
+
 def test_summation_density_golden_fp64_and_fp32(gpu_lib):
     import pathlib
     z = np.load(pathlib.Path(__file__).resolve().parent / "golden" / "cloud_small.npz")

@@ -485,6 +485,8 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     const float hf = static_cast<float>(T.h);
     const float Rf = static_cast<float>(tg::kernel_unit_radius(C.P.kernel)) * hf;
     D.radius2_f = Rf * Rf;
+    D.band_lo_f = static_cast<float>(R * R * (1.0 - 1.0 / 16384.0));
+    D.band_hi_f = static_cast<float>(R * R * (1.0 + 1.0 / 16384.0));
     D.cs_f = static_cast<float>(cs);
     double hinv_d = 1.0;
     for (int k = 0; k < dim; ++k) hinv_d *= D.hinv;

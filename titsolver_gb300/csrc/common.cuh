@@ -58,6 +58,11 @@ struct TankDev {
   // (R (1 + 2^-12) + 2^-19 extent)^2: the wall pass's fluid-box test radius
   // in tank-local FP32 coordinates (extent = the grid's largest side).
   float wall_skip_r2_f;
+  // The compensated form's neighbour band: an FP32 squared distance below
+  // band_lo_f is a neighbour and one above band_hi_f is not (R^2 (1 -+ 2^-14),
+  // far outside the FP32 error of the cell-relative offsets); between them
+  // the pair is decided by the FP64 predicate on the FP64 positions.
+  float band_lo_f, band_hi_f;
 };
 
 struct PhysDev {

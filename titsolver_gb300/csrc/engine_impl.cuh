@@ -480,6 +480,17 @@ class Engine final : public EngineBase {
           staged = true;
         }
       }
+      if (!staged && C.P.staging == 2 && C.force_team == 1 && C.k <= 3 &&
+          C.n < kNbMaxParticles) {
+        if (phys == kPhysTextbook) {
+          launch_forces_nbl<kPhysTextbook>(C, a);
+        } else if (phys == kPhysReference) {
+          launch_forces_nbl<kPhysReference>(C, a);
+        } else {
+          launch_forces_nbl<kPhysGeneric>(C, a);
+        }
+        staged = true;
+      }
       if (staged) {
       } else if (phys == kPhysTextbook) {
         launch_forces<kPhysTextbook>(C, a);
@@ -515,6 +526,17 @@ class Engine final : public EngineBase {
       }
     }
     k_forces<D, F, K, Phys, 1><<<grid_for(C.n, block), block, 0, C.stream>>>(a);
+  }
+
+  // The compensated pass with per-thread neighbour lists (one lane per
+  // target; its lists take kNbCap words of shared memory per thread).
+  template<int Phys>
+  void launch_forces_nbl(Context& C, const StageArgs<D, F>& a) {
+    if constexpr (F == TG_FP32C) {
+      const int block = C.force_block;
+      const size_t smem = sizeof(uint32_t) * kNbCap * static_cast<size_t>(block);
+      k_forces_nbl<D, K, Phys><<<grid_for(C.n, block), block, smem, C.stream>>>(a);
+    }
   }
 
   StateBuf<R> X_{}, Y_{};

@@ -492,6 +492,58 @@ __device__ __forceinline__ float dist2_exact(const float* a, const float* b,
   return s;
 }
 
+// The compensated form's neighbour predicate.  Its FP32 squared distance
+// s2_f comes from cell-relative offsets, each rounded once from an exact
+// FP64 difference.  With u = 2^-24, offsets within a cell size cs (plus a
+// few ulps) of their cell corner and the candidate's cell within k cells of
+// the target's (cs = R / k), each FP32 component of r_ab is within
+// (3k + 3) u cs + u |r_ab| <= 7 u R of the exact one (the FP64 cell corners
+// add 2^-52 of the coordinates, negligible within 2^20 cells of the
+// origin), so |s2_f - s2| < 32 u R^2: far inside the band R^2 (1 -+ 2^-14)
+// = R^2 (1 -+ 1024 u).  Below the band the pair is a neighbour, above it is
+// not; inside it the reference's own predicate decides (dist2_exact on the
+// cell-ordered FP64 positions against the FP64 R^2), so the set is exactly
+// the reference's.  A particle clamped into a border cell may carry an
+// offset of any size, so every candidate seen from or in a border cell is
+// decided in FP64 (border cells are empty unless a particle left the grid).
+struct Band {
+  float lo, hi;
+};
+
+template<int D>
+__device__ __forceinline__ bool border_cell(const TankDev& T, const int* c) {
+  bool b = c[0] <= 0 || c[0] >= T.nc[0] - 1 || c[1] <= 0 || c[1] >= T.nc[1] - 1;
+  if constexpr (D == 3) b = b || c[2] <= 0 || c[2] >= T.nc[2] - 1;
+  return b;
+}
+
+// Band of one visited cell at (dx, dy, dz) from the target's cell c or, with
+// row set, of one row of cells at (dy, dz) whose x range lies within
+// c[0] -+ k.
+template<int D>
+__device__ __forceinline__ Band visit_band(const TankDev& T, const int* c, int k,
+                                           int dx, int dy, int dz, bool row,
+                                           bool target_border) {
+  const int cc[3] = {c[0] + dx, c[1] + dy, D == 3 ? c[2] + dz : 0};
+  bool b = target_border || border_cell<D>(T, cc);
+  if (row) b = b || c[0] - k <= 0 || c[0] + k >= T.nc[0] - 1;
+  return b ? Band{-1.f, __int_as_float(0x7f800000)} : Band{T.band_lo_f, T.band_hi_f};
+}
+
+// The reference predicate |r_a - r_b|^2 <= R^2 on the FP64 positions of
+// cell-order slots a and b.
+template<int D>
+__device__ __forceinline__ bool within_fp64(double* const* pos, uint32_t a,
+                                            uint32_t b, double R2) {
+  double pa[3], pb[3], d[3];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    pa[k] = pos[k][a];
+    pb[k] = pos[k][b];
+  }
+  return dist2_exact<D>(pa, pb, d) <= R2;
+}
+
 __device__ __forceinline__ bool finite_bits(double x) {
   return (static_cast<unsigned long long>(__double_as_longlong(x)) &
           0x7ff0000000000000ull) != 0x7ff0000000000000ull;
@@ -772,7 +824,7 @@ __global__ void __launch_bounds__(128)
     const double inv = 1.0 / rho_e;
     A.datrec[e] = Dat64{0.0, 0.0, 0.0, rho_e, pr * inv * inv, cc, inv, 0.0};
   } else {
-    const float R2 = T.radius2_f, hinv = T.hinv_f;
+    const float hinv = T.hinv_f;
     const float w = T.w_f, m = T.m_f;
     const float csz = T.cs_f;
     float oe[3] = {0.f, 0.f, 0.f};
@@ -795,7 +847,9 @@ __global__ void __launch_bounds__(128)
       for (int k = 0; k < D; ++k) nef[k] = static_cast<float>(ne[k]);
     }
     if (valid && !A.walls_keep && !skip) {
+      const bool tborder = border_cell<D>(T, c);
       auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+        const Band bd = visit_band<D>(T, c, A.k, dx, dy, dz, false, tborder);
         float oes[3];
         oes[0] = oe[0] - dx * csz;
         oes[1] = oe[1] - dy * csz;
@@ -804,7 +858,8 @@ __global__ void __launch_bounds__(128)
           float ob[3], d[3];
           load_pos(A.posrec, j, ob);
           const float s2 = dist2_exact<D>(oes, ob, d);
-          if (s2 > R2) continue;
+          if (s2 > bd.hi) continue;
+          if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, e, j, T.radius2)) continue;
           const Dat32 b = load_dat_coherent(A.datrec, j);
           const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
           const float Vb = m * b.invrho;
@@ -822,6 +877,7 @@ __global__ void __launch_bounds__(128)
         // One range per row of cells (records carry the cell's x index and
         // the wall bit), fluid records only.
         auto visit_row = [&](uint32_t s, uint32_t en, int, int dy, int dz) {
+          const Band bd = visit_band<D>(T, c, A.k, 0, dy, dz, true, tborder);
           const float oey = oe[1] - dy * csz;
           const float oez = oe[2] - dz * csz;
           for (uint32_t j = s; j < en; ++j) {
@@ -834,7 +890,8 @@ __global__ void __launch_bounds__(128)
             d[1] = oey - b.y;
             d[2] = oez - b.z;
             const float s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-            if (s2 > R2) continue;
+            if (s2 > bd.hi) continue;
+            if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, e, j, T.radius2)) continue;
             const Dat32 bd = load_dat_coherent(A.datrec, j);
             const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
             const float Vb = m * bd.invrho;
@@ -918,7 +975,7 @@ template<int D, int K, int Phys = kPhysGeneric>
 struct PairF32 {
   float va[3];
   Dat32 a;
-  float R2, hinv, wg, m, mu2, ah, eps2, dk, rho0x2;
+  float hinv, wg, m, mu2, ah, eps2, dk, rho0x2;
   int visc, diff;
   bool kahan;
   Kahan drho, dv[3];
@@ -948,7 +1005,6 @@ struct PairF32 {
     va[0] = own.vx;
     va[1] = own.vy;
     va[2] = own.vz;
-    R2 = T.radius2_f;
     hinv = T.hinv_f;
     wg = T.wg_f;
     m = T.m_f;
@@ -963,7 +1019,7 @@ struct PairF32 {
     dv[1].s = -P.g_f;
   }
 
-  // One neighbour at r_ab = d (|d|^2 = s2 <= R2, b != a).
+  // One neighbour at r_ab = d (|d|^2 = s2, within the support, b != a).
   __device__ __forceinline__ void add(const float* d, float s2, const Dat32& b) {
     const float rinv = rsqrtf(s2);
     const float r = s2 * rinv;
@@ -1365,21 +1421,25 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
     const float csz = T.cs_f;
+    const bool tborder = border_cell<D>(T, c);
+    const uint32_t ia = static_cast<uint32_t>(i);
     auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      const Band bd = visit_band<D>(T, c, A.k, dx, dy, dz, false, tborder);
       float oas[3];
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
       oas[2] = D == 3 ? oa[2] - dz * csz : 0.f;
       acc.open();
       for (uint32_t j = s; j < en; ++j) {
-        if (j == static_cast<uint32_t>(i)) continue;
+        if (j == ia) continue;
         float ob[3], d[3];
         load_pos(A.posrec, j, ob);
 #pragma unroll
         for (int k = 0; k < D; ++k) d[k] = oas[k] - ob[k];
         float s2 = d[0] * d[0] + d[1] * d[1];
         if constexpr (D == 3) s2 += d[2] * d[2];
-        if (s2 > acc.R2) continue;
+        if (s2 > bd.hi) continue;
+        if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
         acc.add(d, s2, load_dat(A.datrec, j));
       }
       acc.close();
@@ -1389,11 +1449,12 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     // candidates in the same order as the per-cell walk.
     auto visit_row = [&](uint32_t s, uint32_t en, int, int dy, int dz) {
       if constexpr (D == 3) {
+        const Band bd = visit_band<D>(T, c, A.k, 0, dy, dz, true, tborder);
         const float oay = oa[1] - dy * csz;
         const float oaz = oa[2] - dz * csz;
         acc.open();
         for (uint32_t j = s; j < en; ++j) {
-          if (j == static_cast<uint32_t>(i)) continue;
+          if (j == ia) continue;
           const Pos32_3 b = A.posrec[j];
           const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
           float d[3];
@@ -1401,7 +1462,8 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
           d[1] = oay - b.y;
           d[2] = oaz - b.z;
           const float s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-          if (s2 > acc.R2) continue;
+          if (s2 > bd.hi) continue;
+          if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
           acc.add(d, s2, load_dat(A.datrec, j));
         }
         acc.close();
@@ -1445,6 +1507,165 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     }
   }
   forces_epilogue<D, F>(A, i, id, tk, T, c, va, rho_self, dv_out, drho_out);
+}
+
+// Compensated force pass with per-thread neighbour lists, one lane per
+// fluid target, in two phases.  The scan walks the candidates (2D: per
+// cell; 3D: per row of cells, clipped as in k_forces) and keeps each
+// neighbour (the band predicate above) in the thread's column of a
+// shared-memory list as (j << 6) | the range's offset code; the evaluation
+// then runs the pair terms over the list.  A warp thereby steps through the
+// pair terms once per listed neighbour of its busiest lane instead of once
+// per candidate that any of its lanes accepts.  The walk visits the same
+// (2k+1)^(D-1) rows or (2k+1)^2 cells for every lane (clipped ones empty),
+// so after each range the lanes agree by vote to evaluate their lists
+// together once some list holds kNbFlush entries; a list that fills inside
+// one range is evaluated there.  The sums run in chunks of kNbChunk plain
+// pair terms, each chunk one compensated add.  Entries need j < 2^26 and
+// k <= 3 (offsets in [-3, 3]).
+constexpr int kNbCap = 48;
+constexpr int kNbFlush = 28;
+constexpr int kNbChunk = 8;
+constexpr int64_t kNbMaxParticles = int64_t{1} << 26;
+
+template<int D, int K, int Phys>
+__global__ void __launch_bounds__(256, forces_min_blocks<D, TG_FP32C>() / 2)
+    k_forces_nbl(StageArgs<D, TG_FP32C> A) {
+  extern __shared__ uint32_t s_nb[];
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const uint32_t id = A.Y.id[i];
+  if (id & kWallBit) return;
+  const uint32_t key = A.skey[i];
+  const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
+  const TankDev& T = A.tanks[tk];
+  int c[3] = {0, 0, 0};
+  cell_from_key<D>(T, key, c);
+  const uint32_t ia = static_cast<uint32_t>(i);
+  PairF32<D, K, Phys> acc;
+  acc.init(A.phys, T, load_dat(A.datrec, ia), A.kahan);
+  const bool faces = A.fc.on;
+  if (faces) acc.dv[1].s = 0.f;
+  float oa[3] = {0.f, 0.f, 0.f};
+  load_pos(A.posrec, ia, oa);
+  const float csz = T.cs_f;
+  const bool tborder = border_cell<D>(T, c);
+  uint32_t* nb = s_nb + threadIdx.x;
+  const uint32_t stride = blockDim.x;
+  int cnt = 0;
+
+  // r_ab of list entry w (the scan's arithmetic).
+  auto entry_d = [&](uint32_t w, float* d) -> uint32_t {
+    const uint32_t j = w >> 6;
+    const float u = static_cast<float>(static_cast<int>((w >> 3) & 7u) - 3) * csz;
+    const float v = static_cast<float>(static_cast<int>(w & 7u) - 3) * csz;
+    if constexpr (D == 2) {
+      float ob[2];
+      load_pos(A.posrec, j, ob);
+      d[0] = (oa[0] - u) - ob[0];
+      d[1] = (oa[1] - v) - ob[1];
+    } else {
+      const Pos32_3 b = A.posrec[j];
+      const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
+      d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
+      d[1] = (oa[1] - u) - b.y;
+      d[2] = (oa[2] - v) - b.z;
+    }
+    return j;
+  };
+  auto evaluate = [&]() {
+    for (int e0 = 0; e0 < cnt; e0 += kNbChunk) {
+      const int e1 = min(cnt, e0 + kNbChunk);
+      acc.open();
+      for (int e = e0; e < e1; ++e) {
+        float d[3];
+        const uint32_t j = entry_d(nb[e * stride], d);
+        float s2 = d[0] * d[0] + d[1] * d[1];
+        if constexpr (D == 3) s2 += d[2] * d[2];
+        acc.add(d, s2, load_dat(A.datrec, j));
+      }
+      acc.close();
+    }
+    cnt = 0;
+  };
+  auto push = [&](uint32_t j, uint32_t code) {
+    nb[cnt * stride] = (j << 6) | code;
+    if (++cnt == kNbCap) evaluate();
+  };
+  const int k = A.k;
+  const int nx = T.nc[0], ny = T.nc[1];
+  const int side = 2 * k + 1;
+  for (int t = 0; t < side * side; ++t) {
+    // 2D: cell (c0 + u, c1 + v); 3D: row (c1 + u, c2 + v); u runs fastest
+    // (the next range in memory).
+    const int u = t % side - k, v = t / side - k;
+    uint32_t s = 0, en = 0;
+    Band bd{-1.f, -1.f};
+    if constexpr (D == 2) {
+      const int x = c[0] + u, y = c[1] + v;
+      if (x >= 0 && x < nx && y >= 0 && y < ny) {
+        const float gx = (x == 0 || x == nx - 1) ? 0.f : cell_gap(u, oa[0], csz);
+        const float gy = (y == 0 || y == ny - 1) ? 0.f : cell_gap(v, oa[1], csz);
+        if (gx * gx + gy * gy <= T.cull_r2_f) {
+          const uint32_t kc = 2 * (T.cell_off + static_cast<uint32_t>(y) * nx + x);
+          s = __ldg(A.cell_start + kc);
+          en = __ldg(A.cell_start + kc + 2);
+          bd = visit_band<D>(T, c, k, u, v, 0, false, tborder);
+        }
+      }
+    } else {
+      const int y = c[1] + u, z = c[2] + v;
+      int x0, x1;
+      if (y >= 0 && y < ny && z >= 0 && z < T.nc[2] &&
+          clip_row<D>(T, c, oa, y, z, max(c[0] - k, 0), min(c[0] + k, nx - 1), x0, x1)) {
+        const uint32_t row = T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx;
+        s = __ldg(A.cell_start + 2 * (row + x0));
+        en = __ldg(A.cell_start + 2 * (row + x1 + 1));
+        bd = visit_band<D>(T, c, k, 0, u, v, true, tborder);
+      }
+    }
+    const uint32_t code = static_cast<uint32_t>(((u + 3) << 3) | (v + 3));
+    const float su = static_cast<float>(u) * csz, sv = static_cast<float>(v) * csz;
+    for (uint32_t j = s; j < en; ++j) {
+      if (j == ia) continue;
+      float d[3];
+      if constexpr (D == 2) {
+        float ob[2];
+        load_pos(A.posrec, j, ob);
+        d[0] = (oa[0] - su) - ob[0];
+        d[1] = (oa[1] - sv) - ob[1];
+      } else {
+        const Pos32_3 b = A.posrec[j];
+        const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
+        d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
+        d[1] = (oa[1] - su) - b.y;
+        d[2] = (oa[2] - sv) - b.z;
+      }
+      float s2 = d[0] * d[0] + d[1] * d[1];
+      if constexpr (D == 3) s2 += d[2] * d[2];
+      if (s2 > bd.hi) continue;
+      if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
+      push(j, code);
+    }
+    if (__any_sync(__activemask(), cnt >= kNbFlush)) evaluate();
+  }
+  evaluate();
+  float va[3], dv_out[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    va[q] = q < D ? acc.va[q] : 0.f;
+    dv_out[q] = q < D ? acc.dv[q].value() : 0.f;
+  }
+  float drho_out = acc.drho.value();
+  if (faces) {
+    double drho = drho_out;
+    double dv[3] = {dv_out[0], dv_out[1], dv_out[2]};
+    apply_face_terms(A, i, drho, dv);
+    drho_out = static_cast<float>(drho);
+#pragma unroll
+    for (int q = 0; q < D; ++q) dv_out[q] = static_cast<float>(dv[q]);
+  }
+  forces_epilogue<D, TG_FP32C>(A, i, id, tk, T, c, va, acc.a.drho, dv_out, drho_out);
 }
 
 // 2D compensated form with the block's neighbour window staged in shared
@@ -1528,6 +1749,8 @@ __global__ void __launch_bounds__(128, 7)
   float oa[3] = {0.f, 0.f, 0.f};
   load_pos(A.posrec, static_cast<uint32_t>(i), oa);
   const float csz = T.cs_f;
+  const bool tborder = border_cell<2>(T, c);
+  const uint32_t ia = static_cast<uint32_t>(i);
   if (staged) {
     const int xlo = max(c[0] - A.k, 0), xhi = min(c[0] + A.k, T.nc[0] - 1);
     for (int r = 0; r < s_rows; ++r) {
@@ -1540,14 +1763,16 @@ __global__ void __launch_bounds__(128, 7)
       for (int x = xlo; x <= xhi; ++x) {
         const uint32_t ge = __ldg(A.cell_start + 2 * (row + x + 1));
         oas[0] = oa[0] - (x - c[0]) * csz;
+        const Band bd = visit_band<2>(T, c, A.k, x - c[0], y - c[1], 0, false, tborder);
         acc.open();
         for (uint32_t j = gs; j < ge; ++j) {
-          if (j == static_cast<uint32_t>(i)) continue;
+          if (j == ia) continue;
           const int sj = static_cast<int>(j) + shift;
           const float2 ob = s_pos[sj];
           float d[3] = {oas[0] - ob.x, oas[1] - ob.y, 0.f};
           const float s2 = d[0] * d[0] + d[1] * d[1];
-          if (s2 > acc.R2) continue;
+          if (s2 > bd.hi) continue;
+          if (s2 >= bd.lo && !within_fp64<2>(A.Y.pos, ia, j, T.radius2)) continue;
           const float4 b0 = s_dat[2 * sj], b1 = s_dat[2 * sj + 1];
           acc.add(d, s2, Dat32{b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w});
         }
@@ -1558,19 +1783,21 @@ __global__ void __launch_bounds__(128, 7)
   } else {
     for_cells<2, true>(T, c, A.k, A.cell_start,
                        [&](uint32_t s, uint32_t en, int dx, int dy, int) {
+      const Band bd = visit_band<2>(T, c, A.k, dx, dy, 0, false, tborder);
       float oas[3];
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
       acc.open();
       for (uint32_t j = s; j < en; ++j) {
-        if (j == static_cast<uint32_t>(i)) continue;
+        if (j == ia) continue;
         float ob[3], d[3];
         load_pos(A.posrec, j, ob);
         d[0] = oas[0] - ob[0];
         d[1] = oas[1] - ob[1];
         d[2] = 0.f;
         const float s2 = d[0] * d[0] + d[1] * d[1];
-        if (s2 > acc.R2) continue;
+        if (s2 > bd.hi) continue;
+        if (s2 >= bd.lo && !within_fp64<2>(A.Y.pos, ia, j, T.radius2)) continue;
         acc.add(d, s2, load_dat(A.datrec, j));
       }
       acc.close();
@@ -1628,8 +1855,11 @@ __global__ void __launch_bounds__(128)
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
     const float csz = T.cs_f;
+    const bool tborder = border_cell<D>(T, c);
+    const uint32_t ia = static_cast<uint32_t>(i);
     for_cells<D, true>(T, c, A.k, A.cell_start,
                        [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      const Band bd = visit_band<D>(T, c, A.k, dx, dy, dz, false, tborder);
       float oas[3];
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
@@ -1641,7 +1871,8 @@ __global__ void __launch_bounds__(128)
         for (int k = 0; k < D; ++k) d[k] = oas[k] - ob[k];
         float s2 = d[0] * d[0] + d[1] * d[1];
         if constexpr (D == 3) s2 += d[2] * d[2];
-        if (s2 > T.radius2_f) continue;
+        if (s2 > bd.hi) continue;
+        if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
         const uint32_t lid = (A.Y.id[j] & kIdMask) - base;
         ++cnt;
         hs += splitmix64(static_cast<uint64_t>(lid) + 1u);
