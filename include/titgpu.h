@@ -61,7 +61,10 @@ enum {
 enum {
   TG_DEV_NONFINITE_STATE = 1u << 0, /* NaN/Inf position, velocity or density */
   TG_DEV_OUTSIDE_GRID = 1u << 1,    /* particle clamped into the border cells */
-  TG_DEV_BAD_DT = 1u << 2           /* non-positive or non-finite time step */
+  TG_DEV_BAD_DT = 1u << 2,          /* non-positive or non-finite time step */
+  TG_DEV_COPY_TIMEOUT = 1u << 3     /* a bulk copy into shared memory did not
+                                       complete within its wait limit (the
+                                       pass read global memory instead) */
 };
 
 /* ---- enumerations ------------------------------------------------------ */
@@ -142,8 +145,9 @@ typedef struct tg_params {
   int32_t cells_per_radius; /* grid cells per support radius, 1..3 */
   int32_t kahan;            /* FP32C: 1 = compensated sums, 0 = plain */
   int32_t device;           /* CUDA device ordinal; -1 = the current one */
-  int32_t staging;          /* 2D FP32C: read neighbour windows from
-                               shared memory (1) or through L1 (0, default;
+  int32_t staging;          /* 2D FP32C: copy each block's neighbour
+                               window into shared memory with bulk copies
+                               (1) or read it through L1 (0, default;
                                measured faster on GB300) */
   int32_t eos;              /* TG_EOS_TAIT (default) | TG_EOS_LINEAR_TAIT */
   int32_t face_fp32;        /* TG_FP32C with face walls: the closed-form face
@@ -298,7 +302,10 @@ int tg_host_free(void* ptr);
  * default stream) without synchronising; results are ready when the stream
  * reaches that point.  The first call on a device looks up the scratch
  * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  Every call shares the one
+ * make that first call before any stream capture.  The address is kept for
+ * the life of the process: resetting a device (cudaDeviceReset, or a reset
+ * of its primary context) after the first call on it is not supported, as
+ * the reloaded module may place the array elsewhere.  Every call shares the one
  * array, which keeps the last call's contents (each call rewrites all it
  * reads), so calls that overlap on the GPU (different streams or threads
  * without ordering) race and corrupt each other. */

@@ -51,7 +51,7 @@ void Context::release_all() {
   faces = FaceArgs{};
   keys_a = keys_b = vals_a = vals_b = nullptr;
   sort_scratch = nullptr;
-  cell_start = wall_list = nullptr;
+  cell_start = wall_list = wall_active = nullptr;
   cell_scratch = nullptr;
   d_stage = d_stage2 = d_stage3 = d_stage4 = nullptr;
   d_sd_rho = nullptr;
@@ -454,12 +454,14 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     }
     // Headroom above the tank for splashes (particles beyond the grid are
     // clamped into its border cells, which stays exact but slows them).
+    // Margins of R + 2 cells keep every particle's block of cells within k
+    // of its own off the border cells.
     const double headroom = 0.25 * (hi[1] - lo[1]);
     uint64_t cells = 1;
     for (int k = 0; k < 3; ++k) {
       if (k < dim) {
-        D.lo[k] = lo[k] - (R + cs);
-        double top = hi[k] + (R + cs) + (k == 1 ? headroom : 0.0);
+        D.lo[k] = lo[k] - (R + 2.0 * cs);
+        double top = hi[k] + (R + 2.0 * cs) + (k == 1 ? headroom : 0.0);
         const double ncf = std::max(1.0, std::ceil((top - D.lo[k]) / cs));
         if (ncf > 2.0e9) {
           return fail(&C, TG_ERR_INVALID_ARGUMENT, "tank grid too large");
@@ -550,7 +552,7 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, A(C.d_dt_last, sizeof(double) * n_tanks));
   TG_CUDA(&C, A(C.d_time, sizeof(double) * n_tanks));
   TG_CUDA(&C, A(C.d_err, sizeof(uint32_t)));
-  TG_CUDA(&C, A(C.d_wall_count, sizeof(uint32_t)));
+  TG_CUDA(&C, A(C.d_wall_count, 2 * sizeof(uint32_t)));
   TG_CUDA(&C, A(C.d_fbox, sizeof(unsigned) * 6 * n_tanks));
   TG_CUDA(&C, A(C.keys_a, sizeof(uint32_t) * nn));
   TG_CUDA(&C, A(C.keys_b, sizeof(uint32_t) * nn));
@@ -560,6 +562,7 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, A(C.cell_start, sizeof(uint32_t) * (2 * total_cells + 1)));
   TG_CUDA(&C, C.alloc(&C.cell_scratch, tg::cell_table_scratch_bytes(C.total_keys)));
   TG_CUDA(&C, A(C.wall_list, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
+  TG_CUDA(&C, A(C.wall_active, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
   TG_CUDA(&C, A(C.d_stage, sizeof(double) * nn * dim));
   TG_CUDA(&C, A(C.d_stage2, sizeof(double) * nn * dim));
   TG_CUDA(&C, A(C.d_stage3, sizeof(double) * nn * dim));

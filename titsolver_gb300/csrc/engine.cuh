@@ -134,7 +134,7 @@ struct Context {
   double* d_dt_last = nullptr;
   double* d_time = nullptr;
   uint32_t* d_err = nullptr;
-  uint32_t* d_wall_count = nullptr;
+  uint32_t* d_wall_count = nullptr;  // [0] walls listed, [1] walls near fluid
   // Per tank: order-preserving encodings of the fluid bounding box of the
   // current stage (FP32, rounded outwards), mins [ntanks x 3] then maxes.
   unsigned* d_fbox = nullptr;
@@ -146,6 +146,7 @@ struct Context {
   uint32_t* cell_start = nullptr;
   void* cell_scratch = nullptr;
   uint32_t* wall_list = nullptr;
+  uint32_t* wall_active = nullptr;  // walls near fluid this stage (k_wall_select)
   double* d_stage = nullptr;  // n * dim doubles: upload / download staging
   double* d_stage2 = nullptr;
   double* d_stage3 = nullptr;

@@ -74,8 +74,10 @@ class Engine final : public EngineBase {
       }
       A(U.rho, n);
     }
-    A(posrec_, n);
-    A(datrec_, n);
+    // Two spare records: the staged force pass copies row segments rounded
+    // out to 16-byte boundaries, which may reach one record past the end.
+    A(posrec_, n + 2);
+    A(datrec_, n + 2);
     post_ = PostArgs<D, F>{};
     if (C.P.post_integrate == TG_POST_SHIFTING) {
       A(post_.N, n * D);
@@ -186,9 +188,7 @@ class Engine final : public EngineBase {
     tok = C.group_begin(kGroupWalls);
     if (C.n_wall > 0) {
       enqueue_gamma(C, a);
-      k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
-          a, C.n_wall);
-      C.launches += 1;
+      launch_walls(C, a);
     }
     k_commit<D, F><<<grid_for(C.n, 256), 256, 0, C.stream>>>(a);
     C.launches += 1;
@@ -272,10 +272,12 @@ class Engine final : public EngineBase {
   int64_t launches_per_step(Context& C) override {
     const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
     const int stages = force_passes(C.P.integrator);
-    const int per_stage = 3 * passes + 2 + 2 + (C.n_wall > 0 ? 1 : 0);
+    // The wall pass lists the walls near fluid first when it has a fluid box.
+    const int walls = C.n_wall > 0 ? (4 * C.n_wall >= C.n_fluid ? 2 : 1) : 0;
+    const int per_stage = 3 * passes + 2 + 2 + walls;
     const int gam = C.faces.on ? 3 : 0;  // k_gamma_init, k_gamma_faces, k_face_terms
     const int post = C.P.post_integrate == TG_POST_SHIFTING
-                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? 1 + (gam > 0 ? 2 : 0) : 0) + 5 +
+                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? walls + (gam > 0 ? 2 : 0) : 0) + 5 +
                                (gam > 0 ? 1 : 0)
                          : 0;
     return static_cast<int64_t>(stages) * (per_stage + gam) + post + 1;
@@ -300,6 +302,7 @@ class Engine final : public EngineBase {
     a.dt = C.d_dt;
     a.wall_list = C.wall_list;
     a.wall_count = C.d_wall_count;
+    a.wall_active = C.wall_active;
     // The wall pass's fluid-box early-out pays when walls are a sizeable
     // share of the particles (it costs a fold in every reorder).
     a.fbox = C.n_wall > 0 && 4 * C.n_wall >= C.n_fluid ? C.d_fbox : nullptr;
@@ -319,7 +322,7 @@ class Engine final : public EngineBase {
   }
 
   cudaError_t reorder(Context& C, const StageArgs<D, F>& a) {
-    cudaError_t e = cudaMemsetAsync(C.d_wall_count, 0, sizeof(uint32_t), C.stream);
+    cudaError_t e = cudaMemsetAsync(C.d_wall_count, 0, 2 * sizeof(uint32_t), C.stream);
     if (e != cudaSuccess) return e;
     if (a.fbox != nullptr) {
       // Empty fluid boxes: mins at the top encoding, maxes at the bottom.
@@ -369,9 +372,7 @@ class Engine final : public EngineBase {
     if (e != cudaSuccess) return e;
     if (C.n_wall > 0) {
       enqueue_gamma(C, a);
-      k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
-          a, C.n_wall);
-      C.launches += 1;
+      launch_walls(C, a);
     }
     PostArgs<D, F> p = post_;
     p.S = a;
@@ -458,9 +459,7 @@ class Engine final : public EngineBase {
     if (C.n_wall > 0) {
       tok = C.group_begin(kGroupWalls);
       enqueue_gamma(C, a);
-      k_walls<D, F, K><<<grid_for(C.n_wall * kWallTeam, 128), 128, 0, C.stream>>>(
-          a, C.n_wall);
-      C.launches += 1;
+      launch_walls(C, a);
       C.group_end(tok);
     }
     if (a.fc.on) {
@@ -479,17 +478,6 @@ class Engine final : public EngineBase {
           k_forces_staged2<K><<<grid_for(C.n, 128), 128, 0, C.stream>>>(a);
           staged = true;
         }
-      }
-      if (!staged && C.P.staging == 2 && C.force_team == 1 && C.k <= 3 &&
-          C.n < kNbMaxParticles) {
-        if (phys == kPhysTextbook) {
-          launch_forces_nbl<kPhysTextbook>(C, a);
-        } else if (phys == kPhysReference) {
-          launch_forces_nbl<kPhysReference>(C, a);
-        } else {
-          launch_forces_nbl<kPhysGeneric>(C, a);
-        }
-        staged = true;
       }
       if (staged) {
       } else if (phys == kPhysTextbook) {
@@ -515,28 +503,35 @@ class Engine final : public EngineBase {
   template<int Phys>
   void launch_forces(Context& C, const StageArgs<D, F>& a) {
     const int block = C.force_block;
+    // The compensated form's band lists (1 + 2 kBandCap words per thread).
+    const size_t smem =
+        F == TG_FP32C ? sizeof(uint32_t) * (1 + 2 * kBandCap) * static_cast<size_t>(block) : 0;
     if constexpr (team_kernel(K)) {
       if (C.force_team == 4) {
-        k_forces<D, F, K, Phys, 4><<<grid_for(C.n * 4, block), block, 0, C.stream>>>(a);
+        k_forces<D, F, K, Phys, 4><<<grid_for(C.n * 4, block), block, smem, C.stream>>>(a);
         return;
       }
       if (C.force_team == 2) {
-        k_forces<D, F, K, Phys, 2><<<grid_for(C.n * 2, block), block, 0, C.stream>>>(a);
+        k_forces<D, F, K, Phys, 2><<<grid_for(C.n * 2, block), block, smem, C.stream>>>(a);
         return;
       }
     }
-    k_forces<D, F, K, Phys, 1><<<grid_for(C.n, block), block, 0, C.stream>>>(a);
+    k_forces<D, F, K, Phys, 1><<<grid_for(C.n, block), block, smem, C.stream>>>(a);
   }
 
-  // The compensated pass with per-thread neighbour lists (one lane per
-  // target; its lists take kNbCap words of shared memory per thread).
-  template<int Phys>
-  void launch_forces_nbl(Context& C, const StageArgs<D, F>& a) {
-    if constexpr (F == TG_FP32C) {
-      const int block = C.force_block;
-      const size_t smem = sizeof(uint32_t) * kNbCap * static_cast<size_t>(block);
-      k_forces_nbl<D, K, Phys><<<grid_for(C.n, block), block, smem, C.stream>>>(a);
+  // The wall pass: the walls near fluid listed first (when the pass has a
+  // fluid box), then teams of kWallTeam lanes over the list, at most 16
+  // blocks per multiprocessor taking walls in turn.
+  void launch_walls(Context& C, const StageArgs<D, F>& a) {
+    if (a.fbox != nullptr) {
+      k_wall_select<D, F><<<grid_for(C.n_wall, 256), 256, 0, C.stream>>>(a, C.n_wall);
+      C.launches += 1;
     }
+    const int64_t cap = 16 * static_cast<int64_t>(C.sm_count > 0 ? C.sm_count : 152);
+    const unsigned grid = static_cast<unsigned>(
+        std::max<int64_t>(1, std::min<int64_t>(grid_for(C.n_wall * kWallTeam, 128), cap)));
+    k_walls<D, F, K><<<grid, 128, 0, C.stream>>>(a);
+    C.launches += 1;
   }
 
   StateBuf<R> X_{}, Y_{};

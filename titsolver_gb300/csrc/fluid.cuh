@@ -137,7 +137,8 @@ struct StageArgs {
   PhysDev phys;
   double* dt;
   uint32_t* wall_list;
-  uint32_t* wall_count;
+  uint32_t* wall_count;   // [0] walls listed, [1] walls near fluid
+  uint32_t* wall_active;  // the walls near fluid (k_wall_select)
   uint32_t* err;
   int64_t n;
   int k;             // cells per radius
@@ -504,29 +505,21 @@ __device__ __forceinline__ float dist2_exact(const float* a, const float* b,
 // not; inside it the reference's own predicate decides (dist2_exact on the
 // cell-ordered FP64 positions against the FP64 R^2), so the set is exactly
 // the reference's.  A particle clamped into a border cell may carry an
-// offset of any size, so every candidate seen from or in a border cell is
-// decided in FP64 (border cells are empty unless a particle left the grid).
+// offset of any size, so a target whose block of cells reaches a border
+// cell decides every candidate in FP64 (the grid's margins keep every
+// particle more than k cells from its border unless it left the grid).
 struct Band {
   float lo, hi;
 };
 
+// Band of a target in cell c whose traversal covers cells c -+ k: the
+// tank's band, or (lo, hi) = (-1, inf), every candidate decided in FP64,
+// when that block of cells reaches a border cell.
 template<int D>
-__device__ __forceinline__ bool border_cell(const TankDev& T, const int* c) {
-  bool b = c[0] <= 0 || c[0] >= T.nc[0] - 1 || c[1] <= 0 || c[1] >= T.nc[1] - 1;
-  if constexpr (D == 3) b = b || c[2] <= 0 || c[2] >= T.nc[2] - 1;
-  return b;
-}
-
-// Band of one visited cell at (dx, dy, dz) from the target's cell c or, with
-// row set, of one row of cells at (dy, dz) whose x range lies within
-// c[0] -+ k.
-template<int D>
-__device__ __forceinline__ Band visit_band(const TankDev& T, const int* c, int k,
-                                           int dx, int dy, int dz, bool row,
-                                           bool target_border) {
-  const int cc[3] = {c[0] + dx, c[1] + dy, D == 3 ? c[2] + dz : 0};
-  bool b = target_border || border_cell<D>(T, cc);
-  if (row) b = b || c[0] - k <= 0 || c[0] + k >= T.nc[0] - 1;
+__device__ __forceinline__ Band target_band(const TankDev& T, const int* c, int k) {
+  bool b = c[0] - k <= 0 || c[0] + k >= T.nc[0] - 1 || c[1] - k <= 0 ||
+           c[1] + k >= T.nc[1] - 1;
+  if constexpr (D == 3) b = b || c[2] - k <= 0 || c[2] + k >= T.nc[2] - 1;
   return b ? Band{-1.f, __int_as_float(0x7f800000)} : Band{T.band_lo_f, T.band_hi_f};
 }
 
@@ -535,13 +528,15 @@ __device__ __forceinline__ Band visit_band(const TankDev& T, const int* c, int k
 template<int D>
 __device__ __forceinline__ bool within_fp64(double* const* pos, uint32_t a,
                                             uint32_t b, double R2) {
-  double pa[3], pb[3], d[3];
+  // (d0^2 + d1^2) + d2^2 axis by axis, rounded as dist2_exact.
+  double d = __dsub_rn(pos[0][a], pos[0][b]);
+  double s = __dmul_rn(d, d);
 #pragma unroll
-  for (int k = 0; k < D; ++k) {
-    pa[k] = pos[k][a];
-    pb[k] = pos[k][b];
+  for (int k = 1; k < D; ++k) {
+    d = __dsub_rn(pos[k][a], pos[k][b]);
+    s = __dadd_rn(s, __dmul_rn(d, d));
   }
-  return dist2_exact<D>(pa, pb, d) <= R2;
+  return s <= R2;
 }
 
 __device__ __forceinline__ bool finite_bits(double x) {
@@ -578,6 +573,57 @@ __global__ void __launch_bounds__(256)
     atomicOr(err, finite ? static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID)
                          : static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));
   }
+}
+
+// Record of a wall whose sums are empty (rho(0)), or that keeps its
+// carried density rho (a split pass without a prepare): zero velocity and
+// the equation of state of the density, as k_walls writes them.
+template<int D>
+__device__ __forceinline__ Dat64 wall_record(const PhysDev& P, const TankDev& T,
+                                             double rho, bool keep) {
+  const double rho_e = keep ? rho : density_from_potential_f64(P, T, 0.0);
+  double pr, cc;
+  tait_f64(P, T, rho_e, pr, cc);
+  const double inv = 1.0 / rho_e;
+  return Dat64{0.0, 0.0, 0.0, rho_e, pr * inv * inv, cc, inv, 0.0};
+}
+template<int D>
+__device__ __forceinline__ Dat32 wall_record(const PhysDev& P, const TankDev& T,
+                                             float rho, bool keep) {
+  const float rho_e = keep ? rho : deviation_from_potential_f32(P, T, 0.f);
+  float pr, cc;
+  tait_f32(P, T, rho_e, pr, cc);
+  const float inv = 1.f / (T.rho0_f + rho_e);
+  return Dat32{0.f, 0.f, 0.f, rho_e, pr * inv * inv, cc, inv, 0.f};
+}
+
+// Home state of the wall at cell-order slot e, written by the pass over all
+// particles that follows the wall pass (force pass, prepare commit or
+// shift): its gathered position and id, zero velocity, acceleration and
+// density rate, the density of its record, its sorted key and, in the
+// compensated form, its cell offset.
+template<int D, int F>
+__device__ __forceinline__ void commit_wall(const StageArgs<D, F>& A, int64_t e,
+                                            uint32_t id) {
+  using R = typename StageArgs<D, F>::R;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    A.X.pos[k][e] = A.Y.pos[k][e];
+    A.X.vel[k][e] = R(0);
+    A.X.dv[k][e] = R(0);
+  }
+  if constexpr (F == TG_FP64) {
+    A.X.rho[e] = A.datrec[e].rho;
+  } else {
+    A.X.rho[e] = A.datrec[e].drho;
+    float o[3] = {0.f, 0.f, 0.f};
+    load_pos(A.posrec, static_cast<uint32_t>(e), o);
+#pragma unroll
+    for (int k = 0; k < D; ++k) A.X.off[k][e] = o[k];
+  }
+  A.X.drho[e] = R(0);
+  A.X.id[e] = id;
+  A.X.key[e] = A.skey[e];
 }
 
 // ---------------------------------------------------------------------------
@@ -670,6 +716,9 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
     if (id & kWallBit) {
       const uint32_t slot = atomicAdd(A.wall_count, 1u);
       A.wall_list[slot] = static_cast<uint32_t>(j);
+      // rho(0), or the carried density: k_walls overwrites the records of
+      // the walls near fluid.
+      A.datrec[j] = wall_record<D>(A.phys, T, rho, A.walls_keep != 0);
     } else {
       // Tait state of the fluid particle.
       if constexpr (F == TG_FP64) {
@@ -746,55 +795,91 @@ __global__ void __launch_bounds__(256) k_reorder(StageArgs<D, F> A) {
 // Wall extrapolation (fluid_equations.hpp:122-164) with a zero wall normal:
 //   rho_e = rho(H),  H = sum_b V_b H(rho_b) W_be / sum_b V_b W_be over fluid
 //   neighbours b (H = 0 when the Shepard sum is tiny); v_e = 0.
-// With walls_keep (a split pass with no prepare before it) the wall keeps
-// its carried density and only its records and home state are written.
-// A wall farther than the support radius from its tank's fluid bounding
-// box skips the neighbour walk: its sums are empty either way.
-// A team of kWallTeam lanes shares one wall: the lanes split the cells of
-// the wall's block (fluid ranges only), then the team reduces by shuffles.
+// k_reorder writes every wall's record with rho(0) (or, in a split pass
+// with no prepare before it, the carried density); this pass overwrites
+// the records of the walls within the support radius of their tank's fluid
+// bounding box (for the others the sums are empty, so rho(0) is their
+// value).  k_wall_select lists those walls (all of them when the pass has
+// no fluid box); k_walls then runs a grid of teams of kWallTeam lanes over
+// the list, each team taking walls in turn, so no team idles while others
+// hold long runs of listed walls.  A team splits the wall's cells (2D) or
+// rows of cells (3D, fluid records only) and reduces by shuffles.  The
+// walls' home state is written by the next pass over all particles
+// (commit_wall).
 constexpr int kWallTeam = 8;
+
+template<int D, int F>
+__global__ void __launch_bounds__(256)
+    k_wall_select(StageArgs<D, F> A, int64_t n_walls) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  bool act = false;
+  uint32_t e = 0;
+  if (t < n_walls) {
+    e = A.wall_list[t];
+    const uint32_t key = A.skey[e];
+    const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
+    const TankDev& T = A.tanks[tk];
+    float xl[3] = {0.f, 0.f, 0.f};
+    if constexpr (F == TG_FP64) {
+      double pe[3] = {0.0, 0.0, 0.0};
+      load_pos(A.posrec, e, pe);
+      local_coords<D>(T, pe, xl);
+    } else {
+      int c[3] = {0, 0, 0};
+      float oe[3] = {0.f, 0.f, 0.f};
+      cell_from_key<D>(T, key, c);
+      load_pos(A.posrec, e, oe);
+      local_coords<D>(T, c, oe, xl);
+    }
+    act = !beyond_fluid<D>(A.fbox, A.ntanks, tk, T, xl);
+  }
+  // One atomic per warp.
+  const unsigned mask = __ballot_sync(0xffffffffu, act);
+  const int lane = static_cast<int>(threadIdx.x & 31u);
+  uint32_t base = 0;
+  if (lane == 0 && mask != 0u) base = atomicAdd(A.wall_count + 1, static_cast<uint32_t>(__popc(mask)));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (act) A.wall_active[base + __popc(mask & ((1u << lane) - 1u))] = e;
+}
 
 template<int D, int F, int K>
 __global__ void __launch_bounds__(128)
-    k_walls(StageArgs<D, F> A, int64_t n_walls) {
-  using R = typename StageArgs<D, F>::R;
-  const int64_t t =
-      (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / kWallTeam;
-  const int lane = threadIdx.x % kWallTeam;
-  const bool valid = t < n_walls;
-  const uint32_t e = valid ? A.wall_list[t] : 0u;
-  const uint32_t key = valid ? A.skey[e] : 0u;
-  const uint32_t tk = valid ? tank_of_key(key, A.tank_off, A.ntanks) : 0u;
-  const TankDev& T = A.tanks[tk];
-  int c[3] = {0, 0, 0};
-  cell_from_key<D>(T, key, c);
-  R rho_e = R(0);
-  if constexpr (F == TG_FP64) {
-    double pe[3] = {0.0, 0.0, 0.0};
-    if (valid) load_pos(A.posrec, e, pe);
-    const double R2 = T.radius2, hinv = T.hinv, w = T.w, m = T.m;
-    double S = 0.0, H = 0.0;
-    // The box test once per team (FP64 conversions are scarce), shared.
-    bool skip = false;
-    if (valid && lane == 0) {
-      float xl[3] = {0.f, 0.f, 0.f};
-      local_coords<D>(T, pe, xl);
-      skip = beyond_fluid<D>(A.fbox, A.ntanks, tk, T, xl);
-    }
-    skip = __shfl_sync(0xffffffffu, skip, 0, kWallTeam);
-    // Face boundaries: the wall normal n_e = normalize(grad gamma) and the
-    // hydrostatic term g (r_be . n_e) n_e[1] (fluid_equations.hpp:146-160);
-    // zero with particle walls.
-    double ne[3] = {0.0, 0.0, 0.0};
-    if (A.fc.on && valid) normalize_d<D>(A.fc.ggam + D * static_cast<size_t>(e), ne);
-    if (valid && !A.walls_keep && !skip) {
+    k_walls(StageArgs<D, F> A) {
+  // A split pass without a prepare: the walls keep the carried densities
+  // k_reorder put in their records.
+  if (A.walls_keep) return;
+  const bool all = A.fbox == nullptr;
+  const uint32_t* list = all ? A.wall_list : A.wall_active;
+  const int64_t count = all ? A.wall_count[0] : A.wall_count[1];
+  const int tl = static_cast<int>(threadIdx.x % kWallTeam);
+  const int team_in_warp = static_cast<int>((threadIdx.x & 31u) / kWallTeam);
+  const unsigned tmask = 0xffu << (team_in_warp * kWallTeam);
+  const int64_t teams = static_cast<int64_t>(gridDim.x) * blockDim.x / kWallTeam;
+  for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / kWallTeam;
+       w < count; w += teams) {
+    const uint32_t ew = list[w];
+    const uint32_t key = A.skey[ew];
+    const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
+    const TankDev& T = A.tanks[tk];
+    int c[3] = {0, 0, 0};
+    cell_from_key<D>(T, key, c);
+    if constexpr (F == TG_FP64) {
+      double pe[3] = {0.0, 0.0, 0.0};
+      load_pos(A.posrec, ew, pe);
+      const double R2 = T.radius2, hinv = T.hinv, w = T.w, m = T.m;
+      double S = 0.0, H = 0.0;
+      // Face boundaries: the wall normal n_e = normalize(grad gamma) and the
+      // hydrostatic term g (r_be . n_e) n_e[1] (fluid_equations.hpp:146-160);
+      // zero with particle walls.
+      double ne[3] = {0.0, 0.0, 0.0};
+      if (A.fc.on) normalize_d<D>(A.fc.ggam + D * static_cast<size_t>(ew), ne);
       auto visit = [&](uint32_t s, uint32_t en, int, int, int) {
         for (uint32_t j = s; j < en; ++j) {
           double pb[3], d[3];
           load_pos(A.posrec, j, pb);
           const double s2 = dist2_exact<D>(pb, pe, d);
           if (s2 > R2) continue;
-          const Dat64 b = load_dat_coherent(A.datrec, j);
+          const Dat64 b = load_dat(A.datrec, j);
           const double W = w * KernelPoly<K>::value(sqrt(s2) * hinv);
           const double Vb = m * b.invrho;
           double Hb = potential_f64(A.phys, T, b.rho);
@@ -805,79 +890,41 @@ __global__ void __launch_bounds__(128)
       };
       float oc[3] = {0.f, 0.f, 0.f};
       cell_offset<D>(T, c, pe, oc);
-      for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit, oc);
-    }
+      for_cells_team<D, true>(T, c, A.k, A.cell_start, tl, kWallTeam, visit, oc);
 #pragma unroll
-    for (int o = kWallTeam / 2; o > 0; o >>= 1) {
-      S += __shfl_xor_sync(0xffffffffu, S, o, kWallTeam);
-      H += __shfl_xor_sync(0xffffffffu, H, o, kWallTeam);
-    }
-    if (!valid || lane != 0) return;
-    if (A.walls_keep) {
-      rho_e = A.Y.rho[e];
+      for (int o = kWallTeam / 2; o > 0; o >>= 1) {
+        S += __shfl_xor_sync(tmask, S, o, kWallTeam);
+        H += __shfl_xor_sync(tmask, H, o, kWallTeam);
+      }
+      if (tl == 0) {
+        const double Hs = fabs(S) <= 6.0554544523933395e-06 ? 0.0 : H / S;
+        const double rho_e = density_from_potential_f64(A.phys, T, Hs);
+        double pr, cc;
+        tait_f64(A.phys, T, rho_e, pr, cc);
+        const double inv = 1.0 / rho_e;
+        A.datrec[ew] = Dat64{0.0, 0.0, 0.0, rho_e, pr * inv * inv, cc, inv, 0.0};
+      }
     } else {
-      const double Hs = fabs(S) <= 6.0554544523933395e-06 ? 0.0 : H / S;
-      rho_e = density_from_potential_f64(A.phys, T, Hs);
-    }
-    double pr, cc;
-    tait_f64(A.phys, T, rho_e, pr, cc);
-    const double inv = 1.0 / rho_e;
-    A.datrec[e] = Dat64{0.0, 0.0, 0.0, rho_e, pr * inv * inv, cc, inv, 0.0};
-  } else {
-    const float hinv = T.hinv_f;
-    const float w = T.w_f, m = T.m_f;
-    const float csz = T.cs_f;
-    float oe[3] = {0.f, 0.f, 0.f};
-    if (valid) load_pos(A.posrec, e, oe);
-    Kahan S, H;
-    bool skip = false;
-    if (valid && lane == 0) {
-      float xl[3] = {0.f, 0.f, 0.f};
-      local_coords<D>(T, c, oe, xl);
-      skip = beyond_fluid<D>(A.fbox, A.ntanks, tk, T, xl);
-    }
-    skip = __shfl_sync(0xffffffffu, skip, 0, kWallTeam);
-    // Face boundaries: wall normal and hydrostatic term (see the FP64 path);
-    // here r_be = -d.
-    float nef[3] = {0.f, 0.f, 0.f};
-    if (A.fc.on && valid) {
-      double ne[3];
-      normalize_d<D>(A.fc.ggam + D * static_cast<size_t>(e), ne);
+      const float hinv = T.hinv_f;
+      const float w = T.w_f, m = T.m_f;
+      const float csz = T.cs_f;
+      float oe[3] = {0.f, 0.f, 0.f};
+      load_pos(A.posrec, ew, oe);
+      Kahan S, H;
+      // Face boundaries: wall normal and hydrostatic term (see the FP64
+      // path); here r_be = -d.
+      float nef[3] = {0.f, 0.f, 0.f};
+      if (A.fc.on) {
+        double ne[3];
+        normalize_d<D>(A.fc.ggam + D * static_cast<size_t>(ew), ne);
 #pragma unroll
-      for (int k = 0; k < D; ++k) nef[k] = static_cast<float>(ne[k]);
-    }
-    if (valid && !A.walls_keep && !skip) {
-      const bool tborder = border_cell<D>(T, c);
-      auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
-        const Band bd = visit_band<D>(T, c, A.k, dx, dy, dz, false, tborder);
-        float oes[3];
-        oes[0] = oe[0] - dx * csz;
-        oes[1] = oe[1] - dy * csz;
-        oes[2] = D == 3 ? oe[2] - dz * csz : 0.f;
-        for (uint32_t j = s; j < en; ++j) {
-          float ob[3], d[3];
-          load_pos(A.posrec, j, ob);
-          const float s2 = dist2_exact<D>(oes, ob, d);
-          if (s2 > bd.hi) continue;
-          if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, e, j, T.radius2)) continue;
-          const Dat32 b = load_dat_coherent(A.datrec, j);
-          const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
-          const float Vb = m * b.invrho;
-          float Hb = potential_f32(A.phys, T, b.drho);
-          if (A.fc.on) {
-            float dn = d[0] * nef[0] + d[1] * nef[1];
-            if constexpr (D == 3) dn += d[2] * nef[2];
-            Hb -= A.phys.g_f * dn * nef[1];
-          }
-          S.add(Vb * W);
-          H.add(Vb * Hb * W);
-        }
-      };
+        for (int k = 0; k < D; ++k) nef[k] = static_cast<float>(ne[k]);
+      }
+      const Band bd = target_band<D>(T, c, A.k);
       if constexpr (D == 3) {
         // One range per row of cells (records carry the cell's x index and
         // the wall bit), fluid records only.
         auto visit_row = [&](uint32_t s, uint32_t en, int, int dy, int dz) {
-          const Band bd = visit_band<D>(T, c, A.k, 0, dy, dz, true, tborder);
           const float oey = oe[1] - dy * csz;
           const float oez = oe[2] - dz * csz;
           for (uint32_t j = s; j < en; ++j) {
@@ -891,11 +938,11 @@ __global__ void __launch_bounds__(128)
             d[2] = oez - b.z;
             const float s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
             if (s2 > bd.hi) continue;
-            if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, e, j, T.radius2)) continue;
-            const Dat32 bd = load_dat_coherent(A.datrec, j);
+            if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ew, j, T.radius2)) continue;
+            const Dat32 bdat = load_dat(A.datrec, j);
             const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
-            const float Vb = m * bd.invrho;
-            float Hb = potential_f32(A.phys, T, bd.drho);
+            const float Vb = m * bdat.invrho;
+            float Hb = potential_f32(A.phys, T, bdat.drho);
             if (A.fc.on) {
               Hb -= A.phys.g_f * (d[0] * nef[0] + d[1] * nef[1] + d[2] * nef[2]) * nef[1];
             }
@@ -903,42 +950,50 @@ __global__ void __launch_bounds__(128)
             H.add(Vb * Hb * W);
           }
         };
-        for_rows_team<D>(T, c, A.k, A.cell_start, lane, kWallTeam, visit_row, oe);
+        for_rows_team<D>(T, c, A.k, A.cell_start, tl, kWallTeam, visit_row, oe);
       } else {
-        for_cells_team<D, true>(T, c, A.k, A.cell_start, lane, kWallTeam, visit, oe);
+        auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+          float oes[3];
+          oes[0] = oe[0] - dx * csz;
+          oes[1] = oe[1] - dy * csz;
+          oes[2] = D == 3 ? oe[2] - dz * csz : 0.f;
+          for (uint32_t j = s; j < en; ++j) {
+            float ob[3], d[3];
+            load_pos(A.posrec, j, ob);
+            const float s2 = dist2_exact<D>(oes, ob, d);
+            if (s2 > bd.hi) continue;
+            if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ew, j, T.radius2)) continue;
+            const Dat32 b = load_dat(A.datrec, j);
+            const float W = w * KernelPoly<K>::value(sqrtf(s2) * hinv);
+            const float Vb = m * b.invrho;
+            float Hb = potential_f32(A.phys, T, b.drho);
+            if (A.fc.on) {
+              float dn = d[0] * nef[0] + d[1] * nef[1];
+              if constexpr (D == 3) dn += d[2] * nef[2];
+              Hb -= A.phys.g_f * dn * nef[1];
+            }
+            S.add(Vb * W);
+            H.add(Vb * Hb * W);
+          }
+        };
+        for_cells_team<D, true>(T, c, A.k, A.cell_start, tl, kWallTeam, visit, oe);
+      }
+      float Ss = S.value(), Hv = H.value();
+#pragma unroll
+      for (int o = kWallTeam / 2; o > 0; o >>= 1) {
+        Ss += __shfl_xor_sync(tmask, Ss, o, kWallTeam);
+        Hv += __shfl_xor_sync(tmask, Hv, o, kWallTeam);
+      }
+      if (tl == 0) {
+        const float Hs = fabsf(Ss) <= 6.0554544523933395e-06f ? 0.f : Hv / Ss;
+        const float rho_e = deviation_from_potential_f32(A.phys, T, Hs);
+        float pr, cc;
+        tait_f32(A.phys, T, rho_e, pr, cc);
+        const float inv = 1.f / (T.rho0_f + rho_e);
+        A.datrec[ew] = Dat32{0.f, 0.f, 0.f, rho_e, pr * inv * inv, cc, inv, 0.f};
       }
     }
-    float Ss = S.value(), Hv = H.value();
-#pragma unroll
-    for (int o = kWallTeam / 2; o > 0; o >>= 1) {
-      Ss += __shfl_xor_sync(0xffffffffu, Ss, o, kWallTeam);
-      Hv += __shfl_xor_sync(0xffffffffu, Hv, o, kWallTeam);
-    }
-    if (!valid || lane != 0) return;
-    if (A.walls_keep) {
-      rho_e = A.Y.rho[e];
-    } else {
-      const float Hs = fabsf(Ss) <= 6.0554544523933395e-06f ? 0.f : Hv / Ss;
-      rho_e = deviation_from_potential_f32(A.phys, T, Hs);
-    }
-    float pr, cc;
-    tait_f32(A.phys, T, rho_e, pr, cc);
-    const float inv = 1.f / (T.rho0_f + rho_e);
-    A.datrec[e] = Dat32{0.f, 0.f, 0.f, rho_e, pr * inv * inv, cc, inv, 0.f};
-#pragma unroll
-    for (int k = 0; k < D; ++k) A.X.off[k][e] = oe[k];
   }
-  // The wall's home state.
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    A.X.pos[k][e] = A.Y.pos[k][e];
-    A.X.vel[k][e] = R(0);
-    A.X.dv[k][e] = R(0);
-  }
-  A.X.rho[e] = rho_e;
-  A.X.drho[e] = R(0);
-  A.X.id[e] = A.Y.id[e];
-  A.X.key[e] = key;
 }
 
 // ---------------------------------------------------------------------------
@@ -956,13 +1011,20 @@ __global__ void __launch_bounds__(128)
 // SSPRK stages, u = (1 - w) u_n + w u'.  Last, the key (and FP32 offset)
 // of the new position for the next sort.
 
-// Resident 128-thread blocks per SM requested for k_forces: 10 for the 2D
-// compensated form (48 registers; latency hiding for its L1-bound loop
-// measured worth a small spill), 8 in 3D (64 registers), 4 for FP64 (its
+// Band-list entries per thread of the compensated force pass (shared
+// memory: a count and kBandCap slots of two words each), and the band's upper
+// end over its lower end: (1 + 2^-14) / (1 - 2^-14) rounded up to
+// 1 + 2^-13 + 2^-26 (any band containing R^2 (1 -+ 2^-15) is exact).
+constexpr int kBandCap = 4;
+constexpr float kBandRatio = 1.0f + 1.0f / 8192.0f + 1.0f / 67108864.0f;
+
+// Resident 128-thread blocks per SM requested for k_forces: 8 for the
+// compensated form (64 registers; in 2D measured 2% faster than 10 blocks
+// at 48 registers once the band handling joined the pass), 4 for FP64 (its
 // FP64 pipe is the limit).
 template<int D, int F>
 constexpr int forces_min_blocks() {
-  return F == TG_FP32C ? (D == 2 ? 10 : 8) : 4;
+  return F == TG_FP32C ? 8 : 4;
 }
 
 // Physics presets the compensated force kernel is specialised for (the
@@ -1315,6 +1377,99 @@ __device__ __forceinline__ void apply_face_terms(const StageArgs<D, F>& A,
   dv[1] -= A.phys.g;
 }
 
+// The compensated form's band handling for one target (see target_band):
+// candidates in the band around R^2 are deferred during the walk to this
+// thread's column of a short shared-memory list (slot and the offset code
+// of their cell, 2D, or row, 3D), then decided by the FP64 predicate; a full
+// list leaves them to a second walk over the band.  The sorted keys cannot
+// give a deferred candidate's cell: the force pass rewrites the home keys,
+// which may share their buffer.  `exact` is the walk that decides in FP64:
+// every candidate (a target whose block reaches a border cell) or the
+// band's only (after an overflow).
+template<int D, int K, int Phys>
+struct BandWalk {
+  const StageArgs<D, TG_FP32C>& A;
+  const TankDev& T;
+  PairF32<D, K, Phys>& acc;
+  const float* oa;
+  const int* c;
+  float csz, lo;
+  uint32_t ia;
+  uint32_t *n, *slot, *code;
+
+  __device__ __forceinline__ void init(uint32_t* smem) {
+    n = smem + threadIdx.x;
+    slot = smem + blockDim.x + threadIdx.x;
+    code = smem + (1 + kBandCap) * blockDim.x + threadIdx.x;
+    *n = 0u;
+  }
+  __device__ __forceinline__ void defer(uint32_t j, uint32_t cd) {
+    const uint32_t e = *n;
+    if (e < static_cast<uint32_t>(kBandCap)) {
+      slot[e * blockDim.x] = j;
+      code[e * blockDim.x] = cd;
+    }
+    *n = e + 1u;
+  }
+  // r_ab of candidate j seen from offset (u, v) cells: 2D (dx, dy); 3D
+  // (dy, dz), the x offset from the record's cell index.
+  __device__ __forceinline__ void rab(uint32_t j, int u, int v, float* d) const {
+    if constexpr (D == 2) {
+      float ob[2];
+      load_pos(A.posrec, j, ob);
+      d[0] = (oa[0] - u * csz) - ob[0];
+      d[1] = (oa[1] - v * csz) - ob[1];
+    } else {
+      const Pos32_3 b = A.posrec[j];
+      const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
+      d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
+      d[1] = (oa[1] - u * csz) - b.y;
+      d[2] = (oa[2] - v * csz) - b.z;
+    }
+  }
+  __device__ __forceinline__ void exact(uint32_t s, uint32_t en, int dx, int dy, int dz,
+                                        bool band_only) {
+    float oas[3];
+    oas[0] = oa[0] - dx * csz;
+    oas[1] = oa[1] - dy * csz;
+    oas[2] = D == 3 ? oa[2] - dz * csz : 0.f;
+    acc.open();
+    for (uint32_t j = s; j < en; ++j) {
+      if (j == ia) continue;
+      float ob[3], d[3];
+      load_pos(A.posrec, j, ob);
+#pragma unroll
+      for (int k = 0; k < D; ++k) d[k] = oas[k] - ob[k];
+      float s2 = d[0] * d[0] + d[1] * d[1];
+      if constexpr (D == 3) s2 += d[2] * d[2];
+      if (band_only && (s2 < lo || s2 > lo * kBandRatio)) continue;
+      if (!within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
+      acc.add(d, s2, load_dat(A.datrec, j));
+    }
+    acc.close();
+  }
+  // The deferred candidates: the FP64 decision, then r_ab as the walk
+  // computed it.  False when the list overflowed.
+  __device__ __forceinline__ bool decide() {
+    const uint32_t nb = *n;
+    if (nb == 0u) return true;
+    if (nb > static_cast<uint32_t>(kBandCap)) return false;
+    acc.open();
+    for (uint32_t e = 0; e < nb; ++e) {
+      const uint32_t j = slot[e * blockDim.x];
+      if (!within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
+      const uint32_t cd = code[e * blockDim.x];
+      float d[3];
+      rab(j, static_cast<int>(cd >> 3) - 3, static_cast<int>(cd & 7u) - 3, d);
+      float s2 = d[0] * d[0] + d[1] * d[1];
+      if constexpr (D == 3) s2 += d[2] * d[2];
+      acc.add(d, s2, load_dat(A.datrec, j));
+    }
+    acc.close();
+    return true;
+  }
+};
+
 // Team lanes share one target: each takes every Team-th cell of the block
 // and the team merges its partial sums by shuffles (compensated merges in
 // the FP32 form), so a warp advances 32 / Team targets.  The block size is
@@ -1330,7 +1485,10 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
   // Every exit below is uniform over a team (its lanes share i).
   if (i >= A.n) return;
   const uint32_t id = A.Y.id[i];
-  if (id & kWallBit) return;
+  if (id & kWallBit) {
+    if (lane == 0) commit_wall(A, i, id);
+    return;
+  }
   const uint32_t key = A.skey[i];
   const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
   const TankDev& T = A.tanks[tk];
@@ -1421,14 +1579,23 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
     const float csz = T.cs_f;
-    const bool tborder = border_cell<D>(T, c);
     const uint32_t ia = static_cast<uint32_t>(i);
+    // The band around the support radius (see target_band and BandWalk):
+    // the walk keeps one FP32 threshold on its common path; below band_lo a
+    // candidate is a neighbour, at or above it it is dropped unless it lies
+    // in the band, where it is deferred.
+    const Band bd = target_band<D>(T, c, A.k);
+    const float lo = bd.lo;
+    extern __shared__ uint32_t s_band[];
+    BandWalk<D, K, Phys> bw{A, T, acc, oa, c, csz, lo, ia};
+    bw.init(s_band);
     auto visit = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
-      const Band bd = visit_band<D>(T, c, A.k, dx, dy, dz, false, tborder);
       float oas[3];
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
       oas[2] = D == 3 ? oa[2] - dz * csz : 0.f;
+      const uint32_t code = D == 2 ? static_cast<uint32_t>(((dx + 3) << 3) | (dy + 3))
+                                   : static_cast<uint32_t>(((dy + 3) << 3) | (dz + 3));
       acc.open();
       for (uint32_t j = s; j < en; ++j) {
         if (j == ia) continue;
@@ -1438,8 +1605,10 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
         for (int k = 0; k < D; ++k) d[k] = oas[k] - ob[k];
         float s2 = d[0] * d[0] + d[1] * d[1];
         if constexpr (D == 3) s2 += d[2] * d[2];
-        if (s2 > bd.hi) continue;
-        if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
+        if (s2 >= lo) {
+          if (s2 <= lo * kBandRatio) bw.defer(j, code);
+          continue;
+        }
         acc.add(d, s2, load_dat(A.datrec, j));
       }
       acc.close();
@@ -1449,34 +1618,67 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
     // candidates in the same order as the per-cell walk.
     auto visit_row = [&](uint32_t s, uint32_t en, int, int dy, int dz) {
       if constexpr (D == 3) {
-        const Band bd = visit_band<D>(T, c, A.k, 0, dy, dz, true, tborder);
         const float oay = oa[1] - dy * csz;
         const float oaz = oa[2] - dz * csz;
+        const uint32_t code = static_cast<uint32_t>(((dy + 3) << 3) | (dz + 3));
         acc.open();
+        // The next record is loaded while this one is tested (3D: measured
+        // 2.6% faster per step; slower in 2D).
+        Pos32_3 bn{};
+        if (s < en) bn = A.posrec[s];
         for (uint32_t j = s; j < en; ++j) {
+          const Pos32_3 b = bn;
+          if (j + 1 < en) bn = A.posrec[j + 1];
           if (j == ia) continue;
-          const Pos32_3 b = A.posrec[j];
           const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
           float d[3];
           d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
           d[1] = oay - b.y;
           d[2] = oaz - b.z;
           const float s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-          if (s2 > bd.hi) continue;
-          if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
+          if (s2 >= lo) {
+            if (s2 <= lo * kBandRatio) bw.defer(j, code);
+            continue;
+          }
           acc.add(d, s2, load_dat(A.datrec, j));
         }
         acc.close();
       }
     };
-    if constexpr (Team == 1 && D == 3) {
+    auto exact_all = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      bw.exact(s, en, dx, dy, dz, false);
+    };
+    auto exact_band = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+      bw.exact(s, en, dx, dy, dz, true);
+    };
+    auto decide_band = [&]() {
+      if (bw.decide()) return;
+      if constexpr (Team == 1) {
+        for_cells<D, true>(T, c, A.k, A.cell_start, exact_band, oa);
+      } else {
+        for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, exact_band, oa);
+      }
+    };
+    if (lo < 0.f) {
+      // Near the grid border: every candidate in FP64.
+      if constexpr (Team == 1) {
+        for_cells<D, true>(T, c, A.k, A.cell_start, exact_all, oa);
+      } else {
+        for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, exact_all, oa);
+      }
+    } else if constexpr (Team == 1 && D == 3) {
       for_cells<D, false>(T, c, A.k, A.cell_start, visit_row, oa);
+      decide_band();
     } else if constexpr (Team == 1) {
       // 2D: per cell (8-byte records; measured faster than row ranges over
       // 16-byte records).
       for_cells<D, true>(T, c, A.k, A.cell_start, visit, oa);
+      decide_band();
     } else {
       for_cells_team<D, false>(T, c, A.k, A.cell_start, lane, Team, visit, oa);
+      decide_band();
+    }
+    if constexpr (Team > 1) {
       const unsigned mask = team_mask<Team>();
 #pragma unroll
       for (int o = Team / 2; o > 0; o >>= 1) {
@@ -1509,174 +1711,55 @@ __global__ void __launch_bounds__(256, forces_min_blocks<D, F>() / 2)
   forces_epilogue<D, F>(A, i, id, tk, T, c, va, rho_self, dv_out, drho_out);
 }
 
-// Compensated force pass with per-thread neighbour lists, one lane per
-// fluid target, in two phases.  The scan walks the candidates (2D: per
-// cell; 3D: per row of cells, clipped as in k_forces) and keeps each
-// neighbour (the band predicate above) in the thread's column of a
-// shared-memory list as (j << 6) | the range's offset code; the evaluation
-// then runs the pair terms over the list.  A warp thereby steps through the
-// pair terms once per listed neighbour of its busiest lane instead of once
-// per candidate that any of its lanes accepts.  The walk visits the same
-// (2k+1)^(D-1) rows or (2k+1)^2 cells for every lane (clipped ones empty),
-// so after each range the lanes agree by vote to evaluate their lists
-// together once some list holds kNbFlush entries; a list that fills inside
-// one range is evaluated there.  The sums run in chunks of kNbChunk plain
-// pair terms, each chunk one compensated add.  Entries need j < 2^26 and
-// k <= 3 (offsets in [-3, 3]).
-constexpr int kNbCap = 48;
-constexpr int kNbFlush = 28;
-constexpr int kNbChunk = 8;
-constexpr int64_t kNbMaxParticles = int64_t{1} << 26;
-
-template<int D, int K, int Phys>
-__global__ void __launch_bounds__(256, forces_min_blocks<D, TG_FP32C>() / 2)
-    k_forces_nbl(StageArgs<D, TG_FP32C> A) {
-  extern __shared__ uint32_t s_nb[];
-  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= A.n) return;
-  const uint32_t id = A.Y.id[i];
-  if (id & kWallBit) return;
-  const uint32_t key = A.skey[i];
-  const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
-  const TankDev& T = A.tanks[tk];
-  int c[3] = {0, 0, 0};
-  cell_from_key<D>(T, key, c);
-  const uint32_t ia = static_cast<uint32_t>(i);
-  PairF32<D, K, Phys> acc;
-  acc.init(A.phys, T, load_dat(A.datrec, ia), A.kahan);
-  const bool faces = A.fc.on;
-  if (faces) acc.dv[1].s = 0.f;
-  float oa[3] = {0.f, 0.f, 0.f};
-  load_pos(A.posrec, ia, oa);
-  const float csz = T.cs_f;
-  const bool tborder = border_cell<D>(T, c);
-  uint32_t* nb = s_nb + threadIdx.x;
-  const uint32_t stride = blockDim.x;
-  int cnt = 0;
-
-  // r_ab of list entry w (the scan's arithmetic).
-  auto entry_d = [&](uint32_t w, float* d) -> uint32_t {
-    const uint32_t j = w >> 6;
-    const float u = static_cast<float>(static_cast<int>((w >> 3) & 7u) - 3) * csz;
-    const float v = static_cast<float>(static_cast<int>(w & 7u) - 3) * csz;
-    if constexpr (D == 2) {
-      float ob[2];
-      load_pos(A.posrec, j, ob);
-      d[0] = (oa[0] - u) - ob[0];
-      d[1] = (oa[1] - v) - ob[1];
-    } else {
-      const Pos32_3 b = A.posrec[j];
-      const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
-      d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
-      d[1] = (oa[1] - u) - b.y;
-      d[2] = (oa[2] - v) - b.z;
-    }
-    return j;
-  };
-  auto evaluate = [&]() {
-    for (int e0 = 0; e0 < cnt; e0 += kNbChunk) {
-      const int e1 = min(cnt, e0 + kNbChunk);
-      acc.open();
-      for (int e = e0; e < e1; ++e) {
-        float d[3];
-        const uint32_t j = entry_d(nb[e * stride], d);
-        float s2 = d[0] * d[0] + d[1] * d[1];
-        if constexpr (D == 3) s2 += d[2] * d[2];
-        acc.add(d, s2, load_dat(A.datrec, j));
-      }
-      acc.close();
-    }
-    cnt = 0;
-  };
-  auto push = [&](uint32_t j, uint32_t code) {
-    nb[cnt * stride] = (j << 6) | code;
-    if (++cnt == kNbCap) evaluate();
-  };
-  const int k = A.k;
-  const int nx = T.nc[0], ny = T.nc[1];
-  const int side = 2 * k + 1;
-  for (int t = 0; t < side * side; ++t) {
-    // 2D: cell (c0 + u, c1 + v); 3D: row (c1 + u, c2 + v); u runs fastest
-    // (the next range in memory).
-    const int u = t % side - k, v = t / side - k;
-    uint32_t s = 0, en = 0;
-    Band bd{-1.f, -1.f};
-    if constexpr (D == 2) {
-      const int x = c[0] + u, y = c[1] + v;
-      if (x >= 0 && x < nx && y >= 0 && y < ny) {
-        const float gx = (x == 0 || x == nx - 1) ? 0.f : cell_gap(u, oa[0], csz);
-        const float gy = (y == 0 || y == ny - 1) ? 0.f : cell_gap(v, oa[1], csz);
-        if (gx * gx + gy * gy <= T.cull_r2_f) {
-          const uint32_t kc = 2 * (T.cell_off + static_cast<uint32_t>(y) * nx + x);
-          s = __ldg(A.cell_start + kc);
-          en = __ldg(A.cell_start + kc + 2);
-          bd = visit_band<D>(T, c, k, u, v, 0, false, tborder);
-        }
-      }
-    } else {
-      const int y = c[1] + u, z = c[2] + v;
-      int x0, x1;
-      if (y >= 0 && y < ny && z >= 0 && z < T.nc[2] &&
-          clip_row<D>(T, c, oa, y, z, max(c[0] - k, 0), min(c[0] + k, nx - 1), x0, x1)) {
-        const uint32_t row = T.cell_off + (static_cast<uint32_t>(z) * ny + y) * nx;
-        s = __ldg(A.cell_start + 2 * (row + x0));
-        en = __ldg(A.cell_start + 2 * (row + x1 + 1));
-        bd = visit_band<D>(T, c, k, 0, u, v, true, tborder);
-      }
-    }
-    const uint32_t code = static_cast<uint32_t>(((u + 3) << 3) | (v + 3));
-    const float su = static_cast<float>(u) * csz, sv = static_cast<float>(v) * csz;
-    for (uint32_t j = s; j < en; ++j) {
-      if (j == ia) continue;
-      float d[3];
-      if constexpr (D == 2) {
-        float ob[2];
-        load_pos(A.posrec, j, ob);
-        d[0] = (oa[0] - su) - ob[0];
-        d[1] = (oa[1] - sv) - ob[1];
-      } else {
-        const Pos32_3 b = A.posrec[j];
-        const int dxc = static_cast<int>(__float_as_uint(b.w) & ~kWallBit) - c[0];
-        d[0] = (oa[0] - static_cast<float>(dxc) * csz) - b.x;
-        d[1] = (oa[1] - su) - b.y;
-        d[2] = (oa[2] - sv) - b.z;
-      }
-      float s2 = d[0] * d[0] + d[1] * d[1];
-      if constexpr (D == 3) s2 += d[2] * d[2];
-      if (s2 > bd.hi) continue;
-      if (s2 >= bd.lo && !within_fp64<D>(A.Y.pos, ia, j, T.radius2)) continue;
-      push(j, code);
-    }
-    if (__any_sync(__activemask(), cnt >= kNbFlush)) evaluate();
-  }
-  evaluate();
-  float va[3], dv_out[3];
-#pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    va[q] = q < D ? acc.va[q] : 0.f;
-    dv_out[q] = q < D ? acc.dv[q].value() : 0.f;
-  }
-  float drho_out = acc.drho.value();
-  if (faces) {
-    double drho = drho_out;
-    double dv[3] = {dv_out[0], dv_out[1], dv_out[2]};
-    apply_face_terms(A, i, drho, dv);
-    drho_out = static_cast<float>(drho);
-#pragma unroll
-    for (int q = 0; q < D; ++q) dv_out[q] = static_cast<float>(dv[q]);
-  }
-  forces_epilogue<D, TG_FP32C>(A, i, id, tk, T, c, va, acc.a.drho, dv_out, drho_out);
+// Bulk copies (cp.async.bulk, global to this CTA's shared memory) behind
+// an mbarrier.  Addresses and sizes are multiples of 16 bytes.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Waits for phase `parity` of the barrier, at most `spins` polls; false
+// when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int spins) {
+  for (int it = 0; it < spins; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+constexpr int kCopySpins = 1 << 20;
 
 // 2D compensated form with the block's neighbour window staged in shared
 // memory.  A block of 128 consecutive (cell-ordered) targets whose first
 // and last target share a tank and a row of cells needs, for every target,
 // only the 2k+1 rows around that row over x in [x_first - k, x_last + k];
-// each of those row segments is contiguous in cell order, so the block
-// copies them (position and data records) into shared memory with coalesced
-// 16-byte loads and every target then reads its candidates from there.
-// Blocks that straddle rows or tanks, or whose window exceeds the staging
-// capacity, read from global memory as k_forces does.
+// each of those row segments is contiguous in cell order, so one thread
+// copies them (position and data records, rounded out to 16-byte
+// boundaries) into shared memory with bulk copies that complete on an
+// mbarrier, and every target then reads its candidates from there.  Blocks
+// that straddle rows or tanks, or whose window exceeds the staging
+// capacity, read from global memory as k_forces does; so does a block
+// whose copies do not complete within the wait limit (flagged in the
+// device error word).
 constexpr int kStageCap = 800;  // records: 800 x (8 + 32) B = 32 KB
 constexpr int kStageRows = 7;   // 2k + 1 for k <= 3
 
@@ -1687,10 +1770,13 @@ __global__ void __launch_bounds__(128, 7)
   __shared__ __align__(16) float4 s_dat[2 * kStageCap];
   __shared__ uint32_t s_gbeg[kStageRows], s_goff[kStageRows + 1];
   __shared__ int s_ok, s_rows, s_ylo;
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_band[(1 + 2 * kBandCap) * 128];
   const int64_t i0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
   const int64_t i = i0 + threadIdx.x;
   if (threadIdx.x == 0) {
     s_ok = 0;
+    mbar_init(&s_bar, 1);
     const int64_t ilast = min(i0 + static_cast<int64_t>(blockDim.x), A.n) - 1;
     const uint32_t k0 = A.skey[i0], k1 = A.skey[ilast];
     const uint32_t t0 = tank_of_key(k0, A.tank_off, A.ntanks);
@@ -1706,8 +1792,9 @@ __global__ void __launch_bounds__(128, 7)
         uint32_t off = 0;
         for (int y = ylo; y <= yhi; ++y) {
           const uint32_t row = T.cell_off + static_cast<uint32_t>(y) * T.nc[0];
-          const uint32_t gb = __ldg(A.cell_start + 2 * (row + xlo));
-          const uint32_t ge = __ldg(A.cell_start + 2 * (row + xhi + 1));
+          // Even record bounds: 8-byte position records start on 16 bytes.
+          const uint32_t gb = __ldg(A.cell_start + 2 * (row + xlo)) & ~1u;
+          const uint32_t ge = (__ldg(A.cell_start + 2 * (row + xhi + 1)) + 1u) & ~1u;
           s_gbeg[y - ylo] = gb;
           s_goff[y - ylo] = off;
           off += ge - gb;
@@ -1715,30 +1802,39 @@ __global__ void __launch_bounds__(128, 7)
         s_goff[yhi - ylo + 1] = off;
         s_rows = yhi - ylo + 1;
         s_ylo = ylo;
-        s_ok = off <= static_cast<uint32_t>(kStageCap) ? 1 : 0;
+        if (off > 0 && off <= static_cast<uint32_t>(kStageCap)) {
+          s_ok = 1;
+          mbar_arrive_expect(&s_bar, off * static_cast<uint32_t>(sizeof(float2) + 2 * sizeof(float4)));
+          for (int r = 0; r < s_rows; ++r) {
+            const uint32_t gb = s_gbeg[r], o = s_goff[r], len = s_goff[r + 1] - o;
+            if (len == 0) continue;
+            bulk_copy_g2s(s_pos + o, reinterpret_cast<const float2*>(A.posrec) + gb,
+                          len * static_cast<uint32_t>(sizeof(float2)), &s_bar);
+            bulk_copy_g2s(s_dat + 2 * o, reinterpret_cast<const float4*>(A.datrec) + 2 * gb,
+                          len * static_cast<uint32_t>(2 * sizeof(float4)), &s_bar);
+          }
+        }
       }
     }
   }
   __syncthreads();
-  const bool staged = s_ok != 0;
-  if (staged) {
-    const float2* gpos = reinterpret_cast<const float2*>(A.posrec);
-    const float4* gdat = reinterpret_cast<const float4*>(A.datrec);
-    for (int r = 0; r < s_rows; ++r) {
-      const uint32_t gb = s_gbeg[r], off = s_goff[r];
-      const uint32_t len = s_goff[r + 1] - off;
-      for (uint32_t t = threadIdx.x; t < len; t += blockDim.x) {
-        s_pos[off + t] = __ldg(gpos + gb + t);
-      }
-      for (uint32_t t = threadIdx.x; t < 2 * len; t += blockDim.x) {
-        s_dat[2 * off + t] = __ldg(gdat + 2 * static_cast<size_t>(gb) + t);
-      }
-    }
+  bool staged = s_ok != 0;
+  if (staged && !mbar_wait(&s_bar, 0, kCopySpins)) {
+    staged = false;
+    atomicOr(A.err, static_cast<uint32_t>(TG_DEV_COPY_TIMEOUT));
   }
-  __syncthreads();
+  // Every thread keeps its answer: a late copy must not leave part of the
+  // block on the staged path.
+  staged = __syncthreads_and(staged) != 0;
+  // Copies still in flight after a timed-out wait: a second bounded wait
+  // before any thread leaves (the block's shared memory outlives them).
+  if (s_ok != 0 && !staged) mbar_wait(&s_bar, 0, kCopySpins);
   if (i >= A.n) return;
   const uint32_t id = A.Y.id[i];
-  if (id & kWallBit) return;
+  if (id & kWallBit) {
+    commit_wall(A, i, id);
+    return;
+  }
   const uint32_t key = A.skey[i];
   const uint32_t tk = tank_of_key(key, A.tank_off, A.ntanks);
   const TankDev& T = A.tanks[tk];
@@ -1749,59 +1845,78 @@ __global__ void __launch_bounds__(128, 7)
   float oa[3] = {0.f, 0.f, 0.f};
   load_pos(A.posrec, static_cast<uint32_t>(i), oa);
   const float csz = T.cs_f;
-  const bool tborder = border_cell<2>(T, c);
   const uint32_t ia = static_cast<uint32_t>(i);
-  if (staged) {
-    const int xlo = max(c[0] - A.k, 0), xhi = min(c[0] + A.k, T.nc[0] - 1);
-    for (int r = 0; r < s_rows; ++r) {
-      const int y = s_ylo + r;
-      const uint32_t row = T.cell_off + static_cast<uint32_t>(y) * T.nc[0];
-      const int32_t shift = static_cast<int32_t>(s_goff[r]) - static_cast<int32_t>(s_gbeg[r]);
-      float oas[3];
-      oas[1] = oa[1] - (y - c[1]) * csz;
-      uint32_t gs = __ldg(A.cell_start + 2 * (row + xlo));
-      for (int x = xlo; x <= xhi; ++x) {
-        const uint32_t ge = __ldg(A.cell_start + 2 * (row + x + 1));
-        oas[0] = oa[0] - (x - c[0]) * csz;
-        const Band bd = visit_band<2>(T, c, A.k, x - c[0], y - c[1], 0, false, tborder);
+  // The band handling of k_forces (BandWalk), so that both passes visit
+  // the same candidates and sum them in the same order.
+  const float lo = target_band<2>(T, c, A.k).lo;
+  BandWalk<2, K, kPhysGeneric> bw{A, T, acc, oa, c, csz, lo, ia};
+  bw.init(s_band);
+  auto exact_all = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+    bw.exact(s, en, dx, dy, dz, false);
+  };
+  auto exact_band = [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
+    bw.exact(s, en, dx, dy, dz, true);
+  };
+  if (lo < 0.f) {
+    for_cells<2, true>(T, c, A.k, A.cell_start, exact_all, oa);
+  } else {
+    if (staged) {
+      const int xlo = max(c[0] - A.k, 0), xhi = min(c[0] + A.k, T.nc[0] - 1);
+      for (int r = 0; r < s_rows; ++r) {
+        const int y = s_ylo + r;
+        const uint32_t row = T.cell_off + static_cast<uint32_t>(y) * T.nc[0];
+        const int32_t shift = static_cast<int32_t>(s_goff[r]) - static_cast<int32_t>(s_gbeg[r]);
+        float oas[3];
+        oas[1] = oa[1] - (y - c[1]) * csz;
+        uint32_t gs = __ldg(A.cell_start + 2 * (row + xlo));
+        for (int x = xlo; x <= xhi; ++x) {
+          const uint32_t ge = __ldg(A.cell_start + 2 * (row + x + 1));
+          oas[0] = oa[0] - (x - c[0]) * csz;
+          const uint32_t code = static_cast<uint32_t>(((x - c[0] + 3) << 3) | (y - c[1] + 3));
+          acc.open();
+          for (uint32_t j = gs; j < ge; ++j) {
+            if (j == ia) continue;
+            const int sj = static_cast<int>(j) + shift;
+            const float2 ob = s_pos[sj];
+            float d[3] = {oas[0] - ob.x, oas[1] - ob.y, 0.f};
+            const float s2 = d[0] * d[0] + d[1] * d[1];
+            if (s2 >= lo) {
+              if (s2 <= lo * kBandRatio) bw.defer(j, code);
+              continue;
+            }
+            const float4 b0 = s_dat[2 * sj], b1 = s_dat[2 * sj + 1];
+            acc.add(d, s2, Dat32{b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w});
+          }
+          acc.close();
+          gs = ge;
+        }
+      }
+    } else {
+      for_cells<2, true>(T, c, A.k, A.cell_start,
+                         [&](uint32_t s, uint32_t en, int dx, int dy, int) {
+        float oas[3];
+        oas[0] = oa[0] - dx * csz;
+        oas[1] = oa[1] - dy * csz;
+        const uint32_t code = static_cast<uint32_t>(((dx + 3) << 3) | (dy + 3));
         acc.open();
-        for (uint32_t j = gs; j < ge; ++j) {
+        for (uint32_t j = s; j < en; ++j) {
           if (j == ia) continue;
-          const int sj = static_cast<int>(j) + shift;
-          const float2 ob = s_pos[sj];
-          float d[3] = {oas[0] - ob.x, oas[1] - ob.y, 0.f};
+          float ob[3], d[3];
+          load_pos(A.posrec, j, ob);
+          d[0] = oas[0] - ob[0];
+          d[1] = oas[1] - ob[1];
+          d[2] = 0.f;
           const float s2 = d[0] * d[0] + d[1] * d[1];
-          if (s2 > bd.hi) continue;
-          if (s2 >= bd.lo && !within_fp64<2>(A.Y.pos, ia, j, T.radius2)) continue;
-          const float4 b0 = s_dat[2 * sj], b1 = s_dat[2 * sj + 1];
-          acc.add(d, s2, Dat32{b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w});
+          if (s2 >= lo) {
+            if (s2 <= lo * kBandRatio) bw.defer(j, code);
+            continue;
+          }
+          acc.add(d, s2, load_dat(A.datrec, j));
         }
         acc.close();
-        gs = ge;
-      }
+      });
     }
-  } else {
-    for_cells<2, true>(T, c, A.k, A.cell_start,
-                       [&](uint32_t s, uint32_t en, int dx, int dy, int) {
-      const Band bd = visit_band<2>(T, c, A.k, dx, dy, 0, false, tborder);
-      float oas[3];
-      oas[0] = oa[0] - dx * csz;
-      oas[1] = oa[1] - dy * csz;
-      acc.open();
-      for (uint32_t j = s; j < en; ++j) {
-        if (j == ia) continue;
-        float ob[3], d[3];
-        load_pos(A.posrec, j, ob);
-        d[0] = oas[0] - ob[0];
-        d[1] = oas[1] - ob[1];
-        d[2] = 0.f;
-        const float s2 = d[0] * d[0] + d[1] * d[1];
-        if (s2 > bd.hi) continue;
-        if (s2 >= bd.lo && !within_fp64<2>(A.Y.pos, ia, j, T.radius2)) continue;
-        acc.add(d, s2, load_dat(A.datrec, j));
-      }
-      acc.close();
-    });
+    if (!bw.decide()) for_cells<2, true>(T, c, A.k, A.cell_start, exact_band, oa);
   }
   float va[3], dv_out[3];
 #pragma unroll
@@ -1855,11 +1970,10 @@ __global__ void __launch_bounds__(128)
     float oa[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(i), oa);
     const float csz = T.cs_f;
-    const bool tborder = border_cell<D>(T, c);
+    const Band bd = target_band<D>(T, c, A.k);
     const uint32_t ia = static_cast<uint32_t>(i);
     for_cells<D, true>(T, c, A.k, A.cell_start,
                        [&](uint32_t s, uint32_t en, int dx, int dy, int dz) {
-      const Band bd = visit_band<D>(T, c, A.k, dx, dy, dz, false, tborder);
       float oas[3];
       oas[0] = oa[0] - dx * csz;
       oas[1] = oa[1] - dy * csz;
@@ -2109,13 +2223,16 @@ __global__ void __launch_bounds__(128) k_gamma_faces(StageArgs<D, F> A) {
 
 // ---------------------------------------------------------------------------
 // Prepare-only commit: the fluid home state takes the gathered cell-order
-// copy (walls were written by k_walls).
+// copy, the walls theirs from commit_wall.
 template<int D, int F>
 __global__ void __launch_bounds__(256) k_commit(StageArgs<D, F> A) {
   const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (j >= A.n) return;
   const uint32_t id = A.Y.id[j];
-  if (id & kWallBit) return;
+  if (id & kWallBit) {
+    commit_wall(A, j, id);
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     A.X.pos[k][j] = A.Y.pos[k][j];

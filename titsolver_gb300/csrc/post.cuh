@@ -438,7 +438,10 @@ __global__ void __launch_bounds__(128) k_post_shift(PostArgs<D, F> A) {
   const TankDev* Tp;
   int c[3] = {0, 0, 0};
   if (!post_target(A, i, id, Tp, c)) return;
-  if (id & kWallBit) return;  // k_walls wrote the wall's home state
+  if (id & kWallBit) {
+    commit_wall(A.S, i, id);
+    return;
+  }
   const TankDev& T = *Tp;
   const StateBuf<R>& Y = A.S.Y;
   const StateBuf<R>& X = A.S.X;
