@@ -9,7 +9,8 @@
 //
 // The array's name is only a host-side stand-in in host code; its device
 // address comes from cudaGetSymbolAddress, taken once per device (with that
-// device current) on the first call made on that device.
+// device current) on the first call made on that device and kept for the
+// life of the process (a device reset after that call is not supported).
 #include <cuda_runtime.h>
 
 #include <cmath>
