@@ -1,43 +1,55 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 WCSPH hot path (one JSON line on rank 0).
 
-Workload (default, ``--config c1``): 2D dam break at scale, H = 1,
-dx = H/800 (1,280,000 fluid particles at dx (i+1, j+1)) in a 5.366H x 3H
-tank with three layers of fixed wall particles, Wendland C2 kernel (h = 2dx),
-Tait EOS (rho0 = 1000, xi = 7, cs0 = 10 sqrt(gH)), hydrostatic start,
-Monaghan alpha = 0.02, delta-SPH delta = 0.1, SSPRK3 at CFL 0.25.  A step is
-one full SSPRK3 step (three neighbour rebuilds, three fused force passes).
+Workload (default, ``--config c4``): the 3D dam break, H = 1, column
+2H x H x H at dx = H/200 (16,000,000 fluid particles at dx (i+1, j+1, k+1))
+in a 5.366H x 3H x (H + dx) tank with three layers of fixed wall particles,
+Wendland C2 kernel (h = 1.3dx), Tait EOS (rho0 = 1000, xi = 7,
+cs0 = 10 sqrt(gH)), hydrostatic start, Monaghan alpha = 0.02, delta-SPH
+delta = 0.1, SSPRK3 at CFL 0.25.  A step is one full SSPRK3 step (three
+neighbour rebuilds, three fused force passes).
 
 * ``value``: FP32-compensated form, particle-updates/s = fluid particles x
   steps / device time, state resident in HBM (working set > L2), CUDA-graph
   replay, timed with CUDA events on the library's stream.
 * ``forms.fp64``: the plain FP64 form on the same workload.
-* ``l2_error_vs_fp64``: relative L2 error of rho, r and v, and the drift of
-  total momentum (|sum m v32 - sum m v64| / sum m |v64|), FP32C vs FP64, after
-  the same number of steps from the same start.
+* ``l2_error_vs_fp64``: relative L2 error of rho, r and v (field-relative,
+  and r also against the displacement from the start), the drift of total
+  momentum (|sum m v32 - sum m v64| / sum m |v64|), FP32C against FP64
+  after ``--err-steps`` (1000) steps from the same start, run outside the
+  timed region on ``--err-config`` (for the 3D workloads the 3D dam break at
+  dx = H/100, 2,000,000 fluid: 1000 plain-FP64 steps of the 16M workload
+  would take eleven minutes).
 * ``e2e``: the same metric through the C ABI with host buffers: every step
   uploads r, v, rho, dv/dt from pinned host memory, steps, and downloads
   them again (tg_particles_update / tg_step / tg_particles_download_state).
 * ``roofline``: the fused force kernel (k_forces): algorithmic bytes per
   launch = fluid particles x 3S (S = state bytes per particle) over its mean
   launch time from a profiled pass with CUDA events on the same stream.
-  The kernel is not HBM-bound; ``ncu_working_ceiling`` carries, from its
-  recorded ncu capture under ``profiles/``, the unit that bounds it and how
-  busy that unit was.
+  The kernel is not HBM-bound; ``compute`` gives its FP32 work per launch
+  (FLOPs per neighbour pair counted from the kernel source, pairs counted
+  live) against the FP32 pipe and the recorded instruction count against
+  the issue rate, and ``ncu_working_ceiling`` the recorded ncu capture's
+  busiest unit.
+* ``extra_workloads``: the 2D dam break at scale (c1), the 512 batched 2D
+  tanks (c3) and 64 batched 3D tanks (c5), both forms, and c3's FP32C error
+  after 500 steps.
 * ``cpu_baseline``: the oracle (the C++ restatement of the reference's CPU
   path) on the host cores, on a bounded sample of the same workload.
 
-Other workloads (``--config``): c0, c3, c4, c4q, c4half, c5 (2D / 3D /
+Other workloads (``--config``): c0, c1, c3, c4q, c4half, c5 (2D / 3D /
 batched dam breaks, the same report), c2 (point-cloud search + summation
 density), f2 and f3 (the reference's face-wall mode: the titwcsph pool in
 2D, a triangulated 3D pool; reference physics with shifting; device time
 per step of each form: fp32c with FP64 face integrals, fp32c_face32 with
-tg_params.face_fp32, fp64; and each compensated form's drift from fp64).
+tg_params.face_fp32, fp64; each compensated form's drift from fp64; and the
+oracle's rate on the same workload on the host cores).
 
-``--impl reference`` times that CPU path alone (the reference itself needs
-C++26 / GCC 16 and cannot be built here).  ``--gpus N`` under
-torch.distributed.run runs N independent replicas (the path does not shard
-across GPUs) and reports their summed throughput over the slowest rank.
+``--impl reference`` times that CPU path alone on a sample of the same
+workload (the reference itself needs C++26 / GCC 16 and cannot be built
+here).  ``--gpus N`` under torch.distributed.run runs N independent replicas
+(the path does not shard across GPUs) and reports their summed throughput
+over the slowest rank.
 """
 
 from __future__ import annotations
@@ -195,6 +207,59 @@ def forces_traffic(dim: int, form: str, n_fluid: int):
     return None if d is None else float(d["dram_bytes_per_fluid_particle"]) * n_fluid
 
 
+def forces_traffic_source(dim: int, form: str) -> str | None:
+    d = _forces_profile(dim, form)
+    if d is None:
+        return None
+    return (f"recorded, not measured in this run: DRAM bytes per fluid particle of one ncu "
+            f"capture of {d['kernel']} ({d['source']}) x the fluid count")
+
+
+# FP32 floating-point operations of the compensated force pass, counted from
+# the kernel source (fluid.cuh, PairF32::add with the textbook terms:
+# Wendland C2, delta-SPH diffusion, Monaghan viscosity; an FMA counts 2, a
+# reciprocal square root or reciprocal 1).  Per accepted pair: rsqrt 1,
+# r and q 2, kernel gradient factor 6, v_ab . r_ab 3d - 1, density
+# difference 1, diffusion 3, continuity term 2, Monaghan term 9, momentum
+# coefficient 4, sums 1 + 2d.  Per candidate: r_ab d (plus the 3D row
+# shift 2) and |r_ab|^2 2d - 1.
+FLOPS_PER_PAIR = {2: 38, 3: 43}
+FLOPS_PER_CANDIDATE = {2: 5, 3: 10}
+SM_COUNT = 152
+FP32_LANES_PER_SM = 128
+ISSUE_PER_SM_CLK = 4
+
+
+def forces_compute(dim: int, n_fluid: int, pairs: int, avg_ms: float,
+                   clk: dict | None) -> dict:
+    """Compute-side roofline of the compensated force pass: FP32 work per
+    launch (pairs counted live in this run, the per-pair FLOPs from the
+    source) against the FP32 pipe's nominal rate at the sampled SM clock,
+    and the recorded ncu instruction count against the issue rate."""
+    mhz = float(clk["sm_mhz"]) if clk and clk.get("sm_mhz") else 2070.0
+    sec = avg_ms / 1e3
+    flops = pairs * FLOPS_PER_PAIR[dim]
+    fp32_peak = SM_COUNT * FP32_LANES_PER_SM * 2 * mhz * 1e6
+    out = {"pairs_per_launch": pairs, "pairs_per_fluid_particle": pairs / max(n_fluid, 1),
+           "flops_per_pair": FLOPS_PER_PAIR[dim],
+           "flops_per_candidate": FLOPS_PER_CANDIDATE[dim],
+           "pair_flops_per_launch": flops,
+           "fp32_tflops": flops / sec / 1e12,
+           "fp32_peak_tflops": fp32_peak / 1e12,
+           "fp32_frac": flops / sec / fp32_peak,
+           "fp32_peak_source": (f"nominal: {SM_COUNT} SMs x {FP32_LANES_PER_SM} FP32 lanes x "
+                                f"2 (FMA) x {mhz:.0f} MHz (median SM clock of this run)")}
+    d = _forces_profile(dim, "fp32c")
+    if d is not None and "warp_inst_per_fluid_particle" in d:
+        inst = d["warp_inst_per_fluid_particle"] * n_fluid
+        issue_peak = SM_COUNT * ISSUE_PER_SM_CLK * mhz * 1e6
+        out.update({"warp_inst_per_launch": inst,
+                    "thread_inst_per_pair": 32.0 * inst / max(pairs, 1),
+                    "issue_frac": inst / sec / issue_peak,
+                    "inst_source": f"recorded: smsp__inst_executed.sum of {d['source']}"})
+    return out
+
+
 def forces_ceiling(dim: int, form: str) -> dict | None:
     """The unit that bounds k_forces in its ncu capture (issue slots for the
     compensated form, the FP64 pipe for the plain one) and how busy it was:
@@ -205,67 +270,100 @@ def forces_ceiling(dim: int, form: str) -> dict | None:
     return {**d["working_ceiling"], "source": d["source"]}
 
 
-def cpu_sample(budget_s: float, steps: int, threads: int, fill: bool = False,
-               workload: dict | None = None) -> dict:
-    """Time the oracle (CPU restatement of the reference path) on a dam break
-    sized so that `steps` steps take about budget_s seconds (with fill, more
-    steps when the largest sample size is reached first).  A 2D one-tank
-    workload smaller than that size is timed itself, with as many steps as
-    fill the budget (nx_per_H = 0 in the result)."""
-    import oracle
-    from titsolver_gb300 import physics, scenarios
+def sample_scenario(dim: int, nx: int, cfg: str | None = None):
+    """A dam break of the workload's dimension at resolution dx = H/nx (the
+    2D and 3D workloads' own geometry and physics at a coarser lattice)."""
+    from titsolver_gb300 import scenarios
 
-    P = physics.baseline_params(2)
-    cal = scenarios.dam_break_2d(nx_per_H=40)
+    if cfg == "c4half":
+        return scenarios.dam_break_3d(nx_per_H=nx, column=(2.0, 1.0, 0.5))
+    if dim == 3:
+        return scenarios.dam_break_3d(nx_per_H=nx)
+    return scenarios.dam_break_2d(nx_per_H=nx)
+
+
+def cpu_sample(budget_s: float, steps: int, threads: int, dim: int = 2,
+               workload: dict | None = None, warmup: int = 0,
+               cfg: str | None = None) -> dict:
+    """Time the oracle (CPU restatement of the reference path) on a dam
+    break of the workload's dimension sized so that warmup + steps steps take
+    about budget_s seconds; the warm-up steps run untimed.  A one-tank
+    workload without faces that is no larger than that size is timed itself
+    (nx_per_H = 0 in the result).  One step at a small calibration size
+    gives the host time per particle (fluid and walls), which picks the
+    size."""
+    import oracle
+    from titsolver_gb300 import physics
+
+    P = physics.baseline_params(dim)
+    nx_cal, nx_max = (40, 800) if dim == 2 else (16, 200)
+    cal = sample_scenario(dim, nx_cal, cfg)
     st = oracle.State(cal)
+    oracle.step(P, st, 1, nthreads=threads)  # thread pool start-up
     t0 = time.perf_counter()
     oracle.step(P, st, 1, nthreads=threads)
-    rate = cal["tanks"][0]["n_fluid"] / max(time.perf_counter() - t0, 1e-6)
-    want = rate * budget_s / max(steps, 1)
-    nx = int(max(40, min(800, math.sqrt(want / 2.0))))
-    scn = scenarios.dam_break_2d(nx_per_H=nx)
-    if (workload is not None and workload["dim"] == 2 and len(workload["tanks"]) == 1
+    per_particle = max(time.perf_counter() - t0, 1e-6) / cal["r"].shape[0]
+    want = budget_s / max(steps + warmup, 1) / per_particle  # particles per sample
+    scale = (want / cal["r"].shape[0]) ** (1.0 / dim)
+    nx = int(max(nx_cal, min(nx_max, nx_cal * scale)))
+    scn = sample_scenario(dim, nx, cfg)
+    if (workload is not None and workload["dim"] == dim and len(workload["tanks"]) == 1
             and not any(workload.get("faces") or [])
-            and workload["tanks"][0]["n_fluid"] < scn["tanks"][0]["n_fluid"]):
+            and workload["r"].shape[0] <= scn["r"].shape[0]):
         scn, nx = workload, 0
     st = oracle.State(scn)
     nf = scn["tanks"][0]["n_fluid"]
-    if fill:
-        # At the largest sample size, more steps fill the time budget: one
-        # untimed step at this size gives the rate (the small calibration
-        # case underestimates it: thread start-up dominates there).
-        t0 = time.perf_counter()
-        oracle.step(P, st, 1, nthreads=threads)
-        one = max(time.perf_counter() - t0, 1e-6)
-        steps = max(steps, min(50 if nx else 200, int(budget_s / one)))
+    if warmup:
+        oracle.step(P, st, warmup, nthreads=threads)
     t0 = time.perf_counter()
     oracle.step(P, st, steps, nthreads=threads)
     sec = time.perf_counter() - t0
-    return {"value": nf * steps / sec, "seconds": sec, "fluid": nf, "nx_per_H": nx,
-            "steps": steps, "threads": threads}
+    return {"value": nf * steps / sec, "seconds": sec, "fluid": nf,
+            "walls": scn["tanks"][0]["n_wall"], "nx_per_H": nx, "steps": steps,
+            "warmup": warmup, "threads": threads}
+
+
+def sample_text(res: dict, dim: int) -> str:
+    what = (f"the workload itself ({res['fluid']} fluid)" if res["nx_per_H"] == 0 else
+            f"{dim}D dam break of the same geometry at dx=H/{res['nx_per_H']} "
+            f"({res['fluid']} fluid, {res['walls']} walls)")
+    return (f"{what}, same physics, {res['warmup']} untimed + {res['steps']} timed SSPRK3 "
+            f"steps ({res['seconds']:.1f} s), oracle built g++ -O3 -ffp-contract=off")
+
+
+def describe(scn: dict, workload: str) -> dict:
+    """The workload part of the bench line's config: the same dictionary in
+    both arms."""
+    from titsolver_gb300 import scenarios
+
+    nf = scenarios.n_fluid(scn)
+    nw = int(sum(t["n_wall"] for t in scn["tanks"]))
+    ws = scn["r"].shape[0] * (200 if scn["dim"] == 2 else 270)
+    return {"workload": workload, "fluid_particles": nf, "wall_particles": nw,
+            "tanks": len(scn["tanks"]), "parallelism": "replicas (no exchange between GPUs)",
+            "l2": f"inputs larger than L2 (working set ~{ws / 1e6:.0f} MB > 129 MB)"}
 
 
 def run_reference(args, ranks) -> dict:
     import oracle
 
     threads = oracle.default_threads()
-    # Each timed step is one SSPRK3 step of a dam break sized so the whole
-    # run takes about two minutes of host time.
     workload, make = make_config(args.config)
-    # c0 is the one 2D single-tank workload smaller than the sample size.
-    res = cpu_sample(120.0, args.steps, threads,
-                     workload=make() if args.config == "c0" else None)
-    what = (f"the workload itself ({res['fluid']} fluid)" if res["nx_per_H"] == 0 else
-            f"2D dam break dx=H/{res['nx_per_H']} ({res['fluid']} fluid)")
-    sample = (f"{what}, same physics, {res['steps']} SSPRK3 steps per timed run "
-              f"({res['seconds']:.1f} s)")
+    scn = make()
+    dim = scn["dim"]
+    # Each timed step is one SSPRK3 step of a dam break of the workload's
+    # dimension sized so that the warm-up and timed steps take about
+    # --ref-budget seconds of host time.
+    res = cpu_sample(args.ref_budget, args.steps, threads, dim=dim, workload=scn,
+                     warmup=args.warmup, cfg=args.config)
+    sample = sample_text(res, dim)
     return {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * res["seconds"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded dam-break lattice, hydrostatic start)",
-        "config": {"workload": workload, "sample": sample},
+        "config": describe(scn, workload),
         "impl": "reference",
         "cpu_baseline": {"value": res["value"], "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
@@ -282,7 +380,7 @@ def tune(P, args) -> None:
 
 
 def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks,
-            autotune: bool = False):
+            autotune: bool = False, tuning: dict | None = None):
     from titsolver_gb300 import _abi
 
     ctx = _abi.Context(params)
@@ -290,7 +388,10 @@ def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks,
     for t, fc in enumerate(scn.get("faces") or []):
         if fc is not None:
             ctx.set_faces(t, fc["face_verts"], fc["poly"])
-    if autotune:
+    if tuning is not None:
+        ctx.set_tuning(tuning["cells_per_radius"], tuning["block_size"],
+                       tuning["lanes_per_particle"])
+    elif autotune:
         # Untimed setup: the autotuner times a few steps per launch shape and
         # leaves the context at the fastest, with the uploaded state.
         ctx.autotune(3)
@@ -312,6 +413,114 @@ def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks,
     return ctx, ms, launches, prof
 
 
+def fluid_mask(scn: dict) -> np.ndarray:
+    return np.concatenate([np.r_[np.ones(t["n_fluid"], bool), np.zeros(t["n_wall"], bool)]
+                           for t in scn["tanks"]])
+
+
+def form_errors(scn: dict, ctx32, ctx64, steps: int) -> dict:
+    """FP32C against FP64 on the fluid after the same number of steps from
+    the same start: relative L2 of rho, r, v (field-relative), r against the
+    displacement and rho against its deviation from rho0, the drift of total
+    momentum and the time offset; total mass is exact (constant masses)."""
+    from titsolver_gb300 import _abi
+
+    f = fluid_mask(scn)
+    r32, r64 = ctx32.download(_abi.TG_FIELD_R)[f], ctx64.download(_abi.TG_FIELD_R)[f]
+    d32, d64 = ctx32.download(_abi.TG_FIELD_RHO)[f], ctx64.download(_abi.TG_FIELD_RHO)[f]
+    v32, v64 = ctx32.download(_abi.TG_FIELD_V)[f], ctx64.download(_abi.TG_FIELD_V)[f]
+    t32, t64 = ctx32.time(), ctx64.time()
+    r0 = scn["r"][f]
+    rho0 = np.concatenate([np.full(t["n_fluid"], t["rho0"]) for t in scn["tanks"]])
+    # Equal masses within a tank: total momentum is m * sum(v) per tank.
+    m = np.concatenate([np.full(t["n_fluid"], t["m"]) for t in scn["tanks"]])[:, None]
+    p32, p64 = (m * v32).sum(axis=0), (m * v64).sum(axis=0)
+    return {"steps": steps,
+            "rho": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
+            "r": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
+            "v": float(np.linalg.norm(v32 - v64) / max(np.linalg.norm(v64), 1e-300)),
+            "r_vs_displacement": float(np.linalg.norm(r32 - r64) /
+                                       max(np.linalg.norm(r64 - r0), 1e-300)),
+            "rho_vs_deviation": float(np.linalg.norm(d32 - d64) /
+                                      max(np.linalg.norm(d64 - rho0), 1e-300)),
+            "momentum_drift": float(np.linalg.norm(p32 - p64) /
+                                    max(float((m * np.linalg.norm(v64, axis=1)[:, None]).sum()),
+                                        1e-300)),
+            "time_rel_diff": float(np.max(np.abs(t32 - t64) / np.maximum(t64, 1e-300))),
+            "mass_exact": True,
+            "normalisation": "field-relative ||x32 - x64|| / ||x64|| for r, rho and v; "
+                             "r_vs_displacement divides by ||r64 - r0||"}
+
+
+def error_leg(name: str, steps: int, tuning32: dict, tuning64: dict, dev: int) -> dict:
+    """Both forms for `steps` steps from the start of workload `name` at the
+    headline's launch shapes (untimed), and the FP32C error against FP64."""
+    from titsolver_gb300 import _abi, physics
+
+    workload, make = make_config(name)
+    scn = make()
+    ctxs = []
+    for prec, tn in ((_abi.TG_FP32C, tuning32), (_abi.TG_FP64, tuning64)):
+        P = physics.baseline_params(scn["dim"], precision=prec)
+        P.device = dev
+        ctx = _abi.Context(P)
+        ctx.upload(scn["tanks"], scn["r"], scn["v"], scn["rho"])
+        ctx.set_tuning(tn["cells_per_radius"], tn["block_size"], tn["lanes_per_particle"])
+        ctx.step(steps)
+        ctxs.append(ctx)
+    err = form_errors(scn, ctxs[0], ctxs[1], steps)
+    for c in ctxs:
+        c.close()
+    err["workload"] = workload
+    err["fluid_particles"] = int(sum(t["n_fluid"] for t in scn["tanks"]))
+    return err
+
+
+def shares(p: dict) -> dict:
+    """Share of the step's device time per kernel group (fractions)."""
+    keys = (("sort", "sort_ms"), ("reorder", "reorder_ms"), ("walls", "walls_ms"),
+            ("forces", "forces_ms"))
+    tot = sum(p[k] for _, k in keys)
+    return {n: round(p[k] / tot, 4) for n, k in keys}
+
+
+def extra_workload(name: str, args, ranks, err_steps: int) -> dict:
+    """Both forms on another workload (autotuned, warm-up, timed steps) and,
+    with err_steps, the FP32C error against FP64 after err_steps steps (the
+    contexts continue from the timed steps; untimed)."""
+    from titsolver_gb300 import _abi, physics, scenarios
+
+    workload, make = make_config(name)
+    scn = make()
+    nf = scenarios.n_fluid(scn)
+    out = {"workload": workload, "fluid_particles": nf, "tanks": len(scn["tanks"])}
+    ctxs = {}
+    k = min(args.steps, 20)
+    for form, prec in (("fp32c", _abi.TG_FP32C), ("fp64", _abi.TG_FP64)):
+        P = physics.baseline_params(scn["dim"], precision=prec)
+        P.device = ranks.local_rank
+        ctx, ms, _, prof = gpu_leg(scn, P, args.warmup, k, 5, ranks, True)
+        out[form] = {"value": nf * k / (ms / 1e3), "ms_per_step": ms / k, "steps": k,
+                     "kernel_shares": shares(prof), "launch_shape": ctx.get_tuning()}
+        ctxs[form] = ctx
+    out["speedup_fp32c_over_fp64"] = out["fp32c"]["value"] / out["fp64"]["value"]
+    done = args.warmup + k + 5
+    if err_steps > done:
+        for ctx in ctxs.values():
+            ctx.step(err_steps - done)
+        out["l2_error_vs_fp64"] = form_errors(scn, ctxs["fp32c"], ctxs["fp64"], err_steps)
+    for ctx in ctxs.values():
+        ctx.close()
+    return out
+
+
+def err_config(name: str) -> str:
+    """Workload of the error leg: 1000 plain-FP64 steps of the 3D workloads
+    at dx = H/200 take over ten minutes, so they use the 2M-fluid 3D dam
+    break at dx = H/100; the others their own workload."""
+    return "c4q" if name in ("c4", "c4half") else name
+
+
 def run_gpu(args, ranks) -> dict | None:
     from titsolver_gb300 import _abi, physics, scenarios
 
@@ -319,7 +528,6 @@ def run_gpu(args, ranks) -> dict | None:
     scn = make()
     dim = scn["dim"]
     nf = scenarios.n_fluid(scn)
-    nw = int(sum(t["n_wall"] for t in scn["tanks"]))
     dev = ranks.local_rank
     peaks = _peaks()
 
@@ -345,36 +553,15 @@ def run_gpu(args, ranks) -> dict | None:
     P64.device = dev
     tune(P64, args)
     k64 = args.steps if args.fp64_steps is None else args.fp64_steps
-    ctx64, ms64, _, prof64 = gpu_leg(scn, P64, args.warmup, k64, min(k64, 20), ranks, auto)
+    ctx64, ms64, _, prof64 = gpu_leg(scn, P64, args.warmup, k64, min(k64, 5), ranks, auto)
     tuning64 = ctx64.get_tuning()
     value64 = nf * k64 / (ms64 / 1e3)
-
-    # Error of the compensated form against FP64 after the same steps.
-    err = None
-    total32 = args.warmup + args.steps + min(args.steps, 20)
-    total64 = args.warmup + k64 + min(k64, 20)
-    if total32 == total64:
-        f = np.concatenate([np.r_[np.ones(t["n_fluid"], bool), np.zeros(t["n_wall"], bool)]
-                            for t in scn["tanks"]])
-        r32, r64 = ctx32.download(_abi.TG_FIELD_R)[f], ctx64.download(_abi.TG_FIELD_R)[f]
-        d32, d64 = ctx32.download(_abi.TG_FIELD_RHO)[f], ctx64.download(_abi.TG_FIELD_RHO)[f]
-        v32, v64 = ctx32.download(_abi.TG_FIELD_V)[f], ctx64.download(_abi.TG_FIELD_V)[f]
-        r0 = scn["r"][f]
-        # Equal masses within a tank: total momentum is m * sum(v) per tank.
-        m = np.concatenate([np.full(t["n_fluid"], t["m"]) for t in scn["tanks"]])[:, None]
-        p32, p64 = (m * v32).sum(axis=0), (m * v64).sum(axis=0)
-        err = {"steps": total32,
-               "rho": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
-               "r": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
-               "v": float(np.linalg.norm(v32 - v64) / max(np.linalg.norm(v64), 1e-300)),
-               "momentum_drift": float(np.linalg.norm(p32 - p64) /
-                                       max(float((m * np.linalg.norm(v64, axis=1)[:, None]).sum()),
-                                           1e-300)),
-               "r_vs_displacement": float(np.linalg.norm(r32 - r64) /
-                                          max(np.linalg.norm(r64 - r0), 1e-300)),
-               "rho_vs_deviation": float(np.linalg.norm(d32 - d64) /
-                                         max(np.linalg.norm(d64 - 1000.0), 1e-300))}
     ctx64.close()
+
+    # Live pair count of the compensated state (fluid targets, self excluded)
+    # for the compute-side roofline.
+    cnt, _ = ctx32.neighbour_counts()
+    pairs = int(cnt[fluid_mask(scn)].sum()) - nf
 
     # End to end through the C ABI with pinned host buffers.
     n = scn["r"].shape[0]
@@ -405,22 +592,32 @@ def run_gpu(args, ranks) -> dict | None:
         e2e_value, _ = aggregate(nf * ke, te, ranks)
     hd_bytes = n * 8 * (3 * dim + 1)
     ctx32.close()
+    del pin
+
+    # Error of the compensated form against FP64 (untimed).
+    err = None
+    if args.err_steps > 0:
+        err = error_leg(args.err_config or err_config(args.config), args.err_steps,
+                        tuning32, tuning64, dev)
 
     # Roofline of the fused force kernel.
     forces_avg_ms = prof32["forces_ms"] / max(prof32["forces_launches"], 1)
     alg = nf * 3 * state_bytes(dim, "fp32c")
     achieved = alg / (forces_avg_ms / 1e3) / 1e9
-    traffic = forces_traffic(dim, "fp32c", nf)
     roofline = {"bound": "hbm", "kernel": "k_forces (fused continuity+momentum+RK update)",
                 "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "frac": achieved / peaks["hbm_gbs"],
+                "traffic": forces_traffic(dim, "fp32c", nf),
+                "traffic_source": forces_traffic_source(dim, "fp32c"),
                 "peak_source": f"{peaks['source']} hbm_gbs",
                 "alg_bytes_per_launch": alg, "avg_launch_ms": forces_avg_ms,
+                "compute": forces_compute(dim, nf, pairs, forces_avg_ms, clk),
                 "ncu_working_ceiling": forces_ceiling(dim, "fp32c")}
 
-    def shares(p):
-        tot = p["sort_ms"] + p["reorder_ms"] + p["walls_ms"] + p["forces_ms"]
-        return {k: round(p[k] / tot, 4) for k in ("sort_ms", "reorder_ms", "walls_ms", "forces_ms")}
+    extras = {}
+    for name in [x for x in args.extra.split(",") if x and x != args.config]:
+        extras[name] = extra_workload(name, args, ranks,
+                                      args.extra_err_steps if name == "c3" else 0)
 
     out = None
     if ranks.rank == 0:
@@ -428,13 +625,10 @@ def run_gpu(args, ranks) -> dict | None:
         if ranks.world_size == 1 and not args.no_cpu:
             import oracle
             threads = oracle.default_threads()
-            c = cpu_sample(args.cpu_budget, 2, threads, fill=True, workload=scn)
-            what = (f"the workload itself ({c['fluid']} fluid)" if c["nx_per_H"] == 0 else
-                    f"2D dam break dx=H/{c['nx_per_H']} ({c['fluid']} fluid)")
+            c = cpu_sample(args.cpu_budget, 3, threads, dim=dim, workload=scn, warmup=1,
+                           cfg=args.config)
             cpu = {"value": c["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": (f"{what}, same physics, {c['steps']} SSPRK3 steps, "
-                              f"{c['seconds']:.1f} s, oracle built g++ -O3 -ffp-contract=off")}
-        ws = scn["r"].shape[0] * 260
+                   "sample": sample_text(c, dim)}
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
@@ -442,9 +636,8 @@ def run_gpu(args, ranks) -> dict | None:
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (compensated sums; f64 positions and time)",
             "data": "synthetic (seeded dam-break lattice, hydrostatic start)",
-            "config": {"workload": workload, "fluid_particles": nf, "wall_particles": nw,
-                       "form": "fp32c", "kahan": True, "parallelism": "replicas",
-                       "l2": f"inputs larger than L2 (working set ~{ws / 1e6:.0f} MB > 129 MB)"},
+            "config": describe(scn, workload),
+            "form": {"name": "fp32c", "kahan": bool(P32.kahan)},
             "forms": {
                 "fp32c": {"value": value, "ms_per_step": ms32 / args.steps,
                           "kernel_shares": shares(prof32), "launch_shape": tuning32},
@@ -461,6 +654,7 @@ def run_gpu(args, ranks) -> dict | None:
                     "d2h_bytes_per_step": hd_bytes, "steps": ke},
             "gpu_launches": launches,
             "clocks": clk,
+            "extra_workloads": extras,
         }
     return out
 
@@ -560,12 +754,33 @@ def run_faces(args, ranks) -> dict | None:
                 err[form] = {k: float(np.linalg.norm(a[k] - b[k]) /
                                       max(np.linalg.norm(b[k]), 1e-300))
                              for k in ("rho", "r", "v")}
+    cpu = None
+    if ranks.world_size == 1 and not args.no_cpu:
+        # The oracle on the same workload and physics (plain FP64, face walls,
+        # shifting): one untimed step, then as many steps as fill the budget.
+        import oracle
+        threads = oracle.default_threads()
+        P = physics.reference_params(scn["dim"], precision=_abi.TG_FP64)
+        P.post_integrate = _abi.TG_POST_SHIFTING
+        st = oracle.State(scn)
+        t0 = time.perf_counter()
+        oracle.step(P, st, 1, nthreads=threads)
+        one = max(time.perf_counter() - t0, 1e-6)
+        k = int(max(2, min(200, args.cpu_budget / one)))
+        t0 = time.perf_counter()
+        oracle.step(P, st, k, nthreads=threads)
+        sec = time.perf_counter() - t0
+        cpu = {"value": nf * k / sec, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"the workload itself ({nf} fluid), reference physics with face "
+                          f"walls and shifting, 1 untimed + {k} timed SSPRK3 steps "
+                          f"({sec:.1f} s), oracle built g++ -O3 -ffp-contract=off")}
     head = res[forms[0]]
     return {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
             "higher_is_better": True, "forms": res, "l2_error_vs_fp64": err,
             "faces": int(sum(fc["face_verts"].shape[0] for fc in scn["faces"] if fc)),
-            "config": {"workload": workload}, "gpu_launches": launches}
+            "config": describe(scn, workload), "cpu_baseline": cpu,
+            "gpu_launches": launches}
 
 
 def run_single_form(args, ranks) -> dict | None:
@@ -597,10 +812,20 @@ def run_single_form(args, ranks) -> dict | None:
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gpu", "reference"), default="gpu")
-    ap.add_argument("--config", default="c1")
+    ap.add_argument("--config", default="c4")
+    ap.add_argument("--err-steps", type=int, default=1000,
+                    help="steps of the FP32C-vs-FP64 error leg (0: skip)")
+    ap.add_argument("--err-config", default=None,
+                    help="workload of the error leg (default: c4q for c4/c4half, else --config)")
+    ap.add_argument("--extra", default="c1,c3,c5",
+                    help="further workloads timed in both forms (comma-separated)")
+    ap.add_argument("--extra-err-steps", type=int, default=500,
+                    help="steps after which c3's FP32C error is taken (0: skip)")
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="host seconds of the reference arm (warm-up + timed steps)")
     ap.add_argument("--fp64-steps", type=int, default=None,
                     help="FP64 timed steps (default: --steps)")
     ap.add_argument("--e2e-steps", type=int, default=50)
