@@ -339,9 +339,11 @@ def describe(scn: dict, workload: str) -> dict:
     nf = scenarios.n_fluid(scn)
     nw = int(sum(t["n_wall"] for t in scn["tanks"]))
     ws = scn["r"].shape[0] * (200 if scn["dim"] == 2 else 270)
+    l2 = (f"inputs larger than L2 (working set ~{ws / 1e6:.0f} MB > 129 MB)" if ws > 129e6 else
+          f"inputs smaller than L2 (working set ~{ws / 1e6:.0f} MB < 129 MB): L2-resident")
     return {"workload": workload, "fluid_particles": nf, "wall_particles": nw,
             "tanks": len(scn["tanks"]), "parallelism": "replicas (no exchange between GPUs)",
-            "l2": f"inputs larger than L2 (working set ~{ws / 1e6:.0f} MB > 129 MB)"}
+            "l2": l2}
 
 
 def run_reference(args, ranks) -> dict:
