@@ -379,6 +379,7 @@ def tune(P, args) -> None:
         P.cells_per_radius = args.cells_per_radius
     P.kahan = args.kahan
     P.staging = args.staging
+    P.resort = args.resort
 
 
 def gpu_leg(scn, params, warmup: int, steps: int, profile_steps: int, ranks,
@@ -840,6 +841,9 @@ def main() -> int:
                     help="pick the launch shape with tg_autotune before warm-up "
                          "(skipped when --cells-per-radius is given)")
     ap.add_argument("--staging", type=int, choices=(0, 1), default=0)
+    ap.add_argument("--resort", type=int, choices=(0, 1), default=1,
+                    help="re-sort only the particles whose cell changed (1) or a full "
+                         "radix sort every stage (0)")
     ap.add_argument("--only", choices=("fp32c", "fp64", "fp32c_face32"), default=None,
                     help="time one form only (profiling runs); prints its value; "
                          "fp32c_face32 = fp32c with FP32 face integrals")

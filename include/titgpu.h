@@ -155,6 +155,10 @@ typedef struct tg_params {
                                FP32 runs the face passes ~1.7x faster in 3D
                                at a larger drift from the FP64 form; must be
                                0 with TG_FP64. */
+  int32_t resort;           /* 1 (default): between stages, re-sort only the
+                               particles whose cell changed and merge them
+                               into the previous order; 0: a full radix sort
+                               every stage.  Same order either way. */
   double xi;      /* Tait polytropic index */
   double g;       /* gravity, acting along -axis 1 */
   double mu;      /* Morris dynamic viscosity */

@@ -31,9 +31,10 @@ def test_library_exports_every_declared_symbol(gpu_lib):
 
 
 def test_struct_layouts_match_header():
-    # 13 int32 fields, 4 bytes of padding, 8 doubles.
-    assert ctypes.sizeof(_abi.TgParams) == 13 * 4 + 4 + 8 * 8
+    # 14 int32 fields, then 8 doubles.
+    assert ctypes.sizeof(_abi.TgParams) == 14 * 4 + 8 * 8
     assert _abi.TgParams.xi.offset == 56
+    assert _abi.TgParams.resort.offset == 52
     assert ctypes.sizeof(_abi.TgTank) == 2 * 8 + 4 * 8
     assert ctypes.sizeof(_abi.TgProfile) == 5 * 8 + 3 * 8
 

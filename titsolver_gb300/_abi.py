@@ -61,6 +61,7 @@ class TgParams(ctypes.Structure):
         ("staging", ctypes.c_int32),
         ("eos", ctypes.c_int32),
         ("face_fp32", ctypes.c_int32),
+        ("resort", ctypes.c_int32),
         ("xi", ctypes.c_double),
         ("g", ctypes.c_double),
         ("mu", ctypes.c_double),

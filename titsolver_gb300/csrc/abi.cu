@@ -52,6 +52,8 @@ void Context::release_all() {
   keys_a = keys_b = vals_a = vals_b = nullptr;
   sort_scratch = nullptr;
   cell_start = wall_list = wall_active = nullptr;
+  near_scratch = nullptr;
+  order_valid = false;
   cell_scratch = nullptr;
   d_stage = d_stage2 = d_stage3 = d_stage4 = nullptr;
   d_sd_rho = nullptr;
@@ -207,6 +209,10 @@ bool valid_params(const tg_params* P, std::string* why) {
     *why = "unknown equation of state";
     return false;
   }
+  if (P->resort != 0 && P->resort != 1) {
+    *why = "resort must be 0 or 1";
+    return false;
+  }
   if (P->face_fp32 != 0 && !(P->face_fp32 == 1 && P->precision == TG_FP32C)) {
     *why = "face_fp32 must be 0, or 1 with the FP32C form";
     return false;
@@ -271,6 +277,7 @@ void tg_params_default(tg_params* p) {
   p->kahan = 1;
   p->device = -1;
   p->staging = 0;
+  p->resort = 1;
   p->xi = 7.0;
   p->g = 9.81;
   p->mu = 0.001;
@@ -559,6 +566,7 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, A(C.vals_a, sizeof(uint32_t) * nn));
   TG_CUDA(&C, A(C.vals_b, sizeof(uint32_t) * nn));
   TG_CUDA(&C, C.alloc(&C.sort_scratch, tg::radix_sort_scratch_bytes(nn)));
+  TG_CUDA(&C, C.alloc(&C.near_scratch, tg::near_sort_scratch_bytes(nn)));
   TG_CUDA(&C, A(C.cell_start, sizeof(uint32_t) * (2 * total_cells + 1)));
   TG_CUDA(&C, C.alloc(&C.cell_scratch, tg::cell_table_scratch_bytes(C.total_keys)));
   TG_CUDA(&C, A(C.wall_list, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
@@ -679,7 +687,17 @@ int tg_step(tg_context* ctx, int32_t n_steps, double* dt_out) {
   if (n_steps > 0 && C.n > 0) {
     TG_CUDA(&C, C.engine->ensure_keys(C));
     if (C.use_graph && !C.profile) {
+      // The re-sort is taken only in the home order of an earlier sort, a
+      // host-side choice baked into the graph: run a step directly when the
+      // order is not there yet, and capture again when it changed.
+      if (C.graph_exec != nullptr && C.graph_order != C.order_valid) C.invalidate_graph();
+      if (!C.order_valid && C.P.resort != 0 && n_steps > 1) {
+        TG_CUDA(&C, C.engine->enqueue_step(C));
+        --n_steps;
+        C.prof.steps += 1;
+      }
       if (C.graph_exec == nullptr) {
+        C.graph_order = C.order_valid;
         cudaGraph_t graph = nullptr;
         const int64_t before = C.launches;
         TG_CUDA(&C, cudaStreamBeginCapture(C.stream,

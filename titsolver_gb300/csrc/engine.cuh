@@ -146,6 +146,7 @@ struct Context {
   uint32_t* cell_start = nullptr;
   void* cell_scratch = nullptr;
   uint32_t* wall_list = nullptr;
+  void* near_scratch = nullptr;  // the re-sort's buffers (near_sort)
   uint32_t* wall_active = nullptr;  // walls near fluid this stage (k_wall_select)
   double* d_stage = nullptr;  // n * dim doubles: upload / download staging
   double* d_stage2 = nullptr;
@@ -172,6 +173,8 @@ struct Context {
 
   bool walls_fresh = false;
   bool keys_valid = false;  // home keys match the home positions
+  bool order_valid = false; // home state in the order of its last sort (pkey)
+  bool graph_order = false; // order_valid when the step graph was captured
 
   // Profiling.
   bool profile = false;

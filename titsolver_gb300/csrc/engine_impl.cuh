@@ -63,6 +63,7 @@ class Engine final : public EngineBase {
     }
     // The home keys live in the sort's first key buffer.
     X_.key = C.keys_a;
+    A(X_.pkey, n);
     if constexpr (F == TG_FP32C) {
       for (int k = 0; k < D; ++k) A(X_.off[k], n);
     }
@@ -99,6 +100,7 @@ class Engine final : public EngineBase {
         X_, r, v, rho, dv, C.d_tank_of, C.d_tanks, C.d_wall_from, C.n);
     C.launches += 1;
     C.keys_valid = false;
+    C.order_valid = false;  // the home order is the upload order
     return ensure_keys(C);
   }
 
@@ -194,6 +196,7 @@ class Engine final : public EngineBase {
     C.launches += 1;
     C.group_end(tok);
     C.keys_valid = true;
+    C.order_valid = true;
     return cudaGetLastError();
   }
 
@@ -339,17 +342,29 @@ class Engine final : public EngineBase {
   }
 
   // Sort the home keys (valid on entry) into cell order and build the cell
-  // table.  The sort uses the home key buffer as scratch.
+  // table.  When the home state is in the order of an earlier sort (every
+  // pass over all particles writes it so, with that sort's keys in pkey),
+  // the re-sort moves only the particles whose key changed; otherwise the
+  // full radix sort runs, with the home key buffer as scratch.  Both give
+  // the same order.
   cudaError_t enqueue_sort(Context& C) {
     cudaError_t e = ensure_keys(C);
     if (e != cudaSuccess) return e;
     const int tok = C.group_begin(kGroupSort);
-    bool in_b = false;
-    e = radix_sort(C.keys_a, C.vals_a, C.keys_b, C.vals_b, C.n, C.key_bits,
-                   true, C.sort_scratch, &in_b, C.stream, &C.launches);
-    if (e != cudaSuccess) return e;
-    C.sorted_keys = in_b ? C.keys_b : C.keys_a;
-    C.perm = in_b ? C.vals_b : C.vals_a;
+    if (C.order_valid && C.P.resort != 0) {
+      e = near_sort(C.keys_a, X_.pkey, C.n, C.key_bits, C.keys_b, C.vals_b,
+                    C.near_scratch, C.stream, &C.launches);
+      if (e != cudaSuccess) return e;
+      C.sorted_keys = C.keys_b;
+      C.perm = C.vals_b;
+    } else {
+      bool in_b = false;
+      e = radix_sort(C.keys_a, C.vals_a, C.keys_b, C.vals_b, C.n, C.key_bits,
+                     true, C.sort_scratch, &in_b, C.stream, &C.launches);
+      if (e != cudaSuccess) return e;
+      C.sorted_keys = in_b ? C.keys_b : C.keys_a;
+      C.perm = in_b ? C.vals_b : C.vals_a;
+    }
     e = build_cell_table(C.sorted_keys, C.n, C.total_keys, C.cell_start,
                          C.cell_scratch, C.stream, &C.launches);
     C.group_end(tok);
@@ -394,6 +409,7 @@ class Engine final : public EngineBase {
     C.launches += 5;
     C.group_end(tok);
     C.keys_valid = true;
+    C.order_valid = true;
     return cudaGetLastError();
   }
 
@@ -492,8 +508,9 @@ class Engine final : public EngineBase {
     }
     C.launches += 1;
     C.group_end(tok);
-    // k_forces and k_walls wrote the keys of the new positions.
+    // k_forces wrote the keys of the new positions, in this sort's order.
     C.keys_valid = true;
+    C.order_valid = true;
     return cudaGetLastError();
   }
 

@@ -110,6 +110,8 @@ struct StateBuf {
   R* drho;
   uint32_t* id;   // upload index | kWallBit for walls
   uint32_t* key;  // global cell key (home state only)
+  uint32_t* pkey;  // key of each slot at the sort that set the home order
+                   // (home state only; the re-sort's previous keys)
   float* off[3];  // FP32C: offset from the cell corner (home state only)
 };
 
@@ -624,6 +626,7 @@ __device__ __forceinline__ void commit_wall(const StageArgs<D, F>& A, int64_t e,
   A.X.drho[e] = R(0);
   A.X.id[e] = id;
   A.X.key[e] = A.skey[e];
+  A.X.pkey[e] = A.skey[e];
 }
 
 // ---------------------------------------------------------------------------
@@ -1216,6 +1219,7 @@ __device__ __forceinline__ void forces_epilogue(
     }
     if (outside) atomicOr(A.err, static_cast<uint32_t>(TG_DEV_OUTSIDE_GRID));
   }
+  A.X.pkey[i] = A.skey[i];  // read before the key write: the buffers may alias
   A.X.key[i] = key_of(flat_cell<D>(T, cn), false);
   bool finite = true;
 #pragma unroll
@@ -2243,6 +2247,7 @@ __global__ void __launch_bounds__(256) k_commit(StageArgs<D, F> A) {
   A.X.drho[j] = A.Y.drho[j];
   A.X.id[j] = id;
   A.X.key[j] = A.skey[j];
+  A.X.pkey[j] = A.skey[j];
   if constexpr (F == TG_FP32C) {
     float o[3] = {0.f, 0.f, 0.f};
     load_pos(A.posrec, static_cast<uint32_t>(j), o);

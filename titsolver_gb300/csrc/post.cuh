@@ -497,6 +497,7 @@ __global__ void __launch_bounds__(128) k_post_shift(PostArgs<D, F> A) {
   }
   X.drho[i] = Y.drho[i];
   X.id[i] = id;
+  X.pkey[i] = A.S.skey[i];  // read before the key write: the buffers may alias
   X.key[i] = key_of(flat_cell<D>(T, cn), false);
   if (!(finite && finite_bits(rho))) {
     atomicOr(A.S.err, static_cast<uint32_t>(TG_DEV_NONFINITE_STATE));

@@ -26,8 +26,10 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_upsweep(const uint32_t* __restrict__ keys, int64_t n, int shift,
-                    uint32_t* __restrict__ hist, int ntiles) {
+                    uint32_t* __restrict__ hist, int ntiles,
+                    const uint32_t* __restrict__ n_dev) {
   __shared__ uint32_t s_hist[kRadixBins];
+  if (n_dev != nullptr) n = *n_dev;  // count known on the device only
   for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) s_hist[i] = 0;
   __syncthreads();
   const int64_t base = static_cast<int64_t>(blockIdx.x) * kSortTile;
@@ -100,8 +102,12 @@ __global__ void __launch_bounds__(kSortThreads)
                       uint32_t* __restrict__ keys_out,
                       uint32_t* __restrict__ vals_out, int64_t n, int shift,
                       const uint32_t* __restrict__ row_scan,
-                      const uint32_t* __restrict__ row_total, int ntiles) {
+                      const uint32_t* __restrict__ row_total, int ntiles,
+                      const uint32_t* __restrict__ n_dev) {
   __shared__ uint32_t s_base[kRadixBins];
+  if (n_dev != nullptr) n = *n_dev;
+  // Tiles past a count known on the device only have nothing to move.
+  if (static_cast<int64_t>(blockIdx.x) * kSortTile >= n) return;
   __shared__ uint32_t s_cnt[kWarps][kRadixBins];
   __shared__ uint32_t s_warp[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -258,7 +264,8 @@ size_t radix_sort_scratch_bytes(int64_t n) {
 cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
                        uint32_t* vals_b, int64_t n, int key_bits,
                        bool identity_vals, void* scratch, bool* result_in_b,
-                       cudaStream_t stream, int64_t* launches) {
+                       cudaStream_t stream, int64_t* launches,
+                       const uint32_t* n_dev) {
   *result_in_b = false;
   if (n <= 0) return cudaSuccess;
   const int ntiles = static_cast<int>((n + kSortTile - 1) / kSortTile);
@@ -272,11 +279,11 @@ cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
   for (int p = 0; p < passes; ++p) {
     const int shift = p * kRadixBits;
     k_radix_upsweep<<<ntiles, kSortThreads, 0, stream>>>(ki, n, shift, hist,
-                                                         ntiles);
+                                                         ntiles, n_dev);
     k_radix_rowscan<<<kRadixBins, 256, 0, stream>>>(hist, ntiles, row_total);
     k_radix_downsweep<<<ntiles, kSortThreads, 0, stream>>>(
         ki, (p == 0 && identity_vals) ? nullptr : vi, ko, vo, n, shift, hist,
-        row_total, ntiles);
+        row_total, ntiles, n_dev);
     *launches += 3;
     uint32_t* tk = ki;
     ki = ko;

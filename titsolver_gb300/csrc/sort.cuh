@@ -25,11 +25,25 @@ size_t radix_sort_scratch_bytes(int64_t n);
 // the input (identity_vals: the payload is 0..n-1 and vals_a is not read);
 // the result lands in (keys_a, vals_a) or (keys_b, vals_b), as returned
 // through *result_in_b.  Each pass issues three kernels; *launches counts
-// them.
+// them.  With n_dev, the count is *n_dev (read on the device, at most n):
+// the launches are sized for n and the tiles past the count do nothing.
 cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
                        uint32_t* vals_b, int64_t n, int key_bits,
                        bool identity_vals, void* scratch, bool* result_in_b,
-                       cudaStream_t stream, int64_t* launches);
+                       cudaStream_t stream, int64_t* launches,
+                       const uint32_t* n_dev = nullptr);
+
+// Re-sort of keys whose previous sorted order is known: keys[i] is the new
+// key of the particle at slot i of the previous order, prev[i] the key that
+// slot held when that order was sorted.  The particles whose key changed
+// (movers) are compacted and radix-sorted alone; the others keep their
+// relative order, and both runs are merged by rank.  The result equals the
+// stable sort of keys (ties in slot order), as radix_sort gives it: out_keys
+// the sorted keys, out_perm the slot of each.  About a dozen small kernels.
+size_t near_sort_scratch_bytes(int64_t n);
+cudaError_t near_sort(const uint32_t* keys, const uint32_t* prev, int64_t n,
+                      int key_bits, uint32_t* out_keys, uint32_t* out_perm,
+                      void* scratch, cudaStream_t stream, int64_t* launches);
 
 // Scratch needed by build_cell_table (bytes).
 size_t cell_table_scratch_bytes(uint32_t total_cells);
