@@ -29,7 +29,10 @@ __global__ void __launch_bounds__(kSortThreads)
                     uint32_t* __restrict__ hist, int ntiles,
                     const uint32_t* __restrict__ n_dev) {
   __shared__ uint32_t s_hist[kRadixBins];
-  if (n_dev != nullptr) n = *n_dev;  // count known on the device only
+  if (n_dev != nullptr) {
+    n = *n_dev;  // count known on the device only
+    if (static_cast<int64_t>(blockIdx.x) * kSortTile >= n) return;
+  }
   for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) s_hist[i] = 0;
   __syncthreads();
   const int64_t base = static_cast<int64_t>(blockIdx.x) * kSortTile;
@@ -81,16 +84,22 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v,
 
 __global__ void __launch_bounds__(256)
     k_radix_rowscan(uint32_t* __restrict__ hist, int ntiles,
-                    uint32_t* __restrict__ row_total) {
+                    uint32_t* __restrict__ row_total,
+                    const uint32_t* __restrict__ n_dev) {
   __shared__ uint32_t s_warp[32];
   uint32_t* row = hist + static_cast<int64_t>(blockIdx.x) * ntiles;
+  // With a count known on the device only, the tiles past it hold no keys
+  // (and their histograms were not written).
+  const int used = n_dev != nullptr
+                       ? static_cast<int>((static_cast<int64_t>(*n_dev) + kSortTile - 1) / kSortTile)
+                       : ntiles;
   uint32_t carry = 0;
-  for (int base = 0; base < ntiles; base += blockDim.x) {
+  for (int base = 0; base < used; base += blockDim.x) {
     const int i = base + threadIdx.x;
-    const uint32_t v = i < ntiles ? row[i] : 0u;
+    const uint32_t v = i < used ? row[i] : 0u;
     uint32_t tot;
     const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
-    if (i < ntiles) row[i] = carry + ex;
+    if (i < used) row[i] = carry + ex;
     carry += tot;
   }
   if (threadIdx.x == 0) row_total[blockIdx.x] = carry;
@@ -280,7 +289,7 @@ cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
     const int shift = p * kRadixBits;
     k_radix_upsweep<<<ntiles, kSortThreads, 0, stream>>>(ki, n, shift, hist,
                                                          ntiles, n_dev);
-    k_radix_rowscan<<<kRadixBins, 256, 0, stream>>>(hist, ntiles, row_total);
+    k_radix_rowscan<<<kRadixBins, 256, 0, stream>>>(hist, ntiles, row_total, n_dev);
     k_radix_downsweep<<<ntiles, kSortThreads, 0, stream>>>(
         ki, (p == 0 && identity_vals) ? nullptr : vi, ko, vo, n, shift, hist,
         row_total, ntiles, n_dev);
