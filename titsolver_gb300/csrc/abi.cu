@@ -568,7 +568,7 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
   TG_CUDA(&C, C.alloc(&C.sort_scratch, tg::radix_sort_scratch_bytes(nn)));
   TG_CUDA(&C, C.alloc(&C.near_scratch, tg::near_sort_scratch_bytes(nn)));
   TG_CUDA(&C, A(C.cell_start, sizeof(uint32_t) * (2 * total_cells + 1)));
-  TG_CUDA(&C, C.alloc(&C.cell_scratch, tg::cell_table_scratch_bytes(C.total_keys)));
+  TG_CUDA(&C, C.alloc(&C.cell_scratch, tg::cell_fill_scratch_bytes(C.total_keys)));
   TG_CUDA(&C, A(C.wall_list, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
   TG_CUDA(&C, A(C.wall_active, sizeof(uint32_t) * (nw > 0 ? nw : 1)));
   TG_CUDA(&C, A(C.d_stage, sizeof(double) * nn * dim));

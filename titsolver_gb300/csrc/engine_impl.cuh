@@ -365,8 +365,8 @@ class Engine final : public EngineBase {
       C.sorted_keys = in_b ? C.keys_b : C.keys_a;
       C.perm = in_b ? C.vals_b : C.vals_a;
     }
-    e = build_cell_table(C.sorted_keys, C.n, C.total_keys, C.cell_start,
-                         C.cell_scratch, C.stream, &C.launches);
+    e = build_cell_table_fill(C.sorted_keys, C.n, C.total_keys, C.cell_start,
+                              C.cell_scratch, C.sm_count, C.stream, &C.launches);
     C.group_end(tok);
     return e;
   }

@@ -262,7 +262,96 @@ __global__ void __launch_bounds__(kTableCells)
   }
 }
 
+// cell_start from the sorted keys in one pass: sorted index j starts every
+// cell c with key[j-1] < c <= key[j] (j = n: the cells past the last key and
+// the sentinel).  Who writes a run of cells depends on its length: up to
+// kThreadRun cells the thread of j (a cell boundary inside the fluid, where a
+// fluid key is followed by its cell's empty wall key), up to kBlockRun the
+// whole warp, one run after another with consecutive lanes on consecutive
+// cells, and longer runs (empty stretches of the grid, up to all the cells
+// above the fluid) go to a list in chunks of at most kFillChunk cells, which
+// k_fill_runs writes with one block per chunk.
+constexpr int kThreadRun = 4;
+constexpr int kBlockRun = 1024;
+constexpr int kFillChunk = 16384;
+
+struct FillRun {
+  uint32_t lo, hi, value;  // cells [lo, hi] start at sorted index value
+};
+
+__global__ void __launch_bounds__(256)
+    k_fill_starts(const uint32_t* __restrict__ keys, int64_t n, uint32_t total_keys,
+                  uint32_t* __restrict__ cell_start, FillRun* __restrict__ runs,
+                  uint32_t* __restrict__ run_count) {
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  // Every lane reaches the vote below, the ones past n with an empty run.
+  int64_t lo = 1, hi = 0;
+  if (j <= n) {
+    lo = j == 0 ? 0 : static_cast<int64_t>(__ldg(keys + j - 1)) + 1;
+    hi = j == n ? static_cast<int64_t>(total_keys) : __ldg(keys + j);
+  }
+  const int64_t len = hi - lo + 1;
+  if (len > 0 && len <= kThreadRun) {
+    for (int64_t c = lo; c <= hi; ++c) cell_start[c] = static_cast<uint32_t>(j);
+  } else if (len >= kBlockRun) {
+    const uint32_t chunks = static_cast<uint32_t>((len + kFillChunk - 1) / kFillChunk);
+    const uint32_t r = atomicAdd(run_count, chunks);
+    for (uint32_t q = 0; q < chunks; ++q) {
+      const int64_t a = lo + static_cast<int64_t>(q) * kFillChunk;
+      const int64_t b = min(hi, a + kFillChunk - 1);
+      runs[r + q] = FillRun{static_cast<uint32_t>(a), static_cast<uint32_t>(b),
+                            static_cast<uint32_t>(j)};
+    }
+  }
+  unsigned mid = __ballot_sync(0xffffffffu, len > kThreadRun && len < kBlockRun);
+  while (mid != 0u) {
+    const int src = __ffs(mid) - 1;
+    mid &= mid - 1u;
+    const uint32_t lo_s = __shfl_sync(0xffffffffu, static_cast<uint32_t>(lo), src);
+    const uint32_t len_s = __shfl_sync(0xffffffffu, static_cast<uint32_t>(len), src);
+    const uint32_t val_s = __shfl_sync(0xffffffffu, static_cast<uint32_t>(j), src);
+    for (uint32_t k = lane; k < len_s; k += 32u) cell_start[lo_s + k] = val_s;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_fill_runs(uint32_t* __restrict__ cell_start, const FillRun* __restrict__ runs,
+                const uint32_t* __restrict__ run_count) {
+  const uint32_t nr = *run_count;
+  for (uint32_t r = blockIdx.x; r < nr; r += gridDim.x) {
+    const FillRun f = runs[r];
+    for (uint32_t c = f.lo + threadIdx.x; c <= f.hi && c >= f.lo; c += blockDim.x) {
+      cell_start[c] = f.value;
+    }
+  }
+}
+
 }  // namespace
+
+size_t cell_fill_scratch_bytes(uint32_t total_keys) {
+  // Runs of at least kBlockRun cells are disjoint, so at most
+  // (total_keys + 1) / kBlockRun of them, each split into at most
+  // len / kFillChunk + 1 chunks: at most 2 (total_keys + 1) / kBlockRun
+  // chunks, plus the counter.
+  return 256 + sizeof(FillRun) * (2 * (static_cast<size_t>(total_keys) + 1) / kBlockRun + 2);
+}
+
+cudaError_t build_cell_table_fill(const uint32_t* sorted_keys, int64_t n,
+                                  uint32_t total_keys, uint32_t* cell_start,
+                                  void* scratch, int sm_count, cudaStream_t stream,
+                                  int64_t* launches) {
+  auto* count = static_cast<uint32_t*>(scratch);
+  auto* runs = reinterpret_cast<FillRun*>(static_cast<unsigned char*>(scratch) + 256);
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  k_fill_starts<<<static_cast<unsigned>((n + 1 + 255) / 256), 256, 0, stream>>>(
+      sorted_keys, n, total_keys, cell_start, runs, count);
+  k_fill_runs<<<static_cast<unsigned>(8 * (sm_count > 0 ? sm_count : 152)), 256, 0, stream>>>(
+      cell_start, runs, count);
+  *launches += 2;
+  return cudaGetLastError();
+}
 
 size_t radix_sort_scratch_bytes(int64_t n) {
   const int64_t ntiles = (n + kSortTile - 1) / kSortTile;

@@ -55,4 +55,15 @@ cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
                              void* scratch, cudaStream_t stream,
                              int64_t* launches);
 
+// The same table in one pass over the sorted keys: each sorted index writes
+// the starts of the cells between its key and the previous one, and long
+// empty stretches are filled by whole blocks from a list.  Writes each entry
+// once; the scratch holds that list (cell_fill_scratch_bytes).  A memset and
+// two kernels.
+size_t cell_fill_scratch_bytes(uint32_t total_keys);
+cudaError_t build_cell_table_fill(const uint32_t* sorted_keys, int64_t n,
+                                  uint32_t total_keys, uint32_t* cell_start,
+                                  void* scratch, int sm_count, cudaStream_t stream,
+                                  int64_t* launches);
+
 }  // namespace tg
