@@ -592,6 +592,7 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
                           std::numeric_limits<double>::infinity());
   std::vector<double> zeros(static_cast<size_t>(n_tanks), 0.0);
   cudaStream_t s = C.stream;
+  TG_CUDA(&C, tg::near_sort_reset(C.near_scratch, nn, s));
   TG_CUDA(&C, cudaMemcpyAsync(C.d_tanks, td.data(), sizeof(tg::TankDev) * n_tanks,
                               cudaMemcpyHostToDevice, s));
   TG_CUDA(&C, cudaMemcpyAsync(C.d_id_base, id_base.data(), sizeof(uint32_t) * n_tanks,

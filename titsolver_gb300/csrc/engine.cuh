@@ -61,8 +61,6 @@ struct EngineBase {
   virtual cudaError_t enqueue_sumdens(Context& C, int pos_precision,
                                       double* rho, int32_t* counts,
                                       uint64_t* hashes) = 0;
-  // Kernel launches of one step.
-  virtual int64_t launches_per_step(Context& C) = 0;
   // Whether the force pass has a variant with `team` lanes per target.
   virtual bool supports_team(int team) const = 0;
 };

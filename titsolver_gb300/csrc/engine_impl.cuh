@@ -272,20 +272,6 @@ class Engine final : public EngineBase {
     return team == 1 || (team_kernel(K) && (team == 2 || team == 4));
   }
 
-  int64_t launches_per_step(Context& C) override {
-    const int passes = C.key_bits <= 0 ? 1 : (C.key_bits + kRadixBits - 1) / kRadixBits;
-    const int stages = force_passes(C.P.integrator);
-    // The wall pass lists the walls near fluid first when it has a fluid box.
-    const int walls = C.n_wall > 0 ? (4 * C.n_wall >= C.n_fluid ? 2 : 1) : 0;
-    const int per_stage = 3 * passes + 2 + 2 + walls;
-    const int gam = C.faces.on ? 3 : 0;  // k_gamma_init, k_gamma_faces, k_face_terms
-    const int post = C.P.post_integrate == TG_POST_SHIFTING
-                         ? 3 * passes + 2 + 1 + (C.n_wall > 0 ? walls + (gam > 0 ? 2 : 0) : 0) + 5 +
-                               (gam > 0 ? 1 : 0)
-                         : 0;
-    return static_cast<int64_t>(stages) * (per_stage + gam) + post + 1;
-  }
-
  private:
   StageArgs<D, F> args(Context& C, int stage) {
     StageArgs<D, F> a{};

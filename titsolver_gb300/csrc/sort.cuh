@@ -39,8 +39,12 @@ cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
 // (movers) are compacted and radix-sorted alone; the others keep their
 // relative order, and both runs are merged by rank.  The result equals the
 // stable sort of keys (ties in slot order), as radix_sort gives it: out_keys
-// the sorted keys, out_perm the slot of each.  About a dozen small kernels.
+// the sorted keys, out_perm the slot of each.  Four kernels and the movers'
+// radix passes.  The scratch holds a completion counter that must be zero
+// before the first near_sort (near_sort_reset; every near_sort leaves it
+// zero).
 size_t near_sort_scratch_bytes(int64_t n);
+cudaError_t near_sort_reset(void* scratch, int64_t n, cudaStream_t stream);
 cudaError_t near_sort(const uint32_t* keys, const uint32_t* prev, int64_t n,
                       int key_bits, uint32_t* out_keys, uint32_t* out_perm,
                       void* scratch, cudaStream_t stream, int64_t* launches);

@@ -12,11 +12,12 @@
 //              (key_m, m))
 // which is exactly where radix_sort of the whole array puts it.
 //
-// Kernels: mover flags per 32 slots; an exclusive scan of the flag counts
-// (three kernels); the compaction; the movers' radix sort (their count is
-// known on the device only); the stayers' scatter, each block searching the
-// sorted movers once for its slot range and then in shared memory; the
-// movers' scatter, each searching prev for its key's slot range.
+// Kernels: mover flags per 32 slots with their exclusive scan (one kernel:
+// each block scans its words and the last block to finish scans the block
+// totals); the compaction; the movers' radix sort (their count is known on
+// the device only); the stayers' scatter, each block searching the sorted
+// movers once for its slot range and then in shared memory; the movers'
+// scatter, each searching prev for its key's slot range.
 #include "sort.cuh"
 
 namespace tg {
@@ -30,20 +31,6 @@ __device__ __forceinline__ uint32_t lanemask_lt_ns() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
-}
-
-// Movers of each 32-slot word: mask and count.
-__global__ void __launch_bounds__(kNsBlock)
-    k_ns_flags(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ prev,
-               int64_t n, uint32_t* __restrict__ mask, uint32_t* __restrict__ count) {
-  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool mover = i < n && keys[i] != prev[i];
-  const uint32_t m = __ballot_sync(0xffffffffu, mover);
-  const int64_t w = i >> 5;
-  if ((threadIdx.x & 31u) == 0 && (w << 5) < n) {
-    mask[w] = m;
-    count[w] = static_cast<uint32_t>(__popc(m));
-  }
 }
 
 // Block-wide exclusive scan of one value per thread (blockDim.x a multiple
@@ -76,65 +63,91 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_warp
   return before + x - v;
 }
 
-// Exclusive scan of the word counts: per block, then the block totals (one
-// block), then the block offsets added.
+// Movers of each 32-slot word (mask) and the exclusive scan of their counts:
+// block b takes words [b kScanBlock, (b + 1) kScanBlock), each warp 32 words
+// read slot-coalesced (one ballot per word), and stores the scan within the
+// block (prefix) and its total (bsum).  The block that finishes last (a
+// counter, no waiting) turns bsum into the exclusive scan of the block
+// totals, writes the movers' count to *total and resets the counter.  The
+// movers before word w are prefix[w] + bsum[w / kScanBlock].
 __global__ void __launch_bounds__(kScanBlock)
-    k_ns_scan_blocks(const uint32_t* __restrict__ count, int64_t nwords,
-                     uint32_t* __restrict__ prefix, uint32_t* __restrict__ block_sum) {
+    k_ns_flags_scan(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ prev,
+                    int64_t n, int64_t nwords, int64_t nblocks, uint32_t* __restrict__ mask,
+                    uint32_t* __restrict__ prefix, uint32_t* bsum, uint32_t* __restrict__ total,
+                    uint32_t* done) {
   __shared__ uint32_t s_warp[32];
-  const int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const uint32_t v = w < nwords ? count[w] : 0u;
+  __shared__ uint32_t s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t w0 = static_cast<int64_t>(blockIdx.x) * kScanBlock + warp * 32;
+  uint32_t my_mask = 0;
+#pragma unroll 4
+  for (int q = 0; q < 32; ++q) {
+    const int64_t i = (w0 + q) * 32 + lane;
+    const bool mover = i < n && __ldg(keys + i) != __ldg(prev + i);
+    const uint32_t m = __ballot_sync(0xffffffffu, mover);
+    if (lane == q) my_mask = m;
+  }
+  const int64_t w = w0 + lane;
   uint32_t tot;
-  const uint32_t ex = block_scan_excl(v, s_warp, &tot);
-  if (w < nwords) prefix[w] = ex;
-  if (threadIdx.x == 0) block_sum[blockIdx.x] = tot;
-}
-
-__global__ void __launch_bounds__(kScanBlock)
-    k_ns_scan_tops(uint32_t* __restrict__ block_sum, int64_t nblocks,
-                   uint32_t* __restrict__ total) {
-  __shared__ uint32_t s_warp[32];
+  const uint32_t ex = block_scan_excl(static_cast<uint32_t>(__popc(my_mask)), s_warp, &tot);
+  if (w < nwords) {
+    mask[w] = my_mask;
+    prefix[w] = ex;
+  }
+  if (threadIdx.x == 0) {
+    bsum[blockIdx.x] = tot;
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1 ? 1u : 0u;
+  }
+  __syncthreads();
+  if (s_last == 0u) return;
+  __threadfence();
   uint32_t carry = 0;
   for (int64_t b0 = 0; b0 < nblocks; b0 += blockDim.x) {
     const int64_t b = b0 + threadIdx.x;
-    const uint32_t v = b < nblocks ? block_sum[b] : 0u;
-    uint32_t tot;
-    const uint32_t ex = block_scan_excl(v, s_warp, &tot);
-    if (b < nblocks) block_sum[b] = carry + ex;
-    carry += tot;
+    const uint32_t v = b < nblocks ? __ldcg(bsum + b) : 0u;
+    uint32_t t;
+    const uint32_t e = block_scan_excl(v, s_warp, &t);
+    if (b < nblocks) bsum[b] = carry + e;
+    carry += t;
   }
-  if (threadIdx.x == 0) *total = carry;
+  if (threadIdx.x == 0) {
+    *total = carry;
+    *done = 0u;
+  }
 }
 
-__global__ void __launch_bounds__(kScanBlock)
-    k_ns_scan_add(uint32_t* __restrict__ prefix, int64_t nwords,
-                  const uint32_t* __restrict__ block_sum) {
-  const int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (w < nwords) prefix[w] += block_sum[blockIdx.x];
+// Movers before word w.
+__device__ __forceinline__ uint32_t word_prefix(const uint32_t* __restrict__ prefix,
+                                                const uint32_t* __restrict__ bsum, int64_t w) {
+  return __ldg(prefix + w) + __ldg(bsum + (w / kScanBlock));
 }
 
 // Movers before slot x (x in [0, n]).
 __device__ __forceinline__ uint32_t movers_before(const uint32_t* __restrict__ mask,
                                                   const uint32_t* __restrict__ prefix,
+                                                  const uint32_t* __restrict__ bsum,
                                                   int64_t nwords, const uint32_t* total,
                                                   int64_t x) {
   const int64_t w = x >> 5;
   if (w >= nwords) return *total;
   const uint32_t below = (1u << (x & 31)) - 1u;
-  return __ldg(prefix + w) + static_cast<uint32_t>(__popc(__ldg(mask + w) & below));
+  return word_prefix(prefix, bsum, w) + static_cast<uint32_t>(__popc(__ldg(mask + w) & below));
 }
 
 // Movers in slot order: their keys and slots.
 __global__ void __launch_bounds__(kNsBlock)
     k_ns_compact(const uint32_t* __restrict__ keys, int64_t n,
                  const uint32_t* __restrict__ mask, const uint32_t* __restrict__ prefix,
-                 uint32_t* __restrict__ mkey, uint32_t* __restrict__ mslot) {
+                 const uint32_t* __restrict__ bsum, uint32_t* __restrict__ mkey,
+                 uint32_t* __restrict__ mslot) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t w = i >> 5;
   const uint32_t m = __ldg(mask + w);
   if (!((m >> (i & 31)) & 1u)) return;
-  const uint32_t s = __ldg(prefix + w) + static_cast<uint32_t>(__popc(m & lanemask_lt_ns()));
+  const uint32_t s =
+      word_prefix(prefix, bsum, w) + static_cast<uint32_t>(__popc(m & lanemask_lt_ns()));
   mkey[s] = keys[i];
   mslot[s] = static_cast<uint32_t>(i);
 }
@@ -167,7 +180,7 @@ __device__ __forceinline__ uint32_t movers_less(const uint32_t* __restrict__ mke
 __global__ void __launch_bounds__(kNsBlock)
     k_ns_stayers(const uint32_t* __restrict__ prev, int64_t n,
                  const uint32_t* __restrict__ mask, const uint32_t* __restrict__ prefix,
-                 int64_t nwords, const uint32_t* __restrict__ total,
+                 const uint32_t* __restrict__ bsum, const uint32_t* __restrict__ total,
                  const uint32_t* __restrict__ mkey, const uint32_t* __restrict__ mslot,
                  uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_perm) {
   __shared__ uint32_t s_key[kMoverWindow], s_slot[kMoverWindow];
@@ -213,11 +226,10 @@ __global__ void __launch_bounds__(kNsBlock)
     before = movers_less(mkey, mslot, lo, hi, k, s);
   }
   const uint32_t stayers_before =
-      s - (__ldg(prefix + w) + static_cast<uint32_t>(__popc(m & lanemask_lt_ns())));
+      s - (word_prefix(prefix, bsum, w) + static_cast<uint32_t>(__popc(m & lanemask_lt_ns())));
   const uint32_t pos = stayers_before + before;
   out_keys[pos] = k;
   out_perm[pos] = s;
-  (void)nwords;
 }
 
 // Movers: rank r among the sorted movers plus the stayers before (k, slot):
@@ -226,7 +238,8 @@ __global__ void __launch_bounds__(kNsBlock)
 __global__ void __launch_bounds__(kNsBlock)
     k_ns_movers(const uint32_t* __restrict__ prev, int64_t n,
                 const uint32_t* __restrict__ mask, const uint32_t* __restrict__ prefix,
-                int64_t nwords, const uint32_t* __restrict__ total,
+                const uint32_t* __restrict__ bsum, int64_t nwords,
+                const uint32_t* __restrict__ total,
                 const uint32_t* __restrict__ mkey, const uint32_t* __restrict__ mslot,
                 uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_perm) {
   const uint32_t nm = *total;
@@ -254,11 +267,11 @@ __global__ void __launch_bounds__(kNsBlock)
     }
     const int64_t ub = lo;
     const int64_t cut = min(ub, static_cast<int64_t>(slot));
-    const uint32_t mb_lb = movers_before(mask, prefix, nwords, total, lb);
+    const uint32_t mb_lb = movers_before(mask, prefix, bsum, nwords, total, lb);
     uint32_t stayers = static_cast<uint32_t>(lb) - mb_lb;
     if (cut > lb) {
       stayers += static_cast<uint32_t>(cut - lb) -
-                 (movers_before(mask, prefix, nwords, total, cut) - mb_lb);
+                 (movers_before(mask, prefix, bsum, nwords, total, cut) - mb_lb);
     }
     const uint32_t pos = static_cast<uint32_t>(r) + stayers;
     out_keys[pos] = k;
@@ -268,7 +281,7 @@ __global__ void __launch_bounds__(kNsBlock)
 
 struct NearLayout {
   int64_t nwords, nblocks;
-  size_t off_mask, off_count, off_prefix, off_bsum, off_total, off_mk0, off_ms0, off_mk1,
+  size_t off_mask, off_prefix, off_bsum, off_total, off_done, off_mk0, off_ms0, off_mk1,
       off_ms1, off_radix, bytes;
 };
 
@@ -286,10 +299,10 @@ NearLayout near_layout(int64_t n) {
   };
   const size_t nn = static_cast<size_t>(n > 0 ? n : 1);
   L.off_mask = take(sizeof(uint32_t) * L.nwords);
-  L.off_count = take(sizeof(uint32_t) * L.nwords);
   L.off_prefix = take(sizeof(uint32_t) * (L.nwords + 1));
   L.off_bsum = take(sizeof(uint32_t) * (L.nblocks + 1));
   L.off_total = take(sizeof(uint32_t));
+  L.off_done = take(sizeof(uint32_t));
   L.off_mk0 = take(sizeof(uint32_t) * nn);
   L.off_ms0 = take(sizeof(uint32_t) * nn);
   L.off_mk1 = take(sizeof(uint32_t) * nn);
@@ -303,6 +316,12 @@ NearLayout near_layout(int64_t n) {
 
 size_t near_sort_scratch_bytes(int64_t n) { return near_layout(n).bytes; }
 
+cudaError_t near_sort_reset(void* scratch, int64_t n, cudaStream_t stream) {
+  const NearLayout L = near_layout(n);
+  return cudaMemsetAsync(static_cast<unsigned char*>(scratch) + L.off_done, 0,
+                         sizeof(uint32_t), stream);
+}
+
 cudaError_t near_sort(const uint32_t* keys, const uint32_t* prev, int64_t n,
                       int key_bits, uint32_t* out_keys, uint32_t* out_perm,
                       void* scratch, cudaStream_t stream, int64_t* launches) {
@@ -310,33 +329,29 @@ cudaError_t near_sort(const uint32_t* keys, const uint32_t* prev, int64_t n,
   const NearLayout L = near_layout(n);
   auto* base = static_cast<unsigned char*>(scratch);
   auto* mask = reinterpret_cast<uint32_t*>(base + L.off_mask);
-  auto* count = reinterpret_cast<uint32_t*>(base + L.off_count);
   auto* prefix = reinterpret_cast<uint32_t*>(base + L.off_prefix);
   auto* bsum = reinterpret_cast<uint32_t*>(base + L.off_bsum);
   auto* total = reinterpret_cast<uint32_t*>(base + L.off_total);
+  auto* done = reinterpret_cast<uint32_t*>(base + L.off_done);
   auto* mk0 = reinterpret_cast<uint32_t*>(base + L.off_mk0);
   auto* ms0 = reinterpret_cast<uint32_t*>(base + L.off_ms0);
   auto* mk1 = reinterpret_cast<uint32_t*>(base + L.off_mk1);
   auto* ms1 = reinterpret_cast<uint32_t*>(base + L.off_ms1);
   const unsigned gslots = static_cast<unsigned>((n + kNsBlock - 1) / kNsBlock);
-  k_ns_flags<<<gslots, kNsBlock, 0, stream>>>(keys, prev, n, mask, count);
-  k_ns_scan_blocks<<<static_cast<unsigned>(L.nblocks), kScanBlock, 0, stream>>>(
-      count, L.nwords, prefix, bsum);
-  k_ns_scan_tops<<<1, kScanBlock, 0, stream>>>(bsum, L.nblocks, total);
-  k_ns_scan_add<<<static_cast<unsigned>(L.nblocks), kScanBlock, 0, stream>>>(prefix, L.nwords,
-                                                                             bsum);
-  k_ns_compact<<<gslots, kNsBlock, 0, stream>>>(keys, n, mask, prefix, mk0, ms0);
-  *launches += 5;
+  k_ns_flags_scan<<<static_cast<unsigned>(L.nblocks), kScanBlock, 0, stream>>>(
+      keys, prev, n, L.nwords, L.nblocks, mask, prefix, bsum, total, done);
+  k_ns_compact<<<gslots, kNsBlock, 0, stream>>>(keys, n, mask, prefix, bsum, mk0, ms0);
+  *launches += 2;
   bool in_b = false;
   cudaError_t e = radix_sort(mk0, ms0, mk1, ms1, n, key_bits, false, base + L.off_radix,
                              &in_b, stream, launches, total);
   if (e != cudaSuccess) return e;
   const uint32_t* mkey = in_b ? mk1 : mk0;
   const uint32_t* mslot = in_b ? ms1 : ms0;
-  k_ns_stayers<<<gslots, kNsBlock, 0, stream>>>(prev, n, mask, prefix, L.nwords, total, mkey,
+  k_ns_stayers<<<gslots, kNsBlock, 0, stream>>>(prev, n, mask, prefix, bsum, total, mkey,
                                                  mslot, out_keys, out_perm);
-  k_ns_movers<<<1216, kNsBlock, 0, stream>>>(prev, n, mask, prefix, L.nwords, total, mkey,
-                                             mslot, out_keys, out_perm);
+  k_ns_movers<<<1216, kNsBlock, 0, stream>>>(prev, n, mask, prefix, bsum, L.nwords, total,
+                                             mkey, mslot, out_keys, out_perm);
   *launches += 2;
   return cudaGetLastError();
 }
