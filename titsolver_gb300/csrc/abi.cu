@@ -497,6 +497,7 @@ int upload_particles(tg_context* ctx, int32_t n_tanks, const tg_tank* tanks,
     D.band_lo_f = static_cast<float>(R * R * (1.0 - 1.0 / 16384.0));
     D.band_hi_f = static_cast<float>(R * R * (1.0 + 1.0 / 16384.0));
     D.cs_f = static_cast<float>(cs);
+    D.inv_cs_f = static_cast<float>(1.0 / cs);
     double hinv_d = 1.0;
     for (int k = 0; k < dim; ++k) hinv_d *= D.hinv;
     D.w = kernel_weight(C.P.kernel, dim) * hinv_d;

@@ -42,6 +42,7 @@ struct TankDev {
   double radius2;      // (unit_radius * h)^2 in FP64
   float radius2_f;     // the same rounded from FP32 operands
   float cs_f;          // cell size in FP32
+  float inv_cs_f;      // 1 / cell size in FP32 (row clipping)
   double w;            // kernel weight * h^-d
   double wg;           // w * h^-1 (gradient prefactor)
   double m;            // particle mass
