@@ -523,7 +523,7 @@ class Engine final : public EngineBase {
   }
 
   // The wall pass: the walls near fluid listed first (when the pass has a
-  // fluid box), then teams of kWallTeam lanes over the list, at most 16
+  // fluid box), then teams of wall_team lanes over the list, at most 16
   // blocks per multiprocessor taking walls in turn.
   void launch_walls(Context& C, const StageArgs<D, F>& a) {
     if (a.fbox != nullptr) {
@@ -532,7 +532,7 @@ class Engine final : public EngineBase {
     }
     const int64_t cap = 16 * static_cast<int64_t>(C.sm_count > 0 ? C.sm_count : 152);
     const unsigned grid = static_cast<unsigned>(
-        std::max<int64_t>(1, std::min<int64_t>(grid_for(C.n_wall * kWallTeam, 128), cap)));
+        std::max<int64_t>(1, std::min<int64_t>(grid_for(C.n_wall * wall_team<D, F>(), 128), cap)));
     k_walls<D, F, K><<<grid, 128, 0, C.stream>>>(a);
     C.launches += 1;
   }
