@@ -394,11 +394,6 @@ cudaError_t radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
   return cudaGetLastError();
 }
 
-size_t cell_table_scratch_bytes(uint32_t total_cells) {
-  const int64_t nblocks = (static_cast<int64_t>(total_cells) + kTableCells) / kTableCells;
-  return sizeof(uint32_t) * static_cast<size_t>(nblocks + 2);
-}
-
 cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
                              uint32_t total_cells, uint32_t* cell_start,
                              void* scratch, cudaStream_t stream,

@@ -49,11 +49,11 @@ cudaError_t near_sort(const uint32_t* keys, const uint32_t* prev, int64_t n,
                       int key_bits, uint32_t* out_keys, uint32_t* out_perm,
                       void* scratch, cudaStream_t stream, int64_t* launches);
 
-// Scratch needed by build_cell_table (bytes).
-size_t cell_table_scratch_bytes(uint32_t total_cells);
-
 // cell_start[c] = first sorted index whose key >= c, for c in
-// [0, total_cells]; cell_start[total_cells] = n.  Two kernels.
+// [0, total_cells]; cell_start[total_cells] = n.  Every cell searches the
+// sorted keys (used by the no-allocation density pass, whose scratch is
+// static).  The scratch holds (total_cells + 256) / 256 + 2 words.  Two
+// kernels.
 cudaError_t build_cell_table(const uint32_t* sorted_keys, int64_t n,
                              uint32_t total_cells, uint32_t* cell_start,
                              void* scratch, cudaStream_t stream,
