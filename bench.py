@@ -231,11 +231,13 @@ ISSUE_PER_SM_CLK = 4
 
 
 def forces_compute(dim: int, n_fluid: int, pairs: int, avg_ms: float,
-                   clk: dict | None) -> dict:
+                   clk: dict | None, cells_per_radius: int | None = None) -> dict:
     """Compute-side roofline of the compensated force pass: FP32 work per
     launch (pairs counted live in this run, the per-pair FLOPs from the
     source) against the FP32 pipe's nominal rate at the sampled SM clock,
-    and the recorded ncu instruction count against the issue rate."""
+    and the recorded ncu instruction count (per fluid particle, captured at
+    the cell size the record names; this run's cell size beside it) against
+    the issue rate."""
     mhz = float(clk["sm_mhz"]) if clk and clk.get("sm_mhz") else 2070.0
     sec = avg_ms / 1e3
     flops = pairs * FLOPS_PER_PAIR[dim]
@@ -253,10 +255,14 @@ def forces_compute(dim: int, n_fluid: int, pairs: int, avg_ms: float,
     if d is not None and "warp_inst_per_fluid_particle" in d:
         inst = d["warp_inst_per_fluid_particle"] * n_fluid
         issue_peak = SM_COUNT * ISSUE_PER_SM_CLK * mhz * 1e6
+        rec = d.get("cells_per_radius")
+        at = f" at {rec} cells per radius" if rec else ""
+        run = f" (this run: {cells_per_radius})" if cells_per_radius else ""
         out.update({"warp_inst_per_launch": inst,
                     "thread_inst_per_pair": 32.0 * inst / max(pairs, 1),
                     "issue_frac": inst / sec / issue_peak,
-                    "inst_source": f"recorded: smsp__inst_executed.sum of {d['source']}"})
+                    "inst_source": (f"recorded: smsp__inst_executed.sum of {d['source']}{at}"
+                                    f"{run}, scaled by the fluid count")})
     return out
 
 
@@ -614,7 +620,8 @@ def run_gpu(args, ranks) -> dict | None:
                 "traffic_source": forces_traffic_source(dim, "fp32c"),
                 "peak_source": f"{peaks['source']} hbm_gbs",
                 "alg_bytes_per_launch": alg, "avg_launch_ms": forces_avg_ms,
-                "compute": forces_compute(dim, nf, pairs, forces_avg_ms, clk),
+                "compute": forces_compute(dim, nf, pairs, forces_avg_ms, clk,
+                                          tuning32.get("cells_per_radius")),
                 "ncu_working_ceiling": forces_ceiling(dim, "fp32c")}
 
     extras = {}
